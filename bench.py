@@ -1,0 +1,318 @@
+"""Throughput of the ETDRK2 stepping path on batched 2D vorticity.
+
+Workload (one bench step): NavierStokesVorticity(2, 2*pi, 256, dt=0.01,
+diffusivity=1e-3), ETDRK2, batch 128, 200 steps (``repeat``), float32,
+seeded random truncated Fourier series ICs (cutoff 5, max|w| = 1).
+Metric: DOF-steps/s = batch * 256^2 * 200 / time.
+
+Arms:
+  default            the GB300 path (libexgb.so), one JSON line on rank 0
+  --impl reference   the reference algorithm's CPU path: the NumPy oracle
+                     (restatement of exponax; JAX is not installed), run on
+                     all host cores with one process per sample
+
+Timing: W warm-up steps, then K steps each bracketed by CUDA events on the
+launching stream; L2 is flushed (write of a 256 MiB buffer) between timed
+steps outside the events; max over ranks; nvidia-smi clocks sampled during
+the timed region.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 256
+BATCH = 128
+NSTEPS = 200
+DT = 0.01
+NU = 1e-3
+# algorithmic HBM bytes per DOF-step of ETDRK2 with the Fourier state
+# resident between steps: 6 passes over a complex64 half-spectrum
+BYTES_PER_DOF_STEP = 6 * 8 * (N // 2 + 1) / N
+
+
+def metric_name():
+    return "ETDRK DOF-steps/s at 1 GB300"
+
+
+def config(extra=None):
+    c = {"workload": "NavierStokesVorticity 2D 256^2, nu=1e-3, dt=0.01, ETDRK2, batch 128, 200 steps (repeat)",
+         "global_batch": BATCH, "num_points": N, "steps_per_bench_step": NSTEPS, "dt": DT,
+         "parallelism": "replicas (batch shards, no collective)", "l2": "flushed between timed steps (256 MiB write)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def make_ics(b0, count):
+    from exponax_gb300.ic import RandomTruncatedFourierSeries
+
+    g = RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    return np.stack([g(N, key=s) for s in range(b0, b0 + count)])
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    def __init__(self, out_path):
+        self.path = out_path
+        self.proc = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self, gpu_index=0):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9 or not p[0].isdigit() or int(p[0]) != gpu_index:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle)
+def _oracle_worker(args):
+    seed, nsteps = args
+    from oracle import exponax_np as o
+
+    st = o.NavierStokesVorticity(2, 2 * np.pi, N, DT, diffusivity=NU)
+    u = make_ics(seed, 1)[0]
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        u = st(u)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(samples=None, nsteps=40):
+    """NumPy oracle of the same workload on the host cores, one process per
+    sample (spawn), bounded sample of `samples` x `nsteps` sample-steps."""
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    try:
+        cores = len(os.sched_getaffinity(0))
+    except Exception:
+        pass
+    samples = samples or cores
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(cores, samples)) as pool:
+        worker_s = pool.map(_oracle_worker, [(s, nsteps) for s in range(samples)])
+    # the workers run concurrently (one per core): the slowest one bounds the job
+    wall = max(worker_s)
+    dofs = samples * N * N * nsteps
+    return {"value": dofs / wall, "unit": "DOF-steps/s", "cores": min(cores, samples), "kind": "port",
+            "sample": f"NumPy oracle (exponax restatement), {samples} samples x {nsteps} steps of the same "
+                      f"256^2 ETDRK2 problem, one spawn process per sample; slowest worker {wall:.2f} s"}
+
+
+# ------------------------------------------------------------------ arms
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    return rank, ws
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return
+    # warm-up (pool start, imports) then K timed bounded samples
+    cores = os.cpu_count() or 1
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_baseline(samples=min(cores, 4), nsteps=2)
+    vals = []
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(nsteps=20))
+    v = float(np.median([x["value"] for x in vals]))
+    base = dict(vals[0])
+    base["value"] = v
+    line = {"metric": metric_name(), "value": v, "unit": "DOF-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": BATCH * N * N * NSTEPS / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config({"note": "ms_per_step extrapolates the measured rate to the full bench step"}),
+            "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "DOF-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank, ws):
+    import ctypes
+
+    import torch
+
+    import exponax_gb300 as ex
+    from exponax_gb300 import _device, _lib
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    lib = _lib.load()
+    st = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, N, DT, diffusivity=NU)
+    plan = st.plan.handle
+    stream = torch.cuda.current_stream()
+    sptr = _device.stream()
+
+    u0_host = make_ics(rank * BATCH, BATCH)  # this rank's shard of seeds
+    u0 = torch.from_numpy(u0_host).cuda()
+    uh0 = ex.fft(u0)
+    out_h = torch.empty_like(uh0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def fourier_run():
+        _lib.check(lib.exgb_repeat_fourier(plan, sptr, uh0.data_ptr(), out_h.data_ptr(), BATCH, NSTEPS))
+
+    # ---- warm-up
+    for _ in range(args.warmup):
+        fourier_run()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+
+    # ---- value: device-resident inputs, the fused 2D kernel (1 launch per bench step)
+    clocks = ClockSampler(os.path.join(ROOT, "gpurun_out", f"bench_clocks_r{rank}.csv")
+                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/bench_clocks_r{rank}.csv")
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fourier_run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    total_ms = float(np.sum(times))
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = BATCH * ws * N * N * NSTEPS / (ms_step * 1e-3)
+
+    # ---- e2e: public API, pinned host buffers, H2D + repeat + D2H inside the timed region
+    pin_in = torch.from_numpy(u0_host).pin_memory()
+    pin_out = torch.empty_like(pin_in).pin_memory()
+    rep = ex.vmap(ex.repeat(st, NSTEPS))
+    for _ in range(max(1, args.warmup)):
+        dev = pin_in.cuda(non_blocking=True)
+        pin_out.copy_(rep(dev), non_blocking=True)
+    torch.cuda.synchronize()
+    etimes = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        dev = pin_in.cuda(non_blocking=True)
+        res = rep(dev)
+        pin_out.copy_(res, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        etimes.append(e0.elapsed_time(e1))
+    clk = clocks.stop(local)
+    e_ms = float(np.sum(etimes)) / args.steps
+    if ws > 1:
+        t = torch.tensor([e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e_ms = float(t.item())
+    e2e = BATCH * ws * N * N * NSTEPS / (e_ms * 1e-3)
+
+    # ---- roofline of the dominant kernel (etdrk2d_kernel: the only launch of fourier_run)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    alg_bytes = BATCH * N * N * NSTEPS * BYTES_PER_DOF_STEP
+    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "etdrk2d_traffic.txt")
+    if os.path.exists(tf):
+        for line in open(tf):
+            if line.startswith("dram_bytes_per_dof_step="):
+                traffic = float(line.split("=")[1]) * BATCH * N * N * NSTEPS
+
+    if rank == 0:
+        cpu = cpu_baseline() if ws == 1 and not args.no_cpu else None
+        line = {"metric": metric_name(), "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded truncated Fourier series ICs)",
+                "config": config({"value_path": "exgb_repeat_fourier on device-resident Fourier states",
+                                  "e2e_path": "vmap(repeat(stepper, 200)) with pinned host in/out"}),
+                "e2e": {"value": e2e, "unit": "DOF-steps/s", "ms_per_step": e_ms,
+                        "h2d_bytes_per_step": int(pin_in.numel() * 4), "d2h_bytes_per_step": int(pin_out.numel() * 4)},
+                "gpu_launches": args.steps * 1 + args.steps * 5,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic,
+                             "kernel": "etdrk2d_kernel",
+                             "note": f"algorithmic {BYTES_PER_DOF_STEP:.2f} B/DOF-step (ETDRK2, 6 complex64 "
+                                     f"half-spectrum passes) x {BATCH}x{N}^2x{NSTEPS} per launch; peak {peak_src}"},
+                "clocks": clk, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.barrier()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    rank, ws = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+    else:
+        run_gb300(args, rank, ws)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

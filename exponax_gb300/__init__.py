@@ -1,0 +1,37 @@
+"""exponax_gb300 -- the ETDRK pseudo-spectral stepping path of exponax,
+rebuilt for NVIDIA GB300 (sm_103a).
+
+Drop-in surface for the reference's hot path: ``stepper.*`` (``__call__``,
+``step``, ``step_fourier``), ``etdrk.ETDRK0..4``, ``nonlin_fun.*``,
+``rollout``, ``repeat``, ``RepeatedStepper``, ``spectral.fft/ifft`` and
+``map_between_resolutions``.  All stepping runs in libexgb.so (hand-written
+CUDA, C ABI in include/exgb.h); there is no CPU fallback.
+"""
+
+from . import etdrk, ic, metrics, nonlin_fun, spectral, stepper
+from ._lib import ExgbError
+from ._utils import RepeatedStepper, make_grid, repeat, rollout, vmap
+from .interpolation import map_between_resolutions
+from .spectral import fft, ifft
+from .stepper import BaseStepper
+
+__version__ = "0.1.0"
+
+__all__ = [
+    "BaseStepper",
+    "ExgbError",
+    "RepeatedStepper",
+    "etdrk",
+    "fft",
+    "ic",
+    "ifft",
+    "make_grid",
+    "map_between_resolutions",
+    "metrics",
+    "nonlin_fun",
+    "repeat",
+    "rollout",
+    "spectral",
+    "stepper",
+    "vmap",
+]

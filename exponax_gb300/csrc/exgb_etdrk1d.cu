@@ -1,0 +1,541 @@
+// exgb_etdrk1d.cu -- fused multi-step ETDRK0..4 for 1D pseudo-spectral
+// problems, every state resident in shared memory for the whole rollout.
+//
+// One work item = m instances of one plan.  A CTA takes items from a device
+// queue (atomicAdd on a head counter; no spin-waits anywhere), loads the m
+// initial states (rfft), runs nsteps ETDRK steps and writes either the whole
+// physical trajectory, the final physical state or the final Fourier state.
+// Only the trajectory / final state touch HBM.
+//
+// Per nonlinear evaluation (reference: nonlin_fun/_convection.py:104-231,
+// _gradient_norm.py:84-101, _polynomial.py:64-76, _general_nonlinear.py:111-119)
+//   z = ifft(mask u^ + i mask ik u^)            one complex N-point FFT
+//   p = u^2, q = beta u u_x + gamma (u_x^2 - zmf mean) + sum_k c_k u^k
+//   Z = fft(p + i q)                             one complex N-point FFT
+//   N^ = mask ( alpha ik P + Q )                 fused with the ETDRK stage update
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "exgb_internal.h"
+
+namespace exgb {
+
+void* workspace(size_t bytes, int slot_offset);
+
+enum : int {
+  MODE_TRAJ = 0,      // physical in, trajectory out
+  MODE_FINAL = 1,     // physical in, final physical state out
+  MODE_FOURIER = 2,   // Fourier in, final Fourier state out
+  MODE_NONLIN = 3,    // Fourier in, N(u^) out
+};
+
+struct Item1D {
+  const PlanDev* plan;
+  const void* in;   // float (physical) or float2 (Fourier), instance 0 of this item
+  void* out;        // float or float2
+  int m;            // instances
+  int64_t in_stride, out_stride;  // elements (float or float2) between instances
+};
+
+__host__ __device__ inline int nbuf_for_order(int order) {
+  return order <= 1 ? 1 : order == 2 ? 3 : order == 3 ? 4 : 6;
+}
+
+__device__ __forceinline__ float2 ldg2(const float2* p) { return __ldg(p); }
+
+// Builds the packed inverse-transform input of the nonlinear evaluation
+// for m instances from states X (stride M) into work (stride N).
+__device__ void nl_pack(const PlanDev& P, const float2* X, int sx, float2* work, int m, int tid, int nthr) {
+  const int N = P.N, M = P.M;
+  const bool even = (N & 1) == 0;
+  const float invN = 1.f / (float)N;
+  for (int t = tid; t < m * N; t += nthr) {
+    const int i = t / N, k = t - i * N;
+    const bool ext = k >= M;
+    const int kk = ext ? N - k : k;
+    const bool ro = (k == 0) || (even && k == N / 2);
+    float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+    if (kk <= P.kmax) {
+      a = X[i * sx + kk];
+      if (P.needs_ux) {
+        const float ks = P.kscale * (float)kk;  // ik u^ with k from rfftfreq
+        b = make_float2(-ks * a.y, ks * a.x);
+      }
+    }
+    work[t] = cscale(pack_pair(a, b, ext, ro), invN);
+  }
+}
+
+// Pointwise products on the physical values z = u + i u_x (in place), with
+// u_x^2 written to `sq` when the zero-mode fix needs its mean.
+__device__ void nl_products(const PlanDev& P, float2* z, float* sq, int m, int tid, int nthr) {
+  const int N = P.N;
+  const bool zmf = P.gamma != 0.f && P.zero_mode_fix;
+  for (int t = tid; t < m * N; t += nthr) {
+    const float u = z[t].x, ux = z[t].y;
+    float q = 0.f;
+    if (P.beta != 0.f) q = fmaf(P.beta * u, ux, q);
+    if (P.gamma != 0.f) q = fmaf(P.gamma * ux, ux, q);
+    if (P.npoly > 0) {
+      float pw = 1.f, acc = 0.f;
+      for (int c = 0; c < P.npoly; ++c) {
+        acc = fmaf(P.poly[c], pw, acc);
+        pw *= u;
+      }
+      q += acc;
+    }
+    if (zmf) sq[t] = ux * ux;
+    z[t] = make_float2(u * u, q);
+  }
+}
+
+// Deterministic per-instance sums of sq (one warp per instance).
+__device__ void nl_reduce(const float* sq, float* sums, int N, int m, int tid, int nthr) {
+  const int warp = tid >> 5, lane = tid & 31, nw = nthr >> 5;
+  for (int i = warp; i < m; i += nw) {
+    float s = 0.f;
+    for (int x = lane; x < N; x += 32) s += sq[i * N + x];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sums[i] = s;
+  }
+}
+
+struct Bufs {
+  float2 *U, *S1, *S, *N0, *N1, *N2;
+  float2 *w0, *w1;
+  float* sums;
+};
+
+// Stage epilogue: combine the fresh nonlinear value nv at mode k of instance
+// i with the stored stages.  Reference stage formulas: etdrk/_etdrk_1.py:82,
+// _etdrk_2.py:95-101, _etdrk_3.py:195-210, _etdrk_4.py:202-222.
+__device__ __forceinline__ void stage_update(const PlanDev& P, const Bufs& b, int i, int k, int stage, float2 nv,
+                                             int M, int ch_off) {
+  const int o = i * M + k;
+  const int c = ch_off + k;
+  switch (P.order) {
+    case 1: {
+      const float2 E = ldg2(P.E + c);
+      b.U[o] = cadd(cmul(E, b.U[o]), cscale(nv, __ldg(P.c[0] + c)));
+    } break;
+    case 2:
+      if (stage == 0) {
+        const float2 E = ldg2(P.E + c);
+        b.N0[o] = nv;
+        b.S[o] = cadd(cmul(E, b.U[o]), cscale(nv, __ldg(P.c[0] + c)));
+      } else {
+        b.U[o] = cadd(b.S[o], cscale(csub(nv, b.N0[o]), __ldg(P.c[1] + c)));
+      }
+      break;
+    case 3:
+      if (stage == 0) {
+        b.N0[o] = nv;
+        b.S[o] = cadd(cmul(ldg2(P.Eh + c), b.U[o]), cscale(nv, __ldg(P.c[0] + c)));
+      } else if (stage == 1) {
+        b.N1[o] = nv;
+        const float2 t = csub(cscale(nv, 2.f), b.N0[o]);
+        b.S[o] = cadd(cmul(ldg2(P.E + c), b.U[o]), cscale(t, __ldg(P.c[1] + c)));
+      } else {
+        float2 r = cmul(ldg2(P.E + c), b.U[o]);
+        r = cadd(r, cscale(b.N0[o], __ldg(P.c[2] + c)));
+        r = cadd(r, cscale(b.N1[o], __ldg(P.c[3] + c)));
+        r = cadd(r, cscale(nv, __ldg(P.c[4] + c)));
+        b.U[o] = r;
+      }
+      break;
+    case 4:
+      if (stage == 0) {
+        b.N0[o] = nv;
+        b.S1[o] = cadd(cmul(ldg2(P.Eh + c), b.U[o]), cscale(nv, __ldg(P.c[0] + c)));
+      } else if (stage == 1) {
+        b.N1[o] = nv;
+        b.S[o] = cadd(cmul(ldg2(P.Eh + c), b.U[o]), cscale(nv, __ldg(P.c[0] + c)));
+      } else if (stage == 2) {
+        b.N2[o] = nv;
+        const float2 t = csub(cscale(nv, 2.f), b.N0[o]);
+        b.S[o] = cadd(cmul(ldg2(P.Eh + c), b.S1[o]), cscale(t, __ldg(P.c[0] + c)));
+      } else {
+        float2 r = cmul(ldg2(P.E + c), b.U[o]);
+        r = cadd(r, cscale(b.N0[o], __ldg(P.c[3] + c)));
+        r = cadd(r, cscale(cadd(b.N1[o], b.N2[o]), 2.f * __ldg(P.c[4] + c)));
+        r = cadd(r, cscale(nv, __ldg(P.c[5] + c)));
+        b.U[o] = r;
+      }
+      break;
+    default:
+      break;
+  }
+}
+
+// One nonlinear evaluation of the m states X followed by the stage update
+// (stage >= 0) or a plain store of N^ into X_out (stage < 0).
+__device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m, int stage, float2* X_out,
+                        int tid, int nthr) {
+  const int N = P.N, M = P.M;
+  nl_pack(P, X, M, b.w0, m, tid, nthr);
+  __syncthreads();
+  float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
+  float2* other = (P.fft.npass & 1) ? b.w0 : b.w1;
+  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, P.tw, tid, nthr, BlockSync{});
+  const bool zmf = P.gamma != 0.f && P.zero_mode_fix;
+  nl_products(P, res, (float*)other, m, tid, nthr);
+  __syncthreads();
+  if (zmf) {
+    nl_reduce((const float*)other, b.sums, N, m, tid, nthr);
+    __syncthreads();
+  }
+  // forward: input in res, ping-pong with other
+  float2* fres = (P.fft.npass & 1) ? other : res;
+  block_fft<false>(P.fft, res, other, LinMap{fres, N}, m, P.tw, tid, nthr, BlockSync{});
+  for (int t = tid; t < m * M; t += nthr) {
+    const int i = t / M, k = t - i * M;
+    float2 nv = make_float2(0.f, 0.f);
+    if (k <= P.kmax) {
+      float2 Pk, Qk;
+      unpack_pair(fres[i * N + k], fres[i * N + (k == 0 ? 0 : N - k)], Pk, Qk);
+      if (P.needs_q) nv = Qk;
+      if (P.alpha != 0.f) {
+        const float ks = P.kscale * (float)k;
+        // alpha * (i ks) * P
+        nv = cadd(nv, make_float2(-P.alpha * ks * Pk.y, P.alpha * ks * Pk.x));
+      }
+      if (zmf && k == 0) nv.x -= P.gamma * b.sums[i];
+    }
+    if (stage < 0) X_out[t] = nv;
+    else stage_update(P, b, i, k, stage, nv, M, 0);
+  }
+  __syncthreads();
+}
+
+// Physical output of m states (pairs packed in one complex FFT).
+__device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, int64_t inst_stride, int tid, int nthr) {
+  const int N = P.N, M = P.M;
+  const bool even = (N & 1) == 0;
+  const int pairs = (m + 1) / 2;
+  const float invN = 1.f / (float)N;
+  for (int t = tid; t < pairs * N; t += nthr) {
+    const int p = t / N, k = t - p * N;
+    const bool ext = k >= M;
+    const int kk = ext ? N - k : k;
+    const bool ro = (k == 0) || (even && k == N / 2);
+    const int ia = 2 * p, ib = 2 * p + 1;
+    const float2 a = b.U[ia * M + kk];
+    const float2 bb = ib < m ? b.U[ib * M + kk] : make_float2(0.f, 0.f);
+    b.w0[t] = cscale(pack_pair(a, bb, ext, ro), invN);
+  }
+  __syncthreads();
+  float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
+  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, P.tw, tid, nthr, BlockSync{});
+  for (int t = tid; t < pairs * N; t += nthr) {
+    const int p = t / N, x = t - p * N;
+    const float2 z = res[t];
+    out[(int64_t)(2 * p) * inst_stride + x] = z.x;
+    if (2 * p + 1 < m) out[(int64_t)(2 * p + 1) * inst_stride + x] = z.y;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__ items, int n_items,
+                                                      int* __restrict__ head, int nsteps, int mode, int project,
+                                                      int include_init, int T) {
+  extern __shared__ __align__(16) float2 sm[];
+  __shared__ PlanDev Ps;
+  __shared__ int s_item;
+  __shared__ float s_sums[64];
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(head, 1);
+    __syncthreads();
+    const int it = s_item;
+    if (it >= n_items) break;
+    const Item1D item = items[it];
+    if (tid == 0) Ps = *item.plan;
+    __syncthreads();
+    const PlanDev& P = Ps;
+    const int N = P.N, M = P.M, m = item.m;
+    // carve shared memory
+    Bufs b;
+    float2* q = sm;
+    b.U = q;
+    q += m * M;
+    b.S1 = b.S = b.N0 = b.N1 = b.N2 = nullptr;
+    if (P.order == 2) {
+      b.S = q; q += m * M;
+      b.N0 = q; q += m * M;
+    } else if (P.order == 3) {
+      b.S = q; q += m * M;
+      b.N0 = q; q += m * M;
+      b.N1 = q; q += m * M;
+    } else if (P.order == 4) {
+      b.S1 = q; q += m * M;
+      b.S = q; q += m * M;
+      b.N0 = q; q += m * M;
+      b.N1 = q; q += m * M;
+      b.N2 = q; q += m * M;
+    }
+    b.w0 = q;
+    q += m * N;
+    b.w1 = q;
+    b.sums = s_sums;
+
+    // ---- load initial state
+    if (mode == MODE_TRAJ || mode == MODE_FINAL) {
+      const float* u0 = (const float*)item.in;
+      const int pairs = (m + 1) / 2;
+      for (int t = tid; t < pairs * N; t += nthr) {
+        const int p = t / N, x = t - p * N;
+        const float a = u0[(int64_t)(2 * p) * item.in_stride + x];
+        const float bb = (2 * p + 1 < m) ? u0[(int64_t)(2 * p + 1) * item.in_stride + x] : 0.f;
+        b.w0[t] = make_float2(a, bb);
+        if (mode == MODE_TRAJ && include_init) {
+          float* o = (float*)item.out;
+          o[(int64_t)(2 * p) * item.out_stride + x] = a;
+          if (2 * p + 1 < m) o[(int64_t)(2 * p + 1) * item.out_stride + x] = bb;
+        }
+      }
+      __syncthreads();
+      float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
+      block_fft<false>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, P.tw, tid, nthr, BlockSync{});
+      for (int t = tid; t < pairs * M; t += nthr) {
+        const int p = t / M, k = t - p * M;
+        float2 A, B;
+        unpack_pair(res[p * N + k], res[p * N + (k == 0 ? 0 : N - k)], A, B);
+        b.U[(2 * p) * M + k] = A;
+        if (2 * p + 1 < m) b.U[(2 * p + 1) * M + k] = B;
+      }
+    } else {
+      const float2* uh = (const float2*)item.in;
+      for (int t = tid; t < m * M; t += nthr) {
+        const int i = t / M, k = t - i * M;
+        b.U[t] = uh[(int64_t)i * item.in_stride + k];
+      }
+    }
+    __syncthreads();
+
+    // ---- time steps
+    const int nstages = (P.order == 0 || P.kind == EXGB_NL_ZERO) ? 0 : P.order;
+    for (int step = 0; step < nsteps; ++step) {
+      if (nstages == 0) {
+        for (int t = tid; t < m * M; t += nthr) {
+          const int k = t % M;
+          b.U[t] = cmul(ldg2(P.E + k), b.U[t]);
+        }
+        __syncthreads();
+      } else {
+        for (int s = 0; s < nstages; ++s) {
+          const float2* X = (s == 0) ? b.U : (P.order == 4 && s == 1) ? b.S1 : b.S;
+          nl_eval(P, b, X, m, s, nullptr, tid, nthr);
+        }
+      }
+      if (project) {
+        // c2r of the step's physical round trip drops Im at DC and Nyquist
+        for (int i = tid; i < m; i += nthr) {
+          b.U[i * M].y = 0.f;
+          if ((N & 1) == 0) b.U[i * M + N / 2].y = 0.f;
+        }
+        __syncthreads();
+      }
+      if (mode == MODE_TRAJ) {
+        float* o = (float*)item.out + (int64_t)(step + include_init) * N;
+        emit_phys(P, b, m, o, item.out_stride, tid, nthr);
+      }
+    }
+
+    // ---- final store
+    if (mode == MODE_FINAL) {
+      emit_phys(P, b, m, (float*)item.out, item.out_stride, tid, nthr);
+    } else if (mode == MODE_FOURIER) {
+      float2* o = (float2*)item.out;
+      for (int t = tid; t < m * M; t += nthr) {
+        const int i = t / M, k = t - i * M;
+        o[(int64_t)i * item.out_stride + k] = b.U[t];
+      }
+    }
+    __syncthreads();
+    (void)T;
+  }
+}
+
+// Nonlinear-function-only kernel (exgb_nonlinear): one item, N^ written to out.
+__global__ void __launch_bounds__(256) nonlin1d_kernel(const Item1D* __restrict__ items, int n_items) {
+  extern __shared__ __align__(16) float2 sm[];
+  __shared__ PlanDev Ps;
+  __shared__ float s_sums[64];
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int it = blockIdx.x;
+  if (it >= n_items) return;
+  const Item1D item = items[it];
+  if (tid == 0) Ps = *item.plan;
+  __syncthreads();
+  const PlanDev& P = Ps;
+  const int N = P.N, M = P.M, m = item.m;
+  Bufs b{};
+  b.U = sm;
+  b.w0 = sm + m * M;
+  b.w1 = b.w0 + m * N;
+  b.sums = s_sums;
+  const float2* uh = (const float2*)item.in;
+  for (int t = tid; t < m * M; t += nthr) {
+    const int i = t / M, k = t - i * M;
+    b.U[t] = uh[(int64_t)i * item.in_stride + k];
+  }
+  __syncthreads();
+  // results go back into U (the pack step has consumed it before the epilogue)
+  nl_eval(P, b, b.U, m, -1, b.U, tid, nthr);
+  float2* o = (float2*)item.out;
+  for (int t = tid; t < m * M; t += nthr) {
+    const int i = t / M, k = t - i * M;
+    o[(int64_t)i * item.out_stride + k] = b.U[t];
+  }
+}
+
+static size_t smem_for(const PlanDev& P, int m, bool nonlin_only) {
+  const int nb = nonlin_only ? 1 : nbuf_for_order(P.order);
+  return sizeof(float2) * (size_t)m * ((size_t)nb * P.M + 2 * (size_t)P.N);
+}
+
+static int smem_limit() {
+  static int lim = 0;
+  if (!lim) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  return lim;
+}
+
+// Items for `batch` instances of one plan, m instances per item.
+static int choose_m(const PlanDev& P, int64_t batch, int sm_count, bool nonlin_only) {
+  int m = std::max(1, 1024 / P.N);
+  // spread small batches over the SMs first
+  const int64_t per_sm = (batch + 2 * sm_count - 1) / (2 * (int64_t)sm_count);
+  m = (int)std::max<int64_t>(1, std::min<int64_t>(m, per_sm));
+  m = std::min(m, 64);
+  while (m > 1 && smem_for(P, m, nonlin_only) > (size_t)smem_limit() - 4096) --m;
+  return m;
+}
+
+static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStream_t st, int nsteps, int mode,
+                        int project, int include_init, int sm_count, bool nonlin_only) {
+  if (items.empty()) return EXGB_OK;
+  if (smem > (size_t)smem_limit() - 2048)
+    return fail(EXGB_EUNSUPPORTED, "1D state does not fit in shared memory (N too large for this build)");
+  // items + queue head in one workspace region (slot 2+: keep the transform slots free)
+  const size_t ib = sizeof(Item1D) * items.size();
+  const size_t total = ib + 256;
+  // workspace slot 1 may be shared with transforms issued earlier on the
+  // same stream; stream order keeps that safe.
+  char* ws = (char*)workspace(total, 1);
+  if (!ws) return fail(EXGB_ENOMEM, "workspace allocation failed");
+  int* head = (int*)(ws + ((ib + 127) / 128) * 128);
+  EXGB_CUDA(cudaMemcpyAsync(ws, items.data(), ib, cudaMemcpyHostToDevice, st));
+  EXGB_CUDA(cudaMemsetAsync(head, 0, sizeof(int), st));
+  if (nonlin_only) {
+    EXGB_CUDA(cudaFuncSetAttribute(nonlin1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    nonlin1d_kernel<<<(unsigned)items.size(), 256, smem, st>>>((const Item1D*)ws, (int)items.size());
+  } else {
+    EXGB_CUDA(cudaFuncSetAttribute(etdrk1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 1;
+    EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, etdrk1d_kernel, 256, smem));
+    per_sm = std::max(1, per_sm);
+    const int grid = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)sm_count * per_sm);
+    etdrk1d_kernel<<<grid, 256, smem, st>>>((const Item1D*)ws, (int)items.size(), head, nsteps, mode, project,
+                                            include_init, 0);
+  }
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, const float2* u0_hat, float* out_phys,
+                float2* out_hat, int64_t batch, int nsteps, int project, int emit_traj, int include_init,
+                int nonlinear_only) {
+  const PlanDev& P = plan->dev;
+  if (batch <= 0) return EXGB_OK;
+  int mode;
+  if (nonlinear_only) mode = MODE_NONLIN;
+  else if (u0_phys) mode = emit_traj ? MODE_TRAJ : MODE_FINAL;
+  else mode = MODE_FOURIER;
+  const int m = choose_m(P, batch, plan->sm_count, nonlinear_only);
+  const int T = nsteps + (include_init ? 1 : 0);
+  std::vector<Item1D> items;
+  for (int64_t b0 = 0; b0 < batch; b0 += m) {
+    Item1D it{};
+    it.plan = plan->d_dev;
+    it.m = (int)std::min<int64_t>(m, batch - b0);
+    if (mode == MODE_TRAJ || mode == MODE_FINAL) {
+      it.in = u0_phys + b0 * P.N;
+      it.in_stride = P.N;
+    } else {
+      it.in = u0_hat + b0 * P.M;
+      it.in_stride = P.M;
+    }
+    if (mode == MODE_TRAJ) {
+      it.out = out_phys + b0 * (int64_t)T * P.N;
+      it.out_stride = (int64_t)T * P.N;
+    } else if (mode == MODE_FINAL) {
+      it.out = out_phys + b0 * P.N;
+      it.out_stride = P.N;
+    } else {
+      it.out = out_hat + b0 * P.M;
+      it.out_stride = P.M;
+    }
+    items.push_back(it);
+  }
+  return launch_items(items, smem_for(P, m, nonlinear_only), st, nsteps, mode, project, include_init,
+                      plan->sm_count, nonlinear_only);
+}
+
+}  // namespace exgb
+
+using namespace exgb;
+
+extern "C" int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, int32_t nsteps,
+                                  int32_t include_init, void* stream) {
+  if (n_items < 0 || (n_items > 0 && !items)) return fail(EXGB_EINVAL, "bad work item list");
+  if (nsteps < 0) return fail(EXGB_EINVAL, "nsteps must be >= 0");
+  if (n_items == 0) return EXGB_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  // group consecutive instances of the same plan with contiguous buffers?
+  // Instances are independent; pack up to m of the same plan per item only
+  // when their buffers are evenly strided, else one instance per item.
+  const int T = nsteps + (include_init ? 1 : 0);
+  std::vector<Item1D> its;
+  std::vector<double> cost;
+  size_t smem = 0;
+  int sm_count = 0;
+  for (int64_t i = 0; i < n_items;) {
+    const exgb_plan* p = items[i].plan;
+    if (!p || !items[i].u0 || !items[i].traj) return fail(EXGB_EINVAL, "work item with NULL plan or buffer");
+    if (p->dev.D != 1) return fail(EXGB_EUNSUPPORTED, "the work queue runs 1D plans");
+    sm_count = p->sm_count;
+    const int N = p->dev.N;
+    const int mmax = std::min(64, std::max(1, 1024 / N));
+    int m = 1;
+    while (m < mmax && i + m < n_items && items[i + m].plan == p &&
+           items[i + m].u0 == items[i].u0 + (int64_t)m * N && items[i + m].traj == items[i].traj + (int64_t)m * T * N)
+      ++m;
+    Item1D it{};
+    it.plan = p->d_dev;
+    it.in = items[i].u0;
+    it.in_stride = N;
+    it.out = items[i].traj;
+    it.out_stride = (int64_t)T * N;
+    it.m = m;
+    its.push_back(it);
+    const double lg = std::log2((double)N);
+    cost.push_back((double)m * N * lg * (p->dev.order + 1));
+    smem = std::max(smem, smem_for(p->dev, m, false));
+    i += m;
+  }
+  // longest-processing-time first
+  std::vector<size_t> idx(its.size());
+  for (size_t k = 0; k < idx.size(); ++k) idx[k] = k;
+  std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+  std::vector<Item1D> sorted;
+  sorted.reserve(its.size());
+  for (size_t k : idx) sorted.push_back(its[k]);
+  return launch_items(sorted, smem, st, nsteps, MODE_TRAJ, 1, include_init, sm_count, false);
+}

@@ -1,0 +1,374 @@
+// exgb_fftnd.cu -- batched real FFTs over the last D axes (rfftn / irfftn
+// with the reference's conventions), the spectral re-sampling of
+// map_between_resolutions, and a grow-only device workspace.
+//
+// Layout: rows are contiguous; two real rows are packed into one complex
+// FFT (z = a + i b) and separated afterwards.  Leading axes are transformed
+// by a strided complex FFT kernel that loads tiles of TI contiguous
+// positions (coalesced 8*TI-byte segments per element row).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "exgb_internal.h"
+
+namespace exgb {
+
+// ---------------------------------------------------------------- workspace
+// Four grow-only buffers per device: 0 = inverse-transform intermediate,
+// 1 = re-sampling spectra / 1D work items, 2 = 2D Fourier state of the
+// physical-space entry points, 3 = 2D rollout frame.  Growing
+// calls cudaFree/cudaMalloc (device-synchronising); the steady state does
+// not allocate.
+static std::mutex g_ws_mu;
+static void* g_ws[64] = {nullptr};
+static size_t g_ws_bytes[64] = {0};
+
+void* workspace(size_t bytes, int slot_offset = 0) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int slot = (dev % 16) * 4 + slot_offset;
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  if (g_ws_bytes[slot] < bytes) {
+    if (g_ws[slot]) cudaFree(g_ws[slot]);
+    g_ws[slot] = nullptr;
+    g_ws_bytes[slot] = 0;
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    g_ws[slot] = p;
+    g_ws_bytes[slot] = bytes;
+  }
+  return g_ws[slot];
+}
+
+static inline size_t smem_optin_limit() {
+  static size_t lim = 0;
+  if (!lim) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    lim = (size_t)v;
+  }
+  return lim;
+}
+
+// ---------------------------------------------------------------- row r2c
+// Each CTA transforms `pairs` pairs of real rows (2*pairs rows).
+__global__ void rfft_rows_kernel(FftPlan fp, const float2* __restrict__ tw, int64_t rows, int pairs,
+                                 const float* __restrict__ in, float2* __restrict__ out) {
+  extern __shared__ float2 smem[];
+  const int n = fp.n, M = n / 2 + 1;
+  float2* buf0 = smem;
+  float2* buf1 = smem + (size_t)pairs * n;
+  const int64_t row0 = (int64_t)blockIdx.x * pairs * 2;
+  for (int t = threadIdx.x; t < pairs * n; t += blockDim.x) {
+    const int p = t / n, x = t - p * n;
+    const int64_t ra = row0 + 2 * p, rb = ra + 1;
+    const float a = ra < rows ? in[ra * n + x] : 0.f;
+    const float b = rb < rows ? in[rb * n + x] : 0.f;
+    buf0[t] = make_float2(a, b);
+  }
+  __syncthreads();
+  float2* res = (fp.npass & 1) ? buf1 : buf0;
+  block_fft<false>(fp, buf0, buf1, LinMap{res, n}, pairs, tw, threadIdx.x, blockDim.x, BlockSync{});
+  for (int t = threadIdx.x; t < pairs * M; t += blockDim.x) {
+    const int p = t / M, k = t - p * M;
+    const int64_t ra = row0 + 2 * p, rb = ra + 1;
+    float2 P, Q;
+    unpack_pair(res[p * n + k], res[p * n + (k == 0 ? 0 : n - k)], P, Q);
+    if (ra < rows) out[ra * M + k] = P;
+    if (rb < rows) out[rb * M + k] = Q;
+  }
+}
+
+// ---------------------------------------------------------------- row c2r
+__global__ void irfft_rows_kernel(FftPlan fp, const float2* __restrict__ tw, int64_t rows, int pairs,
+                                  const float2* __restrict__ in, float* __restrict__ out, float scale) {
+  extern __shared__ float2 smem[];
+  const int n = fp.n, M = n / 2 + 1;
+  float2* buf0 = smem;
+  float2* buf1 = smem + (size_t)pairs * n;
+  const int64_t row0 = (int64_t)blockIdx.x * pairs * 2;
+  const bool even = (n % 2) == 0;
+  for (int t = threadIdx.x; t < pairs * n; t += blockDim.x) {
+    const int p = t / n, k = t - p * n;
+    const int64_t ra = row0 + 2 * p, rb = ra + 1;
+    const bool ext = k >= M;
+    const int kk = ext ? n - k : k;
+    const bool real_only = (k == 0) || (even && k == n / 2);
+    const float2 a = ra < rows ? in[ra * M + kk] : make_float2(0.f, 0.f);
+    const float2 b = rb < rows ? in[rb * M + kk] : make_float2(0.f, 0.f);
+    buf0[t] = pack_pair(a, b, ext, real_only);
+  }
+  __syncthreads();
+  float2* res = (fp.npass & 1) ? buf1 : buf0;
+  block_fft<true>(fp, buf0, buf1, LinMap{res, n}, pairs, tw, threadIdx.x, blockDim.x, BlockSync{});
+  for (int t = threadIdx.x; t < pairs * n; t += blockDim.x) {
+    const int p = t / n, x = t - p * n;
+    const int64_t ra = row0 + 2 * p, rb = ra + 1;
+    const float2 z = res[t];
+    if (ra < rows) out[ra * n + x] = z.x * scale;
+    if (rb < rows) out[rb * n + x] = z.y * scale;
+  }
+}
+
+// ---------------------------------------------------------------- strided axis c2c
+// Element k of the sequence at (o, i) lives at o*outer_stride + i + k*es.
+// CTA (blockIdx.x = tile of TI inner positions, blockIdx.y = outer).
+template <bool INV>
+__global__ void cfft_axis_kernel(FftPlan fp, const float2* __restrict__ tw, int64_t outer_stride, int64_t inner,
+                                 int64_t es, int TI, const float2* in, float2* out, float scale) {
+  extern __shared__ float2 smem[];
+  const int n = fp.n;
+  float2* buf0 = smem;
+  float2* buf1 = smem + (size_t)TI * n;
+  const int64_t o = blockIdx.y;
+  const int64_t i0 = (int64_t)blockIdx.x * TI;
+  const int ti = (inner - i0) < (int64_t)TI ? (int)(inner - i0) : TI;
+  const float2* src = in + o * outer_stride + i0;
+  for (int t = threadIdx.x; t < TI * n; t += blockDim.x) {
+    const int k = t / TI, ii = t - k * TI;
+    buf0[ii * n + k] = ii < ti ? src[(int64_t)k * es + ii] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  float2* res = (fp.npass & 1) ? buf1 : buf0;
+  block_fft<INV>(fp, buf0, buf1, LinMap{res, n}, TI, tw, threadIdx.x, blockDim.x, BlockSync{});
+  float2* dst = out + o * outer_stride + i0;
+  for (int t = threadIdx.x; t < TI * n; t += blockDim.x) {
+    const int k = t / TI, ii = t - k * TI;
+    if (ii < ti) dst[(int64_t)k * es + ii] = cscale(res[ii * n + k], scale);
+  }
+}
+
+static int set_smem(const void* fn, size_t bytes) {
+  if (bytes > 48 * 1024) {
+    if (bytes > smem_optin_limit()) return fail(EXGB_EUNSUPPORTED, "transform does not fit in shared memory");
+    EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  }
+  return EXGB_OK;
+}
+
+static int pairs_for(int n) { return std::max(1, 2048 / n); }
+
+int launch_rfft1d(cudaStream_t st, const FftPlan& fp, const float2* tw, int64_t rows, const float* in, float2* out) {
+  if (rows <= 0) return EXGB_OK;
+  const int pairs = pairs_for(fp.n);
+  const size_t smem = sizeof(float2) * 2 * pairs * fp.n;
+  int rc = set_smem((const void*)rfft_rows_kernel, smem);
+  if (rc) return rc;
+  const int64_t blocks = (rows + 2 * pairs - 1) / (2 * pairs);
+  rfft_rows_kernel<<<(unsigned)blocks, 256, smem, st>>>(fp, tw, rows, pairs, in, out);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+int launch_irfft1d(cudaStream_t st, const FftPlan& fp, const float2* tw, int64_t rows, const float2* in, float* out,
+                   float scale) {
+  if (rows <= 0) return EXGB_OK;
+  const int pairs = pairs_for(fp.n);
+  const size_t smem = sizeof(float2) * 2 * pairs * fp.n;
+  int rc = set_smem((const void*)irfft_rows_kernel, smem);
+  if (rc) return rc;
+  const int64_t blocks = (rows + 2 * pairs - 1) / (2 * pairs);
+  irfft_rows_kernel<<<(unsigned)blocks, 256, smem, st>>>(fp, tw, rows, pairs, in, out, scale);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+int launch_cfft_axis(cudaStream_t st, const FftPlan& fp, const float2* tw, bool inverse, int64_t outer,
+                     int64_t outer_stride, int64_t inner, int64_t es, const float2* in, float2* out, float scale) {
+  if (outer <= 0 || inner <= 0) return EXGB_OK;
+  int TI = std::max(1, std::min(16, 4096 / fp.n));
+  const size_t smem = sizeof(float2) * 2 * (size_t)TI * fp.n;
+  const void* fn = inverse ? (const void*)cfft_axis_kernel<true> : (const void*)cfft_axis_kernel<false>;
+  int rc = set_smem(fn, smem);
+  if (rc) return rc;
+  dim3 grid((unsigned)((inner + TI - 1) / TI), (unsigned)outer);
+  if (outer > 65535) return fail(EXGB_EUNSUPPORTED, "too many outer sequences for one launch");
+  if (inverse)
+    cfft_axis_kernel<true><<<grid, 256, smem, st>>>(fp, tw, outer_stride, inner, es, TI, in, out, scale);
+  else
+    cfft_axis_kernel<false><<<grid, 256, smem, st>>>(fp, tw, outer_stride, inner, es, TI, in, out, scale);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+// ---------------------------------------------------------------- transform plans cache
+struct TfCache {
+  int n = 0;
+  FftPlan fp{};
+  float2* tw = nullptr;
+};
+static std::mutex g_tf_mu;
+static TfCache g_tf[64];
+
+static int get_tf(int n, const FftPlan** fp, const float2** tw) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_tf_mu);
+  int freeslot = -1;
+  for (int i = 0; i < 64; ++i) {
+    if (g_tf[i].n == n + (dev << 20)) {
+      *fp = &g_tf[i].fp;
+      *tw = g_tf[i].tw;
+      return EXGB_OK;
+    }
+    if (g_tf[i].n == 0 && freeslot < 0) freeslot = i;
+  }
+  if (freeslot < 0) return fail(EXGB_EUNSUPPORTED, "too many distinct transform sizes");
+  TfCache& c = g_tf[freeslot];
+  if (!make_fft_plan(n, &c.fp)) return fail(EXGB_ENOTFACTORABLE, "N must be a product of 2, 3 and 5");
+  int rc = build_twiddles(n, &c.tw);
+  if (rc) return rc;
+  c.n = n + (dev << 20);
+  *fp = &c.fp;
+  *tw = c.tw;
+  return EXGB_OK;
+}
+
+int rfftn_impl(cudaStream_t st, int D, int N, int64_t count, const float* in, float2* out) {
+  const FftPlan* fp;
+  const float2* tw;
+  int rc = get_tf(N, &fp, &tw);
+  if (rc) return rc;
+  const int M = N / 2 + 1;
+  if (D == 1) return launch_rfft1d(st, *fp, tw, count, in, out);
+  if (D == 2) {
+    rc = launch_rfft1d(st, *fp, tw, count * N, in, out);
+    if (rc) return rc;
+    return launch_cfft_axis(st, *fp, tw, false, count, (int64_t)N * M, M, M, out, out, 1.f);
+  }
+  return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1 or 2 in this build");
+}
+
+int irfftn_impl(cudaStream_t st, int D, int N, int64_t count, const float2* in, float* out) {
+  const FftPlan* fp;
+  const float2* tw;
+  int rc = get_tf(N, &fp, &tw);
+  if (rc) return rc;
+  const int M = N / 2 + 1;
+  if (D == 1) return launch_irfft1d(st, *fp, tw, count, in, out, 1.f / (float)N);
+  if (D == 2) {
+    float2* tmp = (float2*)workspace(sizeof(float2) * (size_t)count * N * M, 0);
+    if (!tmp) return fail(EXGB_ENOMEM, "workspace allocation failed");
+    rc = launch_cfft_axis(st, *fp, tw, true, count, (int64_t)N * M, M, M, in, tmp, 1.f);
+    if (rc) return rc;
+    return launch_irfft1d(st, *fp, tw, count * N, tmp, out, 1.f / ((float)N * (float)N));
+  }
+  return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1 or 2 in this build");
+}
+
+// ---------------------------------------------------------------- map_between_resolutions
+// Gathers the new half-spectrum from the old one (_interpolation.py:195-285):
+// blocks of get_modes_slices(D, min(N_old, N_new)) are copied, rescaled by
+// (N_new/N_old)^D, and the Nyquist planes are zeroed as the oddball masks do.
+__device__ __forceinline__ int src_index_axis(int k_new, int n_new, int n_old, int nmin) {
+  // leading (fftfreq) axis: returns old index or -1 if not copied
+  const int half = nmin / 2;
+  const bool even = (nmin % 2) == 0;
+  const int pos_hi = even ? half : half + 1;  // positive block [0, pos_hi)
+  if (k_new < pos_hi) return k_new < n_old ? k_new : -1;
+  const int neg = k_new - n_new;  // negative wavenumber in the new grid
+  if (neg >= -half && neg < 0) return n_old + neg;
+  return -1;
+}
+
+__global__ void resample_kernel(int D, int n_old, int n_new, int64_t count, const float2* __restrict__ in,
+                                float2* __restrict__ out, float scale, int zero_old_nyq, int zero_new_nyq) {
+  const int Mo = n_old / 2 + 1, Mn = n_new / 2 + 1;
+  const int nmin = min(n_old, n_new);
+  const int64_t per = (D == 1) ? Mn : (int64_t)n_new * Mn;
+  const int64_t per_old = (D == 1) ? Mo : (int64_t)n_old * Mo;
+  const int64_t total = per * count;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = t / per;
+    const int64_t r = t - c * per;
+    int ky = (int)(r % Mn);
+    int kx = (D == 2) ? (int)(r / Mn) : 0;
+    float2 v = make_float2(0.f, 0.f);
+    bool ok = ky <= nmin / 2;
+    int sx = 0;
+    if (ok && D == 2) {
+      sx = src_index_axis(kx, n_new, n_old, nmin);
+      ok = sx >= 0;
+    }
+    if (ok) {
+      // oddball masks: Nyquist of the old grid (upscaling) / new grid (downscaling)
+      if (zero_old_nyq) {
+        const int wy = ky;
+        const int wx = (D == 2) ? (sx <= n_old / 2 - 1 ? sx : sx - n_old) : 0;
+        if (wy >= n_old / 2 || (D == 2 && (wx >= n_old / 2 || wx <= -n_old / 2))) ok = false;
+      }
+      if (zero_new_nyq) {
+        const int wy = ky;
+        const int wx = (D == 2) ? (kx <= n_new / 2 - 1 ? kx : kx - n_new) : 0;
+        if (wy >= n_new / 2 || (D == 2 && (wx >= n_new / 2 || wx <= -n_new / 2))) ok = false;
+      }
+    }
+    if (ok) v = cscale(in[c * per_old + (int64_t)sx * Mo + ky], scale);
+    out[t] = v;
+  }
+}
+
+}  // namespace exgb
+
+using namespace exgb;
+
+extern "C" {
+
+int exgb_rfftn(void* stream, int num_spatial_dims, int num_points, int64_t count, const float* in, void* out) {
+  if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
+  if (count < 0) return fail(EXGB_EINVAL, "negative count");
+  return rfftn_impl((cudaStream_t)stream, num_spatial_dims, num_points, count, in, (float2*)out);
+}
+
+int exgb_irfftn(void* stream, int num_spatial_dims, int num_points, int64_t count, const void* in, float* out) {
+  if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
+  if (count < 0) return fail(EXGB_EINVAL, "negative count");
+  return irfftn_impl((cudaStream_t)stream, num_spatial_dims, num_points, count, (const float2*)in, out);
+}
+
+int exgb_map_between_resolutions(void* stream, int D, int n_old, int n_new, int64_t count, const float* in,
+                                 float* out, int oddball_zero) {
+  if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
+  if (D < 1 || D > 2) return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1 or 2 in this build");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n_old == n_new) {
+    size_t bytes = sizeof(float) * (size_t)count * n_old * (D == 2 ? n_old : 1);
+    EXGB_CUDA(cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, st));
+    return EXGB_OK;
+  }
+  const int Mo = n_old / 2 + 1, Mn = n_new / 2 + 1;
+  const size_t so = (size_t)count * Mo * (D == 2 ? n_old : 1);
+  const size_t sn = (size_t)count * Mn * (D == 2 ? n_new : 1);
+  // slot 1 holds the old spectrum and later the 2D inverse intermediate
+  float2* a = (float2*)workspace(sizeof(float2) * std::max(so, sn), 1);
+  if (!a) return fail(EXGB_ENOMEM, "workspace allocation failed");
+  int rc = rfftn_impl(st, D, n_old, count, in, a);
+  if (rc) return rc;
+  // the new spectrum must not overlap `a`: place it in slot 0
+  float2* b = (float2*)workspace(sizeof(float2) * std::max(sn, (size_t)count * n_new * Mn), 0);
+  if (!b) return fail(EXGB_ENOMEM, "workspace allocation failed");
+  const double ratio = (double)n_new / (double)n_old;
+  const float scale = (float)(D == 2 ? ratio * ratio : ratio);
+  const int zo = (n_new > n_old) && (n_old % 2 == 0) && oddball_zero;
+  const int zn = (n_old > n_new) && (n_new % 2 == 0) && oddball_zero;
+  const int64_t total = (int64_t)sn;
+  const int th = 256;
+  const unsigned blocks = (unsigned)std::min<int64_t>((total + th - 1) / th, 65535);
+  resample_kernel<<<blocks, th, 0, st>>>(D, n_old, n_new, count, a, b, scale, zo, zn);
+  EXGB_CUDA(cudaGetLastError());
+  const FftPlan* fp;
+  const float2* tw;
+  rc = get_tf(n_new, &fp, &tw);
+  if (rc) return rc;
+  if (D == 1) return launch_irfft1d(st, *fp, tw, count, b, out, 1.f / (float)n_new);
+  // 2D inverse: the column pass writes into slot 1 (the old spectrum is no longer needed)
+  float2* tmp = a;
+  rc = launch_cfft_axis(st, *fp, tw, true, count, (int64_t)n_new * Mn, Mn, Mn, b, tmp, 1.f);
+  if (rc) return rc;
+  return launch_irfft1d(st, *fp, tw, count * n_new, tmp, out, 1.f / ((float)n_new * (float)n_new));
+}
+
+}  // extern "C"

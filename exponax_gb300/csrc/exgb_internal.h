@@ -1,0 +1,108 @@
+// exgb_internal.h -- plan object and helpers shared by the .cu files of
+// libexgb.so.  Not part of the public ABI (include/exgb.h is).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/exgb.h"
+#include "exgb_fft.cuh"
+
+namespace exgb {
+
+// Device-visible, trivially copyable description of a plan.  Kernels get it
+// by value (2D) or from a device array (1D work queue).
+struct PlanDev {
+  int D, N, M, C, order, kind;
+  int kmax;        // largest |k| kept by the dealiasing mask on every axis
+  int lin_ch;      // 1 or C coefficient sets
+  FftPlan fft;     // length-N complex FFT
+  const float2* tw;  // N twiddles exp(-2 pi i k / N)
+  // Coefficient tables.  1D: [lin_ch][M].  2D: [lin_ch][ky][kx] (ky-major).
+  const float2* E;
+  const float2* Eh;
+  const float* c[6];
+  float kscale;      // 2 pi / L (float32, as the reference's scaled wavenumbers)
+  // 1D pseudo-spectral form of every 1D nonlinearity:
+  //   N^ = mask . ( alpha ik F[u^2] + F[ beta u u_x + gamma (u_x^2 - zmf*mean) + sum_k poly_k u^k ] )
+  float alpha, beta, gamma;
+  int zero_mode_fix;
+  int npoly;
+  float poly[8];
+  int needs_ux;      // beta != 0 || gamma != 0
+  int needs_q;       // beta, gamma or poly present
+  // 2D vorticity
+  float conv_scale;  // b (the kernel applies -b)
+  float inj_value;   // -k gamma * coef_extraction scaling at (0, k)
+  int inj_mode;      // -1: none
+};
+
+struct Plan2DConfig {
+  int G;        // CTAs per sample (cluster size)
+  int threads;  // threads per CTA
+  int cols_per_cta;   // masked columns owned by one CTA (max)
+  int rows_per_cta;   // physical rows owned by one CTA
+  int CB;       // columns per column-phase batch
+  int RB;       // rows per row-phase batch (even)
+  int mixed_in_smem;
+  size_t smem_bytes;
+  int clusters;       // persistent clusters launched
+  size_t scratch_per_cluster;  // bytes of global scratch per cluster
+};
+
+}  // namespace exgb
+
+struct exgb_plan {
+  exgb_plan_desc desc;
+  exgb::PlanDev dev;
+  exgb::PlanDev* d_dev = nullptr;  // device copy (for the work queue)
+  // owned device allocations
+  float2* d_tw = nullptr;
+  float2* d_E = nullptr;
+  float2* d_Eh = nullptr;
+  float* d_c = nullptr;  // 6 contiguous tables
+  size_t n_modes = 0;    // modes per coefficient set
+  // 2D
+  exgb::Plan2DConfig cfg2d{};
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  int sm_count = 0;
+};
+
+namespace exgb {
+
+// thread-local last error
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define EXGB_CUDA(call)                                   \
+  do {                                                    \
+    cudaError_t _e = (call);                              \
+    if (_e != cudaSuccess) return exgb::cuda_fail(_e, #call); \
+  } while (0)
+
+bool make_fft_plan(int n, FftPlan* p);
+int build_twiddles(int n, float2** d_tw);
+
+// launchers (defined in the kernel .cu files)
+int launch_rfft1d(cudaStream_t st, const exgb::FftPlan& fp, const float2* tw, int64_t rows, const float* in,
+                  float2* out);
+int launch_irfft1d(cudaStream_t st, const exgb::FftPlan& fp, const float2* tw, int64_t rows, const float2* in,
+                   float* out, float scale);
+int launch_cfft_axis(cudaStream_t st, const exgb::FftPlan& fp, const float2* tw, bool inverse, int64_t outer,
+                     int64_t outer_stride, int64_t inner, int64_t elem_stride, const float2* in, float2* out,
+                     float scale);
+
+int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, const float2* u0_hat,
+                float* out_phys, float2* out_hat, int64_t batch, int nsteps, int project, int emit_traj,
+                int include_init, int nonlinear_only);
+int etdrk2d_run(const exgb_plan* plan, cudaStream_t st, const float2* u_hat_in, float2* u_hat_out, int64_t batch,
+                int nsteps, int project, int nonlinear_only);
+int etdrk2d_configure(exgb_plan* plan);
+int etdrk0_apply(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
+                 int project);
+
+}  // namespace exgb

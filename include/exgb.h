@@ -1,0 +1,166 @@
+/*
+ * exgb.h -- C ABI of libexgb.so, the GB300 (sm_103a) ETDRK pseudo-spectral
+ * stepping library.
+ *
+ * Plain C types only: device pointers are `void*`/`float*` to CUDA global
+ * memory, streams are `cudaStream_t` passed as `void*` (NULL = legacy default
+ * stream).  Every call returns 0 on success or a negative EXGB_E* code; the
+ * message of the last failure on the calling thread is exgb_last_error().
+ * No C++ exception crosses this boundary.
+ *
+ * Data layout (C-contiguous, batch first, as jax.vmap over the reference
+ * functions produces):
+ *   physical field   float32   (B, C, N, ..., N)
+ *   Fourier field    complex64 (B, C, N, ..., N/2+1), interleaved re/im
+ *   trajectory       float32   (B, T, C, N, ..., N)
+ * `in` and `out` may alias for the step functions.
+ *
+ * Each entry point names the exponax 0.2.0 function it replaces
+ * (paths inside the exponax project).
+ */
+#ifndef EXGB_H
+#define EXGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EXGB_VERSION 1
+
+/* status codes */
+#define EXGB_OK 0
+#define EXGB_EINVAL (-1)          /* bad argument (NULL pointer, bad enum) */
+#define EXGB_ESHAPE (-2)          /* shape / channel / dimension mismatch */
+#define EXGB_ENOTFACTORABLE (-3)  /* N has a prime factor other than 2, 3, 5 */
+#define EXGB_ECUDA (-4)           /* a CUDA runtime call failed */
+#define EXGB_ETIMEOUT (-5)        /* a bounded device wait gave up */
+#define EXGB_EGUARD (-6)          /* spectral-energy / non-finite guard tripped */
+#define EXGB_ENOMEM (-7)          /* device allocation failed */
+#define EXGB_EUNSUPPORTED (-8)    /* valid for the reference, not built here */
+#define EXGB_ENOTIMPL (-9)        /* ETDRK order outside 0..4 */
+
+/* nonlinear function kinds (exponax/nonlin_fun/*) */
+#define EXGB_NL_ZERO 0               /* ZeroNonlinearFun            _zero.py:7-38 */
+#define EXGB_NL_CONVECTION 1         /* ConvectionNonlinearFun      _convection.py:7-245 */
+#define EXGB_NL_GRADIENT_NORM 2      /* GradientNormNonlinearFun    _gradient_norm.py:8-101 */
+#define EXGB_NL_POLYNOMIAL 3         /* PolynomialNonlinearFun      _polynomial.py:6-76 */
+#define EXGB_NL_GENERAL 4            /* GeneralNonlinearFun         _general_nonlinear.py:9-119 */
+#define EXGB_NL_VORTICITY_2D 5       /* VorticityConvection2d       _vorticity_convection.py:8-99 */
+#define EXGB_NL_VORTICITY_2D_KOLMOGOROV 6 /* VorticityConvection2dKolmogorov :102-182 */
+
+typedef struct exgb_plan exgb_plan;
+
+/* Everything BaseStepper.__init__ (_base_stepper.py:27-157) decides:
+ * the linear operator L (already assembled by the stepper class on the host,
+ * complex128), the ETDRK order and contour parameters, and the nonlinear
+ * function with its scalar parameters. */
+typedef struct {
+  int32_t num_spatial_dims;        /* D: 1 or 2 */
+  int32_t num_points;              /* N (2^a 3^b 5^c) */
+  int32_t num_channels;            /* C */
+  int32_t order;                   /* ETDRK order 0..4 */
+  double domain_extent;            /* L */
+  double dt;
+  const double* linear_operator;   /* host, complex128 interleaved, (lin_ch, N..., N/2+1) */
+  int32_t linear_operator_channels;/* 1 (broadcast) or C */
+  int32_t num_circle_points;       /* contour points, reference default 16 */
+  double circle_radius;            /* reference default 1.0 */
+  int32_t nonlin_kind;             /* EXGB_NL_* */
+  double dealiasing_fraction;      /* < 0: no dealiasing mask */
+  double scale;                    /* b of convection / gradient norm / vorticity */
+  int32_t single_channel;          /* ConvectionNonlinearFun.single_channel */
+  int32_t conservative;            /* ConvectionNonlinearFun.conservative */
+  int32_t zero_mode_fix;           /* GradientNorm / General */
+  double scale_list[3];            /* GeneralNonlinearFun.scale_list */
+  int32_t num_poly;                /* PolynomialNonlinearFun: number of coefficients (<= 8) */
+  double poly[8];
+  int32_t injection_mode;          /* Kolmogorov forcing mode k */
+  double injection_scale;          /* Kolmogorov forcing amplitude */
+} exgb_plan_desc;
+
+/* One instance of an uneven batch (exgb_queue_rollout). */
+typedef struct {
+  const exgb_plan* plan;   /* 1D plan of this instance */
+  const float* u0;         /* device, (C, N) */
+  float* traj;             /* device, (T, C, N), T = nsteps + include_init */
+} exgb_work_item;
+
+/* ---- library ---- */
+int exgb_version(void);
+const char* exgb_last_error(void);
+/* Number of SMs / compute capability of the current device (for tests). */
+int exgb_device_info(int* sm_count, int* cc_major, int* cc_minor);
+
+/* ---- plans ----
+ * exgb_plan_create replaces BaseStepper.__init__ (_base_stepper.py:27-157)
+ * together with the coefficient set-up of ETDRK0..4
+ * (etdrk/_base_etdrk.py:19-62, _etdrk_1.py:63-76, _etdrk_2.py:71-89,
+ * _etdrk_3.py:154-189, _etdrk_4.py:168-196): E = exp(dt L) and the
+ * phi-function contour means are evaluated in FP64 on the GPU and stored
+ * as FP32, real part only, as the reference does. */
+int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out);
+int exgb_plan_destroy(exgb_plan* plan);
+/* Copy the coefficient tables to host (for parity tests).  which: 0 = E,
+ * 1 = E_half (complex64, 2 floats per mode); 2..7 = coef_1..coef_6 (float32).
+ * Layout (lin_ch, N..., N/2+1), row-major like the reference arrays. */
+int exgb_plan_get_table(const exgb_plan* plan, int which, void* host_out, size_t bytes);
+/* Largest dealiasing-mask wavenumber kept per axis (-1: no mask). */
+int exgb_plan_kmax(const exgb_plan* plan);
+
+/* ---- spectral transforms ----
+ * exgb_rfftn replaces spectral.fft  (_spectral.py:614-656): rfftn over the
+ *   last D axes, norm="backward".
+ * exgb_irfftn replaces spectral.ifft (_spectral.py:659-721): irfftn with
+ *   s=(N,)*D; imaginary parts of the c2r axis' DC/Nyquist bins are ignored
+ *   as numpy/pocketfft do.  `count` = B*C fields. */
+int exgb_rfftn(void* stream, int num_spatial_dims, int num_points, int64_t count,
+               const float* in, void* out);
+int exgb_irfftn(void* stream, int num_spatial_dims, int num_points, int64_t count,
+                const void* in, float* out);
+
+/* ---- stepping ----
+ * exgb_step_fourier replaces BaseStepper.step_fourier (_base_stepper.py:222-239)
+ *   = ETDRKn.step_fourier, vmapped over the batch.
+ * exgb_step replaces BaseStepper.__call__/step (_base_stepper.py:201-271).
+ * exgb_nonlinear replaces BaseNonlinearFun.__call__ of the plan's
+ *   nonlinear function (nonlin_fun/*), vmapped. */
+int exgb_step_fourier(const exgb_plan* plan, void* stream, const void* u_hat_in, void* u_hat_out,
+                      int64_t batch);
+int exgb_step(const exgb_plan* plan, void* stream, const float* u_in, float* u_out, int64_t batch);
+int exgb_nonlinear(const exgb_plan* plan, void* stream, const void* u_hat_in, void* n_hat_out,
+                   int64_t batch);
+
+/* exgb_repeat replaces _utils.repeat(stepper, n) (_utils.py:189-254): n
+ *   steps, each through physical space (the c2r projection is applied after
+ *   every step), final state only.
+ * exgb_repeat_fourier replaces RepeatedStepper.step_fourier
+ *   (_repeated_stepper.py:85-102): n steps kept in Fourier space.
+ * exgb_rollout replaces _utils.rollout(stepper, n, include_init)
+ *   (_utils.py:92-186): trajectory (B, n + include_init, C, N...). */
+int exgb_repeat(const exgb_plan* plan, void* stream, const float* u0, float* u_out, int64_t batch,
+                int32_t nsteps);
+int exgb_repeat_fourier(const exgb_plan* plan, void* stream, const void* u_hat0, void* u_hat_out,
+                        int64_t batch, int32_t nsteps);
+int exgb_rollout(const exgb_plan* plan, void* stream, const float* u0, float* traj, int64_t batch,
+                 int32_t nsteps, int32_t include_init);
+
+/* Uneven batch in one persistent launch: instances of different 1D plans
+ * (PDE, N, dt) share a device work queue.  No reference counterpart: the
+ * reference runs one jax.vmap(rollout) per (PDE, N) group in sequence
+ * (_utils.py:92-186 under jax.vmap).  Items are scheduled longest-first. */
+int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, int32_t nsteps,
+                       int32_t include_init, void* stream);
+
+/* map_between_resolutions (_interpolation.py:195-285) for D = 1, 2:
+ * spectral re-sampling of count = B*C fields from N_old to N_new points. */
+int exgb_map_between_resolutions(void* stream, int num_spatial_dims, int n_old, int n_new,
+                                 int64_t count, const float* in, float* out, int oddball_zero);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EXGB_H */

@@ -1,0 +1,319 @@
+"""Parity of the CUDA path (through the C ABI) with the NumPy oracle.
+
+Tolerances follow the target: FP32 results within 1e-5 relative L2 per
+step; 1e-4 after 100 steps on non-chaotic cases; 1e-4 over at most 20 steps
+on chaotic cases.  Every test states its tolerance."""
+
+import numpy as np
+import pytest
+
+import exponax_gb300 as ex
+from oracle import exponax_np as o
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def cu(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+# ------------------------------------------------------------------ transforms
+
+@pytest.mark.parametrize("D,N", [(1, 200), (1, 256), (1, 60), (1, 4096), (1, 45), (2, 60), (2, 64), (2, 128),
+                                 (2, 256)])
+def test_rfftn_irfftn_match_numpy(D, N):
+    rng = np.random.default_rng(N + D)
+    u = rng.standard_normal((3, 1) + (N,) * D).astype(np.float32)
+    uh = host(ex.fft(cu(u), num_spatial_dims=D))
+    ref = np.fft.rfftn(u.astype(np.float64), axes=tuple(range(-D, 0)))
+    assert rel(uh.view(np.float32), ref.astype(np.complex64).view(np.float32)) < 2e-6
+    # irfftn on non-Hermitian input: numpy drops Im of the c2r DC/Nyquist bins
+    z = (rng.standard_normal(ref.shape) + 1j * rng.standard_normal(ref.shape)).astype(np.complex64)
+    back = host(ex.ifft(cu(z), num_spatial_dims=D, num_points=N))
+    refb = np.fft.irfftn(z.astype(np.complex128), s=(N,) * D, axes=tuple(range(-D, 0)))
+    assert rel(back, refb) < 2e-6
+
+
+def test_fft_ifft_roundtrip_abs_1e5():
+    """tests/test_spectral.py:19-31 on the GPU (abs 1e-5)."""
+    u = np.random.default_rng(0).standard_normal((1, 32, 32)).astype(np.float32)
+    back = host(ex.ifft(ex.fft(cu(u))))
+    assert np.max(np.abs(back - u)) < 1e-5
+
+
+# ------------------------------------------------------------------ coefficients
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+@pytest.mark.parametrize("case", ["ks", "kdv", "ns"])
+def test_phi_coefficients_match_fp64_oracle(order, case):
+    if case == "ks":
+        args, mk, mo = (1, 100.0, 200, 0.1), ex.stepper.KuramotoSivashinskyConservative, o.KuramotoSivashinskyConservative
+        kw = {}
+    elif case == "kdv":
+        args, mk, mo = (1, 20.0, 256, 0.01), ex.stepper.KortewegDeVries, o.KortewegDeVries
+        kw = {}
+    else:
+        args, mk, mo = (2, 2 * np.pi, 64, 0.01), ex.stepper.NavierStokesVorticity, o.NavierStokesVorticity
+        kw = {"diffusivity": 1e-3}
+    mine = mk(*args, order=order, **kw)._integrator
+    ref = mo(*args, order=order, dtype="float64", **kw)._integrator
+    np.testing.assert_allclose(mine._exp_term, ref._exp_term, rtol=1e-6, atol=1e-7)
+    names = {1: [1], 2: [1, 2], 3: [1, 2, 3, 4, 5], 4: [1, 2, 3, 4, 5, 6]}[order]
+    for i in names:
+        a = getattr(mine, f"_coef_{i}")
+        b = getattr(ref, f"_coef_{i}")
+        np.testing.assert_allclose(a, b, rtol=2e-6, atol=1e-12 + 1e-6 * np.abs(b).max())
+
+
+# ------------------------------------------------------------------ nonlinear functions
+
+NL_CASES_1D = [
+    ("conv_cons", dict(cls="ConvectionNonlinearFun", kw=dict(scale=1.0, single_channel=True, conservative=True))),
+    ("conv_noncons", dict(cls="ConvectionNonlinearFun", kw=dict(scale=-6.0, single_channel=False, conservative=False))),
+    ("grad_norm", dict(cls="GradientNormNonlinearFun", kw=dict(scale=1.0, zero_mode_fix=True))),
+    ("poly", dict(cls="PolynomialNonlinearFun", kw=dict(coefficients=(0.3, -1.0, 0.5, 2.0)))),
+    ("general", dict(cls="GeneralNonlinearFun", kw=dict(scale_list=(0.5, -1.2, 0.7)))),
+]
+
+
+@pytest.mark.parametrize("name,case", NL_CASES_1D, ids=[c[0] for c in NL_CASES_1D])
+@pytest.mark.parametrize("N", [64, 200])
+def test_nonlinear_fun_1d_matches_oracle(name, case, N):
+    L = 30.0
+    kw = dict(case["kw"])
+    dm = ex.spectral.build_derivative_operator(1, L, N)
+    do = o.build_derivative_operator(1, L, N)
+    if case["cls"] != "PolynomialNonlinearFun":
+        kw_m = dict(kw, derivative_operator=dm)
+        kw_o = dict(kw, derivative_operator=do)
+    else:
+        kw_m, kw_o = dict(kw), dict(kw)
+    fm = getattr(ex.nonlin_fun, case["cls"])(1, N, dealiasing_fraction=2 / 3, **kw_m)
+    fo = getattr(o, case["cls"])(1, N, dealiasing_fraction=2 / 3, **kw_o)
+    u = ex.ic.RandomSineWaves1d(1, cutoff=5)(N, key=1)
+    uh = o.fft(u)
+    got = host(fm(cu(uh)))
+    want = fo(uh)
+    assert rel(got.view(np.float32), want.astype(np.complex64).view(np.float32)) < 1e-5
+
+
+@pytest.mark.parametrize("N", [60, 64, 128, 256])
+@pytest.mark.parametrize("kolmogorov", [False, True])
+def test_vorticity_nonlinearity_matches_oracle(N, kolmogorov):
+    L = 2 * np.pi
+    if kolmogorov:
+        fm = ex.nonlin_fun.VorticityConvection2dKolmogorov(2, N, derivative_operator=ex.spectral.build_derivative_operator(2, L, N), dealiasing_fraction=2 / 3)
+        fo = o.VorticityConvection2dKolmogorov(2, N, derivative_operator=o.build_derivative_operator(2, L, N), dealiasing_fraction=2 / 3)
+    else:
+        fm = ex.nonlin_fun.VorticityConvection2d(2, N, derivative_operator=ex.spectral.build_derivative_operator(2, L, N), dealiasing_fraction=2 / 3)
+        fo = o.VorticityConvection2d(2, N, derivative_operator=o.build_derivative_operator(2, L, N), dealiasing_fraction=2 / 3)
+    u = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)(N, key=2)
+    uh = o.fft(u)
+    got = host(fm(cu(uh)))
+    want = fo(uh)
+    assert rel(got.view(np.float32), want.astype(np.complex64).view(np.float32)) < 1e-5
+
+
+# ------------------------------------------------------------------ single steps
+
+STEP_CASES = [
+    ("ks_cons_200", "KuramotoSivashinskyConservative", (1, 100.0, 200, 0.1), {}),
+    ("ks_128", "KuramotoSivashinsky", (1, 60.0, 128, 0.1), {}),
+    ("burgers_256", "Burgers", (1, 1.0, 256, 1e-3), {"diffusivity": 0.01}),
+    ("kdv_512", "KortewegDeVries", (1, 20.0, 512, 0.01), {}),
+    ("burgers_4096", "Burgers", (1, 1.0, 4096, 1e-3), {"diffusivity": 0.01}),
+    ("ns_64", "NavierStokesVorticity", (2, 2 * np.pi, 64, 0.01), {"diffusivity": 1e-3}),
+    ("ns_256", "NavierStokesVorticity", (2, 2 * np.pi, 256, 0.01), {"diffusivity": 1e-3}),
+    ("kolmo_128", "KolmogorovFlowVorticity", (2, 2 * np.pi, 128, 0.01), {}),
+    ("diffusion_2d", "Diffusion", (2, 1.0, 48, 0.05), {"diffusivity": 0.02}),
+    ("advection_1d", "Advection", (1, 1.0, 64, 0.05), {"velocity": 0.7}),
+]
+
+
+def _ic(D, N, key):
+    if D == 1:
+        return ex.ic.RandomSineWaves1d(1, cutoff=5)(N, key=key)
+    return ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)(N, key=key)
+
+
+@pytest.mark.parametrize("name,cls,args,kw", STEP_CASES, ids=[c[0] for c in STEP_CASES])
+@pytest.mark.parametrize("order", [2, 1, 3, 4])
+def test_single_step_matches_oracle(name, cls, args, kw, order):
+    if cls in ("Diffusion", "Advection"):
+        if order != 2:
+            pytest.skip("linear steppers are ETDRK0")
+        sm = getattr(ex.stepper, cls)(*args, **kw)
+        so = getattr(o, cls)(*args, **kw)
+    else:
+        sm = getattr(ex.stepper, cls)(*args, order=order, **kw)
+        so = getattr(o, cls)(*args, order=order, **kw)
+    D, N = args[0], args[2]
+    B = 3
+    u = np.stack([_ic(D, N, k) for k in range(B)])
+    got = host(ex.vmap(sm)(cu(u)))
+    for b in range(B):
+        assert rel(got[b], so(u[b])) < 1e-5, b
+    # single-sample __call__ path and its shape check
+    np.testing.assert_allclose(host(sm(cu(u[0]))), got[0], rtol=0, atol=1e-6)
+    with pytest.raises(ValueError):
+        sm(cu(u))
+
+
+@pytest.mark.parametrize("name,cls,args,kw", STEP_CASES[:8], ids=[c[0] for c in STEP_CASES[:8]])
+def test_step_fourier_matches_oracle(name, cls, args, kw):
+    sm = getattr(ex.stepper, cls)(*args, **kw)
+    so = getattr(o, cls)(*args, **kw)
+    D, N = args[0], args[2]
+    uh = o.fft(_ic(D, N, 5))
+    got = host(sm.step_fourier(cu(uh)))
+    want = so.step_fourier(uh)
+    assert rel(got.view(np.float32), want.astype(np.complex64).view(np.float32)) < 1e-5
+
+
+# ------------------------------------------------------------------ multi-step
+
+def test_ks_conservative_config_rollout():
+    """Config: KS-conservative 1D, L=100, N=200, dt=0.1, batch 16 (seeds
+    0..15), 500-step rollout with include_init.  Chaotic: within 1e-4
+    relative L2 of the oracle over the first 20 steps; the long-run energy
+    spectra (time-averaged over steps 300..500) agree within 5 %."""
+    B, N, n = 16, 200, 500
+    sm = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, N, 0.1)
+    so = o.KuramotoSivashinskyConservative(1, 100.0, N, 0.1)
+    u0 = np.stack([ex.ic.RandomSineWaves1d(1, cutoff=5)(N, key=s) for s in range(B)])
+    traj = host(ex.vmap(ex.rollout(sm, n, include_init=True))(cu(u0)))
+    assert traj.shape == (B, n + 1, 1, N)
+    np.testing.assert_array_equal(traj[:, 0], u0)
+    spec_m, spec_o = 0, 0
+    for b in range(4):
+        ref = o.rollout(so, n, include_init=True)(u0[b])
+        for t in range(1, 21):
+            assert rel(traj[b, t], ref[t]) < 1e-4, (b, t)
+        spec_m = spec_m + np.mean([o.get_spectrum(traj[b, t]) for t in range(300, 501)], axis=0)
+        spec_o = spec_o + np.mean([o.get_spectrum(ref[t]) for t in range(300, 501)], axis=0)
+    k = slice(1, 40)
+    assert np.max(np.abs(np.log(spec_m[0, k] / spec_o[0, k]))) < np.log(1.05) + 0.25
+    assert rel(spec_m[0, k], spec_o[0, k]) < 0.05
+
+
+def test_burgers_100_steps_non_chaotic():
+    """Non-chaotic: 1e-4 relative L2 after 100 steps."""
+    sm = ex.stepper.Burgers(1, 1.0, 256, 1e-3, diffusivity=0.01)
+    so = o.Burgers(1, 1.0, 256, 1e-3, diffusivity=0.01)
+    u0 = np.stack([ex.ic.RandomSineWaves1d(1, cutoff=5)(256, key=s) for s in range(4)])
+    got = host(ex.vmap(ex.repeat(sm, 100))(cu(u0)))
+    for b in range(4):
+        assert rel(got[b], o.repeat(so, 100)(u0[b])) < 1e-4
+
+
+def test_kdv_repeat_with_complex_linear_operator():
+    """KdV (odd-order L: complex Nyquist bin) 100 steps, 1e-4."""
+    sm = ex.stepper.KortewegDeVries(1, 20.0, 256, 0.01)
+    so = o.KortewegDeVries(1, 20.0, 256, 0.01)
+    u0 = ex.ic.RandomSineWaves1d(1, cutoff=5)(256, key=7)
+    got = host(ex.repeat(sm, 100)(cu(u0)))
+    assert rel(got, o.repeat(so, 100)(u0)) < 1e-4
+
+
+def test_taylor_green_matches_published_errors():
+    """validation/validate_taylor_green.ipynb: N=60, nu=0.1, dt=0.01;
+    published FP32 errors 1.85e-7 / 1.07e-6 / 1.00e-5 after 1/10/100 steps.
+    Allow 3x (FFT rounding differs between backends)."""
+    N, nu, dt = 60, 0.1, 0.01
+    g = ex.make_grid(2, 2 * np.pi, N)
+    sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, N, dt, diffusivity=nu)
+
+    def tg(t):
+        return (2 * np.sin(g[0:1]) * np.sin(g[1:2]) * np.exp(-2 * nu * t)).astype(np.float32)
+
+    for n, pub in ((1, 1.85e-7), (10, 1.07e-6), (100, 1.00e-5)):
+        e = rel(host(ex.repeat(sm, n)(cu(tg(0.0)))), tg(n * dt))
+        assert e < 3 * pub, (n, e)
+
+
+def test_ns_256_config_short_rollout():
+    """Config: NS vorticity 256^2, nu=1e-3, dt=0.01 (batch 4 here): within
+    1e-5 per step and 1e-4 after 20 steps (repeat and rollout paths)."""
+    N = 256
+    sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, N, 0.01, diffusivity=1e-3)
+    so = o.NavierStokesVorticity(2, 2 * np.pi, N, 0.01, diffusivity=1e-3)
+    u0 = np.stack([_ic(2, N, s) for s in range(4)])
+    fin = host(ex.vmap(ex.repeat(sm, 20))(cu(u0)))
+    traj = host(ex.vmap(ex.rollout(sm, 5, include_init=False))(cu(u0[:2])))
+    for b in range(2):
+        ref = o.rollout(so, 20)(u0[b])
+        assert rel(fin[b], ref[-1]) < 1e-4
+        for t in range(5):
+            assert rel(traj[b, t], ref[t]) < 1e-5 * (t + 1)
+
+
+def test_repeated_stepper_stays_in_fourier_space():
+    sm = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.01)
+    so = o.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.01)
+    u0 = _ic(2, 64, 3)
+    got = host(ex.RepeatedStepper(sm, 10)(cu(u0)))
+    assert rel(got, o.RepeatedStepper(so, 10)(u0)) < 1e-4
+
+
+def test_queue_rollout_mixed_pdes_and_sizes():
+    """Uneven batch in one persistent launch: Burgers / KdV / KS-cons with
+    different N; each instance matches its own oracle rollout (20 steps)."""
+    import ctypes
+
+    from exponax_gb300 import _device, _lib
+
+    specs = [
+        (ex.stepper.Burgers(1, 1.0, 128, 1e-3, diffusivity=0.01), o.Burgers(1, 1.0, 128, 1e-3, diffusivity=0.01)),
+        (ex.stepper.KortewegDeVries(1, 20.0, 512, 0.01), o.KortewegDeVries(1, 20.0, 512, 0.01)),
+        (ex.stepper.KuramotoSivashinskyConservative(1, 100.0, 256, 0.1),
+         o.KuramotoSivashinskyConservative(1, 100.0, 256, 0.1)),
+        (ex.stepper.Burgers(1, 1.0, 2048, 1e-3, diffusivity=0.01), o.Burgers(1, 1.0, 2048, 1e-3, diffusivity=0.01)),
+    ]
+    n = 20
+    rng = np.random.default_rng(0)
+    order = rng.integers(0, len(specs), size=12)
+    u0s, trajs, items = [], [], []
+    for i, s in enumerate(order):
+        sm, _ = specs[s]
+        u0 = cu(_ic(1, sm.num_points, i))
+        tr = torch.empty((n + 1, 1, sm.num_points), dtype=torch.float32, device="cuda")
+        u0s.append(u0)
+        trajs.append(tr)
+        items.append(_lib.WorkItem(sm.plan.handle.value, u0.data_ptr(), tr.data_ptr()))
+    arr = (_lib.WorkItem * len(items))(*items)
+    _lib.check(_lib.load().exgb_queue_rollout(arr, len(items), n, 1, _device.stream()))
+    torch.cuda.synchronize()
+    for i, s in enumerate(order):
+        ref = o.rollout(specs[s][1], n, include_init=True)(host(u0s[i]))
+        got = host(trajs[i])
+        assert rel(got[1:], ref[1:]) < 1e-4, (i, s)
+
+
+def test_map_between_resolutions_matches_oracle():
+    u = _ic(2, 256, 9)
+    for new in (64, 128, 512):
+        got = host(ex.map_between_resolutions(cu(u), new))
+        assert rel(got, o.map_between_resolutions(u, new)) < 1e-5
+    u1 = _ic(1, 200, 2)
+    assert rel(host(ex.map_between_resolutions(cu(u1), 50)), o.map_between_resolutions(u1, 50)) < 1e-5
+
+
+def test_errors_follow_the_reference():
+    sm = ex.stepper.Burgers(1, 1.0, 64, 0.01)
+    with pytest.raises(ValueError):
+        sm(cu(np.zeros((2, 64), np.float32)))
+    bad = ex.stepper.Burgers(1, 1.0, 14, 0.01)  # 14 = 2 * 7 cannot be planned
+    with pytest.raises(ValueError):
+        bad(cu(np.zeros((1, 14), np.float32)))
