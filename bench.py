@@ -174,8 +174,6 @@ def run_reference(args, rank, ws):
 
 
 def run_gb300(args, rank, ws):
-    import ctypes
-
     import torch
 
     import exponax_gb300 as ex
@@ -191,7 +189,7 @@ def run_gb300(args, rank, ws):
 
     u0_host = make_ics(rank * BATCH, BATCH)  # this rank's shard of seeds
     u0 = torch.from_numpy(u0_host).cuda()
-    uh0 = ex.fft(u0)
+    uh0 = ex.fft(u0, num_spatial_dims=2)
     out_h = torch.empty_like(uh0)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 

@@ -1,0 +1,60 @@
+"""Run one stepping workload for profiling (e.g. under ncu).
+
+    python -m exponax_gb300.profile_case --dims 2 --n 256 --batch 32 --steps 10 --reps 3
+
+Builds the stepper (NavierStokesVorticity in 2D, KuramotoSivashinsky-
+Conservative in 1D), creates device-resident Fourier states and launches
+``repeat_fourier`` --reps times (one fused-kernel launch each), then
+synchronises.  Prints the CUDA-event time per launch.
+"""
+
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--dims", type=int, default=2)
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--order", type=int, default=2)
+    ap.add_argument("--kolmogorov", action="store_true")
+    a = ap.parse_args()
+
+    import torch
+
+    import exponax_gb300 as ex
+    from exponax_gb300 import _device, _lib
+
+    if a.dims == 2:
+        cls = ex.stepper.KolmogorovFlowVorticity if a.kolmogorov else ex.stepper.NavierStokesVorticity
+        kw = {} if a.kolmogorov else {"diffusivity": 1e-3}
+        st = cls(2, 2 * np.pi, a.n, 0.01, order=a.order, **kw)
+        g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    else:
+        st = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, a.n, 0.1, order=a.order)
+        g = ex.ic.RandomSineWaves1d(1, cutoff=5)
+    u0 = torch.from_numpy(np.stack([g(a.n, key=s) for s in range(a.batch)])).cuda()
+    uh = ex.fft(u0, num_spatial_dims=a.dims)
+    out = torch.empty_like(uh)
+    lib = _lib.load()
+    h = st.plan.handle
+    for _ in range(a.reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.check(lib.exgb_repeat_fourier(h, _device.stream(), uh.data_ptr(), out.data_ptr(), a.batch, a.steps))
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        dofs = a.batch * a.n**a.dims * a.steps
+        print(f"repeat_fourier: {ms:.3f} ms, {dofs / ms * 1e3:.3e} DOF-steps/s")
+
+
+if __name__ == "__main__":
+    main()
