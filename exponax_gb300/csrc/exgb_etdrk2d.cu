@@ -33,6 +33,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 
 #include "exgb_internal.h"
 
@@ -444,6 +445,15 @@ __global__ void __launch_bounds__(512, 1) etdrk2d_kernel(const Args2D a) {
 int etdrk2d_configure(exgb_plan* plan) {
   PlanDev& P = plan->dev;
   Plan2DConfig& c = plan->cfg2d;
+  if (P.kmax < P.N / 2 && !getenv("EXGB_GENERIC_2D")) {
+    const int rc = vort2d_configure(plan);
+    if (rc == EXGB_OK) {
+      c.variant = 1;
+      return EXGB_OK;
+    }
+    if (rc != EXGB_EUNSUPPORTED) return rc;
+  }
+  c.variant = 0;
   const int N = P.N, M = P.M;
   const int K = std::min(P.kmax, N / 2);
   if (K < 0) return fail(EXGB_EUNSUPPORTED, "dealiasing mask removes every mode");
@@ -515,6 +525,7 @@ int etdrk2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2
                 int project, int nonlinear_only) {
   if (batch <= 0) return EXGB_OK;
   const Plan2DConfig& c = plan->cfg2d;
+  if (c.variant == 1) return vort2d_run(plan, st, in, out, batch, nsteps, project, nonlinear_only);
   Args2D a;
   a.P = plan->dev;
   a.G = c.G;

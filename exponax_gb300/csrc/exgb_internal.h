@@ -47,6 +47,7 @@ struct Plan2DConfig {
   int CB;       // columns per column-phase batch
   int RB;       // rows per row-phase batch (even)
   int mixed_in_smem;
+  int variant;   // 0: generic Stockham kernel, 1: register-FFT kernel (compile-time N)
   size_t smem_bytes;
   int clusters;       // persistent clusters launched
   size_t scratch_per_cluster;  // bytes of global scratch per cluster
@@ -102,6 +103,9 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
 int etdrk2d_run(const exgb_plan* plan, cudaStream_t st, const float2* u_hat_in, float2* u_hat_out, int64_t batch,
                 int nsteps, int project, int nonlinear_only);
 int etdrk2d_configure(exgb_plan* plan);
+int vort2d_configure(exgb_plan* plan);
+int vort2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
+               int project, int nonlinear_only);
 int etdrk0_apply(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                  int project);
 

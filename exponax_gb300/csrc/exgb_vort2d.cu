@@ -1,0 +1,518 @@
+// exgb_vort2d.cu -- register-FFT variant of the fused 2D vorticity ETDRK
+// kernel for N in {64, 128, 256} (compile-time N).
+//
+// Same algorithm and cluster decomposition as etdrk2d_kernel
+// (exgb_etdrk2d.cu; reference nonlin_fun/_vorticity_convection.py:78-99,
+// etdrk/_etdrk_1..4.py), but every length-N transform is a group FFT of T
+// lanes holding E points each (exgb_regfft.cuh): no block barrier inside a
+// transform, compile-time index arithmetic, one shared-memory transpose per
+// transform.  Lane l of a group always owns positions l + T j, so
+//   * column inverse:  derived spectrum (registers) -> IFFT -> mixed[f][x][c]
+//   * row phase:       gather over DSMEM -> 2 IFFTs -> product in registers
+//                      -> pair two rows with a warp shuffle -> 1 FFT -> prod
+//   * column forward:  gather prod over DSMEM -> FFT -> ETDRK stage update
+// run without any intermediate layout change.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "exgb_internal.h"
+#include "exgb_regfft.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace exgb {
+
+struct ArgsV2 {
+  PlanDev P;
+  int G, Cl, ClP, Rl, RlP, Kc, Ul;
+  const float2* in;
+  float2* out;
+  int64_t batch;
+  int nsteps;
+  int project;
+  int nonlinear_only;
+  float2* scratch;
+  int64_t scratch_stride;
+};
+
+template <int N, int THREADS>
+struct V2Layout {
+  static constexpr int E = RegCfg<N>::E, T = RegCfg<N>::T;
+  static constexpr int NG = THREADS / T;
+  static constexpr int TS = tile_stride<E, T>();
+  // float2 offsets
+  __host__ __device__ static size_t twl() { return 0; }
+  __host__ __device__ static size_t tiles() { return N; }
+  __host__ __device__ static size_t colbuf() { return tiles() + (size_t)NG * TS; }
+  __host__ __device__ static size_t prod(int Cl) { return colbuf() + (size_t)Cl * N; }
+  __host__ __device__ static size_t mixed(int Cl, int Kc, int RlP) { return prod(Cl) + (size_t)Kc * RlP; }
+  __host__ __device__ static size_t maps(int Cl, int ClP, int Kc, int RlP) { return mixed(Cl, Kc, RlP) + (size_t)4 * N * ClP; }
+  __host__ __device__ static size_t bytes(int Cl, int ClP, int Kc, int RlP) {
+    return sizeof(float2) * maps(Cl, ClP, Kc, RlP) + sizeof(int) * ((size_t)Kc + N);
+  }
+};
+
+struct StageBufs {
+  float2 *U, *S1, *S, *N0, *N1, *N2;
+};
+
+__device__ __forceinline__ float2 stage_upd(const PlanDev& P, const StageBufs& b, int64_t o, int stage, float2 nv) {
+  switch (P.order) {
+    case 1: {
+      const float2 r = cadd(cmul(__ldg(P.E + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
+      b.U[o] = r;
+      return r;
+    }
+    case 2:
+      if (stage == 0) {
+        const float2 s = cadd(cmul(__ldg(P.E + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
+        b.N0[o] = nv;
+        b.S[o] = s;
+        return s;
+      } else {
+        const float2 r = cadd(b.S[o], cscale(csub(nv, b.N0[o]), __ldg(P.c[1] + o)));
+        b.U[o] = r;
+        return r;
+      }
+    case 3:
+      if (stage == 0) {
+        const float2 s = cadd(cmul(__ldg(P.Eh + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
+        b.N0[o] = nv;
+        b.S[o] = s;
+        return s;
+      } else if (stage == 1) {
+        const float2 t = csub(cscale(nv, 2.f), b.N0[o]);
+        const float2 s = cadd(cmul(__ldg(P.E + o), b.U[o]), cscale(t, __ldg(P.c[1] + o)));
+        b.N1[o] = nv;
+        b.S[o] = s;
+        return s;
+      } else {
+        float2 r = cmul(__ldg(P.E + o), b.U[o]);
+        r = cadd(r, cscale(b.N0[o], __ldg(P.c[2] + o)));
+        r = cadd(r, cscale(b.N1[o], __ldg(P.c[3] + o)));
+        r = cadd(r, cscale(nv, __ldg(P.c[4] + o)));
+        b.U[o] = r;
+        return r;
+      }
+    default:
+      if (stage == 0) {
+        const float2 s = cadd(cmul(__ldg(P.Eh + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
+        b.N0[o] = nv;
+        b.S1[o] = s;
+        return s;
+      } else if (stage == 1) {
+        const float2 s = cadd(cmul(__ldg(P.Eh + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
+        b.N1[o] = nv;
+        b.S[o] = s;
+        return s;
+      } else if (stage == 2) {
+        const float2 t = csub(cscale(nv, 2.f), b.N0[o]);
+        const float2 s = cadd(cmul(__ldg(P.Eh + o), b.S1[o]), cscale(t, __ldg(P.c[0] + o)));
+        b.N2[o] = nv;
+        b.S[o] = s;
+        return s;
+      } else {
+        float2 r = cmul(__ldg(P.E + o), b.U[o]);
+        r = cadd(r, cscale(b.N0[o], __ldg(P.c[3] + o)));
+        r = cadd(r, cscale(cadd(b.N1[o], b.N2[o]), 2.f * __ldg(P.c[4] + o)));
+        r = cadd(r, cscale(nv, __ldg(P.c[5] + o)));
+        b.U[o] = r;
+        return r;
+      }
+  }
+}
+
+template <int N>
+__device__ __forceinline__ int sgn_k(int i) {
+  return (i <= (N - 1) / 2) ? i : i - N;
+}
+
+template <int N, int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
+  using Lay = V2Layout<N, THREADS>;
+  constexpr int E = Lay::E, T = Lay::T, NG = Lay::NG, TS = Lay::TS;
+  constexpr int M = N / 2 + 1;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int G = a.G;
+  const int g = (int)cluster.block_rank();
+  const int cid = (int)(blockIdx.x / G);
+  const int ncl = (int)(gridDim.x / G);
+  const PlanDev& P = a.P;
+  const int Kc = a.Kc, K = Kc - 1, Cl = a.Cl, ClP = a.ClP, Rl = a.Rl, RlP = a.RlP;
+  const int tid = threadIdx.x;
+  const int gi = tid / T, l = tid % T;
+  const int lane = tid & 31;
+  const unsigned gmask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
+
+  extern __shared__ __align__(16) float2 sm[];
+  float2* twl = sm + Lay::twl();
+  float2* tile = sm + Lay::tiles() + (size_t)gi * TS;
+  float2* colbuf = sm + Lay::colbuf();
+  float2* prod = sm + Lay::prod(Cl);
+  float2* mixed = sm + Lay::mixed(Cl, Kc, RlP);
+  int* colmap = reinterpret_cast<int*>(sm + Lay::maps(Cl, ClP, Kc, RlP));
+  int* rowmap = colmap + Kc;
+
+  // twiddles w_N^(l k1), [k1][l]
+  for (int t = tid; t < N; t += THREADS) {
+    const int k1 = t / T, ll = t % T;
+    twl[t] = __ldg(P.tw + ((ll * k1) % N));
+  }
+  for (int kk = tid; kk < Kc; kk += THREADS) colmap[kk] = ((kk / Cl) << 16) | (kk % Cl);
+  for (int x = tid; x < N; x += THREADS) rowmap[x] = ((x / Rl) << 16) | (x % Rl);
+  __shared__ float2* s_mixed[16];
+  __shared__ float2* s_prod[16];
+  if (tid < G) {
+    s_mixed[tid] = cluster.map_shared_rank(mixed, tid);
+    s_prod[tid] = cluster.map_shared_rank(prod, tid);
+  }
+  __syncthreads();
+
+  const int col0 = g * Cl;
+  const int ncols = max(0, min(Kc, col0 + Cl) - col0);
+  const int row0 = g * Rl;
+  const float invNN = 1.f / ((float)N * (float)N);
+  const float negb = -P.conv_scale;
+  const float ksc = P.kscale;
+  const int nst = a.nonlinear_only ? 1 : P.order;
+  const int Q = a.nonlinear_only ? 1 : a.nsteps * P.order;
+
+  StageBufs sb;
+  {
+    float2* q = a.scratch + (int64_t)cid * a.scratch_stride;
+    const int64_t colsz = (int64_t)Kc * N;
+    sb.U = q;
+    q += colsz;
+    sb.S1 = sb.S = sb.N0 = sb.N1 = sb.N2 = nullptr;
+    if (P.order == 2) {
+      sb.S = q; q += colsz;
+      sb.N0 = q; q += colsz;
+    } else if (P.order == 3) {
+      sb.S = q; q += colsz;
+      sb.N0 = q; q += colsz;
+      sb.N1 = q; q += colsz;
+    } else if (P.order == 4) {
+      sb.S1 = q; q += colsz;
+      sb.S = q; q += colsz;
+      sb.N0 = q; q += colsz;
+      sb.N1 = q; q += colsz;
+      sb.N2 = q; q += colsz;
+    }
+  }
+
+  for (int64_t smp = cid; smp < a.batch; smp += ncl) {
+    const float2* uin = a.in + smp * (int64_t)N * M;
+    float2* uout = a.out + smp * (int64_t)N * M;
+
+    // ---- owned masked columns -> state buffer and colbuf
+    for (int t = tid; t < ncols * N; t += THREADS) {
+      const int kx = t / ncols, c = t - kx * ncols;
+      const float2 v = uin[(int64_t)kx * M + col0 + c];
+      colbuf[c * N + kx] = v;
+      sb.U[(int64_t)(col0 + c) * N + kx] = v;
+    }
+    __syncthreads();
+
+    for (int q = 0; q <= Q; ++q) {
+      // ================= column inverse: derived spectra -> mixed (stage q)
+      if (q < Q) {
+        for (int task = gi; task < 4 * ncols; task += NG) {
+          const int f = task / ncols, c = task - f * ncols;
+          const int ky = col0 + c;
+          const float kys = ksc * (float)ky;
+          float2 v[E];
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const int kx = l + T * j;
+            const int ks = sgn_k<N>(kx);
+            float2 r = make_float2(0.f, 0.f);
+            if (ks <= K && ks >= -K) {
+              const float2 w = colbuf[c * N + kx];
+              const float kxs = ksc * (float)ks;
+              const float lap = -(kxs * kxs + kys * kys);
+              const float il = (lap == 0.f) ? 1.f : 1.f / lap;
+              if (f == 0) r = make_float2(-kys * il * w.y, kys * il * w.x);        // u^  = i ky psi^
+              else if (f == 1) r = make_float2(kxs * il * w.y, -kxs * il * w.x);  // v^  = -i kx psi^
+              else if (f == 2) r = make_float2(-kxs * w.y, kxs * w.x);            // wx^ = i kx w^
+              else r = make_float2(-kys * w.y, kys * w.x);                        // wy^ = i ky w^
+              r = cscale(r, invNN);
+            }
+            v[j] = r;
+          }
+          group_fft<E, T, true>(v, l, tile, twl, gmask);
+#pragma unroll
+          for (int j = 0; j < E; ++j) mixed[(f * N + l + T * j) * ClP + c] = v[j];
+        }
+        cluster.sync();  // mixed complete
+
+        // ================= row phase: rows gi, gi + NG, ...
+        for (int r0 = 0; r0 < Rl; r0 += NG) {
+          const int r = r0 + gi;
+          const bool valid = r < Rl;
+          const int x = row0 + (valid ? r : 0);
+          float2 z1[E], z2[E];
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const int k = l + T * j;
+            const bool ext = k > N / 2;
+            const int kk = ext ? N - k : k;
+            const bool ro = (k == 0) || (k == N / 2);
+            float2 U = make_float2(0.f, 0.f), V = U, WX = U, WY = U;
+            if (kk <= K) {
+              const int cm = colmap[kk];
+              const float2* mb = s_mixed[cm >> 16];
+              const int c = cm & 0xffff;
+              U = mb[(0 * N + x) * ClP + c];
+              V = mb[(1 * N + x) * ClP + c];
+              WX = mb[(2 * N + x) * ClP + c];
+              WY = mb[(3 * N + x) * ClP + c];
+            }
+            z1[j] = pack_pair(U, V, ext, ro);
+            z2[j] = pack_pair(WX, WY, ext, ro);
+          }
+          group_fft<E, T, true>(z1, l, tile, twl, gmask);
+          group_fft<E, T, true>(z2, l, tile, twl, gmask);
+          float pj[E];
+#pragma unroll
+          for (int j = 0; j < E; ++j) pj[j] = fmaf(z1[j].x, z2[j].x, z1[j].y * z2[j].y);
+          // pair rows (gi even: row a, gi odd: row b) through a warp shuffle
+          float2 w[E];
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const float other = __shfl_xor_sync(0xffffffffu, pj[j], T);
+            w[j] = make_float2(pj[j], other);
+          }
+          if ((gi & 1) == 0 && valid) {
+            group_fft<E, T, false>(w, l, tile, twl, gmask);
+            // unpack the two half spectra: Z[N-k] lives in lane (T-l)%T
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              const float2 snd = w[E - 1 - j];
+              float2 rcv;
+              rcv.x = __shfl_sync(gmask, snd.x, (T - l) % T, T);
+              rcv.y = __shfl_sync(gmask, snd.y, (T - l) % T, T);
+              if (l == 0) rcv = w[(E - j) % E];
+              const int k = l + T * j;
+              if (k <= K) {
+                float2 A, B;
+                unpack_pair(w[j], rcv, A, B);
+                prod[k * RlP + r] = A;
+                if (r + 1 < Rl) prod[k * RlP + r + 1] = B;
+              }
+            }
+          }
+        }
+        cluster.sync();  // prod complete
+      }
+      if (q == Q) break;
+
+      // ================= column forward + ETDRK stage update (stage q)
+      const int st = q % nst;
+      const bool last_of_step = (st == nst - 1);
+      for (int c = gi; c < ncols; c += NG) {
+        const int ky = col0 + c;
+        float2 v[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const int x = l + T * j;
+          const int rm = rowmap[x];
+          v[j] = s_prod[rm >> 16][ky * RlP + (rm & 0xffff)];
+        }
+        group_fft<E, T, false>(v, l, tile, twl, gmask);
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const int kx = l + T * j;
+          const int ks = sgn_k<N>(kx);
+          float2 nv = make_float2(0.f, 0.f);
+          if (ks <= K && ks >= -K) nv = cscale(v[j], negb);
+          if (ky == P.inj_mode && kx == 0) nv.x += P.inj_value;
+          if (a.nonlinear_only) {
+            uout[(int64_t)kx * M + ky] = nv;
+          } else {
+            const int64_t o = (int64_t)ky * N + kx;
+            colbuf[c * N + kx] = stage_upd(P, sb, o, st, nv);
+          }
+        }
+        if (!a.nonlinear_only && last_of_step && a.project && (ky == 0 || ky == N / 2)) {
+          __syncwarp(gmask);
+          float2 pv[E];
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const int kx = l + T * j;
+            const float2 a1 = colbuf[c * N + kx];
+            const float2 a2 = colbuf[c * N + ((N - kx) % N)];
+            pv[j] = make_float2(0.5f * (a1.x + a2.x), 0.5f * (a1.y - a2.y));
+          }
+          __syncwarp(gmask);
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const int kx = l + T * j;
+            colbuf[c * N + kx] = pv[j];
+            sb.U[(int64_t)ky * N + kx] = pv[j];
+          }
+        }
+      }
+      __syncthreads();  // colbuf complete for the next inverse phase
+    }
+
+    // ---- store owned masked columns
+    if (!a.nonlinear_only) {
+      for (int t = tid; t < ncols * N; t += THREADS) {
+        const int kx = t / ncols, c = t - kx * ncols;
+        uout[(int64_t)kx * M + col0 + c] = sb.U[(int64_t)(col0 + c) * N + kx];
+      }
+    }
+    // ---- unmasked columns: linear part only
+    {
+      const int u0c = Kc + g * a.Ul;
+      const int u1c = min(M, u0c + a.Ul);
+      const int nuc = max(0, u1c - u0c);
+      constexpr int half = N / 2 + 1;
+      for (int t = tid; t < nuc * half; t += THREADS) {
+        const int c = t / half, kx = t - c * half;
+        const int ky = u0c + c;
+        const int kx2 = (kx == 0) ? 0 : N - kx;
+        if (a.nonlinear_only) {
+          uout[(int64_t)kx * M + ky] = make_float2(0.f, 0.f);
+          uout[(int64_t)kx2 * M + ky] = make_float2(0.f, 0.f);
+          continue;
+        }
+        float2 v1 = uin[(int64_t)kx * M + ky];
+        float2 v2 = uin[(int64_t)kx2 * M + ky];
+        const float2 E1 = __ldg(P.E + (int64_t)ky * N + kx);
+        const float2 E2 = __ldg(P.E + (int64_t)ky * N + kx2);
+        const bool proj = a.project && (ky == 0 || ky == N / 2);
+        for (int s = 0; s < a.nsteps; ++s) {
+          v1 = cmul(E1, v1);
+          v2 = cmul(E2, v2);
+          if (proj) {
+            const float2 pv = make_float2(0.5f * (v1.x + v2.x), 0.5f * (v1.y - v2.y));
+            v1 = pv;
+            v2 = cconj(pv);
+          }
+        }
+        uout[(int64_t)kx * M + ky] = v1;
+        if (kx2 != kx) uout[(int64_t)kx2 * M + ky] = v2;
+      }
+    }
+    cluster.sync();
+  }
+}
+
+template <int N, int THREADS>
+static int v2_configure(exgb_plan* plan) {
+  using Lay = V2Layout<N, THREADS>;
+  PlanDev& P = plan->dev;
+  Plan2DConfig& c = plan->cfg2d;
+  const int K = std::min(P.kmax, N / 2 - 1);
+  const int Kc = K + 1;
+  int dev = 0, lim = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t limit = (size_t)lim - 1024;
+  for (int G : {1, 2, 4, 8}) {
+    const int Cl = (Kc + G - 1) / G;
+    const int ClP = Cl | 1;
+    const int Rl = N / G;
+    const int RlP = Rl + 1;
+    if (Rl < 2 || (Rl % 2)) continue;
+    const size_t bytes = Lay::bytes(Cl, ClP, Kc, RlP);
+    if (bytes > limit) continue;
+    c.G = G;
+    c.threads = THREADS;
+    c.cols_per_cta = Cl;
+    c.rows_per_cta = Rl;
+    c.CB = ClP;  // padded column stride of `mixed`
+    c.RB = RlP;  // padded row stride of `prod`
+    c.mixed_in_smem = 1;
+    c.smem_bytes = bytes;
+    auto fn = vort2d_kernel<N, THREADS>;
+    EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = G;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(G * plan->sm_count, 1, 1);
+    cfg.blockDim = dim3(THREADS, 1, 1);
+    cfg.dynamicSmemBytes = bytes;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, (void*)fn, &cfg) != cudaSuccess || ncl <= 0) {
+      cudaGetLastError();
+      ncl = std::max(1, plan->sm_count / G);
+    }
+    c.clusters = ncl;
+    const int nb = P.order <= 1 ? 1 : P.order == 2 ? 3 : P.order == 3 ? 4 : 6;
+    c.scratch_per_cluster = (size_t)nb * Kc * N;
+    plan->scratch_bytes = sizeof(float2) * c.scratch_per_cluster * (size_t)ncl;
+    EXGB_CUDA(cudaMalloc(&plan->d_scratch, plan->scratch_bytes));
+    return EXGB_OK;
+  }
+  return EXGB_EUNSUPPORTED;
+}
+
+template <int N, int THREADS>
+static int v2_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
+                  int project, int nonlinear_only) {
+  const Plan2DConfig& c = plan->cfg2d;
+  ArgsV2 a;
+  a.P = plan->dev;
+  a.G = c.G;
+  a.Cl = c.cols_per_cta;
+  a.ClP = c.CB;
+  a.Rl = c.rows_per_cta;
+  a.RlP = c.RB;
+  a.Kc = std::min(plan->dev.kmax, N / 2 - 1) + 1;
+  a.Ul = (N / 2 + 1 - a.Kc + c.G - 1) / c.G;
+  a.in = in;
+  a.out = out;
+  a.batch = batch;
+  a.nsteps = nsteps;
+  a.project = project;
+  a.nonlinear_only = nonlinear_only;
+  a.scratch = (float2*)plan->d_scratch;
+  a.scratch_stride = (int64_t)c.scratch_per_cluster;
+  const int ncl = (int)std::min<int64_t>(c.clusters, batch);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = c.G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(c.G * ncl, 1, 1);
+  cfg.blockDim = dim3(THREADS, 1, 1);
+  cfg.dynamicSmemBytes = c.smem_bytes;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  EXGB_CUDA(cudaLaunchKernelEx(&cfg, vort2d_kernel<N, THREADS>, a));
+  return EXGB_OK;
+}
+
+// Returns EXGB_EUNSUPPORTED when this N has no register-FFT variant.
+int vort2d_configure(exgb_plan* plan) {
+  switch (plan->dev.N) {
+    case 64: return v2_configure<64, 256>(plan);
+    case 128: return v2_configure<128, 512>(plan);
+    case 256: return v2_configure<256, 512>(plan);
+    default: return EXGB_EUNSUPPORTED;
+  }
+}
+
+int vort2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
+               int project, int nonlinear_only) {
+  if (batch <= 0) return EXGB_OK;
+  switch (plan->dev.N) {
+    case 64: return v2_run<64, 256>(plan, st, in, out, batch, nsteps, project, nonlinear_only);
+    case 128: return v2_run<128, 512>(plan, st, in, out, batch, nsteps, project, nonlinear_only);
+    case 256: return v2_run<256, 512>(plan, st, in, out, batch, nsteps, project, nonlinear_only);
+    default: return fail(EXGB_EUNSUPPORTED, "no register-FFT variant for this N");
+  }
+}
+
+}  // namespace exgb
