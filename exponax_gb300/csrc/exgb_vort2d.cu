@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "exgb_internal.h"
 #include "exgb_regfft.cuh"
@@ -26,7 +27,7 @@ namespace exgb {
 
 struct ArgsV2 {
   PlanDev P;
-  int G, Cl, ClP, Rl, RlP, Kc, Ul;
+  int G, Cl, Rl, lgRl, Kc, KcP, Ul;
   const float2* in;
   float2* out;
   int64_t batch;
@@ -42,15 +43,16 @@ struct V2Layout {
   static constexpr int E = RegCfg<N>::E, T = RegCfg<N>::T;
   static constexpr int NG = THREADS / T;
   static constexpr int TS = tile_stride<E, T>();
+  static constexpr int NP = N + 1;  // padded row length of the product receive buffer
   // float2 offsets
   __host__ __device__ static size_t twl() { return 0; }
   __host__ __device__ static size_t tiles() { return N; }
   __host__ __device__ static size_t colbuf() { return tiles() + (size_t)NG * TS; }
-  __host__ __device__ static size_t prod(int Cl) { return colbuf() + (size_t)Cl * N; }
-  __host__ __device__ static size_t mixed(int Cl, int Kc, int RlP) { return prod(Cl) + (size_t)Kc * RlP; }
-  __host__ __device__ static size_t maps(int Cl, int ClP, int Kc, int RlP) { return mixed(Cl, Kc, RlP) + (size_t)4 * N * ClP; }
-  __host__ __device__ static size_t bytes(int Cl, int ClP, int Kc, int RlP) {
-    return sizeof(float2) * maps(Cl, ClP, Kc, RlP) + sizeof(int) * ((size_t)Kc + N);
+  __host__ __device__ static size_t prodr(int Cl) { return colbuf() + (size_t)Cl * N; }
+  __host__ __device__ static size_t mixr(int Cl) { return prodr(Cl) + (size_t)Cl * NP; }
+  __host__ __device__ static size_t maps(int Cl, int Rl, int KcP) { return mixr(Cl) + (size_t)4 * Rl * KcP; }
+  __host__ __device__ static size_t bytes(int Cl, int Rl, int KcP, int Kc) {
+    return sizeof(float2) * maps(Cl, Rl, KcP) + sizeof(int) * (size_t)Kc;
   }
 };
 
@@ -132,7 +134,7 @@ __device__ __forceinline__ int sgn_k(int i) {
 template <int N, int THREADS>
 __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   using Lay = V2Layout<N, THREADS>;
-  constexpr int E = Lay::E, T = Lay::T, NG = Lay::NG, TS = Lay::TS;
+  constexpr int E = Lay::E, T = Lay::T, NG = Lay::NG, TS = Lay::TS, NP = Lay::NP;
   constexpr int M = N / 2 + 1;
   cg::cluster_group cluster = cg::this_cluster();
   const int G = a.G;
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   const int cid = (int)(blockIdx.x / G);
   const int ncl = (int)(gridDim.x / G);
   const PlanDev& P = a.P;
-  const int Kc = a.Kc, K = Kc - 1, Cl = a.Cl, ClP = a.ClP, Rl = a.Rl, RlP = a.RlP;
+  const int Kc = a.Kc, K = Kc - 1, KcP = a.KcP, Cl = a.Cl, Rl = a.Rl, lgRl = a.lgRl;
   const int tid = threadIdx.x;
   const int gi = tid / T, l = tid % T;
   const int lane = tid & 31;
@@ -149,24 +151,21 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   extern __shared__ __align__(16) float2 sm[];
   float2* twl = sm + Lay::twl();
   float2* tile = sm + Lay::tiles() + (size_t)gi * TS;
-  float2* colbuf = sm + Lay::colbuf();
-  float2* prod = sm + Lay::prod(Cl);
-  float2* mixed = sm + Lay::mixed(Cl, Kc, RlP);
-  int* colmap = reinterpret_cast<int*>(sm + Lay::maps(Cl, ClP, Kc, RlP));
-  int* rowmap = colmap + Kc;
+  float2* colbuf = sm + Lay::colbuf();   // [c][kx]   owned columns
+  float2* prodr = sm + Lay::prodr(Cl);   // [c][x]    product spectra received for owned columns
+  float2* mixr = sm + Lay::mixr(Cl);     // [f][r][ky] derived fields received for owned rows
+  int* colmap = reinterpret_cast<int*>(sm + Lay::maps(Cl, Rl, KcP));
 
-  // twiddles w_N^(l k1), [k1][l]
   for (int t = tid; t < N; t += THREADS) {
     const int k1 = t / T, ll = t % T;
-    twl[t] = __ldg(P.tw + ((ll * k1) % N));
+    twl[t] = __ldg(P.tw + ((ll * k1) % N));  // w_N^(l k1), [k1][l]
   }
   for (int kk = tid; kk < Kc; kk += THREADS) colmap[kk] = ((kk / Cl) << 16) | (kk % Cl);
-  for (int x = tid; x < N; x += THREADS) rowmap[x] = ((x / Rl) << 16) | (x % Rl);
-  __shared__ float2* s_mixed[16];
-  __shared__ float2* s_prod[16];
+  __shared__ float2* s_mixr[16];
+  __shared__ float2* s_prodr[16];
   if (tid < G) {
-    s_mixed[tid] = cluster.map_shared_rank(mixed, tid);
-    s_prod[tid] = cluster.map_shared_rank(prod, tid);
+    s_mixr[tid] = cluster.map_shared_rank(mixr, tid);
+    s_prodr[tid] = cluster.map_shared_rank(prodr, tid);
   }
   __syncthreads();
 
@@ -215,111 +214,106 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
     }
     __syncthreads();
 
-    for (int q = 0; q <= Q; ++q) {
-      // ================= column inverse: derived spectra -> mixed (stage q)
-      if (q < Q) {
-        for (int task = gi; task < 4 * ncols; task += NG) {
-          const int f = task / ncols, c = task - f * ncols;
-          const int ky = col0 + c;
-          const float kys = ksc * (float)ky;
-          float2 v[E];
-#pragma unroll
-          for (int j = 0; j < E; ++j) {
-            const int kx = l + T * j;
-            const int ks = sgn_k<N>(kx);
-            float2 r = make_float2(0.f, 0.f);
-            if (ks <= K && ks >= -K) {
-              const float2 w = colbuf[c * N + kx];
-              const float kxs = ksc * (float)ks;
-              const float lap = -(kxs * kxs + kys * kys);
-              const float il = (lap == 0.f) ? 1.f : 1.f / lap;
-              if (f == 0) r = make_float2(-kys * il * w.y, kys * il * w.x);        // u^  = i ky psi^
-              else if (f == 1) r = make_float2(kxs * il * w.y, -kxs * il * w.x);  // v^  = -i kx psi^
-              else if (f == 2) r = make_float2(-kxs * w.y, kxs * w.x);            // wx^ = i kx w^
-              else r = make_float2(-kys * w.y, kys * w.x);                        // wy^ = i ky w^
-              r = cscale(r, invNN);
-            }
-            v[j] = r;
-          }
-          group_fft<E, T, true>(v, l, tile, twl, gmask);
-#pragma unroll
-          for (int j = 0; j < E; ++j) mixed[(f * N + l + T * j) * ClP + c] = v[j];
-        }
-        cluster.sync();  // mixed complete
-
-        // ================= row phase: rows gi, gi + NG, ...
-        for (int r0 = 0; r0 < Rl; r0 += NG) {
-          const int r = r0 + gi;
-          const bool valid = r < Rl;
-          const int x = row0 + (valid ? r : 0);
-          float2 z1[E], z2[E];
-#pragma unroll
-          for (int j = 0; j < E; ++j) {
-            const int k = l + T * j;
-            const bool ext = k > N / 2;
-            const int kk = ext ? N - k : k;
-            const bool ro = (k == 0) || (k == N / 2);
-            float2 U = make_float2(0.f, 0.f), V = U, WX = U, WY = U;
-            if (kk <= K) {
-              const int cm = colmap[kk];
-              const float2* mb = s_mixed[cm >> 16];
-              const int c = cm & 0xffff;
-              U = mb[(0 * N + x) * ClP + c];
-              V = mb[(1 * N + x) * ClP + c];
-              WX = mb[(2 * N + x) * ClP + c];
-              WY = mb[(3 * N + x) * ClP + c];
-            }
-            z1[j] = pack_pair(U, V, ext, ro);
-            z2[j] = pack_pair(WX, WY, ext, ro);
-          }
-          group_fft<E, T, true>(z1, l, tile, twl, gmask);
-          group_fft<E, T, true>(z2, l, tile, twl, gmask);
-          float pj[E];
-#pragma unroll
-          for (int j = 0; j < E; ++j) pj[j] = fmaf(z1[j].x, z2[j].x, z1[j].y * z2[j].y);
-          // pair rows (gi even: row a, gi odd: row b) through a warp shuffle
-          float2 w[E];
-#pragma unroll
-          for (int j = 0; j < E; ++j) {
-            const float other = __shfl_xor_sync(0xffffffffu, pj[j], T);
-            w[j] = make_float2(pj[j], other);
-          }
-          if ((gi & 1) == 0 && valid) {
-            group_fft<E, T, false>(w, l, tile, twl, gmask);
-            // unpack the two half spectra: Z[N-k] lives in lane (T-l)%T
-#pragma unroll
-            for (int j = 0; j < E; ++j) {
-              const float2 snd = w[E - 1 - j];
-              float2 rcv;
-              rcv.x = __shfl_sync(gmask, snd.x, (T - l) % T, T);
-              rcv.y = __shfl_sync(gmask, snd.y, (T - l) % T, T);
-              if (l == 0) rcv = w[(E - j) % E];
-              const int k = l + T * j;
-              if (k <= K) {
-                float2 A, B;
-                unpack_pair(w[j], rcv, A, B);
-                prod[k * RlP + r] = A;
-                if (r + 1 < Rl) prod[k * RlP + r + 1] = B;
-              }
-            }
-          }
-        }
-        cluster.sync();  // prod complete
-      }
-      if (q == Q) break;
-
-      // ================= column forward + ETDRK stage update (stage q)
+    for (int q = 0; q < Q; ++q) {
       const int st = q % nst;
       const bool last_of_step = (st == nst - 1);
+      // ================= column inverse: derived spectra -> IFFT -> pushed to the row owners
+      for (int task = gi; task < 4 * ncols; task += NG) {
+        const int f = task / ncols, c = task - f * ncols;
+        const int ky = col0 + c;
+        const float kys = ksc * (float)ky;
+        float2 v[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const int kx = l + T * j;
+          const int ks = sgn_k<N>(kx);
+          float2 r = make_float2(0.f, 0.f);
+          if (ks <= K && ks >= -K) {
+            const float2 w = colbuf[c * N + kx];
+            const float kxs = ksc * (float)ks;
+            const float lap = -(kxs * kxs + kys * kys);
+            const float il = (lap == 0.f) ? 1.f : 1.f / lap;
+            if (f == 0) r = make_float2(-kys * il * w.y, kys * il * w.x);        // u^  = i ky psi^
+            else if (f == 1) r = make_float2(kxs * il * w.y, -kxs * il * w.x);  // v^  = -i kx psi^
+            else if (f == 2) r = make_float2(-kxs * w.y, kxs * w.x);            // wx^ = i kx w^
+            else r = make_float2(-kys * w.y, kys * w.x);                        // wy^ = i ky w^
+            r = cscale(r, invNN);
+          }
+          v[j] = r;
+        }
+        group_fft<E, T, true>(v, l, tile, twl, gmask);
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const int x = l + T * j;
+          const int d = x >> lgRl, xr = x & (Rl - 1);
+          s_mixr[d][(f * Rl + xr) * KcP + ky] = v[j];
+        }
+      }
+      cluster.sync();  // derived fields delivered
+
+      // ================= row phase: local gather -> 2 IFFTs -> product -> paired FFT -> pushed to column owners
+      for (int r0 = 0; r0 < Rl; r0 += NG) {
+        const int r = r0 + gi;
+        const bool valid = r < Rl;
+        const int rr = valid ? r : 0;
+        float2 z1[E], z2[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const int k = l + T * j;
+          const bool ext = k > N / 2;
+          const int kk = ext ? N - k : k;
+          const bool ro = (k == 0) || (k == N / 2);
+          float2 U = make_float2(0.f, 0.f), V = U, WX = U, WY = U;
+          if (kk <= K) {
+            U = mixr[(0 * Rl + rr) * KcP + kk];
+            V = mixr[(1 * Rl + rr) * KcP + kk];
+            WX = mixr[(2 * Rl + rr) * KcP + kk];
+            WY = mixr[(3 * Rl + rr) * KcP + kk];
+          }
+          z1[j] = pack_pair(U, V, ext, ro);
+          z2[j] = pack_pair(WX, WY, ext, ro);
+        }
+        group_fft<E, T, true>(z1, l, tile, twl, gmask);
+        group_fft<E, T, true>(z2, l, tile, twl, gmask);
+        float pj[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) pj[j] = fmaf(z1[j].x, z2[j].x, z1[j].y * z2[j].y);
+        float2 w[E];
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const float other = __shfl_xor_sync(0xffffffffu, pj[j], T);
+          w[j] = make_float2(pj[j], other);
+        }
+        if ((gi & 1) == 0 && valid) {
+          group_fft<E, T, false>(w, l, tile, twl, gmask);
+          const int xa = row0 + r;
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const float2 snd = w[E - 1 - j];
+            float2 rcv;
+            rcv.x = __shfl_sync(gmask, snd.x, (T - l) % T, T);
+            rcv.y = __shfl_sync(gmask, snd.y, (T - l) % T, T);
+            if (l == 0) rcv = w[(E - j) % E];
+            const int k = l + T * j;
+            if (k <= K) {
+              float2 A, B;
+              unpack_pair(w[j], rcv, A, B);
+              const int cm = colmap[k];
+              float2* dst = s_prodr[cm >> 16] + (cm & 0xffff) * NP + xa;
+              dst[0] = A;
+              if (r + 1 < Rl) dst[1] = B;
+            }
+          }
+        }
+      }
+      cluster.sync();  // product spectra delivered
+
+      // ================= column forward FFT (local gather) -> raw N^ in colbuf
       for (int c = gi; c < ncols; c += NG) {
         const int ky = col0 + c;
         float2 v[E];
 #pragma unroll
-        for (int j = 0; j < E; ++j) {
-          const int x = l + T * j;
-          const int rm = rowmap[x];
-          v[j] = s_prod[rm >> 16][ky * RlP + (rm & 0xffff)];
-        }
+        for (int j = 0; j < E; ++j) v[j] = prodr[c * NP + l + T * j];
         group_fft<E, T, false>(v, l, tile, twl, gmask);
 #pragma unroll
         for (int j = 0; j < E; ++j) {
@@ -328,33 +322,37 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           float2 nv = make_float2(0.f, 0.f);
           if (ks <= K && ks >= -K) nv = cscale(v[j], negb);
           if (ky == P.inj_mode && kx == 0) nv.x += P.inj_value;
-          if (a.nonlinear_only) {
-            uout[(int64_t)kx * M + ky] = nv;
-          } else {
-            const int64_t o = (int64_t)ky * N + kx;
-            colbuf[c * N + kx] = stage_upd(P, sb, o, st, nv);
-          }
+          colbuf[c * N + kx] = nv;
         }
-        if (!a.nonlinear_only && last_of_step && a.project && (ky == 0 || ky == N / 2)) {
-          __syncwarp(gmask);
-          float2 pv[E];
-#pragma unroll
-          for (int j = 0; j < E; ++j) {
-            const int kx = l + T * j;
-            const float2 a1 = colbuf[c * N + kx];
-            const float2 a2 = colbuf[c * N + ((N - kx) % N)];
-            pv[j] = make_float2(0.5f * (a1.x + a2.x), 0.5f * (a1.y - a2.y));
-          }
-          __syncwarp(gmask);
-#pragma unroll
-          for (int j = 0; j < E; ++j) {
-            const int kx = l + T * j;
-            colbuf[c * N + kx] = pv[j];
-            sb.U[(int64_t)ky * N + kx] = pv[j];
+      }
+      __syncthreads();
+      // ================= ETDRK stage update, all threads (latency-bound elementwise pass)
+      if (a.nonlinear_only) {
+        for (int t = tid; t < ncols * N; t += THREADS) {
+          const int c = t / N, kx = t % N;
+          uout[(int64_t)kx * M + col0 + c] = colbuf[t];
+        }
+      } else {
+        for (int t = tid; t < ncols * N; t += THREADS) {
+          const int c = t / N, kx = t % N;
+          const int64_t o = (int64_t)(col0 + c) * N + kx;
+          colbuf[t] = stage_upd(P, sb, o, st, colbuf[t]);
+        }
+        if (last_of_step && a.project && col0 == 0 && ncols > 0) {
+          // c2r projection of the step's physical round trip on ky = 0
+          __syncthreads();
+          for (int kx = tid; kx <= N / 2; kx += THREADS) {
+            const int kx2 = (N - kx) % N;
+            const float2 a1 = colbuf[kx], a2 = colbuf[kx2];
+            const float2 pv = make_float2(0.5f * (a1.x + a2.x), 0.5f * (a1.y - a2.y));
+            colbuf[kx] = pv;
+            colbuf[kx2] = cconj(pv);
+            sb.U[kx] = pv;
+            sb.U[kx2] = cconj(pv);
           }
         }
       }
-      __syncthreads();  // colbuf complete for the next inverse phase
+      __syncthreads();  // colbuf ready for the next inverse phase
     }
 
     // ---- store owned masked columns
@@ -412,20 +410,21 @@ static int v2_configure(exgb_plan* plan) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t limit = (size_t)lim - 1024;
+  const char* envG = getenv("EXGB_CLUSTER");
   for (int G : {1, 2, 4, 8}) {
+    if (envG && atoi(envG) != G) continue;
     const int Cl = (Kc + G - 1) / G;
-    const int ClP = Cl | 1;
     const int Rl = N / G;
-    const int RlP = Rl + 1;
-    if (Rl < 2 || (Rl % 2)) continue;
-    const size_t bytes = Lay::bytes(Cl, ClP, Kc, RlP);
+    const int KcP = Kc | 1;
+    if (Rl < 2) continue;
+    const size_t bytes = Lay::bytes(Cl, Rl, KcP, Kc);
     if (bytes > limit) continue;
     c.G = G;
     c.threads = THREADS;
     c.cols_per_cta = Cl;
     c.rows_per_cta = Rl;
-    c.CB = ClP;  // padded column stride of `mixed`
-    c.RB = RlP;  // padded row stride of `prod`
+    c.CB = KcP;  // padded ky stride of the derived-field receive buffer
+    c.RB = 0;
     c.mixed_in_smem = 1;
     c.smem_bytes = bytes;
     auto fn = vort2d_kernel<N, THREADS>;
@@ -464,10 +463,11 @@ static int v2_run(const exgb_plan* plan, cudaStream_t st, const float2* in, floa
   a.P = plan->dev;
   a.G = c.G;
   a.Cl = c.cols_per_cta;
-  a.ClP = c.CB;
   a.Rl = c.rows_per_cta;
-  a.RlP = c.RB;
+  a.lgRl = 0;
+  while ((1 << a.lgRl) < a.Rl) ++a.lgRl;
   a.Kc = std::min(plan->dev.kmax, N / 2 - 1) + 1;
+  a.KcP = c.CB;
   a.Ul = (N / 2 + 1 - a.Kc + c.G - 1) / c.G;
   a.in = in;
   a.out = out;
