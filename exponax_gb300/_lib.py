@@ -87,6 +87,7 @@ SIGNATURES = [
     ("exgb_repeat", _I, [_VP, _VP, _VP, _VP, _I64, _I32]),
     ("exgb_repeat_fourier", _I, [_VP, _VP, _VP, _VP, _I64, _I32]),
     ("exgb_rollout", _I, [_VP, _VP, _VP, _VP, _I64, _I32, _I32]),
+    ("exgb_repeat_fourier_noalloc", _I, [_VP, _VP, _VP, _VP, _I64, _I32]),
     ("exgb_queue_rollout", _I, [ctypes.POINTER(WorkItem), _I64, _I32, _I32, _VP]),
     ("exgb_map_between_resolutions", _I, [_VP, _I, _I, _I, _I64, _VP, _VP, _I]),
 ]

@@ -516,3 +516,62 @@ int vort2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2*
 }
 
 }  // namespace exgb
+
+namespace exgb {
+
+// Launch of the register-FFT kernel on caller-provided scratch (no
+// allocation): as many persistent clusters as `scratch_elems` float2 of
+// stage buffers hold, at most the configured number.
+template <int N, int THREADS>
+static int v2_run_scratch(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch,
+                          int nsteps, int project, float2* scratch, size_t scratch_elems) {
+  const Plan2DConfig& c = plan->cfg2d;
+  const size_t fit = scratch_elems / c.scratch_per_cluster;
+  if (fit < 1) return fail(EXGB_ENOMEM, "the static scratch array is smaller than one cluster's stage buffers");
+  ArgsV2 a;
+  a.P = plan->dev;
+  a.G = c.G;
+  a.Cl = c.cols_per_cta;
+  a.Rl = c.rows_per_cta;
+  a.lgRl = 0;
+  while ((1 << a.lgRl) < a.Rl) ++a.lgRl;
+  a.Kc = std::min(plan->dev.kmax, N / 2 - 1) + 1;
+  a.KcP = c.CB;
+  a.Ul = (N / 2 + 1 - a.Kc + c.G - 1) / c.G;
+  a.in = in;
+  a.out = out;
+  a.batch = batch;
+  a.nsteps = nsteps;
+  a.project = project;
+  a.nonlinear_only = 0;
+  a.scratch = scratch;
+  a.scratch_stride = (int64_t)c.scratch_per_cluster;
+  const int ncl = (int)std::min<int64_t>(std::min<int64_t>(c.clusters, (int64_t)fit), batch);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = c.G;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(c.G * ncl, 1, 1);
+  cfg.blockDim = dim3(THREADS, 1, 1);
+  cfg.dynamicSmemBytes = c.smem_bytes;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  EXGB_CUDA(cudaLaunchKernelEx(&cfg, vort2d_kernel<N, THREADS>, a));
+  return EXGB_OK;
+}
+
+int vort2d_run_scratch(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch,
+                       int nsteps, int project, float2* scratch, size_t scratch_elems) {
+  if (batch <= 0) return EXGB_OK;
+  switch (plan->dev.N) {
+    case 64: return v2_run_scratch<64, 256>(plan, st, in, out, batch, nsteps, project, scratch, scratch_elems);
+    case 128: return v2_run_scratch<128, 512>(plan, st, in, out, batch, nsteps, project, scratch, scratch_elems);
+    case 256: return v2_run_scratch<256, 512>(plan, st, in, out, batch, nsteps, project, scratch, scratch_elems);
+    default: return fail(EXGB_EUNSUPPORTED, "no register-FFT variant for this N");
+  }
+}
+
+}  // namespace exgb

@@ -147,6 +147,19 @@ int exgb_repeat_fourier(const exgb_plan* plan, void* stream, const void* u_hat0,
 int exgb_rollout(const exgb_plan* plan, void* stream, const float* u0, float* traj, int64_t batch,
                  int32_t nsteps, int32_t include_init);
 
+/* Same result as exgb_repeat_fourier for 2D vorticity plans (N in {64, 128,
+ * 256}, ETDRK order >= 1), for callers that cannot allocate device memory
+ * where they step (e.g. inside a framework's custom call that may only use
+ * the buffers it is given).  No counterpart in the reference.  Calls no
+ * cudaMalloc/cudaFree: the stage buffers live in an 8 MiB file-scope device
+ * array that every GPU loading the library keeps until exit; plans needing
+ * more than 8 MiB per cluster are rejected with EXGB_EUNSUPPORTED.  The
+ * first call on a device looks up the array's address (make it before any
+ * stream capture).  All calls share the array: calls that overlap on the
+ * GPU race and must be serialised by the caller. */
+int exgb_repeat_fourier_noalloc(const exgb_plan* plan, void* stream, const void* u_hat0, void* u_hat_out,
+                                int64_t batch, int32_t nsteps);
+
 /* Uneven batch in one persistent launch: instances of different 1D plans
  * (PDE, N, dt) share a device work queue.  No reference counterpart: the
  * reference runs one jax.vmap(rollout) per (PDE, N) group in sequence
