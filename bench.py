@@ -255,7 +255,7 @@ def run_gb300(args, rank, ws):
         e_ms = float(t.item())
     e2e = BATCH * ws * N * N * NSTEPS / (e_ms * 1e-3)
 
-    # ---- roofline of the dominant kernel (etdrk2d_kernel: the only launch of fourier_run)
+    # ---- roofline of the dominant kernel (vort2d_kernel: the only launch of fourier_run)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -266,11 +266,11 @@ def run_gb300(args, rank, ws):
     alg_bytes = BATCH * N * N * NSTEPS * BYTES_PER_DOF_STEP
     achieved = alg_bytes / (ms_step * 1e-3) / 1e9
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "etdrk2d_traffic.txt")
+    tf = os.path.join(ROOT, "profiles", "vort2d_kernel_ns256_b128_traffic.txt")
     if os.path.exists(tf):
         for line in open(tf):
-            if line.startswith("dram_bytes_per_dof_step="):
-                traffic = float(line.split("=")[1]) * BATCH * N * N * NSTEPS
+            if line.startswith("dram_bytes_per_launch="):
+                traffic = float(line.split("=")[1])
 
     if rank == 0:
         cpu = cpu_baseline() if ws == 1 and not args.no_cpu else None
@@ -284,7 +284,7 @@ def run_gb300(args, rank, ws):
                 "gpu_launches": args.steps * 1 + args.steps * 5,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
-                             "kernel": "etdrk2d_kernel",
+                             "kernel": "vort2d_kernel<256,512>",
                              "note": f"algorithmic {BYTES_PER_DOF_STEP:.2f} B/DOF-step (ETDRK2, 6 complex64 "
                                      f"half-spectrum passes) x {BATCH}x{N}^2x{NSTEPS} per launch; peak {peak_src}"},
                 "clocks": clk, "cpu_baseline": cpu}
