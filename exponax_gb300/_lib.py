@@ -30,6 +30,8 @@ NL_POLYNOMIAL = 3
 NL_GENERAL = 4
 NL_VORTICITY_2D = 5
 NL_VORTICITY_2D_KOLMOGOROV = 6
+NL_PROJECTED_3D = 7
+NL_PROJECTED_3D_KOLMOGOROV = 8
 
 
 class PlanDesc(ctypes.Structure):
@@ -90,6 +92,7 @@ SIGNATURES = [
     ("exgb_repeat_fourier_noalloc", _I, [_VP, _VP, _VP, _VP, _I64, _I32]),
     ("exgb_queue_rollout", _I, [ctypes.POINTER(WorkItem), _I64, _I32, _I32, _VP]),
     ("exgb_map_between_resolutions", _I, [_VP, _I, _I, _I, _I64, _VP, _VP, _I]),
+    ("exgb_leray", _I, [_VP, _I, _I, ctypes.c_double, _I64, _VP, _VP]),
 ]
 
 _lib = None

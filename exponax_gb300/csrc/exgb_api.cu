@@ -224,8 +224,8 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   if (!desc || !out) return fail(EXGB_EINVAL, "exgb_plan_create: NULL argument");
   *out = nullptr;
   const exgb_plan_desc& d = *desc;
-  if (d.num_spatial_dims < 1 || d.num_spatial_dims > 2)
-    return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1 or 2 in this build");
+  if (d.num_spatial_dims < 1 || d.num_spatial_dims > 3)
+    return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1, 2 or 3");
   if (d.order < 0 || d.order > 4)
     return fail(EXGB_ENOTIMPL, "Order " + std::to_string(d.order) + " not implemented.");
   if (!factorable(d.num_points))
@@ -246,11 +246,18 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
       if (d.nonlin_kind > EXGB_NL_GENERAL)
         return fail(EXGB_EUNSUPPORTED, "this nonlinear function needs num_spatial_dims == 2");
       if (d.num_channels != 1) return fail(EXGB_EUNSUPPORTED, "1D plans have one channel");
-    } else {
+    } else if (D == 2) {
       if (d.nonlin_kind != EXGB_NL_VORTICITY_2D && d.nonlin_kind != EXGB_NL_VORTICITY_2D_KOLMOGOROV &&
           d.nonlin_kind != EXGB_NL_ZERO)
         return fail(EXGB_EUNSUPPORTED, "2D plans support the vorticity-convection nonlinearity (and linear ETDRK)");
-      if (d.num_channels != 1) return fail(EXGB_ESHAPE, "vorticity formulation has one channel");
+      if (d.nonlin_kind != EXGB_NL_ZERO && d.num_channels != 1)
+        return fail(EXGB_ESHAPE, "vorticity formulation has one channel");
+    } else {
+      if (d.nonlin_kind != EXGB_NL_PROJECTED_3D && d.nonlin_kind != EXGB_NL_PROJECTED_3D_KOLMOGOROV &&
+          d.nonlin_kind != EXGB_NL_ZERO)
+        return fail(EXGB_EUNSUPPORTED, "3D plans support the projected convection (and linear ETDRK)");
+      if (d.nonlin_kind != EXGB_NL_ZERO && d.num_channels != 3)
+        return fail(EXGB_ESHAPE, "Number of channels in u_hat should match number of spatial dimensions");
     }
   }
 
@@ -323,6 +330,18 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
     case EXGB_NL_VORTICITY_2D:
       v.conv_scale = b;
       break;
+    case EXGB_NL_PROJECTED_3D_KOLMOGOROV: {
+      const int k = d.injection_mode;
+      if (k < 0 || k > N / 2) {
+        exgb_plan_destroy(p);
+        return fail(EXGB_EUNSUPPORTED, "injection_mode out of range");
+      }
+      // coef_extraction scaling at (0, k, 0): N * (N/2 or N) * N, first channel only, no -k factor
+      // (nonlin_fun/_projected_convection.py:202-220)
+      const double mid = (k == 0 || (N % 2 == 0 && k == N / 2)) ? (double)N : (double)N / 2.0;
+      v.inj_mode = k;
+      v.inj_value = (float)(d.injection_scale * ((double)N * mid * (double)N));
+    } break;
     default:
       break;
   }

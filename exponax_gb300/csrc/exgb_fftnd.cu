@@ -16,19 +16,19 @@
 namespace exgb {
 
 // ---------------------------------------------------------------- workspace
-// Four grow-only buffers per device: 0 = inverse-transform intermediate,
-// 1 = re-sampling spectra / 1D work items, 2 = 2D Fourier state of the
-// physical-space entry points, 3 = 2D rollout frame.  Growing
+// Grow-only buffers per device: 0 = inverse-transform intermediate,
+// 1 = re-sampling spectra / 1D work items, 2 = Fourier state of the
+// physical-space entry points, 3 = rollout frame, 4 = 3D stage buffers.  Growing
 // calls cudaFree/cudaMalloc (device-synchronising); the steady state does
 // not allocate.
 static std::mutex g_ws_mu;
-static void* g_ws[64] = {nullptr};
-static size_t g_ws_bytes[64] = {0};
+static void* g_ws[128] = {nullptr};
+static size_t g_ws_bytes[128] = {0};
 
 void* workspace(size_t bytes, int slot_offset = 0) {
   int dev = 0;
   cudaGetDevice(&dev);
-  const int slot = (dev % 16) * 4 + slot_offset;
+  const int slot = (dev % 16) * 8 + slot_offset;
   std::lock_guard<std::mutex> lk(g_ws_mu);
   if (g_ws_bytes[slot] < bytes) {
     if (g_ws[slot]) cudaFree(g_ws[slot]);
@@ -239,7 +239,15 @@ int rfftn_impl(cudaStream_t st, int D, int N, int64_t count, const float* in, fl
     if (rc) return rc;
     return launch_cfft_axis(st, *fp, tw, false, count, (int64_t)N * M, M, M, out, out, 1.f);
   }
-  return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1 or 2 in this build");
+  if (D == 3) {
+    const int64_t plane = (int64_t)N * M;
+    rc = launch_rfft1d(st, *fp, tw, count * N * N, in, out);
+    if (rc) return rc;
+    rc = launch_cfft_axis(st, *fp, tw, false, count * N, plane, M, M, out, out, 1.f);
+    if (rc) return rc;
+    return launch_cfft_axis(st, *fp, tw, false, count, plane * N, plane, plane, out, out, 1.f);
+  }
+  return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1, 2 or 3");
 }
 
 int irfftn_impl(cudaStream_t st, int D, int N, int64_t count, const float2* in, float* out) {
@@ -256,7 +264,17 @@ int irfftn_impl(cudaStream_t st, int D, int N, int64_t count, const float2* in, 
     if (rc) return rc;
     return launch_irfft1d(st, *fp, tw, count * N, tmp, out, 1.f / ((float)N * (float)N));
   }
-  return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1 or 2 in this build");
+  if (D == 3) {
+    const int64_t plane = (int64_t)N * M;
+    float2* tmp = (float2*)workspace(sizeof(float2) * (size_t)count * N * plane, 0);
+    if (!tmp) return fail(EXGB_ENOMEM, "workspace allocation failed");
+    rc = launch_cfft_axis(st, *fp, tw, true, count, plane * N, plane, plane, in, tmp, 1.f);
+    if (rc) return rc;
+    rc = launch_cfft_axis(st, *fp, tw, true, count * N, plane, M, M, tmp, tmp, 1.f);
+    if (rc) return rc;
+    return launch_irfft1d(st, *fp, tw, count * N * N, tmp, out, 1.f / ((float)N * (float)N * (float)N));
+  }
+  return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1, 2 or 3");
 }
 
 // ---------------------------------------------------------------- map_between_resolutions

@@ -68,9 +68,13 @@ int etdrk0_apply(const exgb_plan* plan, cudaStream_t st, const float2* in, float
 
 static bool linear_only(const PlanDev& P) { return P.order == 0 || P.kind == EXGB_NL_ZERO; }
 
-// Fourier-space multi-step for 2D plans.
+int steps3d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
+                int project, int nonlinear_only);
+
+// Fourier-space multi-step for 2D and 3D plans.
 static int fourier_steps_2d(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch,
                             int nsteps, int project) {
+  if (plan->dev.D == 3) return steps3d_run(plan, st, in, out, batch, nsteps, project, 0);
   if (linear_only(plan->dev)) return etdrk0_apply(plan, st, in, out, batch, nsteps, project);
   return etdrk2d_run(plan, st, in, out, batch, nsteps, project, 0);
 }
@@ -116,6 +120,7 @@ int exgb_nonlinear(const exgb_plan* plan, void* stream, const void* u_hat_in, vo
     EXGB_CUDA(cudaMemsetAsync(n_hat_out, 0, sizeof(float2) * hat_elems(P, batch), st));
     return EXGB_OK;
   }
+  if (P.D == 3) return steps3d_run(plan, st, (const float2*)u_hat_in, (float2*)n_hat_out, batch, 0, 0, 1);
   if (P.D == 1)
     return etdrk1d_run(plan, st, nullptr, (const float2*)u_hat_in, nullptr, (float2*)n_hat_out, batch, 0, 0, 0, 0,
                        1);

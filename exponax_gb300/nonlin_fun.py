@@ -11,8 +11,8 @@ from __future__ import annotations
 import numpy as np
 
 from . import _device
-from ._lib import (NL_CONVECTION, NL_GENERAL, NL_GRADIENT_NORM, NL_POLYNOMIAL, NL_VORTICITY_2D,
-                   NL_VORTICITY_2D_KOLMOGOROV, NL_ZERO, check, load)
+from ._lib import (NL_CONVECTION, NL_GENERAL, NL_GRADIENT_NORM, NL_POLYNOMIAL, NL_PROJECTED_3D,
+                   NL_PROJECTED_3D_KOLMOGOROV, NL_VORTICITY_2D, NL_VORTICITY_2D_KOLMOGOROV, NL_ZERO, check, load)
 from ._plan import Plan
 from .spectral import (build_laplace_operator, build_scaling_array, build_wavenumbers, dealias_kmax,
                        low_pass_filter_mask, spatial_shape, wavenumber_shape)
@@ -249,18 +249,71 @@ class VorticityConvection2dKolmogorov(VorticityConvection2d):
 
 
 class Leray(BaseNonlinearFun):
-    """nonlin_fun/_leray.py:8-136.  Host arrays only in this build: the 3D
-    path (Leray projection on the GPU) is not built yet."""
+    """nonlin_fun/_leray.py:8-136: P(u^) = u^ + ik p^, p^ = -inv_lap (ik . u^),
+    inv_lap = 0 at k = 0 (GPU kernel exgb_leray; Laplace order 2)."""
 
     def __init__(self, num_spatial_dims, num_points, *, derivative_operator, order=2):
         super().__init__(num_spatial_dims, num_points)
+        self.order = order
         lap = build_laplace_operator(derivative_operator, order=order)
         with np.errstate(divide="ignore", invalid="ignore"):
             self.inv_laplacian = np.where(lap != 0, 1.0 / lap, 0.0)
         self.derivative_operator = derivative_operator
+        self._domain_extent = _extent_from_derivative(derivative_operator, num_points)
 
-    def __call__(self, u_hat):
-        raise NotImplementedError("the 3D Leray projection is not built in this version of exponax_gb300")
+    def _eval(self, u_hat, batched: bool):
+        if self.order != 2:
+            raise NotImplementedError("the GPU Leray projection uses the order-2 Laplacian")
+        t, back = _device.to_device(u_hat, "complex64")
+        D = self.num_spatial_dims
+        if t.shape[-D - 1] != D:
+            raise ValueError("Leray projection needs as many channels as spatial dimensions")
+        count = t.shape[0] if batched else 1
+        out = _device.empty(t.shape, "complex64")
+        check(load().exgb_leray(_device.stream(), D, self.num_points, self._domain_extent, count, _device.ptr(t),
+                                _device.ptr(out)), "Leray")
+        return back(out)
+
+
+class ProjectedConvection3d(BaseNonlinearFun):
+    """nonlin_fun/_projected_convection.py:19-136: P F[u x (curl u)]."""
+
+    _kind = NL_PROJECTED_3D
+
+    def __init__(self, num_spatial_dims, num_points, *, derivative_operator, dealiasing_fraction=2 / 3):
+        if num_spatial_dims != 3:
+            raise ValueError("ProjectedConvection3d only supports 3 spatial dimensions.")
+        super().__init__(num_spatial_dims, num_points, dealiasing_fraction=dealiasing_fraction)
+        self.derivative_operator = derivative_operator
+        self.leray_projection = Leray(num_spatial_dims, num_points, derivative_operator=derivative_operator)
+        self._domain_extent = _extent_from_derivative(derivative_operator, num_points)
+
+    def _check_channels(self, C):
+        if C != 3:
+            raise ValueError("Number of channels in u_hat should match number of spatial dimensions")
+
+
+class ProjectedConvection3dKolmogorov(ProjectedConvection3d):
+    """nonlin_fun/_projected_convection.py:139-226: forcing gamma * scaling
+    at (0, k, 0) on the first velocity channel."""
+
+    _kind = NL_PROJECTED_3D_KOLMOGOROV
+
+    def __init__(self, num_spatial_dims, num_points, *, injection_mode=4, injection_scale=1.0,
+                 derivative_operator, dealiasing_fraction):
+        super().__init__(num_spatial_dims, num_points, derivative_operator=derivative_operator,
+                         dealiasing_fraction=dealiasing_fraction)
+        self.injection_mode = injection_mode
+        self.injection_scale = injection_scale
+        wn = build_wavenumbers(num_spatial_dims, num_points)
+        m = (wn[0] == 0) & (wn[1] == injection_mode) & (wn[2] == 0)
+        single = np.where(m, injection_scale * build_scaling_array(3, num_points, mode="coef_extraction"), 0.0)
+        self.injection = np.concatenate([single, np.zeros_like(single), np.zeros_like(single)], axis=0)
+
+    def _nl_desc(self):
+        d = super()._nl_desc()
+        d.update(injection_mode=self.injection_mode, injection_scale=self.injection_scale)
+        return d
 
 
 def _extent_from_derivative(derivative_operator, num_points) -> float:

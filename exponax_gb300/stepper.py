@@ -13,8 +13,9 @@ import numpy as np
 from . import _device
 from ._lib import check, load
 from .etdrk import make_integrator
-from .nonlin_fun import (ConvectionNonlinearFun, GradientNormNonlinearFun, VorticityConvection2d,
-                         VorticityConvection2dKolmogorov, ZeroNonlinearFun)
+from .nonlin_fun import (ConvectionNonlinearFun, GradientNormNonlinearFun, ProjectedConvection3d,
+                         ProjectedConvection3dKolmogorov, VorticityConvection2d, VorticityConvection2dKolmogorov,
+                         ZeroNonlinearFun)
 from .spectral import (build_derivative_operator, build_gradient_inner_product_operator, build_laplace_operator,
                        spatial_shape, wavenumber_shape)
 
@@ -281,6 +282,57 @@ class KolmogorovFlowVorticity(BaseStepper):
     def _build_nonlinear_fun(self, d):
         return VorticityConvection2dKolmogorov(self.num_spatial_dims, self.num_points,
                                                convection_scale=self.convection_scale,
+                                               injection_mode=self.injection_mode,
+                                               injection_scale=self.injection_scale, derivative_operator=d,
+                                               dealiasing_fraction=self.dealiasing_fraction)
+
+
+class NavierStokesVelocity(BaseStepper):
+    """stepper/_navier_stokes.py:330-463: 3D velocity form with the projected
+    convection (Leray) nonlinearity; L = nu Lap + drag."""
+
+    def __init__(self, num_spatial_dims, domain_extent, num_points, dt, *, diffusivity=0.01, drag=0.0, order=2,
+                 dealiasing_fraction=2 / 3, num_circle_points=16, circle_radius=1.0):
+        if num_spatial_dims != 3:
+            raise ValueError(f"Expected num_spatial_dims = 3, got {num_spatial_dims}. "
+                             "For 2D, use NavierStokesVorticity instead.")
+        self.diffusivity = diffusivity
+        self.drag = drag
+        self.dealiasing_fraction = dealiasing_fraction
+        super().__init__(num_spatial_dims, domain_extent, num_points, dt, num_channels=3, order=order,
+                         num_circle_points=num_circle_points, circle_radius=circle_radius)
+
+    def _build_linear_operator(self, d):
+        return self.diffusivity * build_laplace_operator(d, order=2) + self.drag * build_laplace_operator(d, order=0)
+
+    def _build_nonlinear_fun(self, d):
+        return ProjectedConvection3d(self.num_spatial_dims, self.num_points, derivative_operator=d,
+                                     dealiasing_fraction=self.dealiasing_fraction)
+
+
+class KolmogorovFlowVelocity(BaseStepper):
+    """stepper/_navier_stokes.py:466-598: 3D Kolmogorov flow (forcing on the
+    first velocity channel at mode (0, k, 0))."""
+
+    def __init__(self, num_spatial_dims, domain_extent, num_points, dt, *, diffusivity=0.01, drag=0.0,
+                 injection_mode=4, injection_scale=1.0, order=2, dealiasing_fraction=2 / 3, num_circle_points=16,
+                 circle_radius=1.0):
+        if num_spatial_dims != 3:
+            raise ValueError(f"Expected num_spatial_dims = 3, got {num_spatial_dims}. "
+                             "For 2D, use KolmogorovFlowVorticity instead.")
+        self.diffusivity = diffusivity
+        self.drag = drag
+        self.injection_mode = injection_mode
+        self.injection_scale = injection_scale
+        self.dealiasing_fraction = dealiasing_fraction
+        super().__init__(num_spatial_dims, domain_extent, num_points, dt, num_channels=3, order=order,
+                         num_circle_points=num_circle_points, circle_radius=circle_radius)
+
+    def _build_linear_operator(self, d):
+        return self.diffusivity * build_laplace_operator(d, order=2) + self.drag * build_laplace_operator(d, order=0)
+
+    def _build_nonlinear_fun(self, d):
+        return ProjectedConvection3dKolmogorov(self.num_spatial_dims, self.num_points,
                                                injection_mode=self.injection_mode,
                                                injection_scale=self.injection_scale, derivative_operator=d,
                                                dealiasing_fraction=self.dealiasing_fraction)

@@ -50,6 +50,8 @@ extern "C" {
 #define EXGB_NL_GENERAL 4            /* GeneralNonlinearFun         _general_nonlinear.py:9-119 */
 #define EXGB_NL_VORTICITY_2D 5       /* VorticityConvection2d       _vorticity_convection.py:8-99 */
 #define EXGB_NL_VORTICITY_2D_KOLMOGOROV 6 /* VorticityConvection2dKolmogorov :102-182 */
+#define EXGB_NL_PROJECTED_3D 7       /* ProjectedConvection3d       _projected_convection.py:19-136 */
+#define EXGB_NL_PROJECTED_3D_KOLMOGOROV 8 /* ProjectedConvection3dKolmogorov :139-226 */
 
 typedef struct exgb_plan exgb_plan;
 
@@ -166,6 +168,12 @@ int exgb_repeat_fourier_noalloc(const exgb_plan* plan, void* stream, const void*
  * (_utils.py:92-186 under jax.vmap).  Items are scheduled longest-first. */
 int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, int32_t nsteps,
                        int32_t include_init, void* stream);
+
+/* Leray projection (nonlin_fun/_leray.py:114-136, order 2): for `count`
+ * vector fields of D = 2 or 3 channels in Fourier space (count, D, N..., N/2+1),
+ * v^ <- v^ + ik p^, p^ = -(ik . v^) / Lap with 1/Lap = 0 at k = 0. */
+int exgb_leray(void* stream, int num_spatial_dims, int num_points, double domain_extent, int64_t count,
+               const void* in, void* out);
 
 /* map_between_resolutions (_interpolation.py:195-285) for D = 1, 2:
  * spectral re-sampling of count = B*C fields from N_old to N_new points. */

@@ -92,6 +92,9 @@ def test_plan_desc_layout_matches_c_header():
     ("Diffusion", (2, 1.0, 32, 0.1), {"diffusivity": 0.02}),
     ("Dispersion", (1, 1.0, 32, 0.1), {}),
     ("HyperDiffusion", (1, 1.0, 32, 0.1), {}),
+    ("NavierStokesVelocity", (3, 2 * np.pi, 16, 0.01), {"diffusivity": 0.01}),
+    ("KolmogorovFlowVelocity", (3, 2 * np.pi, 16, 0.01), {}),
+    ("Diffusion", (3, 1.0, 16, 0.1), {"diffusivity": 0.02}),
 ])
 def test_host_linear_operator_matches_oracle(cls, args, kw):
     mine = getattr(ex.stepper, cls)(*args, **kw)
