@@ -492,20 +492,19 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
 
 using namespace exgb;
 
-extern "C" int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, int32_t nsteps,
-                                  int32_t include_init, void* stream) {
+namespace exgb {
+
+// Groups consecutive instances of the same plan with evenly strided buffers
+// into items of up to m instances and sorts the items longest first.
+static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps, int include_init,
+                       std::vector<Item1D>& sorted, size_t& smem, int& sm_count) {
   if (n_items < 0 || (n_items > 0 && !items)) return fail(EXGB_EINVAL, "bad work item list");
   if (nsteps < 0) return fail(EXGB_EINVAL, "nsteps must be >= 0");
-  if (n_items == 0) return EXGB_OK;
-  cudaStream_t st = (cudaStream_t)stream;
-  // group consecutive instances of the same plan with contiguous buffers?
-  // Instances are independent; pack up to m of the same plan per item only
-  // when their buffers are evenly strided, else one instance per item.
   const int T = nsteps + (include_init ? 1 : 0);
   std::vector<Item1D> its;
   std::vector<double> cost;
-  size_t smem = 0;
-  int sm_count = 0;
+  smem = 0;
+  sm_count = 0;
   for (int64_t i = 0; i < n_items;) {
     const exgb_plan* p = items[i].plan;
     if (!p || !items[i].u0 || !items[i].traj) return fail(EXGB_EINVAL, "work item with NULL plan or buffer");
@@ -530,12 +529,86 @@ extern "C" int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, 
     smem = std::max(smem, smem_for(p->dev, m, false));
     i += m;
   }
-  // longest-processing-time first
   std::vector<size_t> idx(its.size());
   for (size_t k = 0; k < idx.size(); ++k) idx[k] = k;
   std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
-  std::vector<Item1D> sorted;
+  sorted.clear();
   sorted.reserve(its.size());
   for (size_t k : idx) sorted.push_back(its[k]);
-  return launch_items(sorted, smem, st, nsteps, MODE_TRAJ, 1, include_init, sm_count, false);
+  if (smem > (size_t)smem_limit() - 2048)
+    return fail(EXGB_EUNSUPPORTED, "1D state does not fit in shared memory (N too large for this build)");
+  return EXGB_OK;
+}
+
+}  // namespace exgb
+
+struct exgb_queue {
+  exgb::Item1D* d_items = nullptr;
+  int* d_head = nullptr;
+  int n_items = 0;
+  size_t smem = 0;
+  int grid = 1;
+  int nsteps = 0;
+  int include_init = 0;
+};
+
+extern "C" int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, int32_t nsteps,
+                                  int32_t include_init, void* stream) {
+  if (n_items == 0) return EXGB_OK;
+  std::vector<Item1D> sorted;
+  size_t smem = 0;
+  int sm_count = 0;
+  const int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count);
+  if (rc) return rc;
+  return launch_items(sorted, smem, (cudaStream_t)stream, nsteps, MODE_TRAJ, 1, include_init, sm_count, false);
+}
+
+extern "C" int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, int32_t nsteps, int32_t include_init,
+                                  exgb_queue** out) {
+  if (!out) return fail(EXGB_EINVAL, "NULL argument");
+  *out = nullptr;
+  if (n_items < 1) return fail(EXGB_EINVAL, "empty work item list");
+  std::vector<Item1D> sorted;
+  size_t smem = 0;
+  int sm_count = 0;
+  int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count);
+  if (rc) return rc;
+  exgb_queue* q = new exgb_queue();
+  q->n_items = (int)sorted.size();
+  q->smem = smem;
+  q->nsteps = nsteps;
+  q->include_init = include_init ? 1 : 0;
+  cudaError_t e;
+  if ((e = cudaMalloc(&q->d_items, sizeof(Item1D) * sorted.size())) != cudaSuccess ||
+      (e = cudaMalloc(&q->d_head, sizeof(int))) != cudaSuccess ||
+      (e = cudaMemcpy(q->d_items, sorted.data(), sizeof(Item1D) * sorted.size(), cudaMemcpyHostToDevice)) !=
+          cudaSuccess ||
+      (e = cudaFuncSetAttribute(etdrk1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+          cudaSuccess) {
+    exgb_queue_destroy(q);
+    return cuda_fail(e, "exgb_queue_prepare");
+  }
+  int per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, etdrk1d_kernel, 256, smem) != cudaSuccess) per_sm = 1;
+  q->grid = (int)std::min<int64_t>((int64_t)sorted.size(), (int64_t)sm_count * std::max(1, per_sm));
+  *out = q;
+  return EXGB_OK;
+}
+
+extern "C" int exgb_queue_launch(exgb_queue* q, void* stream) {
+  if (!q) return fail(EXGB_EINVAL, "NULL queue");
+  cudaStream_t st = (cudaStream_t)stream;
+  EXGB_CUDA(cudaMemsetAsync(q->d_head, 0, sizeof(int), st));
+  etdrk1d_kernel<<<q->grid, 256, q->smem, st>>>(q->d_items, q->n_items, q->d_head, q->nsteps, MODE_TRAJ, 1,
+                                                q->include_init, 0);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+extern "C" int exgb_queue_destroy(exgb_queue* q) {
+  if (!q) return EXGB_OK;
+  cudaFree(q->d_items);
+  cudaFree(q->d_head);
+  delete q;
+  return EXGB_OK;
 }

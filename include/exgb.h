@@ -169,6 +169,18 @@ int exgb_repeat_fourier_noalloc(const exgb_plan* plan, void* stream, const void*
 int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, int32_t nsteps,
                        int32_t include_init, void* stream);
 
+/* The same launch split in two so that it can be captured in a CUDA graph:
+ * exgb_queue_prepare uploads the (sorted) item list once into a queue object
+ * (allocates); exgb_queue_launch resets the queue head and launches the
+ * persistent kernel (two stream operations, no allocation, no host
+ * synchronisation: capturable by cudaStreamBeginCapture / torch.cuda.graph).
+ * A prepared queue may be launched any number of times, not concurrently. */
+typedef struct exgb_queue exgb_queue;
+int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, int32_t nsteps, int32_t include_init,
+                       exgb_queue** out);
+int exgb_queue_launch(exgb_queue* queue, void* stream);
+int exgb_queue_destroy(exgb_queue* queue);
+
 /* Leray projection (nonlin_fun/_leray.py:114-136, order 2): for `count`
  * vector fields of D = 2 or 3 channels in Fourier space (count, D, N..., N/2+1),
  * v^ <- v^ + ik p^, p^ = -(ik . v^) / Lap with 1/Lap = 0 at k = 0. */
