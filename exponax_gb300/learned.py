@@ -1,0 +1,266 @@
+"""Learned coarse-step correction for 2D Kolmogorov flow.
+
+A small periodic convolutional residual network corrects every coarse
+(64^2, dt = 0.04) ETDRK2 step:  u_{n+1} = v + out_scale * NN(in_scale * v),
+v = coarse_step(u_n).  Network: 3x3 periodic convolutions 1 -> 48 -> 48 x 4
+-> 1 with GELU (six layers, ~84 k parameters), BF16 weights and
+activations, FP32 accumulation; the 48 -> 48 layers run on the tensor cores
+(exgb_conv48).  Training (Adam, lr 1e-3, mean squared error against the
+downsampled fine solution) and inference use only the kernels of
+libexgb.so.  A spectral-energy guard replaces a corrected state by the plain
+coarse state when the correction puts too much energy above |k| > kg or is
+not finite.
+
+No counterpart in the reference (its closest precedent is the 1D CNN
+emulator notebook); the plain method (exponax_gb300.stepper) generates the
+training data and judges the error.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _device
+from ._lib import check, load
+
+C = 48
+NMID = 4
+TAPS = 9
+
+
+def _lib():
+    lib = load()
+    if not hasattr(lib, "_conv_sigs"):
+        V, I, I64, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
+        sigs = {
+            "exgb_conv48": [V, V, I, I, V, V, I, V, V, V],
+            "exgb_conv_in1": [V, V, I, I, V, V, V, V],
+            "exgb_conv_out1": [V, V, I, I, V, V, V, F, V],
+            "exgb_conv_out1_bwd_data": [V, V, I, I, V, V, V],
+            "exgb_wgrad": [V, I, V, V, I, I, V, V, V, V],
+            "exgb_adam": [V, V, V, V, V, I64, F, F, F, F, I64, V, V, I],
+            "exgb_cast_weights": [V, V, I64, V, V, I],
+            "exgb_mse": [V, V, V, I64, F, V, V, I],
+            "exgb_guard": [V, V, V, I, I, I, F, V, V, V],
+        }
+        for name, args in sigs.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        lib._conv_sigs = True
+    return lib
+
+
+def _p(t):
+    return ctypes.c_void_p(int(t.data_ptr()))
+
+
+class PeriodicConvCorrector:
+    """Parameters live in one FP32 device buffer (plus Adam moments and bf16
+    working copies); activations for up to `max_batch` samples are kept for
+    the backward pass."""
+
+    def __init__(self, H: int = 64, *, seed: int = 0, max_batch: int = 256, in_scale: float = 1.0,
+                 out_scale: float = 1.0):
+        torch = _device.torch()
+        _device.require_cuda()
+        if H % 4:
+            raise ValueError("grid height must be a multiple of 4")
+        self.H, self.Wd = H, 64
+        self.in_scale, self.out_scale = float(in_scale), float(out_scale)
+        self.max_batch = int(max_batch)
+        # parameter layout: W1 (9,48), b1 (48), [Wm (9,48,48), bm (48)] x 4, W6 (9,48), b6 (1)
+        sizes = [("W1", TAPS * C), ("b1", C)]
+        for i in range(NMID):
+            sizes += [(f"W{i + 2}", TAPS * C * C), (f"b{i + 2}", C)]
+        sizes += [("W6", TAPS * C), ("b6", 1)]
+        self.layout = {}
+        off = 0
+        for name, n in sizes:
+            self.layout[name] = (off, n)
+            off += n
+        self.num_params = off
+        rng = np.random.default_rng(seed)
+        init = np.zeros(off, np.float32)
+        for name, (o, n) in self.layout.items():
+            if name.startswith("W"):
+                fan_in = TAPS * (1 if name == "W1" else C)
+                gain = np.sqrt(2.0) if name != "W6" else 0.1  # small last layer: start near the plain method
+                init[o:o + n] = rng.standard_normal(n) * gain / np.sqrt(fan_in)
+        dev = "cuda"
+        self.w = torch.from_numpy(init).to(dev)
+        self.g = torch.zeros_like(self.w)
+        self.m = torch.zeros_like(self.w)
+        self.v = torch.zeros_like(self.w)
+        self.t = 0
+        self.w16 = [torch.empty(TAPS * C * C, dtype=torch.bfloat16, device=dev) for _ in range(NMID)]
+        self.wflip = [torch.empty(TAPS * C * C, dtype=torch.bfloat16, device=dev) for _ in range(NMID)]
+        self._alloc(self.max_batch)
+        self._cast()
+
+    # ------------------------------------------------------------------ buffers
+    def _alloc(self, B):
+        torch = _device.torch()
+        px = B * self.H * self.Wd
+        bf = dict(dtype=torch.bfloat16, device="cuda")
+        self.pre = [torch.empty(px * C, **bf) for _ in range(NMID + 1)]
+        self.h = [torch.empty(px * C, **bf) for _ in range(NMID + 1)]
+        self.dpre = [torch.empty(px * C, **bf) for _ in range(2)]
+        self.x0 = torch.empty(px, dtype=torch.float32, device="cuda")
+        self.out = torch.empty(px, dtype=torch.float32, device="cuda")
+        self.dout = torch.empty(px, dtype=torch.float32, device="cuda")
+        nchunk = (px + 511) // 512
+        self.part = torch.empty(nchunk * TAPS * C * C, dtype=torch.float32, device="cuda")
+        self.part_b = torch.empty(nchunk * C, dtype=torch.float32, device="cuda")
+        self.loss_part = torch.empty(1024, dtype=torch.float32, device="cuda")
+
+    def _view(self, t, name):
+        o, n = self.layout[name]
+        return t[o:o + n]
+
+    def _cast(self):
+        lib = _lib()
+        s = _device.stream()
+        for i in range(NMID):
+            wv = self._view(self.w, f"W{i + 2}")
+            check(lib.exgb_cast_weights(s, _p(wv), wv.numel(), _p(self.w16[i]), _p(self.wflip[i]), 1), "cast")
+
+    def set_params(self, flat: np.ndarray):
+        torch = _device.torch()
+        self.w.copy_(torch.from_numpy(np.asarray(flat, np.float32)))
+        self._cast()
+
+    def params_numpy(self):
+        """Parameters in the oracle's layout: list of (w, b) arrays."""
+        w = self.w.cpu().numpy().astype(np.float64)
+        out = []
+        for i in range(NMID + 2):
+            wn, bn = f"W{i + 1}", f"b{i + 1}"
+            wo, wl = self.layout[wn]
+            bo, bl = self.layout[bn]
+            if i == 0:
+                ww = w[wo:wo + wl].reshape(TAPS, C, 1)
+            elif i == NMID + 1:
+                ww = w[wo:wo + wl].reshape(TAPS, 1, C)
+            else:
+                ww = w[wo:wo + wl].reshape(TAPS, C, C)
+            out.append((ww, w[bo:bo + bl]))
+        return out
+
+    # ------------------------------------------------------------------ forward / backward
+    def forward(self, v, out=None):
+        """v: (B, H, 64) float32 CUDA tensor -> corrected state (B, H, 64)."""
+        torch = _device.torch()
+        lib = _lib()
+        s = _device.stream()
+        v = v.contiguous()
+        B = v.shape[0]
+        if B > self.max_batch:
+            self.max_batch = B
+            self._alloc(B)
+        H = self.H
+        torch.mul(v.reshape(-1), self.in_scale, out=self.x0[:B * H * 64])
+        check(lib.exgb_conv_in1(s, _p(self.x0), B, H, _p(self._view(self.w, "W1")), _p(self._view(self.w, "b1")),
+                                _p(self.pre[0]), _p(self.h[0])), "conv_in1")
+        for i in range(NMID):
+            check(lib.exgb_conv48(s, _p(self.h[i]), B, H, _p(self.w16[i]), _p(self._view(self.w, f"b{i + 2}")), 0,
+                                  None, _p(self.pre[i + 1]), _p(self.h[i + 1])), "conv48")
+        if out is None:
+            out = torch.empty_like(v)
+        check(lib.exgb_conv_out1(s, _p(self.h[NMID]), B, H, _p(self._view(self.w, "W6")),
+                                 _p(self._view(self.w, "b6")), _p(v), self.out_scale, _p(out)), "conv_out1")
+        self._B = B
+        return out
+
+    __call__ = forward
+
+    def loss_and_grads(self, v, target):
+        """Forward, MSE loss against `target` and all parameter gradients (in self.g)."""
+        torch = _device.torch()
+        lib = _lib()
+        s = _device.stream()
+        pred = self.forward(v)
+        B, H = self._B, self.H
+        n = B * H * 64
+        nb = 256
+        check(lib.exgb_mse(s, _p(pred), _p(target.contiguous()), n, self.out_scale, _p(self.dout),
+                           _p(self.loss_part), nb), "mse")
+        # last layer (48 -> 1)
+        check(lib.exgb_wgrad(s, 2, _p(self.dout), _p(self.h[NMID]), B, H, _p(self.part), _p(self.part_b),
+                             _p(self._view(self.g, "W6")), _p(self._view(self.g, "b6"))), "wgrad6")
+        check(lib.exgb_conv_out1_bwd_data(s, _p(self.dout), B, H, _p(self._view(self.w, "W6")),
+                                          _p(self.pre[NMID]), _p(self.dpre[0])), "bwd6")
+        cur = 0
+        for i in range(NMID - 1, -1, -1):
+            # layer i+2: input h[i], output pre[i+1]; dpre[cur] = dL/dpre[i+1]
+            check(lib.exgb_wgrad(s, 0, _p(self.dpre[cur]), _p(self.h[i]), B, H, _p(self.part), _p(self.part_b),
+                                 _p(self._view(self.g, f"W{i + 2}")), _p(self._view(self.g, f"b{i + 2}"))),
+                  "wgrad48")
+            check(lib.exgb_conv48(s, _p(self.dpre[cur]), B, H, _p(self.wflip[i]), None, 1, _p(self.pre[i]),
+                                  _p(self.dpre[1 - cur]), None), "conv48 bwd")
+            cur = 1 - cur
+        check(lib.exgb_wgrad(s, 1, _p(self.dpre[cur]), _p(self.x0), B, H, _p(self.part), _p(self.part_b),
+                             _p(self._view(self.g, "W1")), _p(self._view(self.g, "b1"))), "wgrad1")
+        loss = self.loss_part[:nb].sum() / n
+        return loss, pred
+
+    def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        lib = _lib()
+        s = _device.stream()
+        self.t += 1
+        check(lib.exgb_adam(s, _p(self.w), _p(self.m), _p(self.v), _p(self.g), self.num_params, lr, b1, b2, eps,
+                            self.t, None, None, 0), "adam")
+        self._cast()
+
+    def train_step(self, v, target, lr=1e-3):
+        loss, _ = self.loss_and_grads(v, target)
+        self.adam_step(lr)
+        return loss
+
+    def save(self, path):
+        np.savez(path, w=self.w.cpu().numpy(), m=self.m.cpu().numpy(), v=self.v.cpu().numpy(), t=self.t,
+                 in_scale=self.in_scale, out_scale=self.out_scale)
+
+    def load(self, path):
+        torch = _device.torch()
+        d = np.load(path)
+        self.w.copy_(torch.from_numpy(d["w"]))
+        self.m.copy_(torch.from_numpy(d["m"]))
+        self.v.copy_(torch.from_numpy(d["v"]))
+        self.t = int(d["t"])
+        self.in_scale, self.out_scale = float(d["in_scale"]), float(d["out_scale"])
+        self._cast()
+
+
+class GuardedCorrectedStepper:
+    """Coarse ETDRK2 step followed by the corrector, with the spectral-energy
+    guard: a sample whose correction carries more than `thresh` of the plain
+    state's energy above |k| > kg (or is not finite) keeps the plain step."""
+
+    def __init__(self, coarse_stepper, corrector: PeriodicConvCorrector, *, kg: int = 16, thresh: float = 0.05):
+        self.coarse = coarse_stepper
+        self.net = corrector
+        self.kg, self.thresh = int(kg), float(thresh)
+        self.trips = 0
+
+    def step(self, u):
+        """u: (B, 1, H, 64) -> (B, 1, H, 64)."""
+        from ._utils import vmap
+        from .spectral import fft
+
+        torch = _device.torch()
+        lib = _lib()
+        plain = vmap(self.coarse)(u)
+        B, _, H, Wd = plain.shape
+        corrected = self.net(plain.reshape(B, H, Wd)).reshape(B, 1, H, Wd)
+        corr_hat = fft((corrected - plain).reshape(B, H, Wd), num_spatial_dims=2)
+        plain_hat = fft(plain.reshape(B, H, Wd), num_spatial_dims=2)
+        tripped = torch.empty(B, dtype=torch.int32, device="cuda")
+        check(lib.exgb_guard(_device.stream(), _p(corr_hat), _p(plain_hat), B, H, self.kg, self.thresh, _p(plain),
+                             _p(corrected), _p(tripped)), "guard")
+        self.last_tripped = tripped
+        return corrected
+
+    __call__ = step
