@@ -46,6 +46,23 @@ class RandomTruncatedFourierSeries:
     def __call__(self, num_points: int, *, key: int) -> np.ndarray:
         if self.num_spatial_dims == 1:
             u = RandomSineWaves1d(1, cutoff=self.cutoff)(num_points, key=key)[0]
+        elif self.num_spatial_dims == 2:
+            # same draws and modes as the general branch, summed by an inverse
+            # real FFT instead of mode by mode
+            rng = np.random.default_rng(key)
+            c, N = self.cutoff, num_points
+            H = np.zeros((N, N // 2 + 1), dtype=np.complex128)
+            for m in np.ndindex(2 * c + 1, 2 * c + 1):
+                kx, ky = m[0] - c, m[1] - c
+                if (kx, ky) == (0, 0) or ky < 0 or (ky == 0 and kx < 0):
+                    continue
+                a = rng.uniform(-1.0, 1.0)
+                phi = rng.uniform(0.0, 2 * np.pi)
+                z = 0.5 * a * np.exp(1j * phi) * N * N
+                H[kx % N, ky] += z
+                if ky == 0:
+                    H[(-kx) % N, 0] += np.conj(z)
+            u = np.fft.irfft2(H, s=(N, N))
         else:
             rng = np.random.default_rng(key)
             c = self.cutoff

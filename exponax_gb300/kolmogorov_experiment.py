@@ -1,0 +1,205 @@
+"""Learned coarse-step correction of 2D Kolmogorov flow, end to end on the GPU.
+
+    python -m exponax_gb300.kolmogorov_experiment --train-traj 2000 --eval-traj 256 --epochs 4 \
+        --out results.json
+
+1. Fine plain runs (KolmogorovFlowVorticity 512^2, dt = 0.005, ETDRK2,
+   nu = 1e-3, drag -0.1, forcing k = 4, amplitude 1) from random truncated
+   Fourier ICs (cutoff 5): `spinup` steps, then `n_coarse` x 8 steps,
+   downsampled to 64^2 (map_between_resolutions) every 8 steps.
+2. Training pairs (c_t, c_{t+1}); inputs v = plain coarse step (64^2,
+   dt = 0.04) of c_t, targets c_{t+1}.  Adam, lr 1e-3, mean squared error.
+3. Evaluation on held-out seeds: rollouts of `n_coarse` coarse steps of the
+   plain 64^2 stepper and of the learned (guarded) 64^2 stepper against the
+   downsampled fine solution: relative L2 per step, correlation, correlation
+   time (first step with mean correlation < 0.8), GPU time of the learned
+   64^2 rollout against the plain 512^2 run over the same physical time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import _device, ic, stepper
+from ._lib import check, load
+from ._utils import rollout, vmap
+from .interpolation import map_between_resolutions_batched
+from .learned import GuardedCorrectedStepper, PeriodicConvCorrector
+from .spectral import fft, ifft
+
+KW = dict(diffusivity=1e-3, drag=-0.1, injection_mode=4, injection_scale=1.0)
+
+
+def _events():
+    torch = _device.torch()
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def fine_coarse_trajectories(seeds, *, n_fine=512, n_coarse_grid=64, dt=0.005, ratio=8, spinup=1000, n_coarse=200,
+                             batch=256):
+    """Downsampled fine trajectories (len(seeds), n_coarse + 1, n_coarse_grid, n_coarse_grid) on the GPU, and
+    the GPU milliseconds of the post-spin-up fine steps."""
+    torch = _device.torch()
+    fine = stepper.KolmogorovFlowVorticity(2, 2 * np.pi, n_fine, dt, **KW)
+    h = fine.plan.handle
+    lib = load()
+    g = ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    out = torch.empty((len(seeds), n_coarse + 1, n_coarse_grid, n_coarse_grid), dtype=torch.float32, device="cuda")
+    fine_ms = 0.0
+    for b0 in range(0, len(seeds), batch):
+        sb = seeds[b0:b0 + batch]
+        B = len(sb)
+        u0 = torch.from_numpy(np.stack([g(n_fine, key=int(s)) for s in sb])).cuda()
+        uh = fft(u0, num_spatial_dims=2)
+        tmp = torch.empty_like(uh)
+        check(lib.exgb_repeat_fourier(h, _device.stream(), uh.data_ptr(), tmp.data_ptr(), B, spinup), "spin-up")
+        uh, tmp = tmp, uh
+        for t in range(n_coarse + 1):
+            if t > 0:
+                e0, e1 = _events()
+                e0.record()
+                check(lib.exgb_repeat_fourier(h, _device.stream(), uh.data_ptr(), tmp.data_ptr(), B, ratio), "fine")
+                e1.record()
+                uh, tmp = tmp, uh
+                torch.cuda.synchronize()
+                fine_ms += e0.elapsed_time(e1)
+            phys = ifft(uh, num_spatial_dims=2, num_points=n_fine)  # (B, 1, N, N)
+            out[b0:b0 + B, t] = map_between_resolutions_batched(phys, n_coarse_grid)[:, 0]
+    return out, fine_ms
+
+
+def train(net, coarse, data, *, epochs=4, batch=256, lr=1e-3, seed=0, log=None):
+    """data: (T, n_coarse + 1, H, W) coarse snapshots."""
+    torch = _device.torch()
+    T, S, H, W = data.shape
+    x = data[:, :-1].reshape(-1, 1, H, W)
+    y = data[:, 1:].reshape(-1, H, W)
+    v = torch.empty_like(x)
+    for i in range(0, x.shape[0], 4096):
+        v[i:i + 4096] = vmap(coarse)(x[i:i + 4096])
+    v = v.reshape(-1, H, W)
+    net.in_scale = float(1.0 / v.std())
+    net.out_scale = float((y - v).std())
+    rng = np.random.default_rng(seed)
+    n = v.shape[0]
+    hist = []
+    for ep in range(epochs):
+        perm = torch.from_numpy(rng.permutation(n)).cuda()
+        tot, cnt = 0.0, 0
+        for i in range(0, n - batch + 1, batch):
+            idx = perm[i:i + batch]
+            loss = net.train_step(v[idx], y[idx], lr=lr)
+            if (i // batch) % 50 == 0:
+                tot += float(loss)
+                cnt += 1
+        hist.append(tot / max(cnt, 1))
+        if log:
+            log(f"epoch {ep}: mean loss {hist[-1]:.3e} (normalised by out_scale^2: {hist[-1] / net.out_scale ** 2:.3e})")
+    return hist
+
+
+def evaluate(ref, coarse, net, *, kg=16, thresh=0.05):
+    """ref: (B, S, H, W) downsampled fine trajectories.  Returns metrics and GPU ms."""
+    torch = _device.torch()
+    B, S, H, W = ref.shape
+    u0 = ref[:, 0:1].contiguous()  # (B, 1, H, W)
+    roll = vmap(rollout(coarse, S - 1, include_init=True))
+    e0, e1 = _events()
+    e0.record()
+    plain = roll(u0)[:, :, 0]  # (B, S, H, W)
+    e1.record()
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    gs = GuardedCorrectedStepper(coarse, net, kg=kg, thresh=thresh)
+    learned = torch.empty_like(ref)
+    learned[:, 0] = ref[:, 0]
+    u = u0
+    trips = 0
+    e0, e1 = _events()
+    e0.record()
+    for t in range(1, S):
+        u = gs(u)
+        learned[:, t] = u[:, 0]
+        trips += gs.last_tripped.sum()
+    e1.record()
+    torch.cuda.synchronize()
+    learned_ms = e0.elapsed_time(e1)
+
+    def metrics(pred):
+        d = (pred - ref).reshape(B, S, -1)
+        r = ref.reshape(B, S, -1)
+        rel = (d.norm(dim=2) / r.norm(dim=2)).mean(dim=0)  # per step, mean over seeds
+        p = pred.reshape(B, S, -1)
+        corr = ((p * r).sum(dim=2) / (p.norm(dim=2) * r.norm(dim=2))).mean(dim=0)
+        below = (corr < 0.8).nonzero()
+        ct = int(below[0, 0]) if below.numel() else S - 1
+        return rel.cpu().numpy(), corr.cpu().numpy(), ct
+
+    rp, cp, ctp = metrics(plain)
+    rl, cl, ctl = metrics(learned)
+    return {"plain": (rp, cp, ctp), "learned": (rl, cl, ctl), "plain_ms": plain_ms, "learned_ms": learned_ms,
+            "guard_trips": int(trips), "guard_checks": int(B * (S - 1))}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train-traj", type=int, default=2000)
+    ap.add_argument("--eval-traj", type=int, default=256)
+    ap.add_argument("--spinup", type=int, default=1000)
+    ap.add_argument("--n-coarse", type=int, default=200)
+    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--batch", type=int, default=256)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default="kolmogorov_experiment.json")
+    a = ap.parse_args()
+    torch = _device.torch()
+
+    def log(msg):
+        print(f"[{time.strftime('%H:%M:%S')}] {msg}", flush=True)
+
+    coarse = stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.04, **KW)
+    t0 = time.time()
+    train_data, train_fine_ms = fine_coarse_trajectories(list(range(a.train_traj)), spinup=a.spinup,
+                                                         n_coarse=a.n_coarse)
+    log(f"training data: {tuple(train_data.shape)} in {time.time() - t0:.1f} s wall")
+    net = PeriodicConvCorrector(64, seed=0, max_batch=a.batch)
+    t0 = time.time()
+    hist = train(net, coarse, train_data, epochs=a.epochs, batch=a.batch, lr=a.lr, log=log)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    log(f"trained {a.epochs} epochs in {train_s:.1f} s")
+    del train_data
+    seeds = list(range(10_000_000, 10_000_000 + a.eval_traj))
+    ref, fine_ms = fine_coarse_trajectories(seeds, spinup=a.spinup, n_coarse=a.n_coarse)
+    res = evaluate(ref, coarse, net)
+    rp, cp, ctp = res["plain"]
+    rl, cl, ctl = res["learned"]
+    steps = [1, 10, 50, 100, a.n_coarse]
+    out = {
+        "config": {"fine": "KolmogorovFlowVorticity 512^2 dt=0.005 ETDRK2", "coarse": "64^2 dt=0.04 ETDRK2",
+                   "train_trajectories": a.train_traj, "eval_trajectories": a.eval_traj, "spinup": a.spinup,
+                   "coarse_steps": a.n_coarse, "epochs": a.epochs, "batch": a.batch, "lr": a.lr,
+                   "network": "6-layer periodic 3x3 CNN, 48 channels, GELU, residual, bf16, "
+                              f"{net.num_params} parameters"},
+        "train_loss_per_epoch": hist, "train_seconds": train_s,
+        "rel_l2_plain_64": {str(s): float(rp[s]) for s in steps},
+        "rel_l2_learned_64": {str(s): float(rl[s]) for s in steps},
+        "mean_rel_l2_plain_64": float(rp[1:].mean()), "mean_rel_l2_learned_64": float(rl[1:].mean()),
+        "correlation_time_plain_64": ctp, "correlation_time_learned_64": ctl, "correlation_threshold": 0.8,
+        "plain_512_rel_l2": 0.0,
+        "gpu_ms_plain_512_for_eval_horizon": fine_ms, "gpu_ms_learned_64": res["learned_ms"],
+        "gpu_ms_plain_64": res["plain_ms"],
+        "gpu_time_ratio_plain512_over_learned64": fine_ms / res["learned_ms"],
+        "guard_trips": res["guard_trips"], "guard_checks": res["guard_checks"],
+    }
+    with open(a.out, "w") as f:
+        json.dump(out, f, indent=1)
+    log(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()
