@@ -178,7 +178,7 @@ def main():
     res = evaluate(ref, coarse, net)
     rp, cp, ctp = res["plain"]
     rl, cl, ctl = res["learned"]
-    steps = [1, 10, 50, 100, a.n_coarse]
+    steps = sorted({s for s in (1, 10, 50, 100, a.n_coarse) if s <= a.n_coarse})
     out = {
         "config": {"fine": "KolmogorovFlowVorticity 512^2 dt=0.005 ETDRK2", "coarse": "64^2 dt=0.04 ETDRK2",
                    "train_trajectories": a.train_traj, "eval_trajectories": a.eval_traj, "spinup": a.spinup,
