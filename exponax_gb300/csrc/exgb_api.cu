@@ -2,6 +2,7 @@
 // phi-coefficient kernel of libexgb.so.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -439,3 +440,59 @@ int exgb_plan_get_table(const exgb_plan* plan, int which, void* host_out, size_t
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- autotuner knobs
+extern "C" int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int n) {
+  if (!plan || (n > 0 && !values)) return fail(EXGB_EINVAL, "NULL argument");
+  if (kind == EXGB_TUNE_RADICES) {
+    if (n < 1 || n > kMaxPass) return fail(EXGB_EINVAL, "bad number of radix passes");
+    long prod = 1;
+    for (int i = 0; i < n; ++i) {
+      const int r = values[i];
+      if (r != 2 && r != 3 && r != 4 && r != 5 && r != 8) return fail(EXGB_EINVAL, "radices must be 2, 3, 4, 5 or 8");
+      prod *= r;
+    }
+    if (prod != plan->dev.N) return fail(EXGB_EINVAL, "radices must multiply to N");
+    plan->dev.fft.npass = n;
+    for (int i = 0; i < n; ++i) plan->dev.fft.radix[i] = values[i];
+    EXGB_CUDA(cudaMemcpy(plan->d_dev, &plan->dev, sizeof(PlanDev), cudaMemcpyHostToDevice));
+    return EXGB_OK;
+  }
+  if (kind == EXGB_TUNE_CLUSTER) {
+    if (plan->dev.D != 2 || plan->dev.kind == EXGB_NL_ZERO || plan->dev.order == 0)
+      return fail(EXGB_EUNSUPPORTED, "cluster size applies to 2D nonlinear plans");
+    const int G = n > 0 ? values[0] : 0;
+    if (G != 0 && G != 1 && G != 2 && G != 4 && G != 8) return fail(EXGB_EINVAL, "cluster size must be 1, 2, 4 or 8");
+    EXGB_CUDA(cudaDeviceSynchronize());
+    cudaFree(plan->d_scratch);
+    plan->d_scratch = nullptr;
+    const int old = plan->tune_cluster;
+    plan->tune_cluster = G;
+    int rc = etdrk2d_configure(plan);
+    if (rc || (G && plan->cfg2d.variant == 1 && plan->cfg2d.G != G)) {
+      cudaFree(plan->d_scratch);
+      plan->d_scratch = nullptr;
+      plan->tune_cluster = old;
+      const int rc2 = etdrk2d_configure(plan);
+      if (rc2) return rc2;
+      return fail(EXGB_EUNSUPPORTED, "this cluster size does not fit the plan");
+    }
+    return EXGB_OK;
+  }
+  if (kind == EXGB_TUNE_ITEMS_PER_CTA) {
+    if (plan->dev.D != 1) return fail(EXGB_EUNSUPPORTED, "items per CTA applies to 1D plans");
+    plan->tune_items_per_cta = n > 0 ? std::max(0, std::min(64, values[0])) : 0;
+    return EXGB_OK;
+  }
+  return fail(EXGB_EINVAL, "unknown tuning kind");
+}
+
+extern "C" int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n) {
+  // out[0] = npass, out[1..npass] = radices, then cluster size, items per CTA
+  if (!plan || !out || n < 2 + kMaxPass + 1) return fail(EXGB_EINVAL, "bad output buffer");
+  out[0] = plan->dev.fft.npass;
+  for (int i = 0; i < kMaxPass; ++i) out[1 + i] = i < plan->dev.fft.npass ? plan->dev.fft.radix[i] : 0;
+  out[1 + kMaxPass] = plan->cfg2d.G;
+  out[2 + kMaxPass] = plan->tune_items_per_cta;
+  return EXGB_OK;
+}

@@ -458,7 +458,11 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
   if (nonlinear_only) mode = MODE_NONLIN;
   else if (u0_phys) mode = emit_traj ? MODE_TRAJ : MODE_FINAL;
   else mode = MODE_FOURIER;
-  const int m = choose_m(P, batch, plan->sm_count, nonlinear_only);
+  int m = choose_m(P, batch, plan->sm_count, nonlinear_only);
+  if (plan->tune_items_per_cta > 0 && !nonlinear_only) {
+    m = plan->tune_items_per_cta;
+    while (m > 1 && smem_for(P, m, false) > (size_t)smem_limit() - 4096) --m;
+  }
   const int T = nsteps + (include_init ? 1 : 0);
   std::vector<Item1D> items;
   for (int64_t b0 = 0; b0 < batch; b0 += m) {

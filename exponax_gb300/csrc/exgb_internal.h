@@ -70,6 +70,9 @@ struct exgb_plan {
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
   int sm_count = 0;
+  // autotuner overrides (0 = automatic choice)
+  int tune_cluster = 0;          // 2D: CTAs per cluster
+  int tune_items_per_cta = 0;    // 1D: instances per work item
 };
 
 namespace exgb {

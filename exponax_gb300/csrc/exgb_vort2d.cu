@@ -411,8 +411,9 @@ static int v2_configure(exgb_plan* plan) {
   cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t limit = (size_t)lim - 1024;
   const char* envG = getenv("EXGB_CLUSTER");
+  const int wantG = plan->tune_cluster > 0 ? plan->tune_cluster : (envG ? atoi(envG) : 0);
   for (int G : {1, 2, 4, 8}) {
-    if (envG && atoi(envG) != G) continue;
+    if (wantG && wantG != G) continue;
     const int Cl = (Kc + G - 1) / G;
     const int Rl = N / G;
     const int KcP = Kc | 1;

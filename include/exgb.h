@@ -112,6 +112,20 @@ int exgb_plan_get_table(const exgb_plan* plan, int which, void* host_out, size_t
 /* Largest dealiasing-mask wavenumber kept per axis (-1: no mask). */
 int exgb_plan_kmax(const exgb_plan* plan);
 
+/* Autotuner knobs (no reference counterpart; used by exponax_gb300.autotune,
+ * which times candidates on the device and caches the winner):
+ *   EXGB_TUNE_RADICES       values = radix order of the length-N Stockham FFT
+ *                           (1D kernel, transforms, generic 2D kernel)
+ *   EXGB_TUNE_CLUSTER       values[0] = CTAs per cluster of the 2D kernel (0 = auto)
+ *   EXGB_TUNE_ITEMS_PER_CTA values[0] = 1D instances per work item (0 = auto)
+ * exgb_plan_get_tuning writes npass, the kMaxPass (12) radix slots, the
+ * cluster size and the items per CTA (n >= 15). */
+#define EXGB_TUNE_RADICES 0
+#define EXGB_TUNE_CLUSTER 1
+#define EXGB_TUNE_ITEMS_PER_CTA 2
+int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int n);
+int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n);
+
 /* ---- spectral transforms ----
  * exgb_rfftn replaces spectral.fft  (_spectral.py:614-656): rfftn over the
  *   last D axes, norm="backward".

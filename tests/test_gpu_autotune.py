@@ -1,0 +1,50 @@
+"""Autotuner: candidates time on the device, the winner is applied and
+cached, and the tuned plan still matches the oracle (1e-5 per step)."""
+
+import json
+
+import numpy as np
+import pytest
+
+import exponax_gb300 as ex
+from exponax_gb300 import autotune
+from oracle import exponax_np as o
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+def test_radix_candidates_multiply_to_n():
+    for n in (60, 128, 200, 256, 4096):
+        cands = autotune.radix_candidates(n)
+        assert cands
+        for c in cands:
+            assert int(np.prod(c)) == n
+
+
+@pytest.mark.parametrize("case", ["ks1d", "ns2d"])
+def test_tune_apply_cache_and_parity(case, tmp_path, monkeypatch):
+    monkeypatch.setenv("EXGB_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
+    if case == "ks1d":
+        sm = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, 200, 0.1)
+        so = o.KuramotoSivashinskyConservative(1, 100.0, 200, 0.1)
+        u = np.stack([ex.ic.RandomSineWaves1d(1, cutoff=5)(200, key=s) for s in range(3)])
+    else:
+        sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, 128, 0.01, diffusivity=1e-3)
+        so = o.NavierStokesVorticity(2, 2 * np.pi, 128, 0.01, diffusivity=1e-3)
+        g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+        u = np.stack([g(128, key=s) for s in range(3)])
+    res = autotune.tune(sm, batch=32, nsteps=4, repeats=2)
+    assert not res["cached"] and res["best"] and len(res["timings_ms"]) >= 2
+    cache = json.load(open(tmp_path / "cache.json"))
+    assert res["key"] in cache
+    got = ex.vmap(sm)(torch.from_numpy(u).cuda()).cpu().numpy()
+    for b in range(3):
+        assert rel(got[b], so(u[b])) < 1e-5
+    again = autotune.tune(sm, batch=32, nsteps=4)
+    assert again["cached"] and again["best"] == res["best"]
