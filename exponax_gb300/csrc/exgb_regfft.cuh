@@ -157,6 +157,50 @@ __device__ __forceinline__ void group_fft(float2 (&v)[E], int l, float2* tile, c
   __syncwarp(mask);
 }
 
+// Two independent group FFTs of the same size and direction, interleaved
+// for instruction-level parallelism: shared twiddle loads, the transposes
+// one after the other through the same tile.
+template <int E, int T, bool INV>
+__device__ __forceinline__ void group_fft_x2(float2 (&v)[E], float2 (&w)[E], int l, float2* tile,
+                                             const float2* __restrict__ twl, unsigned mask) {
+  static_assert(E % T == 0, "E must be a multiple of T");
+  SmallDft<E, INV>::run(v);
+  SmallDft<E, INV>::run(w);
+#pragma unroll
+  for (int k1 = 1; k1 < E; ++k1) {
+    float2 t = twl[k1 * T + l];
+    if (INV) t.y = -t.y;
+    v[k1] = cmul(v[k1], t);
+    w[k1] = cmul(w[k1], t);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < E; ++k1) tile[k1 * (T + 1) + l] = v[k1];
+  __syncwarp(mask);
+  float2 u[E / T][T];
+#pragma unroll
+  for (int q = 0; q < E / T; ++q)
+#pragma unroll
+    for (int m = 0; m < T; ++m) u[q][m] = tile[(l + T * q) * (T + 1) + m];
+  __syncwarp(mask);
+#pragma unroll
+  for (int k1 = 0; k1 < E; ++k1) tile[k1 * (T + 1) + l] = w[k1];
+  __syncwarp(mask);
+#pragma unroll
+  for (int q = 0; q < E / T; ++q) {
+    float2 z[T];
+#pragma unroll
+    for (int m = 0; m < T; ++m) z[m] = tile[(l + T * q) * (T + 1) + m];
+    SmallDft<T, INV>::run(u[q]);
+    SmallDft<T, INV>::run(z);
+#pragma unroll
+    for (int k2 = 0; k2 < T; ++k2) {
+      v[q + (E / T) * k2] = u[q][k2];
+      w[q + (E / T) * k2] = z[k2];
+    }
+  }
+  __syncwarp(mask);
+}
+
 template <int N>
 struct RegCfg;
 template <>

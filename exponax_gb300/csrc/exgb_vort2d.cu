@@ -218,35 +218,45 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
       const int st = q % nst;
       const bool last_of_step = (st == nst - 1);
       // ================= column inverse: derived spectra -> IFFT -> pushed to the row owners
-      for (int task = gi; task < 4 * ncols; task += NG) {
-        const int f = task / ncols, c = task - f * ncols;
+      // tasks = (column, pair): pair 0 -> (u^, v^) from psi^, pair 1 -> (wx^, wy^) from w^;
+      // the two transforms of a pair are interleaved in one group
+      for (int task = gi; task < 2 * ncols; task += NG) {
+        const int pr = task / ncols, c = task - pr * ncols;
         const int ky = col0 + c;
         const float kys = ksc * (float)ky;
-        float2 v[E];
+        float2 v[E], v2[E];
 #pragma unroll
         for (int j = 0; j < E; ++j) {
           const int kx = l + T * j;
           const int ks = sgn_k<N>(kx);
-          float2 r = make_float2(0.f, 0.f);
+          float2 r1 = make_float2(0.f, 0.f), r2 = r1;
           if (ks <= K && ks >= -K) {
             const float2 w = colbuf[c * N + kx];
             const float kxs = ksc * (float)ks;
-            const float lap = -(kxs * kxs + kys * kys);
-            const float il = (lap == 0.f) ? 1.f : 1.f / lap;
-            if (f == 0) r = make_float2(-kys * il * w.y, kys * il * w.x);        // u^  = i ky psi^
-            else if (f == 1) r = make_float2(kxs * il * w.y, -kxs * il * w.x);  // v^  = -i kx psi^
-            else if (f == 2) r = make_float2(-kxs * w.y, kxs * w.x);            // wx^ = i kx w^
-            else r = make_float2(-kys * w.y, kys * w.x);                        // wy^ = i ky w^
-            r = cscale(r, invNN);
+            if (pr == 0) {
+              const float lap = -(kxs * kxs + kys * kys);
+              const float il = (lap == 0.f) ? 1.f : __frcp_rn(lap);  // correctly rounded 1/lap
+              const float2 psi = cscale(w, il);
+              r1 = make_float2(-kys * psi.y, kys * psi.x);   // u^  = i ky psi^
+              r2 = make_float2(kxs * psi.y, -kxs * psi.x);   // v^  = -i kx psi^
+            } else {
+              r1 = make_float2(-kxs * w.y, kxs * w.x);       // wx^ = i kx w^
+              r2 = make_float2(-kys * w.y, kys * w.x);       // wy^ = i ky w^
+            }
+            r1 = cscale(r1, invNN);
+            r2 = cscale(r2, invNN);
           }
-          v[j] = r;
+          v[j] = r1;
+          v2[j] = r2;
         }
-        group_fft<E, T, true>(v, l, tile, twl, gmask);
+        group_fft_x2<E, T, true>(v, v2, l, tile, twl, gmask);
+        const int f1 = 2 * pr, f2 = 2 * pr + 1;
 #pragma unroll
         for (int j = 0; j < E; ++j) {
           const int x = l + T * j;
           const int d = x >> lgRl, xr = x & (Rl - 1);
-          s_mixr[d][(f * Rl + xr) * KcP + ky] = v[j];
+          s_mixr[d][(f1 * Rl + xr) * KcP + ky] = v[j];
+          s_mixr[d][(f2 * Rl + xr) * KcP + ky] = v2[j];
         }
       }
       cluster.sync();  // derived fields delivered
@@ -273,8 +283,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           z1[j] = pack_pair(U, V, ext, ro);
           z2[j] = pack_pair(WX, WY, ext, ro);
         }
-        group_fft<E, T, true>(z1, l, tile, twl, gmask);
-        group_fft<E, T, true>(z2, l, tile, twl, gmask);
+        group_fft_x2<E, T, true>(z1, z2, l, tile, twl, gmask);
         float pj[E];
 #pragma unroll
         for (int j = 0; j < E; ++j) pj[j] = fmaf(z1[j].x, z2[j].x, z1[j].y * z2[j].y);

@@ -39,7 +39,7 @@ def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def fine_coarse_trajectories(seeds, *, n_fine=512, n_coarse_grid=64, dt=0.005, ratio=8, spinup=1000, n_coarse=200,
+def fine_coarse_trajectories(seeds, *, n_fine=512, n_coarse_grid=64, dt=0.001, ratio=8, spinup=1000, n_coarse=200,
                              batch=256):
     """Downsampled fine trajectories (len(seeds), n_coarse + 1, n_coarse_grid, n_coarse_grid) on the GPU, and
     the GPU milliseconds of the post-spin-up fine steps."""
@@ -154,6 +154,12 @@ def main():
     ap.add_argument("--epochs", type=int, default=4)
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--lr", type=float, default=1e-3)
+    # dt = 0.005 (512^2) / 0.04 (64^2) blow up for these parameters (advective CFL ~3.5): the
+    # float32 oracle of the reference stepper diverges after 83 steps at 64^2 / dt = 0.04 and
+    # after 368 steps at 128^2 / dt = 0.01; 64^2 / dt = 0.008 and 128^2 / dt = 0.004 (the CFL
+    # of 512^2 / dt = 0.001) stay finite over 2000+ steps.
+    ap.add_argument("--fine-dt", type=float, default=0.001)
+    ap.add_argument("--ratio", type=int, default=8)
     ap.add_argument("--out", default="kolmogorov_experiment.json")
     a = ap.parse_args()
     torch = _device.torch()
@@ -161,10 +167,10 @@ def main():
     def log(msg):
         print(f"[{time.strftime('%H:%M:%S')}] {msg}", flush=True)
 
-    coarse = stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.04, **KW)
+    coarse = stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 64, a.fine_dt * a.ratio, **KW)
     t0 = time.time()
     train_data, train_fine_ms = fine_coarse_trajectories(list(range(a.train_traj)), spinup=a.spinup,
-                                                         n_coarse=a.n_coarse)
+                                                         n_coarse=a.n_coarse, dt=a.fine_dt, ratio=a.ratio)
     log(f"training data: {tuple(train_data.shape)} in {time.time() - t0:.1f} s wall")
     net = PeriodicConvCorrector(64, seed=0, max_batch=a.batch)
     t0 = time.time()
@@ -174,13 +180,15 @@ def main():
     log(f"trained {a.epochs} epochs in {train_s:.1f} s")
     del train_data
     seeds = list(range(10_000_000, 10_000_000 + a.eval_traj))
-    ref, fine_ms = fine_coarse_trajectories(seeds, spinup=a.spinup, n_coarse=a.n_coarse)
+    ref, fine_ms = fine_coarse_trajectories(seeds, spinup=a.spinup, n_coarse=a.n_coarse, dt=a.fine_dt,
+                                            ratio=a.ratio)
     res = evaluate(ref, coarse, net)
     rp, cp, ctp = res["plain"]
     rl, cl, ctl = res["learned"]
     steps = sorted({s for s in (1, 10, 50, 100, a.n_coarse) if s <= a.n_coarse})
     out = {
-        "config": {"fine": "KolmogorovFlowVorticity 512^2 dt=0.005 ETDRK2", "coarse": "64^2 dt=0.04 ETDRK2",
+        "config": {"fine": f"KolmogorovFlowVorticity 512^2 dt={a.fine_dt} ETDRK2",
+                   "coarse": f"64^2 dt={a.fine_dt * a.ratio} ETDRK2",
                    "train_trajectories": a.train_traj, "eval_trajectories": a.eval_traj, "spinup": a.spinup,
                    "coarse_steps": a.n_coarse, "epochs": a.epochs, "batch": a.batch, "lr": a.lr,
                    "network": "6-layer periodic 3x3 CNN, 48 channels, GELU, residual, bf16, "
