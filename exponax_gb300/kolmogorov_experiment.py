@@ -3,12 +3,12 @@
     python -m exponax_gb300.kolmogorov_experiment --train-traj 2000 --eval-traj 256 --epochs 4 \
         --out results.json
 
-1. Fine plain runs (KolmogorovFlowVorticity 512^2, dt = 0.005, ETDRK2,
+1. Fine plain runs (KolmogorovFlowVorticity 512^2, dt = 0.001, ETDRK2,
    nu = 1e-3, drag -0.1, forcing k = 4, amplitude 1) from random truncated
    Fourier ICs (cutoff 5): `spinup` steps, then `n_coarse` x 8 steps,
    downsampled to 64^2 (map_between_resolutions) every 8 steps.
 2. Training pairs (c_t, c_{t+1}); inputs v = plain coarse step (64^2,
-   dt = 0.04) of c_t, targets c_{t+1}.  Adam, lr 1e-3, mean squared error.
+   dt = 0.008) of c_t, targets c_{t+1}.  Adam, lr 1e-3, mean squared error.
 3. Evaluation on held-out seeds: rollouts of `n_coarse` coarse steps of the
    plain 64^2 stepper and of the learned (guarded) 64^2 stepper against the
    downsampled fine solution: relative L2 per step, correlation, correlation
