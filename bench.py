@@ -450,6 +450,8 @@ def run_other(args, rank, ws):
 
         Nk, B, n = 128, 1024, 100
         st = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, Nk, 0.01)
+        if args.precision != "fp32":
+            st.set_dft_precision(args.precision)
         g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
         u0h = np.stack([g(Nk, key=s) for s in range(B)])
         uh = ex.fft(torch.from_numpy(u0h).cuda(), num_spatial_dims=2)
@@ -469,7 +471,10 @@ def run_other(args, rank, ws):
         dof = B * Nk * Nk * n
         line.update(value=dof / (ms * 1e-3), ms_per_step=ms,
                     config={"workload": "KolmogorovFlowVorticity 2D 128^2, nu=1e-3, drag=-0.1, forcing k=4 amplitude "
-                                        "1, dt=0.01, ETDRK2, batch 1024, 100 steps (FP32 transforms)"},
+                                        "1, dt=0.01, ETDRK2, batch 1024, 100 steps ("
+                                        + ("FP32 transforms" if args.precision == "fp32" else
+                                           "split-BF16 tcgen05 DFT contractions, FP32 accumulation") + ")"},
+                    dtype="f32" if args.precision == "fp32" else "bf16x3 (split) / f32 accumulate",
                     e2e={"value": dof / (ems * 1e-3), "unit": "DOF-steps/s", "ms_per_step": ems,
                          "h2d_bytes_per_step": int(pin.numel() * 4), "d2h_bytes_per_step": int(pout.numel() * 4)},
                     gpu_launches=args.steps)
@@ -485,7 +490,8 @@ def run_other(args, rank, ws):
                     ref = o.repeat(so64, nn)(u0h[b].astype(np.float64))
                     e.append(float(np.linalg.norm(got[b] - ref) / np.linalg.norm(ref)))
                 errs[f"rel_l2_vs_fp64_after_{nn}"] = float(np.max(e))
-            line["precision"] = dict(errs, note="FP32 Stockham/register transforms vs the float64 oracle, 2 seeds")
+            line["precision"] = dict(errs, note=("FP32 register transforms" if args.precision == "fp32" else
+                                                 "split-BF16 tensor-core DFT") + " vs the float64 oracle, 2 seeds")
     print(json.dumps(line), flush=True)
 
 
@@ -496,6 +502,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "split_bf16"],
+                    help="transform arithmetic of the kolmo128 workload")
     ap.add_argument("--workload", default="ns256", choices=["ns256", "ks1d", "uneven1d", "kolmo128"],
                     help="ns256 (default, the headline metric) or one of the other benchmark configurations")
     args = ap.parse_args()

@@ -87,6 +87,20 @@ class Plan:
     def kmax(self) -> int:
         return load().exgb_plan_kmax(self.handle)
 
+    PRECISIONS = {"fp32": 0, "split_bf16": 1}
+
+    def set_precision(self, mode: str) -> None:
+        """Arithmetic of the 2D vorticity transforms: "fp32" (FP32 FFTs) or
+        "split_bf16" (tcgen05 DFT contractions, split-BF16, FP32 accumulation)."""
+        if mode not in self.PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(self.PRECISIONS)}, got {mode!r}")
+        arr = (ctypes.c_int * 1)(self.PRECISIONS[mode])
+        check(load().exgb_plan_tune(self.handle, 3, arr, 1), "set_precision")
+
+    def status(self) -> None:
+        """Raise if a bounded device wait of this plan's kernels gave up (synchronises)."""
+        check(load().exgb_plan_status(self.handle), "plan status")
+
     def __del__(self):
         try:
             if self._handle is not None:

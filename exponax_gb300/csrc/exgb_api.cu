@@ -217,6 +217,8 @@ int exgb_plan_destroy(exgb_plan* plan) {
   cudaFree(plan->d_Eh);
   cudaFree(plan->d_c);
   cudaFree(plan->d_scratch);
+  cudaFree(plan->d_tc_scratch);
+  cudaFree(plan->d_status);
   delete plan;
   return EXGB_OK;
 }
@@ -479,12 +481,33 @@ extern "C" int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int 
     }
     return EXGB_OK;
   }
+  if (kind == EXGB_TUNE_PRECISION) {
+    const int v = n > 0 ? values[0] : EXGB_DFT_FP32;
+    if (v == EXGB_DFT_FP32) {
+      plan->precision = 0;
+      return EXGB_OK;
+    }
+    if (v != EXGB_DFT_SPLIT_BF16) return fail(EXGB_EINVAL, "precision must be EXGB_DFT_FP32 or EXGB_DFT_SPLIT_BF16");
+    const int rc = tcdft2d_configure(plan);
+    if (rc) return rc;
+    plan->precision = 1;
+    return EXGB_OK;
+  }
   if (kind == EXGB_TUNE_ITEMS_PER_CTA) {
     if (plan->dev.D != 1) return fail(EXGB_EUNSUPPORTED, "items per CTA applies to 1D plans");
     plan->tune_items_per_cta = n > 0 ? std::max(0, std::min(64, values[0])) : 0;
     return EXGB_OK;
   }
   return fail(EXGB_EINVAL, "unknown tuning kind");
+}
+
+extern "C" int exgb_plan_status(const exgb_plan* plan) {
+  if (!plan) return fail(EXGB_EINVAL, "NULL plan");
+  if (!plan->d_status) return EXGB_OK;
+  int h = 0;
+  EXGB_CUDA(cudaMemcpy(&h, plan->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) return fail(h, "a bounded device wait of the tensor-core kernel gave up");
+  return EXGB_OK;
 }
 
 extern "C" int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n) {
@@ -494,5 +517,6 @@ extern "C" int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n) {
   for (int i = 0; i < kMaxPass; ++i) out[1 + i] = i < plan->dev.fft.npass ? plan->dev.fft.radix[i] : 0;
   out[1 + kMaxPass] = plan->cfg2d.G;
   out[2 + kMaxPass] = plan->tune_items_per_cta;
+  if (n >= 4 + kMaxPass) out[3 + kMaxPass] = plan->precision;
   return EXGB_OK;
 }

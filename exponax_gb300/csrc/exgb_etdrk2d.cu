@@ -525,6 +525,7 @@ int etdrk2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2
                 int project, int nonlinear_only) {
   if (batch <= 0) return EXGB_OK;
   const Plan2DConfig& c = plan->cfg2d;
+  if (plan->precision == 1) return tcdft2d_run(plan, st, in, out, batch, nsteps, project, nonlinear_only);
   if (c.variant == 1) return vort2d_run(plan, st, in, out, batch, nsteps, project, nonlinear_only);
   Args2D a;
   a.P = plan->dev;

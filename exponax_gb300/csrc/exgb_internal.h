@@ -73,6 +73,11 @@ struct exgb_plan {
   // autotuner overrides (0 = automatic choice)
   int tune_cluster = 0;          // 2D: CTAs per cluster
   int tune_items_per_cta = 0;    // 1D: instances per work item
+  // 2D vorticity transforms: 0 = FP32 register FFTs, 1 = split-BF16 tensor-core DFT
+  int precision = 0;
+  void* d_tc_scratch = nullptr;
+  size_t tc_scratch_per_cta = 0;
+  int* d_status = nullptr;       // device wait status of the tensor-core kernel (0 = ok)
 };
 
 namespace exgb {
@@ -109,6 +114,10 @@ int etdrk2d_configure(exgb_plan* plan);
 int vort2d_configure(exgb_plan* plan);
 int vort2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                int project, int nonlinear_only);
+bool tcdft2d_supported(const exgb_plan* plan);
+int tcdft2d_configure(exgb_plan* plan);
+int tcdft2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
+                int project, int nonlinear_only);
 int etdrk0_apply(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                  int project);
 

@@ -1,0 +1,192 @@
+// exgb_tc.cuh -- thin inline-PTX layer over the sm_100-family 5th-generation
+// tensor cores (tcgen05) used by the split-BF16 DFT kernels.
+//
+//   * operands: bf16 tiles in shared memory, K-major, no swizzle ("canonical
+//     interleaved" layout): core matrices of 8 rows x 16 bytes (8 bf16 of K),
+//     stored 128 contiguous bytes each; K-adjacent core matrices are 128 B
+//     apart (leading byte offset), 8-row groups are K*16 B apart (stride
+//     byte offset).  Element (r, k) of an R x K tile sits at
+//         (r / 8) * (K * 16) + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2.
+//   * accumulator: FP32 in tensor memory, M = 128 rows -> TMEM lanes 0..127,
+//     N columns -> N consecutive TMEM columns.
+//   * one thread issues tcgen05.mma; completion is signalled through
+//     tcgen05.commit onto an mbarrier that every thread waits on with a
+//     clock-bounded loop (no unbounded spin).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace exgb {
+namespace tc {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// byte offset of element (r, k) inside a K-major no-swizzle tile with K columns
+__host__ __device__ constexpr uint32_t kmaj_off(int r, int k, int K) {
+  return (uint32_t)((r >> 3) * (K * 16) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+// byte offset of the 16-byte chunk holding k = 8 c .. 8 c + 7 of row r
+__host__ __device__ constexpr uint32_t kmaj_chunk(int r, int c, int K) {
+  return (uint32_t)((r >> 3) * (K * 16) + c * 128 + (r & 7) * 16);
+}
+
+// Shared-memory matrix descriptor (sm_100 family): start address, leading
+// and stride byte offsets (all >> 4), descriptor version 1 at bits 46-47,
+// base offset 0, swizzle mode 0 (none) at bits 61-63.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+  d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+// descriptor of a K-major tile with K columns, advanced to the k-step s (16 columns)
+__device__ __forceinline__ uint64_t kmaj_desc(uint32_t tile_saddr, int K, int s) {
+  return smem_desc(tile_saddr + (uint32_t)s * 256u, 128u, (uint32_t)K * 16u);
+}
+
+// Instruction descriptor of kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9 and 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A[smem] . B[smem]^T, one instruction of K = 16
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// arrive on the mbarrier once every tcgen05 operation issued so far by this thread has completed
+__device__ __forceinline__ void mma_commit(uint64_t* mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(mbar))
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy shared-memory writes -> visible to the tensor core (async proxy)
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// ---- tensor memory allocation (one full warp executes these)
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
+               "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// ---- tensor memory -> registers: thread t of the warp reads lane (lane field of taddr) + t,
+// 8 consecutive 32-bit columns; the wait is inside the same asm block so no
+// use of the registers can be scheduled before the data has arrived.
+__device__ __forceinline__ float tmem_ld1(uint32_t taddr) {
+  uint32_t r;
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r)
+      : "r"(taddr)
+      : "memory");
+  return __uint_as_float(r);
+}
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---- mbarrier
+__device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
+}
+// Wait until the phase with the given parity has completed; gives up after
+// `budget` clock cycles and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, long long budget) {
+  const uint32_t a = smem_u32(mbar);
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > budget) return false;
+  }
+}
+
+// ---- split of an FP32 value into two bf16 whose sum carries ~16 significant bits
+__device__ __forceinline__ void split_bf16(float v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __float2bfloat16_rn(v);
+  lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+}
+// 8 FP32 values -> 16-byte hi chunk and 16-byte lo chunk
+__device__ __forceinline__ void split8_store(const float (&v)[8], unsigned char* hi_tile, unsigned char* lo_tile,
+                                             uint32_t off) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    __nv_bfloat16 h0, l0, h1, l1;
+    split_bf16(v[2 * i], h0, l0);
+    split_bf16(v[2 * i + 1], h1, l1);
+    h[i] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+    l[i] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+  }
+  *reinterpret_cast<uint4*>(hi_tile + off) = make_uint4(h[0], h[1], h[2], h[3]);
+  *reinterpret_cast<uint4*>(lo_tile + off) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// Split-BF16 product D (+)= A . B^T over K (multiple of 16) with the three
+// significant terms Ahi Bhi + Ahi Blo + Alo Bhi, FP32 accumulation in TMEM.
+// Issued by one thread.
+__device__ __forceinline__ void mma_split3(uint32_t d_tmem, uint32_t a_hi, uint32_t a_lo, int KA, uint32_t b_hi,
+                                           uint32_t b_lo, int KB, int K, uint32_t idesc, bool accumulate) {
+  for (int s = 0; s < K / 16; ++s) {
+    const uint64_t ah = kmaj_desc(a_hi, KA, s), al = kmaj_desc(a_lo, KA, s);
+    const uint64_t bh = kmaj_desc(b_hi, KB, s), bl = kmaj_desc(b_lo, KB, s);
+    mma_bf16(d_tmem, al, bh, idesc, (accumulate || s > 0) ? 1u : 0u);
+    mma_bf16(d_tmem, ah, bl, idesc, 1u);
+    mma_bf16(d_tmem, ah, bh, idesc, 1u);
+  }
+}
+
+}  // namespace tc
+}  // namespace exgb

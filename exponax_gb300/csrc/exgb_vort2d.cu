@@ -20,6 +20,7 @@
 
 #include "exgb_internal.h"
 #include "exgb_regfft.cuh"
+#include "exgb_stage.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -55,76 +56,6 @@ struct V2Layout {
     return sizeof(float2) * maps(Cl, Rl, KcP) + sizeof(int) * (size_t)Kc;
   }
 };
-
-struct StageBufs {
-  float2 *U, *S1, *S, *N0, *N1, *N2;
-};
-
-__device__ __forceinline__ float2 stage_upd(const PlanDev& P, const StageBufs& b, int64_t o, int stage, float2 nv) {
-  switch (P.order) {
-    case 1: {
-      const float2 r = cadd(cmul(__ldg(P.E + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
-      b.U[o] = r;
-      return r;
-    }
-    case 2:
-      if (stage == 0) {
-        const float2 s = cadd(cmul(__ldg(P.E + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
-        b.N0[o] = nv;
-        b.S[o] = s;
-        return s;
-      } else {
-        const float2 r = cadd(b.S[o], cscale(csub(nv, b.N0[o]), __ldg(P.c[1] + o)));
-        b.U[o] = r;
-        return r;
-      }
-    case 3:
-      if (stage == 0) {
-        const float2 s = cadd(cmul(__ldg(P.Eh + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
-        b.N0[o] = nv;
-        b.S[o] = s;
-        return s;
-      } else if (stage == 1) {
-        const float2 t = csub(cscale(nv, 2.f), b.N0[o]);
-        const float2 s = cadd(cmul(__ldg(P.E + o), b.U[o]), cscale(t, __ldg(P.c[1] + o)));
-        b.N1[o] = nv;
-        b.S[o] = s;
-        return s;
-      } else {
-        float2 r = cmul(__ldg(P.E + o), b.U[o]);
-        r = cadd(r, cscale(b.N0[o], __ldg(P.c[2] + o)));
-        r = cadd(r, cscale(b.N1[o], __ldg(P.c[3] + o)));
-        r = cadd(r, cscale(nv, __ldg(P.c[4] + o)));
-        b.U[o] = r;
-        return r;
-      }
-    default:
-      if (stage == 0) {
-        const float2 s = cadd(cmul(__ldg(P.Eh + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
-        b.N0[o] = nv;
-        b.S1[o] = s;
-        return s;
-      } else if (stage == 1) {
-        const float2 s = cadd(cmul(__ldg(P.Eh + o), b.U[o]), cscale(nv, __ldg(P.c[0] + o)));
-        b.N1[o] = nv;
-        b.S[o] = s;
-        return s;
-      } else if (stage == 2) {
-        const float2 t = csub(cscale(nv, 2.f), b.N0[o]);
-        const float2 s = cadd(cmul(__ldg(P.Eh + o), b.S1[o]), cscale(t, __ldg(P.c[0] + o)));
-        b.N2[o] = nv;
-        b.S[o] = s;
-        return s;
-      } else {
-        float2 r = cmul(__ldg(P.E + o), b.U[o]);
-        r = cadd(r, cscale(b.N0[o], __ldg(P.c[3] + o)));
-        r = cadd(r, cscale(cadd(b.N1[o], b.N2[o]), 2.f * __ldg(P.c[4] + o)));
-        r = cadd(r, cscale(nv, __ldg(P.c[5] + o)));
-        b.U[o] = r;
-        return r;
-      }
-  }
-}
 
 template <int N>
 __device__ __forceinline__ int sgn_k(int i) {

@@ -56,6 +56,15 @@ class BaseStepper:
     def plan(self):
         return self._integrator._plan(self.num_channels)
 
+    def set_dft_precision(self, mode: str = "fp32"):
+        """Arithmetic of the transforms of the 2D vorticity steppers (no
+        reference counterpart): "fp32" (default, FP32 FFTs) or "split_bf16"
+        (dense DFT contractions on the tcgen05 tensor cores in split-BF16
+        three-product form with FP32 accumulation; N = 128, dealiasing on).
+        Returns the stepper."""
+        self.plan.set_precision(mode)
+        return self
+
     def _phys(self, u, batched: bool):
         t, back = _device.to_device(u, "float32")
         expected = (self.num_channels,) + spatial_shape(self.num_spatial_dims, self.num_points)

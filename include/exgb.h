@@ -123,8 +123,20 @@ int exgb_plan_kmax(const exgb_plan* plan);
 #define EXGB_TUNE_RADICES 0
 #define EXGB_TUNE_CLUSTER 1
 #define EXGB_TUNE_ITEMS_PER_CTA 2
+/* EXGB_TUNE_PRECISION values[0] = arithmetic of the 2D vorticity transforms:
+ *   EXGB_DFT_FP32        FP32 register/Stockham FFTs (default)
+ *   EXGB_DFT_SPLIT_BF16  dense DFT contractions on the tcgen05 tensor cores in
+ *                        split-BF16 form (hi.hi + hi.lo + lo.hi, FP32
+ *                        accumulation); N = 128, dealiasing cutoff <= 47.
+ * exgb_plan_get_tuning reports it after the items per CTA when n >= 16. */
+#define EXGB_TUNE_PRECISION 3
+#define EXGB_DFT_FP32 0
+#define EXGB_DFT_SPLIT_BF16 1
 int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int n);
 int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n);
+/* Synchronises the device and returns EXGB_ETIMEOUT if a bounded wait inside
+ * the tensor-core kernel of this plan gave up (its outputs are then invalid). */
+int exgb_plan_status(const exgb_plan* plan);
 
 /* ---- spectral transforms ----
  * exgb_rfftn replaces spectral.fft  (_spectral.py:614-656): rfftn over the
@@ -205,6 +217,13 @@ int exgb_leray(void* stream, int num_spatial_dims, int num_points, double domain
  * spectral re-sampling of count = B*C fields from N_old to N_new points. */
 int exgb_map_between_resolutions(void* stream, int num_spatial_dims, int n_old, int n_new,
                                  int64_t count, const float* in, float* out, int oddball_zero);
+
+/* Self-check of the tcgen05 tensor-core layer (no reference counterpart):
+ * d (128 x n, FP32) = a (128 x k) . b (n x k)^T, device pointers, row-major.
+ * split = 0: inputs rounded to bf16, one product; split = 1: split-BF16
+ * three-product form.  16 <= n <= 256, 16 <= k <= 128, multiples of 16.
+ * Synchronous. */
+int exgb_tc_gemm_check(void* stream, int n, int k, const float* a, const float* b, float* d, int split);
 
 #ifdef __cplusplus
 }
