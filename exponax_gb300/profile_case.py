@@ -1,6 +1,7 @@
 """Run one stepping workload for profiling (e.g. under ncu).
 
     python -m exponax_gb300.profile_case --dims 2 --n 256 --batch 32 --steps 10 --reps 3
+    python -m exponax_gb300.profile_case --dims 2 --n 128 --kolmogorov --precision split_bf16
 
 Builds the stepper (NavierStokesVorticity in 2D, KuramotoSivashinsky-
 Conservative in 1D), creates device-resident Fourier states and launches
@@ -24,6 +25,7 @@ def main():
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--kolmogorov", action="store_true")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "split_bf16"])
     a = ap.parse_args()
 
     import torch
@@ -35,6 +37,8 @@ def main():
         cls = ex.stepper.KolmogorovFlowVorticity if a.kolmogorov else ex.stepper.NavierStokesVorticity
         kw = {} if a.kolmogorov else {"diffusivity": 1e-3}
         st = cls(2, 2 * np.pi, a.n, 0.01, order=a.order, **kw)
+        if a.precision != "fp32":
+            st.set_dft_precision(a.precision)
         g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
     else:
         st = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, a.n, 0.1, order=a.order)
