@@ -77,6 +77,7 @@ struct exgb_plan {
   int precision = 0;
   void* d_tc_scratch = nullptr;
   size_t tc_scratch_per_cta = 0;
+  size_t tc_const_offset = 0;    // byte offset of the constant DFT tiles inside d_tc_scratch
   int* d_status = nullptr;       // device wait status of the tensor-core kernel (0 = ok)
 };
 

@@ -20,21 +20,29 @@
 //     e_j = x_j + x_N-j, o_j = x_j - x_N-j;  C_m = sum_j e_j cos(th m j),
 //     S_m = sum_j o_j sin(th m j);  X_m = C_m - i S_m, X_-m = C_m + i S_m
 //
-// with th = 2 pi / N.  The matrices "Ai" (128 rows of cos/sin over the
-// inverse modes) and "Af" (rows of cos/sin modes over e/o positions) live in
-// shared memory as hi/lo bf16 pairs for the whole launch; rows are ordered
-// so that the cos row and the sin row of one index sit 16 lanes apart in the
-// same warp, and the +-combinations above are one warp shuffle.
+// with th = 2 pi / N.  The derived fields are d = i m(k) w^ with a real
+// multiplier m (u: k_half/Lap, v: -k_full/Lap, wx: k_full, wy: k_half), odd
+// or even in k_full, so S and D of every field come from the two spectra
+// A+ = w^(k) + w^(-k) and A- = w^(k) - w^(-k), kept in shared memory.
+// The constant matrices "Ai" (128 rows of cos/sin over the inverse modes)
+// and "Af" (rows of cos/sin modes over e/o positions) are computed once on
+// the host in FP64, split into hi/lo bf16 in the exact shared-memory layout
+// and copied in at launch; rows are ordered so that the cos row and the sin
+// row of one index sit 16 lanes apart in the same warp, and the
+// +-combinations above are one warp shuffle.
 //
 // Per stage and sample: 4 x (inverse full axis, inverse half axis), the
 // product u wx + v wy in registers, forward half axis, forward full axis,
-// ETDRK stage update (exgb_stage.cuh) -- 10 MMA chains, all operands in
-// shared memory, accumulators in 4 slots of 128 TMEM columns.
-// Modes outside the kept set evolve linearly (E^n, the c2r projection on the
-// half-axis columns 0 and N/2) exactly as in the FP32 kernels.
+// ETDRK stage update (exgb_stage.cuh) by all threads on mode pairs (k, -k)
+// -- 10 MMA chains, all operands in shared memory, accumulators in 4 slots of
+// 128 TMEM columns.  Modes outside the kept set evolve linearly (E^n, the c2r
+// projection on the half-axis columns 0 and N/2) exactly as in the FP32 kernels.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
 
 #include "exgb_internal.h"
 #include "exgb_stage.cuh"
@@ -50,7 +58,7 @@ constexpr int THREADS = 256;
 constexpr int KMAX = 47;
 constexpr int KI = 96;   // inverse contraction: [cos part, modes 0..47 | sin part, modes 0..47]
 constexpr int KF = 128;  // forward contraction: [e_0 .. e_63 | e_64 | o_1 .. o_63]
-constexpr int XS_LD = 48;
+constexpr int LD = 48;   // k_half stride of the A+- planes
 // shared memory (bytes).  Af stores rows 0..95; the MMA also reads rows
 // 96..127, which overlap the next tile (their outputs are never used).
 constexpr uint32_t TILE_AI = 128 * KI * 2;
@@ -59,7 +67,8 @@ constexpr uint32_t OFF_AI_HI = 0;
 constexpr uint32_t OFF_AI_LO = OFF_AI_HI + TILE_AI;
 constexpr uint32_t OFF_AF_HI = OFF_AI_LO + TILE_AI;
 constexpr uint32_t OFF_AF_LO = OFF_AF_HI + TILE_AF;
-constexpr uint32_t OFF_R = OFF_AF_LO + TILE_AF;
+constexpr uint32_t CONST_BYTES = OFF_AF_LO + TILE_AF;  // host-built image of the four constant tiles
+constexpr uint32_t OFF_R = CONST_BYTES;
 constexpr uint32_t TILE_B1 = 96 * KI * 2;   // inverse full-axis data: rows (part, half mode)
 constexpr uint32_t TILE_A2 = 128 * KI * 2;  // inverse half-axis data: rows = full-axis positions
 constexpr uint32_t TILE_B3 = 128 * KF * 2;  // forward half-axis data: rows = full-axis positions
@@ -67,11 +76,13 @@ constexpr uint32_t TILE_B4 = 96 * KF * 2;   // forward full-axis data: rows = Af
 constexpr uint32_t R_B1_HI = 0, R_B1_LO = TILE_B1;
 constexpr uint32_t R_A2_HI = 2 * TILE_B1, R_A2_LO = 2 * TILE_B1 + TILE_A2;
 constexpr uint32_t R_BYTES = 2 * TILE_B1 + 2 * TILE_A2;
-constexpr uint32_t OFF_X = OFF_R + R_BYTES;
-constexpr uint32_t X_BYTES = (2 * KMAX + 1) * XS_LD * 8;
-constexpr uint32_t SMEM_BYTES = OFF_X + X_BYTES;
+constexpr uint32_t PLANE = 48 * LD * 4;     // one float plane [k_full 0..47][k_half]
+constexpr uint32_t OFF_PM = OFF_R + R_BYTES;  // planes A+re, A+im, A-re, A-im
+constexpr uint32_t SMEM_BYTES = OFF_PM + 4 * PLANE;
 static_assert(2 * TILE_B3 <= R_BYTES && 2 * TILE_B4 <= R_BYTES, "region R too small");
+static_assert(48u * N * 8u <= R_BYTES, "nonlinear-term buffer must fit region R");
 static_assert(128 * KF * 2 - TILE_AF <= R_BYTES, "Af overflow rows must stay inside shared memory");
+static_assert(CONST_BYTES % 16 == 0, "constant image is copied in 16-byte pieces");
 constexpr long long WAIT_BUDGET = 4000000000LL;  // clock cycles (~2 s) before a wait gives up
 
 struct Args {
@@ -84,67 +95,59 @@ struct Args {
   int nonlinear_only;
   float2* scratch;
   int64_t scratch_stride;
+  const uint4* consts;
   int* status;
 };
 
-// Ai[r][k]: rows r = 32 w + l, slot s = 16 w + (l & 15); l < 16: cos row of
-// index s; l >= 16: sin row of index s (s >= 1) or the cos row of index N/2 (s = 0).
-__device__ double ai_val(int r, int k, int K) {
-  const int w = r >> 5, l = r & 31, s = 16 * w + (l & 15);
-  const bool sinl = l >= 16;
-  if (!sinl || s == 0) {
-    const int idx = sinl ? H : s;
-    return (k < 48 && k <= K) ? cospi(2.0 * ((k * idx) % N) / N) : 0.0;
-  }
-  const int kk = k - 48;
-  return (k >= 48 && kk >= 1 && kk <= K) ? sinpi(2.0 * ((kk * s) % N) / N) : 0.0;
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
 
-// Af[r][k]: rows r = 32 w + l (w < 3), mode m = 16 w + (l & 15); l < 16: cos
-// row over e_0..e_64 (k = 0..64); l >= 16: sin row over o_1..o_63 (k = 65..127).
-__device__ double af_val(int r, int k, int K) {
-  const int w = r >> 5, l = r & 31, m = 16 * w + (l & 15);
-  if (m > K) return 0.0;
-  if (l < 16) return k <= 64 ? cospi(2.0 * ((m * k) % N) / N) : 0.0;
-  if (m == 0 || k < 65) return 0.0;
-  return sinpi(2.0 * ((m * (k - 64)) % N) / N);
-}
-
-__device__ __forceinline__ void split8d_store(const double (&v)[8], unsigned char* hi, unsigned char* lo, uint32_t off) {
-  uint32_t h[4], q[4];
+// Inverse full-axis data of field F (0 u, 1 v, 2 wx, 3 wy): row n = part * 48
+// + k_half, column k = [S_k (k < 48) | D_(k-48)].  S/D = i m (A+ or A-), the
+// even fields (u, wy) taking A+ for S and the odd ones (v, wx) A- (the
+// multiplier changes sign with k_full).  Values outside the kept set are 0.
+template <int F>
+__device__ __forceinline__ void build_b1(unsigned char* hi, unsigned char* lo, const float* pl, int K, float ksc,
+                                         float invNN, int tid) {
+  constexpr bool odd = (F == 1 || F == 2);
+  for (int t = tid; t < 96 * (KI / 8); t += THREADS) {
+    const int c = t / 96, n = t - c * 96;
+    const int part = n >= 48 ? 1 : 0;
+    const int kh = n - 48 * part;
+    const bool dblk = c >= 6;
+    float v[8];
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    uint32_t hh[2], ll[2];
+    for (int j = 0; j < 8; ++j) v[j] = 0.f;
+    if (kh <= K) {
+      const float kys = ksc * (float)kh;
+      const bool minus = (dblk != odd);
+      const float* P = pl + ((minus ? 2 : 0) + (part ? 0 : 1)) * (int)(PLANE / 4);
+      const float sg = part ? invNN : -invNN;  // i m A = (-m A.im, m A.re)
+      const int kf0 = 8 * c - (dblk ? 48 : 0);
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      const double d = v[2 * i + u];
-      const __nv_bfloat16 b = __float2bfloat16_rn((float)d);
-      const __nv_bfloat16 c = __float2bfloat16_rn((float)(d - (double)__bfloat162float(b)));
-      hh[u] = __bfloat16_as_ushort(b);
-      ll[u] = __bfloat16_as_ushort(c);
+      for (int j = 0; j < 8; ++j) {
+        const int kf = kf0 + j;
+        if (kf <= K) {
+          const float kxs = ksc * (float)kf;
+          float m;
+          if (F == 2) {
+            m = kxs;
+          } else if (F == 3) {
+            m = kys;
+          } else {
+            const float lap = -(kxs * kxs + kys * kys);
+            const float il = (lap == 0.f) ? 1.f : rcp_approx(lap);
+            m = (F == 0) ? kys * il : -kxs * il;
+          }
+          v[j] = sg * m * P[kf * LD + kh];
+        }
+      }
     }
-    h[i] = hh[0] | (hh[1] << 16);
-    q[i] = ll[0] | (ll[1] << 16);
+    tc::split8_store(v, hi, lo, tc::kmaj_chunk(n, c, KI));
   }
-  *reinterpret_cast<uint4*>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
-  *reinterpret_cast<uint4*>(lo + off) = make_uint4(q[0], q[1], q[2], q[3]);
-}
-
-// derived field f of the vorticity spectrum X at (full mode kf, half mode kh), scaled by 1/N^2:
-// 0: u^ = i k_half psi^, 1: v^ = -i k_full psi^, 2: wx^ = i k_full w^, 3: wy^ = i k_half w^,
-// psi^ = w^ / Lap with 1/Lap = 1 at k = 0 (_vorticity_convection.py:76-92)
-__device__ __forceinline__ float2 derived(int f, float2 X, float kxs, float kys, float invNN) {
-  float2 r;
-  if (f < 2) {
-    const float lap = -(kxs * kxs + kys * kys);
-    const float il = (lap == 0.f) ? 1.f : __frcp_rn(lap);
-    const float2 psi = cscale(X, il);
-    r = (f == 0) ? make_float2(-kys * psi.y, kys * psi.x) : make_float2(kxs * psi.y, -kxs * psi.x);
-  } else {
-    const float kk = (f == 2) ? kxs : kys;
-    r = make_float2(-kk * X.y, kk * X.x);
-  }
-  return cscale(r, invNN);
 }
 
 __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
@@ -153,33 +156,20 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
   __shared__ uint32_t s_tbase;
   const PlanDev& P = a.P;
   const int K = min(P.kmax, KMAX);
-  const int Kc = K + 1, NF = 2 * K + 1;
+  const int Kc = K + 1;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, q = warp & 3;
   const bool upper = warp >= 4;
-  unsigned char* ai_hi = sm + OFF_AI_HI;
-  unsigned char* ai_lo = sm + OFF_AI_LO;
-  unsigned char* af_hi = sm + OFF_AF_HI;
-  unsigned char* af_lo = sm + OFF_AF_LO;
   unsigned char* rg = sm + OFF_R;
-  float2* Xs = reinterpret_cast<float2*>(sm + OFF_X);
-  const uint32_t sAiH = tc::smem_u32(ai_hi), sAiL = tc::smem_u32(ai_lo);
-  const uint32_t sAfH = tc::smem_u32(af_hi), sAfL = tc::smem_u32(af_lo);
+  float* pl = reinterpret_cast<float*>(sm + OFF_PM);
+  float2* nvb = reinterpret_cast<float2*>(rg);  // nonlinear term [k_half][k_full index], region R
+  const uint32_t sAiH = tc::smem_u32(sm + OFF_AI_HI), sAiL = tc::smem_u32(sm + OFF_AI_LO);
+  const uint32_t sAfH = tc::smem_u32(sm + OFF_AF_HI), sAfL = tc::smem_u32(sm + OFF_AF_LO);
   const uint32_t sR = tc::smem_u32(rg);
 
-  // ---- constant DFT tiles (angles in FP64, split into bf16 hi/lo)
-  for (int t = tid; t < 128 * (KI / 8); t += THREADS) {
-    const int r = t / (KI / 8), c = t % (KI / 8);
-    double v[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] = ai_val(r, 8 * c + j, K);
-    split8d_store(v, ai_hi, ai_lo, tc::kmaj_chunk(r, c, KI));
-  }
-  for (int t = tid; t < 96 * (KF / 8); t += THREADS) {
-    const int r = t / (KF / 8), c = t % (KF / 8);
-    double v[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] = af_val(r, 8 * c + j, K);
-    split8d_store(v, af_hi, af_lo, tc::kmaj_chunk(r, c, KF));
+  // ---- constant DFT tiles: host-built image, copied as is
+  {
+    uint4* dst = reinterpret_cast<uint4*>(sm);
+    for (int t = tid; t < (int)(CONST_BYTES / 16); t += THREADS) dst[t] = __ldg(a.consts + t);
   }
   if (warp == 0) {
     tc::tmem_alloc(&s_tbase, 512);
@@ -219,37 +209,24 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
     tc::fence_after_sync();
     return anybad == 0;
   };
-
-  // inverse full-axis data of field f: rows n = part * 48 + kh, k = [S_0..S_47 | D_0..D_47]
-  auto build_b1 = [&](int f) {
-    for (int t = tid; t < 96 * (KI / 8); t += THREADS) {
-      const int c = t / 96, n = t - c * 96;
-      const int part = n >= 48 ? 1 : 0;
-      const int kh = n - 48 * part;
-      float v[8];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) v[j] = 0.f;
-      if (kh <= K) {
-        const float kys = ksc * (float)kh;
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int k = 8 * c + j;
-          const bool dp = k >= 48;
-          const int kf = dp ? k - 48 : k;
-          if (kf <= K && !(dp && kf == 0)) {
-            const float kxs = ksc * (float)kf;
-            const float2 xp = derived(f, Xs[(kf + K) * XS_LD + kh], kxs, kys, invNN);
-            float2 cmb = xp;
-            if (kf > 0) {
-              const float2 xm = derived(f, Xs[(K - kf) * XS_LD + kh], -kxs, kys, invNN);
-              cmb = dp ? csub(xp, xm) : cadd(xp, xm);
-            }
-            v[j] = part ? cmb.y : cmb.x;
-          }
-        }
-      }
-      tc::split8_store(v, rg + R_B1_HI, rg + R_B1_LO, tc::kmaj_chunk(n, c, KI));
+  auto b1 = [&](int f) {
+    unsigned char* h = rg + R_B1_HI;
+    unsigned char* l = rg + R_B1_LO;
+    switch (f) {
+      case 0: build_b1<0>(h, l, pl, K, ksc, invNN, tid); break;
+      case 1: build_b1<1>(h, l, pl, K, ksc, invNN, tid); break;
+      case 2: build_b1<2>(h, l, pl, K, ksc, invNN, tid); break;
+      default: build_b1<3>(h, l, pl, K, ksc, invNN, tid); break;
     }
+  };
+  auto put_pm = [&](int kf, int kh, float2 s1, float2 s2) {
+    const float2 ap = (kf == 0) ? s1 : cadd(s1, s2);
+    const float2 am = (kf == 0) ? make_float2(0.f, 0.f) : csub(s1, s2);
+    const int o = kf * LD + kh;
+    pl[o] = ap.x;
+    pl[PLANE / 4 + o] = ap.y;
+    pl[2 * (PLANE / 4) + o] = am.x;
+    pl[3 * (PLANE / 4) + o] = am.y;
   };
 
   // D1 (slot f) -> inverse half-axis data rows (full-axis position i), k = [w Re g | w Im g]
@@ -318,13 +295,17 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
       uout[(int64_t)kx * M + kh] = v1;
       if (kx2 != kx) uout[(int64_t)kx2 * M + kh] = v2;
     }
-    // ---- kept modes -> staging spectrum and state
-    for (int t = tid; t < NF * Kc; t += THREADS) {
-      const int fr = t / Kc, kh = t - fr * Kc;
-      const int kfi = (fr - K + N) % N;
-      const float2 v = uin[(int64_t)kfi * M + kh];
-      Xs[fr * XS_LD + kh] = v;
-      if (!a.nonlinear_only) sb.U[(int64_t)kh * N + kfi] = v;
+    // ---- kept modes, as pairs (k, -k) -> state and A+-
+    for (int t = tid; t < Kc * Kc; t += THREADS) {
+      const int kh = t / Kc, kf = t - kh * Kc;
+      const int kfm = (N - kf) & (N - 1);
+      const float2 x1 = uin[(int64_t)kf * M + kh];
+      const float2 x2 = uin[(int64_t)kfm * M + kh];
+      if (!a.nonlinear_only) {
+        sb.U[(int64_t)kh * N + kf] = x1;
+        sb.U[(int64_t)kh * N + kfm] = x2;
+      }
+      put_pm(kf, kh, x1, x2);
     }
     __syncthreads();
 
@@ -332,7 +313,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
       const int st = qq % nst;
       const bool last_of_step = (st == nst - 1);
       // ===== inverse transforms of the 4 derived fields; D2 of field f ends in TMEM slot f
-      build_b1(0);
+      b1(0);
       sync_for_mma();
       if (tid == 0) {
         tc::fence_after_sync();
@@ -348,7 +329,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
           tc::mma_split3(tmem + 128u * f, sR + R_A2_HI, sR + R_A2_LO, KI, sAiH, sAiL, KI, KI, idI2, false);
         }
         if (f < 3) {
-          build_b1(f + 1);  // B1 is free (its MMA completed); overlaps the MMA above
+          b1(f + 1);  // B1 is free (its MMA completed); overlaps the MMA above
           sync_for_mma();
           if (tid == 0) {
             tc::fence_after_sync();
@@ -436,70 +417,71 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
       bad = !wait_mma();
       if (bad) break;
 
-      // ===== D4 -> nonlinear term at the kept modes -> ETDRK stage update
+      // ===== D4 -> nonlinear term at the kept modes (region R, B4 is no longer read)
       if (q < 3) {
         const bool srow = lane >= 16;
         const int kf = 16 * q + (lane & 15);
         const bool active = kf <= K && !(srow && kf == 0);
-        const int kfs = srow ? -kf : kf;
-        const int kfi = (kfs + N) % N;
+        const int kfi = ((srow ? -kf : kf) + N) & (N - 1);
         const int b0 = upper ? 3 : 0;
         for (int b = b0; b < b0 + 3; ++b) {
           const uint32_t na = 32u * (b >> 1) + 8u * (b & 1);
           float Ca[8], Cb[8];
           tc::tmem_ld8(tl + 128u + na, Ca);
           tc::tmem_ld8(tl + 128u + na + 16u, Cb);
-          float2 res0 = make_float2(0.f, 0.f);
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const float Pa = __shfl_xor_sync(0xffffffffu, Ca[j], 16);
             const float Pb = __shfl_xor_sync(0xffffffffu, Cb[j], 16);
             const int kh = 8 * b + j;
-            float2 Z;
-            if (!srow) {
-              Z = make_float2(Ca[j] - Pb, -Cb[j] - Pa);
-            } else {
-              Z = make_float2(Pa + Cb[j], Ca[j] - Pb);
-            }
+            const float2 Z = srow ? make_float2(Pa + Cb[j], Ca[j] - Pb) : make_float2(Ca[j] - Pb, -Cb[j] - Pa);
             if (active && kh <= K) {
               float2 nv = cscale(Z, negb);
-              if (kh == P.inj_mode && kfs == 0) nv.x += P.inj_value;
-              if (a.nonlinear_only) {
-                uout[(int64_t)kfi * M + kh] = nv;
-              } else {
-                const float2 s = stage_upd(P, sb, (int64_t)kh * N + kfi, st, nv);
-                Xs[(kfs + K) * XS_LD + kh] = s;
-                if (j == 0) res0 = s;
-              }
-            }
-          }
-          if (b == 0 && last_of_step && a.project && !a.nonlinear_only) {
-            // c2r projection of the step's physical round trip on the half-axis column 0
-            const float2 other = make_float2(__shfl_xor_sync(0xffffffffu, res0.x, 16),
-                                             __shfl_xor_sync(0xffffffffu, res0.y, 16));
-            if (active) {
-              const float2 mine = res0;
-              const float2 a1 = srow ? other : mine;          // mode +kf
-              const float2 a2 = (kf == 0) ? mine : (srow ? mine : other);  // mode -kf
-              const float2 pv = make_float2(0.5f * (a1.x + a2.x), 0.5f * (a1.y - a2.y));
-              const float2 val = srow ? cconj(pv) : pv;
-              sb.U[kfi] = val;
-              Xs[(kfs + K) * XS_LD] = val;
+              if (kh == P.inj_mode && kfi == 0) nv.x += P.inj_value;
+              nvb[kh * N + kfi] = nv;
             }
           }
         }
       }
       tc::fence_before_sync();
       __syncthreads();
+      // ===== ETDRK stage update on mode pairs (k, -k), all threads; next stage's A+-
+      if (a.nonlinear_only) {
+        for (int t = tid; t < Kc * Kc; t += THREADS) {
+          const int kh = t / Kc, kf = t - kh * Kc;
+          const int kfm = (N - kf) & (N - 1);
+          uout[(int64_t)kf * M + kh] = nvb[kh * N + kf];
+          uout[(int64_t)kfm * M + kh] = nvb[kh * N + kfm];
+        }
+      } else {
+        for (int t = tid; t < Kc * Kc; t += THREADS) {
+          const int kh = t / Kc, kf = t - kh * Kc;
+          const int kfm = (N - kf) & (N - 1);
+          const int64_t o1 = (int64_t)kh * N + kf, o2 = (int64_t)kh * N + kfm;
+          float2 s1 = stage_upd(P, sb, o1, st, nvb[kh * N + kf]);
+          float2 s2 = (kf > 0) ? stage_upd(P, sb, o2, st, nvb[kh * N + kfm]) : s1;
+          if (last_of_step && a.project && kh == 0) {
+            // c2r projection of the step's physical round trip on the half-axis column 0
+            const float2 pv = make_float2(0.5f * (s1.x + s2.x), 0.5f * (s1.y - s2.y));
+            s1 = pv;
+            s2 = cconj(pv);
+            sb.U[o1] = s1;
+            if (kf > 0) sb.U[o2] = s2;
+          }
+          put_pm(kf, kh, s1, s2);
+        }
+      }
+      __syncthreads();
     }
     if (bad) break;
 
     // ---- kept modes -> output
     if (!a.nonlinear_only) {
-      for (int t = tid; t < NF * Kc; t += THREADS) {
-        const int fr = t / Kc, kh = t - fr * Kc;
-        const int kfi = (fr - K + N) % N;
-        uout[(int64_t)kfi * M + kh] = sb.U[(int64_t)kh * N + kfi];
+      for (int t = tid; t < Kc * Kc; t += THREADS) {
+        const int kh = t / Kc, kf = t - kh * Kc;
+        const int kfm = (N - kf) & (N - 1);
+        uout[(int64_t)kf * M + kh] = sb.U[(int64_t)kh * N + kf];
+        uout[(int64_t)kfm * M + kh] = sb.U[(int64_t)kh * N + kfm];
       }
     }
     __syncthreads();
@@ -513,6 +495,57 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+// ---- host-side image of the constant tiles (FP64 angles, bf16 hi/lo, canonical K-major layout)
+static uint16_t to_bf16(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;
+  u += 0x7fffu + ((u >> 16) & 1u);  // round to nearest even
+  return (uint16_t)(u >> 16);
+}
+static double from_bf16(uint16_t h) {
+  const uint32_t u = (uint32_t)h << 16;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return (double)f;
+}
+static double cos2pi(long m) { return std::cos(2.0 * M_PI * (double)(m % N) / N); }
+static double sin2pi(long m) { return std::sin(2.0 * M_PI * (double)(m % N) / N); }
+
+// Ai[r][k]: rows r = 32 w + l, slot s = 16 w + (l & 15); l < 16: cos row of
+// index s; l >= 16: sin row of index s (s >= 1) or the cos row of index N/2 (s = 0).
+static double ai_val(int r, int k, int K) {
+  const int w = r >> 5, l = r & 31, s = 16 * w + (l & 15);
+  const bool sinl = l >= 16;
+  if (!sinl || s == 0) {
+    const int idx = sinl ? H : s;
+    return (k < 48 && k <= K) ? cos2pi((long)k * idx) : 0.0;
+  }
+  const int kk = k - 48;
+  return (k >= 48 && kk >= 1 && kk <= K) ? sin2pi((long)kk * s) : 0.0;
+}
+// Af[r][k]: rows r = 32 w + l (w < 3), mode m = 16 w + (l & 15); l < 16: cos
+// row over e_0..e_64 (k = 0..64); l >= 16: sin row over o_1..o_63 (k = 65..127).
+static double af_val(int r, int k, int K) {
+  const int w = r >> 5, l = r & 31, m = 16 * w + (l & 15);
+  if (m > K) return 0.0;
+  if (l < 16) return k <= 64 ? cos2pi((long)m * k) : 0.0;
+  if (m == 0 || k < 65) return 0.0;
+  return sin2pi((long)m * (k - 64));
+}
+static void put_tile(std::vector<unsigned char>& img, uint32_t off_hi, uint32_t off_lo, int rows, int kdim, int K,
+                     double (*val)(int, int, int)) {
+  for (int r = 0; r < rows; ++r)
+    for (int k = 0; k < kdim; ++k) {
+      const double d = val(r, k, K);
+      const uint16_t h = to_bf16((float)d);
+      const uint16_t l = to_bf16((float)(d - from_bf16(h)));
+      const uint32_t o = tc::kmaj_off(r, k, kdim);
+      std::memcpy(&img[off_hi + o], &h, 2);
+      std::memcpy(&img[off_lo + o], &l, 2);
+    }
 }
 
 }  // namespace tcd
@@ -538,7 +571,14 @@ int tcdft2d_configure(exgb_plan* plan) {
   const int K = std::min(plan->dev.kmax, tcd::KMAX);
   const size_t per = (size_t)stage_nbufs(plan->dev.order) * (K + 1) * tcd::N;
   if (!plan->d_tc_scratch) {
-    EXGB_CUDA(cudaMalloc(&plan->d_tc_scratch, sizeof(float2) * per * plan->sm_count));
+    std::vector<unsigned char> img(tcd::CONST_BYTES, 0);
+    tcd::put_tile(img, tcd::OFF_AI_HI, tcd::OFF_AI_LO, 128, tcd::KI, K, tcd::ai_val);
+    tcd::put_tile(img, tcd::OFF_AF_HI, tcd::OFF_AF_LO, 96, tcd::KF, K, tcd::af_val);
+    const size_t scratch = sizeof(float2) * per * plan->sm_count;
+    EXGB_CUDA(cudaMalloc(&plan->d_tc_scratch, scratch + tcd::CONST_BYTES));
+    EXGB_CUDA(cudaMemcpy((unsigned char*)plan->d_tc_scratch + scratch, img.data(), img.size(),
+                         cudaMemcpyHostToDevice));
+    plan->tc_const_offset = scratch;
     EXGB_CUDA(cudaMalloc(&plan->d_status, sizeof(int)));
     EXGB_CUDA(cudaMemset(plan->d_status, 0, sizeof(int)));
   }
@@ -559,6 +599,7 @@ int tcdft2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2
   a.nonlinear_only = nonlinear_only;
   a.scratch = (float2*)plan->d_tc_scratch;
   a.scratch_stride = (int64_t)plan->tc_scratch_per_cta;
+  a.consts = reinterpret_cast<const uint4*>((const unsigned char*)plan->d_tc_scratch + plan->tc_const_offset);
   a.status = plan->d_status;
   const int grid = (int)std::min<int64_t>(batch, plan->sm_count);
   tcd::tcdft2d_kernel<<<grid, tcd::THREADS, tcd::SMEM_BYTES, st>>>(a);
