@@ -58,7 +58,7 @@ constexpr int THREADS = 256;
 constexpr int KMAX = 47;
 constexpr int KI = 96;   // inverse contraction: [cos part, modes 0..47 | sin part, modes 0..47]
 constexpr int KF = 128;  // forward contraction: [e_0 .. e_63 | e_64 | o_1 .. o_63]
-constexpr int LD = 48;   // k_half stride of the A+- planes
+constexpr int LD = 49;   // k_half stride of the A+- planes (odd: conflict-free row and column access)
 // shared memory (bytes).  Af stores rows 0..95; the MMA also reads rows
 // 96..127, which overlap the next tile (their outputs are never used).
 constexpr uint32_t TILE_AI = 128 * KI * 2;
