@@ -78,7 +78,9 @@ constexpr uint32_t R_A2_HI = 2 * TILE_B1, R_A2_LO = 2 * TILE_B1 + TILE_A2;
 constexpr uint32_t R_BYTES = 2 * TILE_B1 + 2 * TILE_A2;
 constexpr uint32_t PLANE = 48 * LD * 4;     // one float plane [k_full 0..47][k_half]
 constexpr uint32_t OFF_PM = OFF_R + R_BYTES;  // planes A+re, A+im, A-re, A-im
-constexpr uint32_t SMEM_BYTES = OFF_PM + 4 * PLANE;
+constexpr uint32_t OFF_IL = OFF_PM + 4 * PLANE;  // 1 / (N^2 Lap) on the kept modes [k_full][k_half]
+constexpr uint32_t OFF_TAIL = OFF_IL + PLANE;     // mbarrier (8 B) and TMEM base address (4 B)
+constexpr uint32_t SMEM_BYTES = OFF_TAIL + 16;
 static_assert(2 * TILE_B3 <= R_BYTES && 2 * TILE_B4 <= R_BYTES, "region R too small");
 static_assert(48u * N * 8u <= R_BYTES, "nonlinear-term buffer must fit region R");
 static_assert(128 * KF * 2 - TILE_AF <= R_BYTES, "Af overflow rows must stay inside shared memory");
@@ -109,9 +111,10 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // + k_half, column k = [S_k (k < 48) | D_(k-48)].  S/D = i m (A+ or A-), the
 // even fields (u, wy) taking A+ for S and the odd ones (v, wx) A- (the
 // multiplier changes sign with k_full).  Values outside the kept set are 0.
+// `il` holds 1 / (N^2 Lap) (u, v); wx and wy carry 1 / N^2 directly.
 template <int F>
-__device__ __forceinline__ void build_b1(unsigned char* hi, unsigned char* lo, const float* pl, int K, float ksc,
-                                         float invNN, int tid) {
+__device__ __forceinline__ void build_b1(unsigned char* hi, unsigned char* lo, const float* pl, const float* il,
+                                         int K, float ksc, float invNN, int tid) {
   constexpr bool odd = (F == 1 || F == 2);
   for (int t = tid; t < 96 * (KI / 8); t += THREADS) {
     const int c = t / 96, n = t - c * 96;
@@ -125,7 +128,7 @@ __device__ __forceinline__ void build_b1(unsigned char* hi, unsigned char* lo, c
       const float kys = ksc * (float)kh;
       const bool minus = (dblk != odd);
       const float* P = pl + ((minus ? 2 : 0) + (part ? 0 : 1)) * (int)(PLANE / 4);
-      const float sg = part ? invNN : -invNN;  // i m A = (-m A.im, m A.re)
+      const float sg = part ? 1.f : -1.f;  // i m A = (-m A.im, m A.re)
       const int kf0 = 8 * c - (dblk ? 48 : 0);
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
@@ -134,13 +137,12 @@ __device__ __forceinline__ void build_b1(unsigned char* hi, unsigned char* lo, c
           const float kxs = ksc * (float)kf;
           float m;
           if (F == 2) {
-            m = kxs;
+            m = kxs * invNN;
           } else if (F == 3) {
-            m = kys;
+            m = kys * invNN;
           } else {
-            const float lap = -(kxs * kxs + kys * kys);
-            const float il = (lap == 0.f) ? 1.f : rcp_approx(lap);
-            m = (F == 0) ? kys * il : -kxs * il;
+            const float w = il[kf * LD + kh];
+            m = (F == 0) ? kys * w : -kxs * w;
           }
           v[j] = sg * m * P[kf * LD + kh];
         }
@@ -151,9 +153,9 @@ __device__ __forceinline__ void build_b1(unsigned char* hi, unsigned char* lo, c
 }
 
 __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
-  extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ __align__(8) uint64_t s_mbar;
-  __shared__ uint32_t s_tbase;
+  extern __shared__ __align__(128) unsigned char sm[];
+  uint64_t& s_mbar = *reinterpret_cast<uint64_t*>(sm + OFF_TAIL);
+  uint32_t& s_tbase = *reinterpret_cast<uint32_t*>(sm + OFF_TAIL + 8);
   const PlanDev& P = a.P;
   const int K = min(P.kmax, KMAX);
   const int Kc = K + 1;
@@ -161,6 +163,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
   const bool upper = warp >= 4;
   unsigned char* rg = sm + OFF_R;
   float* pl = reinterpret_cast<float*>(sm + OFF_PM);
+  float* ilt = reinterpret_cast<float*>(sm + OFF_IL);
   float2* nvb = reinterpret_cast<float2*>(rg);  // nonlinear term [k_half][k_full index], region R
   const uint32_t sAiH = tc::smem_u32(sm + OFF_AI_HI), sAiL = tc::smem_u32(sm + OFF_AI_LO);
   const uint32_t sAfH = tc::smem_u32(sm + OFF_AF_HI), sAfL = tc::smem_u32(sm + OFF_AF_LO);
@@ -170,6 +173,12 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
   {
     uint4* dst = reinterpret_cast<uint4*>(sm);
     for (int t = tid; t < (int)(CONST_BYTES / 16); t += THREADS) dst[t] = __ldg(a.consts + t);
+  }
+  for (int t = tid; t < 48 * LD; t += THREADS) {
+    const int kf = t / LD, kh = t - kf * LD;
+    const float kxs = a.P.kscale * (float)kf, kys = a.P.kscale * (float)kh;
+    const float lap = -(kxs * kxs + kys * kys);
+    ilt[t] = (lap == 0.f) ? 0.f : __frcp_rn(lap) * (1.f / ((float)N * (float)N));
   }
   if (warp == 0) {
     tc::tmem_alloc(&s_tbase, 512);
@@ -213,10 +222,10 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
     unsigned char* h = rg + R_B1_HI;
     unsigned char* l = rg + R_B1_LO;
     switch (f) {
-      case 0: build_b1<0>(h, l, pl, K, ksc, invNN, tid); break;
-      case 1: build_b1<1>(h, l, pl, K, ksc, invNN, tid); break;
-      case 2: build_b1<2>(h, l, pl, K, ksc, invNN, tid); break;
-      default: build_b1<3>(h, l, pl, K, ksc, invNN, tid); break;
+      case 0: build_b1<0>(h, l, pl, ilt, K, ksc, invNN, tid); break;
+      case 1: build_b1<1>(h, l, pl, ilt, K, ksc, invNN, tid); break;
+      case 2: build_b1<2>(h, l, pl, ilt, K, ksc, invNN, tid); break;
+      default: build_b1<3>(h, l, pl, ilt, K, ksc, invNN, tid); break;
     }
   };
   auto put_pm = [&](int kf, int kh, float2 s1, float2 s2) {
@@ -238,8 +247,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
     const int b0 = upper ? 3 : 0;
     for (int b = b0; b < b0 + 3; ++b) {
       float re[8], im[8], gr[8], gi[8];
-      tc::tmem_ld8(tl + 128u * f + 8u * b, re);
-      tc::tmem_ld8(tl + 128u * f + 48u + 8u * b, im);
+      tc::tmem_ld8x2(tl + 128u * f + 8u * b, tl + 128u * f + 48u + 8u * b, re, im);
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const float pre = __shfl_xor_sync(0xffffffffu, re[j], 16);
@@ -348,11 +356,8 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
         for (int c = c0; c < c0 + 4; ++c) {
           const uint32_t cc = 32u * (c >> 1) + 8u * (c & 1);
           float Pv[4][8], Qv[4][8];
-#pragma unroll
-          for (int f = 0; f < 4; ++f) {
-            tc::tmem_ld8(tl + 128u * f + cc, Pv[f]);
-            tc::tmem_ld8(tl + 128u * f + cc + 16u, Qv[f]);
-          }
+          tc::tmem_ld8x4(tl + cc, tl + 128u + cc, tl + 256u + cc, tl + 384u + cc, Pv[0], Pv[1], Pv[2], Pv[3]);
+          tc::tmem_ld8x4(tl + cc + 16u, tl + 144u + cc, tl + 272u + cc, tl + 400u + cc, Qv[0], Qv[1], Qv[2], Qv[3]);
           float e[8], o[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
@@ -390,8 +395,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
         const int c0 = upper ? 4 : 0;
         for (int c = c0; c < c0 + 4; ++c) {
           float A[8], B[8];
-          tc::tmem_ld8(tl + 8u * c, A);
-          tc::tmem_ld8(tl + 120u - 8u * c, B);
+          tc::tmem_ld8x2(tl + 8u * c, tl + 120u - 8u * c, A, B);
           const float X1 = tc::tmem_ld1(tl + (c == 0 ? 64u : 128u - 8u * c));
           float e[8], o[8];
 #pragma unroll
@@ -427,8 +431,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
         for (int b = b0; b < b0 + 3; ++b) {
           const uint32_t na = 32u * (b >> 1) + 8u * (b & 1);
           float Ca[8], Cb[8];
-          tc::tmem_ld8(tl + 128u + na, Ca);
-          tc::tmem_ld8(tl + 128u + na + 16u, Cb);
+          tc::tmem_ld8x2(tl + 128u + na, tl + 128u + na + 16u, Ca, Cb);
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
             const float Pa = __shfl_xor_sync(0xffffffffu, Ca[j], 16);
@@ -452,6 +455,73 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
           const int kfm = (N - kf) & (N - 1);
           uout[(int64_t)kf * M + kh] = nvb[kh * N + kf];
           uout[(int64_t)kfm * M + kh] = nvb[kh * N + kfm];
+        }
+      } else if (P.order == 2) {
+        // ETDRK2 (etdrk/_etdrk_2.py:91-102), four mode pairs per thread with all loads issued first
+        const int total = Kc * Kc;
+        for (int t0 = tid; t0 < total; t0 += 4 * THREADS) {
+          float2 n1[4], n2[4], x1[4], x2[4], y1[4], y2[4], e1[4], e2[4];
+          float c1[4], c2[4];
+          int kfv[4], khv[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int t = min(t0 + u * THREADS, total - 1);
+            const int kh = t / Kc, kf = t - kh * Kc;
+            const int kfm = (N - kf) & (N - 1);
+            const int64_t o1 = (int64_t)kh * N + kf, o2 = (int64_t)kh * N + kfm;
+            khv[u] = kh;
+            kfv[u] = kf;
+            n1[u] = nvb[kh * N + kf];
+            n2[u] = nvb[kh * N + kfm];
+            if (st == 0) {
+              x1[u] = sb.U[o1];
+              x2[u] = sb.U[o2];
+              e1[u] = __ldg(P.E + o1);
+              e2[u] = __ldg(P.E + o2);
+              c1[u] = __ldg(P.c[0] + o1);
+              c2[u] = __ldg(P.c[0] + o2);
+            } else {
+              x1[u] = sb.S[o1];
+              x2[u] = sb.S[o2];
+              y1[u] = sb.N0[o1];
+              y2[u] = sb.N0[o2];
+              c1[u] = __ldg(P.c[1] + o1);
+              c2[u] = __ldg(P.c[1] + o2);
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (t0 + u * THREADS >= total) break;
+            const int kh = khv[u], kf = kfv[u];
+            const int kfm = (N - kf) & (N - 1);
+            const int64_t o1 = (int64_t)kh * N + kf, o2 = (int64_t)kh * N + kfm;
+            float2 s1, s2;
+            if (st == 0) {
+              s1 = cadd(cmul(e1[u], x1[u]), cscale(n1[u], c1[u]));
+              s2 = cadd(cmul(e2[u], x2[u]), cscale(n2[u], c2[u]));
+              sb.N0[o1] = n1[u];
+              sb.S[o1] = s1;
+              if (kf > 0) {
+                sb.N0[o2] = n2[u];
+                sb.S[o2] = s2;
+              } else {
+                s2 = s1;
+              }
+            } else {
+              s1 = cadd(x1[u], cscale(csub(n1[u], y1[u]), c1[u]));
+              s2 = cadd(x2[u], cscale(csub(n2[u], y2[u]), c2[u]));
+              if (kf == 0) s2 = s1;
+              if (a.project && kh == 0) {
+                // c2r projection of the step's physical round trip on the half-axis column 0
+                const float2 pv = make_float2(0.5f * (s1.x + s2.x), 0.5f * (s1.y - s2.y));
+                s1 = pv;
+                s2 = cconj(pv);
+              }
+              sb.U[o1] = s1;
+              if (kf > 0) sb.U[o2] = s2;
+            }
+            put_pm(kf, kh, s1, s2);
+          }
         }
       } else {
         for (int t = tid; t < Kc * Kc; t += THREADS) {
