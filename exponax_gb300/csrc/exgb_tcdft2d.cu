@@ -113,42 +113,55 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // multiplier changes sign with k_full).  Values outside the kept set are 0.
 // `il` holds 1 / (N^2 Lap) (u, v); wx and wy carry 1 / N^2 directly.
 template <int F>
+__device__ __forceinline__ void b1_chunk(int t, float (&v)[8], const float* pl, const float* il, int K, float ksc,
+                                         float invNN) {
+  constexpr bool odd = (F == 1 || F == 2);
+  const int c = t / 96, n = t - c * 96;
+  const int part = n >= 48 ? 1 : 0;
+  const int kh = n - 48 * part;
+  const bool dblk = c >= 6;
+  const bool minus = (dblk != odd);
+  const float* P = pl + ((minus ? 2 : 0) + (part ? 0 : 1)) * (int)(PLANE / 4);
+  const float sg = part ? 1.f : -1.f;  // i m A = (-m A.im, m A.re)
+  const float kys = ksc * (float)kh;
+  const int kf0 = 8 * c - (dblk ? 48 : 0);
+  const int khc = min(kh, 47);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int kf = kf0 + j;
+    const bool ok = (kh <= K) && (kf <= K);
+    const int o = min(kf, 47) * LD + khc;  // in-bounds address also for masked entries
+    const float kxs = ksc * (float)kf;
+    float m;
+    if (F == 2) {
+      m = kxs * invNN;
+    } else if (F == 3) {
+      m = kys * invNN;
+    } else {
+      m = (F == 0) ? kys * il[o] : -kxs * il[o];
+    }
+    v[j] = ok ? sg * m * P[o] : 0.f;
+  }
+}
+
+// Inverse full-axis data of field F (0 u, 1 v, 2 wx, 3 wy): row n = part * 48
+// + k_half, column k = [S_k (k < 48) | D_(k-48)].  S/D = i m (A+ or A-), the
+// even fields (u, wy) taking A+ for S and the odd ones (v, wx) A- (the
+// multiplier changes sign with k_full).  Values outside the kept set are 0.
+// `il` holds 1 / (N^2 Lap) (u, v); wx and wy carry 1 / N^2 directly.  Two
+// 8-column chunks per iteration for instruction-level parallelism.
+template <int F>
 __device__ __forceinline__ void build_b1(unsigned char* hi, unsigned char* lo, const float* pl, const float* il,
                                          int K, float ksc, float invNN, int tid) {
-  constexpr bool odd = (F == 1 || F == 2);
-  for (int t = tid; t < 96 * (KI / 8); t += THREADS) {
-    const int c = t / 96, n = t - c * 96;
-    const int part = n >= 48 ? 1 : 0;
-    const int kh = n - 48 * part;
-    const bool dblk = c >= 6;
-    float v[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] = 0.f;
-    if (kh <= K) {
-      const float kys = ksc * (float)kh;
-      const bool minus = (dblk != odd);
-      const float* P = pl + ((minus ? 2 : 0) + (part ? 0 : 1)) * (int)(PLANE / 4);
-      const float sg = part ? 1.f : -1.f;  // i m A = (-m A.im, m A.re)
-      const int kf0 = 8 * c - (dblk ? 48 : 0);
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int kf = kf0 + j;
-        if (kf <= K) {
-          const float kxs = ksc * (float)kf;
-          float m;
-          if (F == 2) {
-            m = kxs * invNN;
-          } else if (F == 3) {
-            m = kys * invNN;
-          } else {
-            const float w = il[kf * LD + kh];
-            m = (F == 0) ? kys * w : -kxs * w;
-          }
-          v[j] = sg * m * P[kf * LD + kh];
-        }
-      }
-    }
-    tc::split8_store(v, hi, lo, tc::kmaj_chunk(n, c, KI));
+  constexpr int TOTAL = 96 * (KI / 8);
+  for (int t = tid; t < TOTAL; t += 2 * THREADS) {
+    const int t2 = t + THREADS;
+    const bool has2 = t2 < TOTAL;
+    float va[8], vb[8];
+    b1_chunk<F>(t, va, pl, il, K, ksc, invNN);
+    b1_chunk<F>(has2 ? t2 : t, vb, pl, il, K, ksc, invNN);
+    tc::split8_store(va, hi, lo, tc::kmaj_chunk(t - (t / 96) * 96, t / 96, KI));
+    if (has2) tc::split8_store(vb, hi, lo, tc::kmaj_chunk(t2 - (t2 / 96) * 96, t2 / 96, KI));
   }
 }
 
@@ -245,24 +258,28 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
     const int iout = sinl ? (s == 0 ? H : N - s) : s;
     const bool eonly = (s == 0);
     const int b0 = upper ? 3 : 0;
-    for (int b = b0; b < b0 + 3; ++b) {
-      float re[8], im[8], gr[8], gi[8];
-      tc::tmem_ld8x2(tl + 128u * f + 8u * b, tl + 128u * f + 48u + 8u * b, re, im);
+    float re[32], im[32];
+    tc::tmem_ld32x2(tl + 128u * f + 8u * b0, tl + 128u * f + 48u + 8u * b0, re, im);
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb) {
+      const int b = b0 + bb;
+      float gr[8], gi[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const float pre = __shfl_xor_sync(0xffffffffu, re[j], 16);
-        const float pim = __shfl_xor_sync(0xffffffffu, im[j], 16);
+        const float r0 = re[8 * bb + j], i0 = im[8 * bb + j];
+        const float pre = __shfl_xor_sync(0xffffffffu, r0, 16);
+        const float pim = __shfl_xor_sync(0xffffffffu, i0, 16);
         const float w = (b == 0 && j == 0) ? 1.f : 2.f;
         float r1, r2;
         if (eonly) {
-          r1 = re[j];
-          r2 = im[j];
+          r1 = r0;
+          r2 = i0;
         } else if (!sinl) {
-          r1 = re[j] - pim;  // E + i O
-          r2 = im[j] + pre;
+          r1 = r0 - pim;  // E + i O
+          r2 = i0 + pre;
         } else {
-          r1 = pre + im[j];  // E - i O
-          r2 = pim - re[j];
+          r1 = pre + i0;  // E - i O
+          r2 = pim - r0;
         }
         gr[j] = w * r1;
         gi[j] = w * r2;
