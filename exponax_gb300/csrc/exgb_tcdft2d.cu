@@ -112,56 +112,50 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // even fields (u, wy) taking A+ for S and the odd ones (v, wx) A- (the
 // multiplier changes sign with k_full).  Values outside the kept set are 0.
 // `il` holds 1 / (N^2 Lap) (u, v); wx and wy carry 1 / N^2 directly.
-template <int F>
-__device__ __forceinline__ void b1_chunk(int t, float (&v)[8], const float* pl, const float* il, int K, float ksc,
-                                         float invNN) {
-  constexpr bool odd = (F == 1 || F == 2);
-  const int c = t / 96, n = t - c * 96;
-  const int part = n >= 48 ? 1 : 0;
-  const int kh = n - 48 * part;
-  const bool dblk = c >= 6;
-  const bool minus = (dblk != odd);
-  const float* P = pl + ((minus ? 2 : 0) + (part ? 0 : 1)) * (int)(PLANE / 4);
-  const float sg = part ? 1.f : -1.f;  // i m A = (-m A.im, m A.re)
-  const float kys = ksc * (float)kh;
-  const int kf0 = 8 * c - (dblk ? 48 : 0);
-  const int khc = min(kh, 47);
-#pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const int kf = kf0 + j;
-    const bool ok = (kh <= K) && (kf <= K);
-    const int o = min(kf, 47) * LD + khc;  // in-bounds address also for masked entries
-    const float kxs = ksc * (float)kf;
-    float m;
-    if (F == 2) {
-      m = kxs * invNN;
-    } else if (F == 3) {
-      m = kys * invNN;
-    } else {
-      m = (F == 0) ? kys * il[o] : -kxs * il[o];
-    }
-    v[j] = ok ? sg * m * P[o] : 0.f;
-  }
-}
-
 // Inverse full-axis data of field F (0 u, 1 v, 2 wx, 3 wy): row n = part * 48
 // + k_half, column k = [S_k (k < 48) | D_(k-48)].  S/D = i m (A+ or A-), the
 // even fields (u, wy) taking A+ for S and the odd ones (v, wx) A- (the
 // multiplier changes sign with k_full).  Values outside the kept set are 0.
-// `il` holds 1 / (N^2 Lap) (u, v); wx and wy carry 1 / N^2 directly.  Two
-// 8-column chunks per iteration for instruction-level parallelism.
+// `il` holds 1 / (N^2 Lap) (u, v); wx and wy carry 1 / N^2 directly.  One
+// task = one 8-column chunk of both rows (re part, im part) of a k_half:
+// i m A = (-m A.im, m A.re) shares the multiplier and the address.
 template <int F>
 __device__ __forceinline__ void build_b1(unsigned char* hi, unsigned char* lo, const float* pl, const float* il,
                                          int K, float ksc, float invNN, int tid) {
-  constexpr int TOTAL = 96 * (KI / 8);
-  for (int t = tid; t < TOTAL; t += 2 * THREADS) {
-    const int t2 = t + THREADS;
-    const bool has2 = t2 < TOTAL;
-    float va[8], vb[8];
-    b1_chunk<F>(t, va, pl, il, K, ksc, invNN);
-    b1_chunk<F>(has2 ? t2 : t, vb, pl, il, K, ksc, invNN);
-    tc::split8_store(va, hi, lo, tc::kmaj_chunk(t - (t / 96) * 96, t / 96, KI));
-    if (has2) tc::split8_store(vb, hi, lo, tc::kmaj_chunk(t2 - (t2 / 96) * 96, t2 / 96, KI));
+  constexpr bool odd = (F == 1 || F == 2);
+  for (int t = tid; t < 48 * (KI / 8); t += THREADS) {
+    const int c = t / 48, kh = t - c * 48;
+    const bool dblk = c >= 6;
+    const bool minus = (dblk != odd);
+    const float* Pre = pl + (minus ? 2 : 0) * (int)(PLANE / 4);
+    const float* Pim = Pre + PLANE / 4;
+    float vr[8], vi[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) vr[j] = vi[j] = 0.f;
+    if (kh <= K) {
+      const float kys = ksc * (float)kh;
+      const int kf0 = 8 * c - (dblk ? 48 : 0);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int kf = kf0 + j;
+        if (kf <= K) {
+          const int o = kf * LD + kh;
+          const float kxs = ksc * (float)kf;
+          float m;
+          if (F == 2) {
+            m = kxs * invNN;
+          } else if (F == 3) {
+            m = kys * invNN;
+          } else {
+            m = (F == 0) ? kys * il[o] : -kxs * il[o];
+          }
+          vr[j] = -m * Pim[o];
+          vi[j] = m * Pre[o];
+        }
+      }
+    }
+    tc::split8_store(vr, hi, lo, tc::kmaj_chunk(kh, c, KI));
+    tc::split8_store(vi, hi, lo, tc::kmaj_chunk(48 + kh, c, KI));
   }
 }
 
