@@ -294,6 +294,21 @@ def run_gb300(args, rank, ws):
 
 
 # ------------------------------------------------------------------ other benchmark configurations
+# MMA work of tcdft2d_kernel per sample and ETDRK2 step (N = 128): per stage 4 x (128x96x96 + 128x128x96)
+# + 128x128x128 + 128x96x128 multiply-adds, x 2 flop, x 3 split-BF16 products; 2 stages.
+TC128_MMA_FLOPS_PER_SAMPLE_STEP = 2 * 3 * 2 * (4 * (128 * 96 * 96 + 128 * 128 * 96) + 128 * 128 * 128 + 128 * 96 * 128)
+
+
+def _traffic(name):
+    """DRAM bytes per launch from the committed ncu summary profiles/<name>_traffic.txt, or None."""
+    tf = os.path.join(ROOT, "profiles", f"{name}_traffic.txt")
+    if os.path.exists(tf):
+        for ln in open(tf):
+            if ln.startswith("dram_bytes_per_launch="):
+                return float(ln.split("=")[1])
+    return None
+
+
 def _timed(fn, steps, warmup, flush=None):
     import torch
 
@@ -478,6 +493,31 @@ def run_other(args, rank, ws):
                     e2e={"value": dof / (ems * 1e-3), "unit": "DOF-steps/s", "ms_per_step": ems,
                          "h2d_bytes_per_step": int(pin.numel() * 4), "d2h_bytes_per_step": int(pout.numel() * 4)},
                     gpu_launches=args.steps)
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        if args.precision == "fp32":
+            peak = float(peaks.get("hbm_gbs", 6800.0))
+            bpd = 6 * 8 * (Nk // 2 + 1) / Nk  # 6 complex64 half-spectrum passes per ETDRK2 step
+            achieved = dof * bpd / (ms * 1e-3) / 1e9
+            line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                "frac": achieved / peak, "traffic": _traffic("vort2d_kernel_kolmo128_b1024"),
+                                "kernel": "vort2d_kernel<128,512>",
+                                "note": f"algorithmic {bpd:.3f} B/DOF-step x {B}x{Nk}^2x{n} per launch; peak "
+                                        + ("measured" if "hbm_gbs" in peaks else "fallback")}
+        else:
+            peak = float(peaks.get("bf16_tflops", 1900.0))
+            flops = TC128_MMA_FLOPS_PER_SAMPLE_STEP * B * n
+            achieved = flops / (ms * 1e-3) / 1e12
+            line["roofline"] = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                                "frac": achieved / peak, "traffic": _traffic("tcdft2d_kernel_kolmo128_b1024"),
+                                "kernel": "tcdft2d_kernel",
+                                "note": f"{TC128_MMA_FLOPS_PER_SAMPLE_STEP} MMA flop per sample-step (10 split-BF16 "
+                                        "contraction chains, 3 products each, as issued) x "
+                                        f"{B}x{n} per launch; peak bf16 burst "
+                                        + ("measured" if "bf16_tflops" in peaks else "fallback")}
         if not args.no_cpu:
             from oracle import exponax_np as o
 
