@@ -125,7 +125,7 @@ def tune(stepper, *, batch=64, nsteps=10, repeats=3, use_cache=True, write_cache
     cfg = get_tuning(plan)
     is_reg2d = D == 2 and cfg["cluster"] > 0 and N in (64, 128, 256) and stepper.order > 0
     if is_reg2d:
-        for G in (1, 2, 4, 8):
+        for G in range(1, 9):
             if _set(plan, 1, [G]) != EXGB_OK:
                 continue
             results.append(({"cluster": G}, _time(plan, uh, out, batch, nsteps, repeats)))

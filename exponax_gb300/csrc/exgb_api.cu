@@ -464,7 +464,7 @@ extern "C" int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int 
     if (plan->dev.D != 2 || plan->dev.kind == EXGB_NL_ZERO || plan->dev.order == 0)
       return fail(EXGB_EUNSUPPORTED, "cluster size applies to 2D nonlinear plans");
     const int G = n > 0 ? values[0] : 0;
-    if (G != 0 && G != 1 && G != 2 && G != 4 && G != 8) return fail(EXGB_EINVAL, "cluster size must be 1, 2, 4 or 8");
+    if (G < 0 || G > 8) return fail(EXGB_EINVAL, "cluster size must be 1..8 (0 = automatic)");
     EXGB_CUDA(cudaDeviceSynchronize());
     cudaFree(plan->d_scratch);
     plan->d_scratch = nullptr;

@@ -28,7 +28,7 @@ namespace exgb {
 
 struct ArgsV2 {
   PlanDev P;
-  int G, Cl, Rl, lgRl, Kc, KcP, Ul;
+  int G, Cl, Rl, Kc, KcP, Ul;
   const float2* in;
   float2* out;
   int64_t batch;
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   const int cid = (int)(blockIdx.x / G);
   const int ncl = (int)(gridDim.x / G);
   const PlanDev& P = a.P;
-  const int Kc = a.Kc, K = Kc - 1, KcP = a.KcP, Cl = a.Cl, Rl = a.Rl, lgRl = a.lgRl;
+  const int Kc = a.Kc, K = Kc - 1, KcP = a.KcP, Cl = a.Cl, Rl = a.Rl;
   const int tid = threadIdx.x;
   const int gi = tid / T, l = tid % T;
   const int lane = tid & 31;
@@ -103,6 +103,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   const int col0 = g * Cl;
   const int ncols = max(0, min(Kc, col0 + Cl) - col0);
   const int row0 = g * Rl;
+  const int Rg = max(0, min(Rl, N - row0));  // rows owned by this CTA (the last one may own fewer)
   const float invNN = 1.f / ((float)N * (float)N);
   const float negb = -P.conv_scale;
   const float ksc = P.kscale;
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
 #pragma unroll
         for (int j = 0; j < E; ++j) {
           const int x = l + T * j;
-          const int d = x >> lgRl, xr = x & (Rl - 1);
+          const int d = x / Rl, xr = x - d * Rl;
           s_mixr[d][(f1 * Rl + xr) * KcP + ky] = v[j];
           s_mixr[d][(f2 * Rl + xr) * KcP + ky] = v2[j];
         }
@@ -193,9 +194,9 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
       cluster.sync();  // derived fields delivered
 
       // ================= row phase: local gather -> 2 IFFTs -> product -> paired FFT -> pushed to column owners
-      for (int r0 = 0; r0 < Rl; r0 += NG) {
+      for (int r0 = 0; r0 < Rg; r0 += NG) {
         const int r = r0 + gi;
-        const bool valid = r < Rl;
+        const bool valid = r < Rg;
         const int rr = valid ? r : 0;
         float2 z1[E], z2[E];
 #pragma unroll
@@ -241,7 +242,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
               const int cm = colmap[k];
               float2* dst = s_prodr[cm >> 16] + (cm & 0xffff) * NP + xa;
               dst[0] = A;
-              if (r + 1 < Rl) dst[1] = B;
+              if (r + 1 < Rg) dst[1] = B;
             }
           }
         }
@@ -352,23 +353,20 @@ static int v2_configure(exgb_plan* plan) {
   const size_t limit = (size_t)lim - 1024;
   const char* envG = getenv("EXGB_CLUSTER");
   const int wantG = plan->tune_cluster > 0 ? plan->tune_cluster : (envG ? atoi(envG) : 0);
-  for (int G : {1, 2, 4, 8}) {
+  // Candidates: every cluster size whose shared memory fits; the automatic choice is the one that
+  // keeps the most SMs busy (active clusters x G from the occupancy query: clusters must fit in one
+  // GPC, so e.g. 6 can cover more SMs than 8), ties going to the smaller cluster.
+  auto fn = vort2d_kernel<N, THREADS>;
+  int bestG = 0, bestN = 0, bestSM = -1;
+  size_t bestBytes = 0;
+  for (int G = 1; G <= 8; ++G) {
     if (wantG && wantG != G) continue;
     const int Cl = (Kc + G - 1) / G;
-    const int Rl = N / G;
+    const int Rl = (N + G - 1) / G;
     const int KcP = Kc | 1;
     if (Rl < 2) continue;
     const size_t bytes = Lay::bytes(Cl, Rl, KcP, Kc);
     if (bytes > limit) continue;
-    c.G = G;
-    c.threads = THREADS;
-    c.cols_per_cta = Cl;
-    c.rows_per_cta = Rl;
-    c.CB = KcP;  // padded ky stride of the derived-field receive buffer
-    c.RB = 0;
-    c.mixed_in_smem = 1;
-    c.smem_bytes = bytes;
-    auto fn = vort2d_kernel<N, THREADS>;
     EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
@@ -386,10 +384,28 @@ static int v2_configure(exgb_plan* plan) {
       cudaGetLastError();
       ncl = std::max(1, plan->sm_count / G);
     }
-    c.clusters = ncl;
+    if (ncl * G > bestSM) {
+      bestSM = ncl * G;
+      bestG = G;
+      bestN = ncl;
+      bestBytes = bytes;
+    }
+  }
+  if (bestG > 0) {
+    const int G = bestG;
+    c.G = G;
+    c.threads = THREADS;
+    c.cols_per_cta = (Kc + G - 1) / G;
+    c.rows_per_cta = (N + G - 1) / G;
+    c.CB = Kc | 1;  // padded ky stride of the derived-field receive buffer
+    c.RB = 0;
+    c.mixed_in_smem = 1;
+    c.smem_bytes = bestBytes;
+    EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bestBytes));
+    c.clusters = bestN;
     const int nb = P.order <= 1 ? 1 : P.order == 2 ? 3 : P.order == 3 ? 4 : 6;
     c.scratch_per_cluster = (size_t)nb * Kc * N;
-    plan->scratch_bytes = sizeof(float2) * c.scratch_per_cluster * (size_t)ncl;
+    plan->scratch_bytes = sizeof(float2) * c.scratch_per_cluster * (size_t)bestN;
     EXGB_CUDA(cudaMalloc(&plan->d_scratch, plan->scratch_bytes));
     return EXGB_OK;
   }
@@ -405,8 +421,6 @@ static int v2_run(const exgb_plan* plan, cudaStream_t st, const float2* in, floa
   a.G = c.G;
   a.Cl = c.cols_per_cta;
   a.Rl = c.rows_per_cta;
-  a.lgRl = 0;
-  while ((1 << a.lgRl) < a.Rl) ++a.lgRl;
   a.Kc = std::min(plan->dev.kmax, N / 2 - 1) + 1;
   a.KcP = c.CB;
   a.Ul = (N / 2 + 1 - a.Kc + c.G - 1) / c.G;
@@ -474,8 +488,6 @@ static int v2_run_scratch(const exgb_plan* plan, cudaStream_t st, const float2* 
   a.G = c.G;
   a.Cl = c.cols_per_cta;
   a.Rl = c.rows_per_cta;
-  a.lgRl = 0;
-  while ((1 << a.lgRl) < a.Rl) ++a.lgRl;
   a.Kc = std::min(plan->dev.kmax, N / 2 - 1) + 1;
   a.KcP = c.CB;
   a.Ul = (N / 2 + 1 - a.Kc + c.G - 1) / c.G;

@@ -116,7 +116,7 @@ int exgb_plan_kmax(const exgb_plan* plan);
  * which times candidates on the device and caches the winner):
  *   EXGB_TUNE_RADICES       values = radix order of the length-N Stockham FFT
  *                           (1D kernel, transforms, generic 2D kernel)
- *   EXGB_TUNE_CLUSTER       values[0] = CTAs per cluster of the 2D kernel (0 = auto)
+ *   EXGB_TUNE_CLUSTER       values[0] = CTAs per cluster of the 2D kernel, 1..8 (0 = auto)
  *   EXGB_TUNE_ITEMS_PER_CTA values[0] = 1D instances per work item (0 = auto)
  * exgb_plan_get_tuning writes npass, the kMaxPass (12) radix slots, the
  * cluster size and the items per CTA (n >= 15). */

@@ -48,3 +48,27 @@ def test_tune_apply_cache_and_parity(case, tmp_path, monkeypatch):
         assert rel(got[b], so(u[b])) < 1e-5
     again = autotune.tune(sm, batch=32, nsteps=4)
     assert again["cached"] and again["best"] == res["best"]
+
+
+@pytest.mark.parametrize("n", [64, 128, 256])
+def test_every_cluster_size_matches_oracle(n):
+    """The register-FFT 2D kernel with each cluster size 1..8 that fits (rows split unevenly when
+    G does not divide N): one ETDRK2 step within 1e-5 of the oracle; sizes that do not fit are
+    refused with EXGB_EUNSUPPORTED and leave the plan usable."""
+    from exponax_gb300._lib import EXGB_OK
+    sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
+    so = o.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
+    g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    u = np.stack([g(n, key=s) for s in range(3)])
+    want = [so(u[b]) for b in range(3)]
+    ran = []
+    for G in range(1, 9):
+        if autotune._set(sm.plan, 1, [G]) != EXGB_OK:
+            continue
+        assert autotune.get_tuning(sm.plan)["cluster"] == G
+        got = ex.vmap(sm)(torch.from_numpy(u).cuda()).cpu().numpy()
+        for b in range(3):
+            assert rel(got[b], want[b]) < 1e-5, (G, b)
+        ran.append(G)
+    assert len(ran) >= 2, ran
+    assert autotune._set(sm.plan, 1, [0]) == EXGB_OK
