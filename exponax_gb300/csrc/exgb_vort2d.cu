@@ -49,7 +49,9 @@ struct V2Layout {
   __host__ __device__ static size_t twl() { return 0; }
   __host__ __device__ static size_t tiles() { return N; }
   __host__ __device__ static size_t colbuf() { return tiles() + (size_t)NG * TS; }
-  __host__ __device__ static size_t prodr(int Cl) { return colbuf() + (size_t)Cl * N; }
+  // the product spectra received for the owned columns overwrite the stage input in place: the
+  // stage input is consumed by the column inverse before the first cluster barrier of a stage
+  __host__ __device__ static size_t prodr(int) { return colbuf(); }
   __host__ __device__ static size_t mixr(int Cl) { return prodr(Cl) + (size_t)Cl * NP; }
   __host__ __device__ static size_t maps(int Cl, int Rl, int KcP) { return mixr(Cl) + (size_t)4 * Rl * KcP; }
   __host__ __device__ static size_t bytes(int Cl, int Rl, int KcP, int Kc) {
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   extern __shared__ __align__(16) float2 sm[];
   float2* twl = sm + Lay::twl();
   float2* tile = sm + Lay::tiles() + (size_t)gi * TS;
-  float2* colbuf = sm + Lay::colbuf();   // [c][kx]   owned columns
+  float2* colbuf = sm + Lay::colbuf();   // [c][kx]   owned columns (row stride NP, shared with prodr)
   float2* prodr = sm + Lay::prodr(Cl);   // [c][x]    product spectra received for owned columns
   float2* mixr = sm + Lay::mixr(Cl);     // [f][r][ky] derived fields received for owned rows
   int* colmap = reinterpret_cast<int*>(sm + Lay::maps(Cl, Rl, KcP));
@@ -141,7 +143,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
     for (int t = tid; t < ncols * N; t += THREADS) {
       const int kx = t / ncols, c = t - kx * ncols;
       const float2 v = uin[(int64_t)kx * M + col0 + c];
-      colbuf[c * N + kx] = v;
+      colbuf[c * NP + kx] = v;
       sb.U[(int64_t)(col0 + c) * N + kx] = v;
     }
     __syncthreads();
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           const int ks = sgn_k<N>(kx);
           float2 r1 = make_float2(0.f, 0.f), r2 = r1;
           if (ks <= K && ks >= -K) {
-            const float2 w = colbuf[c * N + kx];
+            const float2 w = colbuf[c * NP + kx];
             const float kxs = ksc * (float)ks;
             if (pr == 0) {
               const float lap = -(kxs * kxs + kys * kys);
@@ -263,7 +265,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           float2 nv = make_float2(0.f, 0.f);
           if (ks <= K && ks >= -K) nv = cscale(v[j], negb);
           if (ky == P.inj_mode && kx == 0) nv.x += P.inj_value;
-          colbuf[c * N + kx] = nv;
+          colbuf[c * NP + kx] = nv;
         }
       }
       __syncthreads();
@@ -271,13 +273,13 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
       if (a.nonlinear_only) {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
-          uout[(int64_t)kx * M + col0 + c] = colbuf[t];
+          uout[(int64_t)kx * M + col0 + c] = colbuf[c * NP + kx];
         }
       } else {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
           const int64_t o = (int64_t)(col0 + c) * N + kx;
-          colbuf[t] = stage_upd(P, sb, o, st, colbuf[t]);
+          colbuf[c * NP + kx] = stage_upd(P, sb, o, st, colbuf[c * NP + kx]);
         }
         if (last_of_step && a.project && col0 == 0 && ncols > 0) {
           // c2r projection of the step's physical round trip on ky = 0
