@@ -12,6 +12,7 @@ from . import etdrk, ic, metrics, nonlin_fun, spectral, stepper
 from ._lib import ExgbError
 from ._utils import RepeatedStepper, make_grid, repeat, rollout, vmap
 from .interpolation import map_between_resolutions
+from .metrics import get_spectrum
 from .spectral import fft, ifft
 from .stepper import BaseStepper
 
@@ -23,6 +24,7 @@ __all__ = [
     "RepeatedStepper",
     "etdrk",
     "fft",
+    "get_spectrum",
     "ic",
     "ifft",
     "make_grid",

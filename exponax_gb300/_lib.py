@@ -97,6 +97,8 @@ SIGNATURES = [
     ("exgb_plan_get_tuning", _I, [_VP, ctypes.POINTER(_I), _I]),
     ("exgb_plan_status", _I, [_VP]),
     ("exgb_tc_gemm_check", _I, [_VP, _I, _I, _VP, _VP, _VP, _I]),
+    ("exgb_spectrum", _I, [_VP, _I, _I, _I64, _VP, _VP, _I, _I]),
+    ("exgb_field_sums", _I, [_VP, _I64, _I64, _VP, _VP, _VP]),
     ("exgb_queue_prepare", _I, [ctypes.POINTER(WorkItem), _I64, _I32, _I32, ctypes.POINTER(_VP)]),
     ("exgb_queue_launch", _I, [_VP, _VP]),
     ("exgb_queue_destroy", _I, [_VP]),

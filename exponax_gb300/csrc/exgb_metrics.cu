@@ -1,0 +1,169 @@
+// exgb_metrics.cu -- evaluation kernels on device fields: the radially binned
+// power / amplitude spectrum (reference _spectral.py:866-1030, get_spectrum)
+// and the per-field sums behind nRMSE (metrics/_spatial.py:537-586) and
+// correlation (metrics/_correlation.py:33-60).
+//
+// Spectrum of one field from its rfftn (N..., N/2+1 modes):
+//   power:      q = 0.5 * (|u^| / recon) * (|u^| / norm)
+//   amplitude:  q = |u^| / recon
+// with norm = N^D on every mode and recon = N^D / 2 on the rfft-axis modes
+// 0 < k < N/2 (N^D on k = 0 and, for even N, k = N/2) -- the reference's
+// "reconstruction" / "norm_compensation" scaling arrays, evaluated in FP32.
+// 1D: q itself.  D >= 2: bin i in [0, N/2] sums (or averages) the q of the
+// modes whose integer wavenumber norm r = sqrt(sum k_d^2) (FP32) satisfies
+// i - 1/2 <= r < i + 1/2; NaN values are skipped as nansum / nanmean do, an
+// empty bin averages to NaN.  Summation order differs from the reference
+// (shared-memory atomics), so results agree to FP32 rounding, not bit for bit.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "exgb_internal.h"
+
+namespace exgb {
+
+namespace {
+
+constexpr int SPEC_THREADS = 256;
+constexpr int SPEC_MAX_BINS = 2049;  // N <= 4096
+
+__global__ void __launch_bounds__(SPEC_THREADS) spectrum_kernel(int D, int N, int64_t modes_per_field, int per_field_ctas,
+                                                                 const float2* __restrict__ hat, float* sums,
+                                                                 int* counts, int power) {
+  extern __shared__ float s_bins[];  // [nb] sums, then [nb] counts as int
+  const int M = N / 2 + 1;
+  const int nb = M;
+  int* s_cnt = reinterpret_cast<int*>(s_bins + nb);
+  const int field = blockIdx.x / per_field_ctas;
+  const int part = blockIdx.x % per_field_ctas;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    s_bins[i] = 0.f;
+    s_cnt[i] = 0;
+  }
+  __syncthreads();
+  const float nd = (D == 1) ? (float)N : (D == 2) ? (float)N * (float)N : (float)N * (float)N * (float)N;
+  const float2* f = hat + (int64_t)field * modes_per_field;
+  const int64_t chunk = (modes_per_field + per_field_ctas - 1) / per_field_ctas;
+  const int64_t m0 = (int64_t)part * chunk;
+  const int64_t m1 = min(modes_per_field, m0 + chunk);
+  for (int64_t m = m0 + threadIdx.x; m < m1; m += blockDim.x) {
+    const int kl = (int)(m % M);  // rfft axis
+    int64_t rest = m / M;
+    float r2 = (float)kl * (float)kl;
+    for (int d = 0; d < D - 1; ++d) {
+      const int idx = (int)(rest % N);
+      rest /= N;
+      const int k = (idx <= (N - 1) / 2) ? idx : idx - N;  // fftfreq
+      r2 += (float)k * (float)k;
+    }
+    const bool full = (kl == 0) || (N % 2 == 0 && kl == N / 2);
+    const float recon = full ? nd : nd / 2.f;
+    const float2 v = f[m];
+    const float a = hypotf(v.x, v.y);
+    const float mag = a / recon;
+    const float q = power ? 0.5f * mag * (a / nd) : mag;
+    if (D == 1) {
+      sums[(int64_t)field * nb + kl] = q;
+      continue;
+    }
+    if (isnan(q)) continue;
+    const float r = sqrtf(r2);
+    int b = (int)floorf(r + 0.5f);
+    if (r < (float)b - 0.5f) --b;
+    if (r >= (float)b + 0.5f) ++b;
+    if (b < 0 || b >= nb) continue;
+    atomicAdd(&s_bins[b], q);
+    atomicAdd(&s_cnt[b], 1);
+  }
+  __syncthreads();
+  if (D == 1) return;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    if (s_cnt[i]) {
+      atomicAdd(&sums[(int64_t)field * nb + i], s_bins[i]);
+      atomicAdd(&counts[(int64_t)field * nb + i], s_cnt[i]);
+    }
+  }
+}
+
+__global__ void spectrum_average_kernel(int64_t n, float* sums, const int* counts) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) sums[i] = counts[i] ? sums[i] / (float)counts[i] : nanf("");
+}
+
+// per field: sum (a-b)^2, sum b^2, sum a b, sum a^2 in FP64 (one CTA per field, block reduction)
+__global__ void __launch_bounds__(256) field_sums_kernel(int64_t n, const float* __restrict__ a,
+                                                         const float* __restrict__ b, double* out) {
+  const float* pa = a + (int64_t)blockIdx.x * n;
+  const float* pb = b + (int64_t)blockIdx.x * n;
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const double x = pa[i], y = pb[i];
+    s[0] += (x - y) * (x - y);
+    s[1] += y * y;
+    s[2] += x * y;
+    s[3] += x * x;
+  }
+  __shared__ double red[4][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[k][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double v = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) v += red[threadIdx.x][i];
+    out[(int64_t)blockIdx.x * 4 + threadIdx.x] = v;
+  }
+}
+
+}  // namespace
+}  // namespace exgb
+
+using namespace exgb;
+
+extern "C" int exgb_spectrum(void* stream, int num_spatial_dims, int num_points, int64_t count, const void* u_hat,
+                             float* out, int power, int average) {
+  const int D = num_spatial_dims, N = num_points;
+  if (!u_hat || !out) return fail(EXGB_EINVAL, "exgb_spectrum: NULL pointer");
+  if (D < 1 || D > 3) return fail(EXGB_ESHAPE, "exgb_spectrum: num_spatial_dims must be 1, 2 or 3");
+  if (N < 2 || N / 2 + 1 > SPEC_MAX_BINS) return fail(EXGB_ESHAPE, "exgb_spectrum: num_points out of range");
+  if (count < 0) return fail(EXGB_EINVAL, "exgb_spectrum: negative count");
+  if (count == 0) return EXGB_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int M = N / 2 + 1;
+  int64_t modes = M;
+  for (int d = 0; d < D - 1; ++d) modes *= N;
+  const int64_t nout = count * M;
+  int* counts = nullptr;
+  if (D > 1) {
+    EXGB_CUDA(cudaMemsetAsync(out, 0, sizeof(float) * nout, st));
+    EXGB_CUDA(cudaMallocAsync(&counts, sizeof(int) * nout, st));
+    EXGB_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * nout, st));
+  }
+  const int per = (int)std::max<int64_t>(1, std::min<int64_t>(64, modes / (16 * SPEC_THREADS)));
+  const size_t smem = (size_t)M * (sizeof(float) + sizeof(int));
+  spectrum_kernel<<<(unsigned)(count * per), SPEC_THREADS, smem, st>>>(D, N, modes, per, (const float2*)u_hat, out,
+                                                                      counts, power);
+  EXGB_CUDA(cudaGetLastError());
+  if (D > 1) {
+    if (average) {
+      spectrum_average_kernel<<<(unsigned)((nout + 255) / 256), 256, 0, st>>>(nout, out, counts);
+      EXGB_CUDA(cudaGetLastError());
+    }
+    EXGB_CUDA(cudaFreeAsync(counts, st));
+  }
+  return EXGB_OK;
+}
+
+extern "C" int exgb_field_sums(void* stream, int64_t count, int64_t n, const float* a, const float* b, double* out) {
+  if (!a || !b || !out) return fail(EXGB_EINVAL, "exgb_field_sums: NULL pointer");
+  if (count < 0 || n < 0) return fail(EXGB_EINVAL, "exgb_field_sums: negative size");
+  if (count == 0) return EXGB_OK;
+  field_sums_kernel<<<(unsigned)count, 256, 0, (cudaStream_t)stream>>>(n, a, b, out);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}

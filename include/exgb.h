@@ -218,6 +218,18 @@ int exgb_leray(void* stream, int num_spatial_dims, int num_points, double domain
 int exgb_map_between_resolutions(void* stream, int num_spatial_dims, int n_old, int n_new,
                                  int64_t count, const float* in, float* out, int oddball_zero);
 
+/* ---- evaluation ----
+ * exgb_spectrum replaces get_spectrum (_spectral.py:866-1030) on count = B*C
+ * Fourier fields (count, N..., N/2+1) of D = 1..3 axes: out (count, N/2+1)
+ * float32, power (power != 0) or amplitude spectrum, radial bins summed
+ * (average = 0) or averaged (average != 0; empty bins NaN).  D = 1: no binning.
+ * exgb_field_sums: for count fields of n floats, out[4 f + 0..3] = sum (a-b)^2,
+ * sum b^2, sum a b, sum a^2 (FP64) -- the sums behind nRMSE
+ * (metrics/_spatial.py:537-586) and correlation (metrics/_correlation.py:33-60). */
+int exgb_spectrum(void* stream, int num_spatial_dims, int num_points, int64_t count, const void* u_hat,
+                  float* out, int power, int average);
+int exgb_field_sums(void* stream, int64_t count, int64_t n, const float* a, const float* b, double* out);
+
 /* Self-check of the tcgen05 tensor-core layer (no reference counterpart):
  * d (128 x n, FP32) = a (128 x k) . b (n x k)^T, device pointers, row-major.
  * split = 0: inputs rounded to bf16, one product; split = 1: split-BF16
