@@ -10,7 +10,7 @@ CUDA, C ABI in include/exgb.h); there is no CPU fallback.
 
 from . import etdrk, ic, metrics, nonlin_fun, spectral, stepper
 from ._lib import ExgbError
-from ._utils import RepeatedStepper, make_grid, repeat, rollout, vmap
+from ._utils import ForcedStepper, RepeatedStepper, make_grid, repeat, rollout, vmap
 from .interpolation import map_between_resolutions
 from .metrics import get_spectrum
 from .spectral import fft, ifft
@@ -21,6 +21,7 @@ __version__ = "0.1.0"
 __all__ = [
     "BaseStepper",
     "ExgbError",
+    "ForcedStepper",
     "RepeatedStepper",
     "etdrk",
     "fft",

@@ -59,10 +59,109 @@ class _Rollout:
 
 
 def rollout(stepper_fn, n: int, *, include_init: bool = False, takes_aux: bool = False, constant_aux: bool = True):
-    """_utils.py:92-186: callable returning the trajectory (n [+1], C, N...)."""
+    """_utils.py:92-186: callable returning the trajectory (n [+1], C, N...).
+    takes_aux: the callable is (u0, aux) -> trajectory with stepper_fn(u, aux);
+    aux is the same every step (constant_aux) or has a leading time axis of n."""
     if takes_aux:
-        raise NotImplementedError("rollouts with auxiliary inputs (ForcedStepper) are not built in this version")
+        return _AuxLoop(stepper_fn, n, include_init, constant_aux, trajectory=True)
     return _Rollout(stepper_fn, n, include_init)
+
+
+def _aux_at(aux, t, constant, batched):
+    if constant:
+        return aux
+    return aux[:, t] if batched else aux[t]
+
+
+class _AuxLoop:
+    """Time loop over stepper_fn(u, aux) (_utils.py:137-163 for rollout, :212-229 for repeat)."""
+
+    def __init__(self, stepper_fn, n, include_init, constant_aux, trajectory):
+        self.stepper_fn = stepper_fn
+        self.n = int(n)
+        self.include_init = bool(include_init)
+        self.constant_aux = bool(constant_aux)
+        self.trajectory = trajectory
+
+    def _run(self, u0, aux, batched):
+        fn = self.stepper_fn
+        if batched:
+            fn = fn._batched if hasattr(fn, "_batched") else _looped2(fn)
+        u = u0
+        frames = [u0] if self.include_init else []
+        for t in range(self.n):
+            u = fn(u, _aux_at(aux, t, self.constant_aux, batched))
+            if self.trajectory:
+                frames.append(u)
+        if not self.trajectory:
+            return u
+        tt = _device.torch()
+        ax = 1 if batched else 0
+        if isinstance(u0, tt.Tensor):
+            return tt.stack(frames, dim=ax)
+        return np.stack([np.asarray(f) for f in frames], axis=ax)
+
+    def __call__(self, u0, aux):
+        return self._run(u0, aux, batched=False)
+
+    def _batched(self, u0, aux):
+        return self._run(u0, aux, batched=True)
+
+
+def _looped2(fn):
+    def looped(u, aux):
+        t = _device.torch()
+        outs = [fn(u[i], aux[i]) for i in range(u.shape[0])]
+        return t.stack(outs) if isinstance(outs[0], t.Tensor) else np.stack(outs)
+
+    return looped
+
+
+class ForcedStepper:
+    """_forced_stepper.py:7-108: turns a stepper u -> u_next of u_t = Lu + N(u)
+    into (u, f) -> u_next of u_t = Lu + N(u) + f by operator splitting: one
+    explicit Euler substep with the forcing (u + dt f, exgb_axpy on the device)
+    followed by the wrapped stepper (first order in time, as in the reference)."""
+
+    def __init__(self, stepper):
+        self.stepper = stepper
+
+    def __getattr__(self, name):
+        if name in ("num_spatial_dims", "domain_extent", "num_points", "num_channels", "dt", "dx"):
+            return getattr(self.stepper, name)
+        raise AttributeError(name)
+
+    def _add_forcing(self, u, f, dtype):
+        from ._lib import check, load
+
+        t, back = _device.to_device(u, dtype)
+        tf, _ = _device.to_device(f, dtype)
+        if tuple(t.shape) != tuple(tf.shape):
+            raise ValueError(f"Forcing shape {tuple(tf.shape)} does not match the state shape {tuple(t.shape)}")
+        out = _device.torch().empty_like(t)
+        n = t.numel() * (2 if dtype == "complex64" else 1)
+        check(load().exgb_axpy(_device.stream(), n, float(self.stepper.dt), t.data_ptr(), tf.data_ptr(),
+                               out.data_ptr()), "forcing")
+        return out, back
+
+    def step(self, u, f):
+        w, back = self._add_forcing(u, f, "float32")
+        return back(self.stepper.step(w))
+
+    def step_fourier(self, u_hat, f_hat):
+        w, back = self._add_forcing(u_hat, f_hat, "complex64")
+        return back(self.stepper.step_fourier(w))
+
+    def __call__(self, u, f):
+        return self.step(u, f)
+
+    def _batched(self, u, f):
+        w, back = self._add_forcing(u, f, "float32")
+        return back(vmap(self.stepper)(w))
+
+    def _batched_step_fourier(self, u_hat, f_hat):
+        w, back = self._add_forcing(u_hat, f_hat, "complex64")
+        return back(vmap(self.stepper.step_fourier)(w))
 
 
 class _Repeat:
@@ -91,7 +190,7 @@ class _Repeat:
 def repeat(stepper_fn, n: int, *, takes_aux: bool = False, constant_aux: bool = True):
     """_utils.py:189-254: callable returning the state after n steps."""
     if takes_aux:
-        raise NotImplementedError("repeat with auxiliary inputs (ForcedStepper) is not built in this version")
+        return _AuxLoop(stepper_fn, n, False, constant_aux, trajectory=False)
     return _Repeat(stepper_fn, n)
 
 

@@ -1,0 +1,97 @@
+// exgb_util.cu -- small device helpers behind the Python surface:
+//   exgb_axpy             out = x + alpha y (ForcedStepper's explicit forcing
+//                         substep, reference _forced_stepper.py:64-65, :86-87)
+//   exgb_scatter_modes    zero `count` Fourier fields and write per-field
+//                         values at fixed mode positions (random-series ICs)
+//   exgb_normalize_fields subtract the mean and/or divide by max |u| per field
+//                         (reference ic/_base_ic.py:18-32, normalize_ic)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "exgb_internal.h"
+
+namespace exgb {
+namespace {
+
+__global__ void axpy_kernel(int64_t n, float alpha, const float* __restrict__ x, const float* __restrict__ y,
+                            float* out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = fmaf(alpha, y[i], x[i]);
+}
+
+__global__ void scatter_kernel(int64_t count, int64_t field_elems, int nmodes, const int64_t* __restrict__ idx,
+                               const float2* __restrict__ vals, float2* hat) {
+  const int64_t n = count * nmodes;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = i / nmodes;
+    const int m = (int)(i - f * nmodes);
+    hat[f * field_elems + idx[m]] = vals[i];
+  }
+}
+
+// one CTA per field: FP64 mean, then max |u - mean|, then the rescale
+__global__ void __launch_bounds__(256) normalize_kernel(int64_t n, float* u, int zero_mean, int max_one) {
+  float* p = u + (int64_t)blockIdx.x * n;
+  __shared__ double red[8];
+  __shared__ float redf[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double s = 0.0;
+  if (zero_mean)
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += p[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) red[w] = s;
+  __syncthreads();
+  double tot = 0.0;
+  for (int i = 0; i < nw; ++i) tot += red[i];
+  const float mean = zero_mean ? (float)(tot / (double)n) : 0.f;
+  float mx = 0.f;
+  if (max_one)
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) mx = fmaxf(mx, fabsf(p[i] - mean));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) redf[w] = mx;
+  __syncthreads();
+  float m = 0.f;
+  for (int i = 0; i < nw; ++i) m = fmaxf(m, redf[i]);
+  const float inv = (max_one && m > 0.f) ? 1.f / m : 1.f;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) p[i] = (p[i] - mean) * inv;
+}
+
+int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 152 * 16); }
+
+}  // namespace
+}  // namespace exgb
+
+using namespace exgb;
+
+extern "C" int exgb_axpy(void* stream, int64_t n, float alpha, const float* x, const float* y, float* out) {
+  if (!x || !y || !out) return fail(EXGB_EINVAL, "exgb_axpy: NULL pointer");
+  if (n < 0) return fail(EXGB_EINVAL, "exgb_axpy: negative size");
+  if (n == 0) return EXGB_OK;
+  axpy_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(n, alpha, x, y, out);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+extern "C" int exgb_scatter_modes(void* stream, int64_t count, int64_t field_elems, int nmodes, const int64_t* idx,
+                                  const void* vals, void* hat) {
+  if (!idx || !vals || !hat) return fail(EXGB_EINVAL, "exgb_scatter_modes: NULL pointer");
+  if (count < 0 || field_elems <= 0 || nmodes < 0) return fail(EXGB_EINVAL, "exgb_scatter_modes: bad size");
+  cudaStream_t st = (cudaStream_t)stream;
+  EXGB_CUDA(cudaMemsetAsync(hat, 0, sizeof(float2) * (size_t)(count * field_elems), st));
+  if (count == 0 || nmodes == 0) return EXGB_OK;
+  scatter_kernel<<<grid_for(count * nmodes), 256, 0, st>>>(count, field_elems, nmodes, idx, (const float2*)vals,
+                                                          (float2*)hat);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+extern "C" int exgb_normalize_fields(void* stream, int64_t count, int64_t n, float* u, int zero_mean, int max_one) {
+  if (!u) return fail(EXGB_EINVAL, "exgb_normalize_fields: NULL pointer");
+  if (count < 0 || n <= 0) return fail(EXGB_EINVAL, "exgb_normalize_fields: bad size");
+  if (count == 0) return EXGB_OK;
+  normalize_kernel<<<(unsigned)count, 256, 0, (cudaStream_t)stream>>>(n, u, zero_mean, max_one);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}

@@ -230,6 +230,18 @@ int exgb_spectrum(void* stream, int num_spatial_dims, int num_points, int64_t co
                   float* out, int power, int average);
 int exgb_field_sums(void* stream, int64_t count, int64_t n, const float* a, const float* b, double* out);
 
+/* ---- helpers of the Python surface ----
+ * exgb_axpy: out = x + alpha y over n floats (ForcedStepper, _forced_stepper.py:64-65, :86-87;
+ *   complex fields pass 2n floats).
+ * exgb_scatter_modes: zero count Fourier fields of field_elems complex64 each, then write
+ *   vals[f * nmodes + m] at element idx[m] of field f (random-series initial conditions).
+ * exgb_normalize_fields: per field of n floats subtract the mean (zero_mean) and divide by
+ *   max |u| (max_one) (ic/_base_ic.py:18-32). */
+int exgb_axpy(void* stream, int64_t n, float alpha, const float* x, const float* y, float* out);
+int exgb_scatter_modes(void* stream, int64_t count, int64_t field_elems, int nmodes, const int64_t* idx,
+                       const void* vals, void* hat);
+int exgb_normalize_fields(void* stream, int64_t count, int64_t n, float* u, int zero_mean, int max_one);
+
 /* Self-check of the tcgen05 tensor-core layer (no reference counterpart):
  * d (128 x n, FP32) = a (128 x k) . b (n x k)^T, device pointers, row-major.
  * split = 0: inputs rounded to bf16, one product; split = 1: split-BF16

@@ -1050,30 +1050,58 @@ class Poisson:
 # --------------------------------------------------------------------------
 
 
-def rollout(stepper_fn, n, *, include_init=False):
-    """_utils.py:92-186 (takes_aux=False): stack of n successive states."""
+def rollout(stepper_fn, n, *, include_init=False, takes_aux=False, constant_aux=True):
+    """_utils.py:92-186: stack of n successive states; with takes_aux the
+    callable is (u0, aux) and stepper_fn(u, aux_t), aux_t = aux (constant_aux)
+    or aux[t] (:137-163)."""
 
-    def run(u0):
+    def run(u0, aux=None):
         u = u0
         out = [u0] if include_init else []
-        for _ in range(n):
-            u = stepper_fn(u)
+        for t in range(n):
+            if takes_aux:
+                u = stepper_fn(u, aux if constant_aux else aux[t])
+            else:
+                u = stepper_fn(u)
             out.append(u)
         return np.stack(out)
 
     return run
 
 
-def repeat(stepper_fn, n):
-    """_utils.py:189-254 (takes_aux=False): final state after n steps."""
+def repeat(stepper_fn, n, *, takes_aux=False, constant_aux=True):
+    """_utils.py:189-254: final state after n steps (aux as in rollout, :212-229)."""
 
-    def run(u0):
+    def run(u0, aux=None):
         u = u0
-        for _ in range(n):
-            u = stepper_fn(u)
+        for t in range(n):
+            if takes_aux:
+                u = stepper_fn(u, aux if constant_aux else aux[t])
+            else:
+                u = stepper_fn(u)
         return u
 
     return run
+
+
+class ForcedStepper:
+    """_forced_stepper.py:7-108: u_t = Lu + N(u) + f by splitting: one explicit
+    Euler substep with the forcing, then the wrapped stepper."""
+
+    def __init__(self, stepper):
+        self.stepper = stepper
+
+    def step(self, u, f):
+        """:44-65"""
+        return self.stepper.step(u + self.stepper.dt * f)
+
+    def step_fourier(self, u_hat, f_hat):
+        """:67-87"""
+        return self.stepper.step_fourier(u_hat + self.stepper.dt * f_hat)
+
+    def __call__(self, u, f):
+        """:89-108"""
+        return self.step(u, f)
 
 
 class RepeatedStepper:

@@ -354,3 +354,21 @@ def test_nrmse_and_correlation():
     assert o.nRMSE(u, u) == 0.0
     assert o.nRMSE(2 * u, u) == pytest.approx(1.0)
     assert o.correlation(3 * u, u) == pytest.approx(1.0)
+
+
+def test_forced_stepper_oracle_splitting():
+    """_forced_stepper.py: zero forcing reproduces the stepper; for a linear stepper the forced step
+    is linear in f: step(u, f) = step(u) + step(dt f) (ETDRK0 diffusion)."""
+    st = o.Diffusion(1, 1.0, 32, 0.01, diffusivity=0.05)
+    fs = o.ForcedStepper(st)
+    rng = np.random.default_rng(0)
+    u = rng.standard_normal((1, 32)).astype(np.float64)
+    f = rng.standard_normal((1, 32)).astype(np.float64)
+    np.testing.assert_allclose(fs(u, 0 * f), st(u), rtol=0, atol=1e-6)
+    np.testing.assert_allclose(fs(u, f), st(u) + st(0.01 * f), rtol=0, atol=1e-5)
+    traj = o.rollout(fs, 3, takes_aux=True)(u, f)
+    assert traj.shape == (3, 1, 32)
+    np.testing.assert_allclose(traj[-1], o.repeat(fs, 3, takes_aux=True)(u, f), rtol=0, atol=0)
+    fs_t = np.stack([f, 2 * f, 3 * f])
+    traj2 = o.rollout(fs, 3, takes_aux=True, constant_aux=False)(u, fs_t)
+    np.testing.assert_allclose(traj2[0], fs(u, f), rtol=0, atol=0)
