@@ -210,13 +210,9 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
   const StageBufs sb = stage_bufs(a.scratch + (int64_t)blockIdx.x * a.scratch_stride, P.order, (int64_t)Kc * N);
   const uint32_t idI1 = tc::idesc_bf16(128, 96), idI2 = tc::idesc_bf16(128, 128);
   const uint32_t idF1 = tc::idesc_bf16(128, 128), idF2 = tc::idesc_bf16(128, 96);
-  // base shared-memory descriptors of every operand tile (k-step 0)
-  const uint64_t dAiH = tc::kmaj_desc(sAiH, KI, 0), dAiL = tc::kmaj_desc(sAiL, KI, 0);
-  const uint64_t dAfH = tc::kmaj_desc(sAfH, KF, 0), dAfL = tc::kmaj_desc(sAfL, KF, 0);
-  const uint64_t dB1H = tc::kmaj_desc(sR + R_B1_HI, KI, 0), dB1L = tc::kmaj_desc(sR + R_B1_LO, KI, 0);
-  const uint64_t dA2H = tc::kmaj_desc(sR + R_A2_HI, KI, 0), dA2L = tc::kmaj_desc(sR + R_A2_LO, KI, 0);
-  const uint64_t dB3H = tc::kmaj_desc(sR, KF, 0), dB3L = tc::kmaj_desc(sR + TILE_B3, KF, 0);
-  const uint64_t dB4H = tc::kmaj_desc(sR, KF, 0), dB4L = tc::kmaj_desc(sR + TILE_B4, KF, 0);
+  // base shared-memory descriptors of the operand tiles (k-step 0), built by the issuing thread
+#define DESC_I(addr) tc::kmaj_desc((addr), KI, 0)
+#define DESC_F(addr) tc::kmaj_desc((addr), KF, 0)
   uint32_t phase = 0;
   bool bad = false;
 
@@ -343,7 +339,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
       sync_for_mma();
       if (tid == 0) {
         tc::fence_after_sync();
-        tc::mma3<KI / 16>(tmem, dAiH, dAiL, dB1H, dB1L, idI1);
+        tc::mma3<KI / 16>(tmem, DESC_I(sAiH), DESC_I(sAiL), DESC_I(sR + R_B1_HI), DESC_I(sR + R_B1_LO), idI1);
         tc::mma_commit(&s_mbar);
       }
       bad = !wait_mma();
@@ -352,14 +348,16 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
         sync_for_mma();
         if (tid == 0) {
           tc::fence_after_sync();
-          tc::mma3<KI / 16>(tmem + 128u * f, dA2H, dA2L, dAiH, dAiL, idI2);
+          tc::mma3<KI / 16>(tmem + 128u * f, DESC_I(sR + R_A2_HI), DESC_I(sR + R_A2_LO), DESC_I(sAiH), DESC_I(sAiL),
+                            idI2);
         }
         if (f < 3) {
           b1(f + 1);  // B1 is free (its MMA completed); overlaps the MMA above
           sync_for_mma();
           if (tid == 0) {
             tc::fence_after_sync();
-            tc::mma3<KI / 16>(tmem + 128u * (f + 1), dAiH, dAiL, dB1H, dB1L, idI1);
+            tc::mma3<KI / 16>(tmem + 128u * (f + 1), DESC_I(sAiH), DESC_I(sAiL), DESC_I(sR + R_B1_HI),
+                              DESC_I(sR + R_B1_LO), idI1);
           }
         }
         if (tid == 0) tc::mma_commit(&s_mbar);
@@ -401,7 +399,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
       sync_for_mma();
       if (tid == 0) {
         tc::fence_after_sync();
-        tc::mma3<KF / 16>(tmem, dAfH, dAfL, dB3H, dB3L, idF1);
+        tc::mma3<KF / 16>(tmem, DESC_F(sAfH), DESC_F(sAfL), DESC_F(sR), DESC_F(sR + TILE_B3), idF1);
         tc::mma_commit(&s_mbar);
       }
       bad = !wait_mma();
@@ -433,7 +431,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
       sync_for_mma();
       if (tid == 0) {
         tc::fence_after_sync();
-        tc::mma3<KF / 16>(tmem + 128u, dAfH, dAfL, dB4H, dB4L, idF2);
+        tc::mma3<KF / 16>(tmem + 128u, DESC_F(sAfH), DESC_F(sAfL), DESC_F(sR), DESC_F(sR + TILE_B4), idF2);
         tc::mma_commit(&s_mbar);
       }
       bad = !wait_mma();
@@ -575,6 +573,8 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
     __syncthreads();
   }
 
+#undef DESC_I
+#undef DESC_F
   if (bad) {
     // let any MMA still in flight finish before the tensor memory is released
     tc::mbar_wait(&s_mbar, phase ^ 1u, WAIT_BUDGET);
