@@ -242,21 +242,6 @@ __device__ __forceinline__ void split8_store(const float (&v)[8], unsigned char*
   *reinterpret_cast<uint4*>(lo_tile + off) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
-// Same with precomputed base descriptors and a compile-time number of k-steps:
-// advancing a K-major no-swizzle descriptor by one k-step (256 bytes) adds 16
-// to its start-address field (addresses stay below 256 KB, so no carry out).
-template <int STEPS>
-__device__ __forceinline__ void mma3(uint32_t d_tmem, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
-                                     uint32_t idesc) {
-#pragma unroll
-  for (int s = 0; s < STEPS; ++s) {
-    const uint64_t o = (uint64_t)(16 * s);
-    mma_bf16(d_tmem, al + o, bh + o, idesc, s > 0 ? 1u : 0u);
-    mma_bf16(d_tmem, ah + o, bl + o, idesc, 1u);
-    mma_bf16(d_tmem, ah + o, bh + o, idesc, 1u);
-  }
-}
-
 // Split-BF16 product D (+)= A . B^T over K (multiple of 16) with the three
 // significant terms Ahi Bhi + Ahi Blo + Alo Bhi, FP32 accumulation in TMEM.
 // Issued by one thread.

@@ -210,9 +210,6 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
   const StageBufs sb = stage_bufs(a.scratch + (int64_t)blockIdx.x * a.scratch_stride, P.order, (int64_t)Kc * N);
   const uint32_t idI1 = tc::idesc_bf16(128, 96), idI2 = tc::idesc_bf16(128, 128);
   const uint32_t idF1 = tc::idesc_bf16(128, 128), idF2 = tc::idesc_bf16(128, 96);
-  // base shared-memory descriptors of the operand tiles (k-step 0), built by the issuing thread
-#define DESC_I(addr) tc::kmaj_desc((addr), KI, 0)
-#define DESC_F(addr) tc::kmaj_desc((addr), KF, 0)
   uint32_t phase = 0;
   bool bad = false;
 
@@ -339,7 +336,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
       sync_for_mma();
       if (tid == 0) {
         tc::fence_after_sync();
-        tc::mma3<KI / 16>(tmem, DESC_I(sAiH), DESC_I(sAiL), DESC_I(sR + R_B1_HI), DESC_I(sR + R_B1_LO), idI1);
+        tc::mma_split3(tmem, sAiH, sAiL, KI, sR + R_B1_HI, sR + R_B1_LO, KI, KI, idI1, false);
         tc::mma_commit(&s_mbar);
       }
       bad = !wait_mma();
@@ -348,16 +345,14 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
         sync_for_mma();
         if (tid == 0) {
           tc::fence_after_sync();
-          tc::mma3<KI / 16>(tmem + 128u * f, DESC_I(sR + R_A2_HI), DESC_I(sR + R_A2_LO), DESC_I(sAiH), DESC_I(sAiL),
-                            idI2);
+          tc::mma_split3(tmem + 128u * f, sR + R_A2_HI, sR + R_A2_LO, KI, sAiH, sAiL, KI, KI, idI2, false);
         }
         if (f < 3) {
           b1(f + 1);  // B1 is free (its MMA completed); overlaps the MMA above
           sync_for_mma();
           if (tid == 0) {
             tc::fence_after_sync();
-            tc::mma3<KI / 16>(tmem + 128u * (f + 1), DESC_I(sAiH), DESC_I(sAiL), DESC_I(sR + R_B1_HI),
-                              DESC_I(sR + R_B1_LO), idI1);
+            tc::mma_split3(tmem + 128u * (f + 1), sAiH, sAiL, KI, sR + R_B1_HI, sR + R_B1_LO, KI, KI, idI1, false);
           }
         }
         if (tid == 0) tc::mma_commit(&s_mbar);
@@ -399,7 +394,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
       sync_for_mma();
       if (tid == 0) {
         tc::fence_after_sync();
-        tc::mma3<KF / 16>(tmem, DESC_F(sAfH), DESC_F(sAfL), DESC_F(sR), DESC_F(sR + TILE_B3), idF1);
+        tc::mma_split3(tmem, sAfH, sAfL, KF, sR, sR + TILE_B3, KF, KF, idF1, false);
         tc::mma_commit(&s_mbar);
       }
       bad = !wait_mma();
@@ -431,7 +426,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
       sync_for_mma();
       if (tid == 0) {
         tc::fence_after_sync();
-        tc::mma3<KF / 16>(tmem + 128u, DESC_F(sAfH), DESC_F(sAfL), DESC_F(sR), DESC_F(sR + TILE_B4), idF2);
+        tc::mma_split3(tmem + 128u, sAfH, sAfL, KF, sR, sR + TILE_B4, KF, KF, idF2, false);
         tc::mma_commit(&s_mbar);
       }
       bad = !wait_mma();
@@ -573,8 +568,6 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
     __syncthreads();
   }
 
-#undef DESC_I
-#undef DESC_F
   if (bad) {
     // let any MMA still in flight finish before the tensor memory is released
     tc::mbar_wait(&s_mbar, phase ^ 1u, WAIT_BUDGET);
