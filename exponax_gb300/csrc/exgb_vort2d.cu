@@ -44,7 +44,9 @@ struct V2Layout {
   static constexpr int E = RegCfg<N>::E, T = RegCfg<N>::T;
   static constexpr int NG = THREADS / T;
   static constexpr int TS = tile_stride<E, T>();
-  static constexpr int NP = N + 1;  // padded row length of the product receive buffer
+  // Exchange buffers are laid out so that consecutive lanes (consecutive positions of one
+  // transform) write consecutive addresses of the receiving CTA, with odd row strides (ClP, RlP)
+  // so that the local column reads stay free of bank conflicts.
   // float2 offsets
   __host__ __device__ static size_t twl() { return 0; }
   __host__ __device__ static size_t tiles() { return N; }
@@ -52,10 +54,10 @@ struct V2Layout {
   // the product spectra received for the owned columns overwrite the stage input in place: the
   // stage input is consumed by the column inverse before the first cluster barrier of a stage
   __host__ __device__ static size_t prodr(int) { return colbuf(); }
-  __host__ __device__ static size_t mixr(int Cl) { return prodr(Cl) + (size_t)Cl * NP; }
-  __host__ __device__ static size_t maps(int Cl, int Rl, int KcP) { return mixr(Cl) + (size_t)4 * Rl * KcP; }
-  __host__ __device__ static size_t bytes(int Cl, int Rl, int KcP, int Kc) {
-    return sizeof(float2) * maps(Cl, Rl, KcP) + sizeof(int) * (size_t)Kc;
+  __host__ __device__ static size_t mixr(int Cl) { return prodr(Cl) + (size_t)N * (Cl | 1); }
+  __host__ __device__ static size_t maps(int Cl, int Rl, int Kc) { return mixr(Cl) + (size_t)4 * Kc * (Rl | 1); }
+  __host__ __device__ static size_t bytes(int Cl, int Rl, int Kc) {
+    return sizeof(float2) * maps(Cl, Rl, Kc) + sizeof(int) * (size_t)(Kc + N);
   }
 };
 
@@ -67,7 +69,7 @@ __device__ __forceinline__ int sgn_k(int i) {
 template <int N, int THREADS>
 __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   using Lay = V2Layout<N, THREADS>;
-  constexpr int E = Lay::E, T = Lay::T, NG = Lay::NG, TS = Lay::TS, NP = Lay::NP;
+  constexpr int E = Lay::E, T = Lay::T, NG = Lay::NG, TS = Lay::TS;
   constexpr int M = N / 2 + 1;
   cg::cluster_group cluster = cg::this_cluster();
   const int G = a.G;
@@ -75,7 +77,8 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   const int cid = (int)(blockIdx.x / G);
   const int ncl = (int)(gridDim.x / G);
   const PlanDev& P = a.P;
-  const int Kc = a.Kc, K = Kc - 1, KcP = a.KcP, Cl = a.Cl, Rl = a.Rl;
+  const int Kc = a.Kc, K = Kc - 1, Cl = a.Cl, Rl = a.Rl;
+  const int ClP = Cl | 1, RlP = Rl | 1;
   const int tid = threadIdx.x;
   const int gi = tid / T, l = tid % T;
   const int lane = tid & 31;
@@ -84,16 +87,18 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   extern __shared__ __align__(16) float2 sm[];
   float2* twl = sm + Lay::twl();
   float2* tile = sm + Lay::tiles() + (size_t)gi * TS;
-  float2* colbuf = sm + Lay::colbuf();   // [c][kx]   owned columns (row stride NP, shared with prodr)
-  float2* prodr = sm + Lay::prodr(Cl);   // [c][x]    product spectra received for owned columns
-  float2* mixr = sm + Lay::mixr(Cl);     // [f][r][ky] derived fields received for owned rows
-  int* colmap = reinterpret_cast<int*>(sm + Lay::maps(Cl, Rl, KcP));
+  float2* colbuf = sm + Lay::colbuf();   // [kx][c]    owned columns (row stride ClP, shared with prodr)
+  float2* prodr = sm + Lay::prodr(Cl);   // [x][c]     product spectra received for owned columns
+  float2* mixr = sm + Lay::mixr(Cl);     // [f][ky][r] derived fields received for owned rows (stride RlP)
+  int* colmap = reinterpret_cast<int*>(sm + Lay::maps(Cl, Rl, Kc));  // ky -> (owner << 16) | column
+  int* rowmap = colmap + Kc;                                          // x  -> (owner << 16) | row
 
   for (int t = tid; t < N; t += THREADS) {
     const int k1 = t / T, ll = t % T;
     twl[t] = __ldg(P.tw + ((ll * k1) % N));  // w_N^(l k1), [k1][l]
   }
   for (int kk = tid; kk < Kc; kk += THREADS) colmap[kk] = ((kk / Cl) << 16) | (kk % Cl);
+  for (int x = tid; x < N; x += THREADS) rowmap[x] = ((x / Rl) << 16) | (x % Rl);
   __shared__ float2* s_mixr[16];
   __shared__ float2* s_prodr[16];
   if (tid < G) {
@@ -143,7 +148,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
     for (int t = tid; t < ncols * N; t += THREADS) {
       const int kx = t / ncols, c = t - kx * ncols;
       const float2 v = uin[(int64_t)kx * M + col0 + c];
-      colbuf[c * NP + kx] = v;
+      colbuf[kx * ClP + c] = v;
       sb.U[(int64_t)(col0 + c) * N + kx] = v;
     }
     __syncthreads();
@@ -165,7 +170,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           const int ks = sgn_k<N>(kx);
           float2 r1 = make_float2(0.f, 0.f), r2 = r1;
           if (ks <= K && ks >= -K) {
-            const float2 w = colbuf[c * NP + kx];
+            const float2 w = colbuf[kx * ClP + c];
             const float kxs = ksc * (float)ks;
             if (pr == 0) {
               const float lap = -(kxs * kxs + kys * kys);
@@ -188,9 +193,10 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
 #pragma unroll
         for (int j = 0; j < E; ++j) {
           const int x = l + T * j;
-          const int d = x / Rl, xr = x - d * Rl;
-          s_mixr[d][(f1 * Rl + xr) * KcP + ky] = v[j];
-          s_mixr[d][(f2 * Rl + xr) * KcP + ky] = v2[j];
+          const int rm = rowmap[x];
+          const int d = rm >> 16, xr = rm & 0xffff;
+          s_mixr[d][(f1 * Kc + ky) * RlP + xr] = v[j];
+          s_mixr[d][(f2 * Kc + ky) * RlP + xr] = v2[j];
         }
       }
       cluster.sync();  // derived fields delivered
@@ -209,10 +215,10 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           const bool ro = (k == 0) || (k == N / 2);
           float2 U = make_float2(0.f, 0.f), V = U, WX = U, WY = U;
           if (kk <= K) {
-            U = mixr[(0 * Rl + rr) * KcP + kk];
-            V = mixr[(1 * Rl + rr) * KcP + kk];
-            WX = mixr[(2 * Rl + rr) * KcP + kk];
-            WY = mixr[(3 * Rl + rr) * KcP + kk];
+            U = mixr[(0 * Kc + kk) * RlP + rr];
+            V = mixr[(1 * Kc + kk) * RlP + rr];
+            WX = mixr[(2 * Kc + kk) * RlP + rr];
+            WY = mixr[(3 * Kc + kk) * RlP + rr];
           }
           z1[j] = pack_pair(U, V, ext, ro);
           z2[j] = pack_pair(WX, WY, ext, ro);
@@ -242,9 +248,9 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
               float2 A, B;
               unpack_pair(w[j], rcv, A, B);
               const int cm = colmap[k];
-              float2* dst = s_prodr[cm >> 16] + (cm & 0xffff) * NP + xa;
+              float2* dst = s_prodr[cm >> 16] + xa * ClP + (cm & 0xffff);
               dst[0] = A;
-              if (r + 1 < Rg) dst[1] = B;
+              if (r + 1 < Rg) dst[ClP] = B;
             }
           }
         }
@@ -256,7 +262,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
         const int ky = col0 + c;
         float2 v[E];
 #pragma unroll
-        for (int j = 0; j < E; ++j) v[j] = prodr[c * NP + l + T * j];
+        for (int j = 0; j < E; ++j) v[j] = prodr[(l + T * j) * ClP + c];
         group_fft<E, T, false>(v, l, tile, twl, gmask);
 #pragma unroll
         for (int j = 0; j < E; ++j) {
@@ -265,7 +271,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           float2 nv = make_float2(0.f, 0.f);
           if (ks <= K && ks >= -K) nv = cscale(v[j], negb);
           if (ky == P.inj_mode && kx == 0) nv.x += P.inj_value;
-          colbuf[c * NP + kx] = nv;
+          colbuf[kx * ClP + c] = nv;
         }
       }
       __syncthreads();
@@ -273,23 +279,23 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
       if (a.nonlinear_only) {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
-          uout[(int64_t)kx * M + col0 + c] = colbuf[c * NP + kx];
+          uout[(int64_t)kx * M + col0 + c] = colbuf[kx * ClP + c];
         }
       } else {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
           const int64_t o = (int64_t)(col0 + c) * N + kx;
-          colbuf[c * NP + kx] = stage_upd(P, sb, o, st, colbuf[c * NP + kx]);
+          colbuf[kx * ClP + c] = stage_upd(P, sb, o, st, colbuf[kx * ClP + c]);
         }
         if (last_of_step && a.project && col0 == 0 && ncols > 0) {
           // c2r projection of the step's physical round trip on ky = 0
           __syncthreads();
           for (int kx = tid; kx <= N / 2; kx += THREADS) {
             const int kx2 = (N - kx) % N;
-            const float2 a1 = colbuf[kx], a2 = colbuf[kx2];
+            const float2 a1 = colbuf[kx * ClP], a2 = colbuf[kx2 * ClP];
             const float2 pv = make_float2(0.5f * (a1.x + a2.x), 0.5f * (a1.y - a2.y));
-            colbuf[kx] = pv;
-            colbuf[kx2] = cconj(pv);
+            colbuf[kx * ClP] = pv;
+            colbuf[kx2 * ClP] = cconj(pv);
             sb.U[kx] = pv;
             sb.U[kx2] = cconj(pv);
           }
@@ -365,9 +371,8 @@ static int v2_configure(exgb_plan* plan) {
     if (wantG && wantG != G) continue;
     const int Cl = (Kc + G - 1) / G;
     const int Rl = (N + G - 1) / G;
-    const int KcP = Kc | 1;
     if (Rl < 2) continue;
-    const size_t bytes = Lay::bytes(Cl, Rl, KcP, Kc);
+    const size_t bytes = Lay::bytes(Cl, Rl, Kc);
     if (bytes > limit) continue;
     EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     cudaLaunchConfig_t cfg = {};
