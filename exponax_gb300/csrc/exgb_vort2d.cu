@@ -45,8 +45,10 @@ struct V2Layout {
   static constexpr int NG = THREADS / T;
   static constexpr int TS = tile_stride<E, T>();
   // Exchange buffers are laid out so that consecutive lanes (consecutive positions of one
-  // transform) write consecutive addresses of the receiving CTA, with odd row strides (ClP, RlP)
-  // so that the local column reads stay free of bank conflicts.
+  // transform) write consecutive addresses of the receiving CTA; the row strides (ClP, RlP) are
+  // padded so that the local column reads of one half-warp hit distinct banks: odd for groups
+  // of 16 lanes, = 2 (mod 16) for groups of 8 (two groups, on neighbouring rows, per half-warp).
+  __host__ __device__ static int pad(int v) { return T >= 16 ? (v | 1) : v + ((2 - v) & 15); }
   // float2 offsets
   __host__ __device__ static size_t twl() { return 0; }
   __host__ __device__ static size_t tiles() { return N; }
@@ -54,8 +56,8 @@ struct V2Layout {
   // the product spectra received for the owned columns overwrite the stage input in place: the
   // stage input is consumed by the column inverse before the first cluster barrier of a stage
   __host__ __device__ static size_t prodr(int) { return colbuf(); }
-  __host__ __device__ static size_t mixr(int Cl) { return prodr(Cl) + (size_t)N * (Cl | 1); }
-  __host__ __device__ static size_t maps(int Cl, int Rl, int Kc) { return mixr(Cl) + (size_t)4 * Kc * (Rl | 1); }
+  __host__ __device__ static size_t mixr(int Cl) { return prodr(Cl) + (size_t)N * pad(Cl); }
+  __host__ __device__ static size_t maps(int Cl, int Rl, int Kc) { return mixr(Cl) + (size_t)4 * Kc * pad(Rl); }
   __host__ __device__ static size_t bytes(int Cl, int Rl, int Kc) {
     return sizeof(float2) * maps(Cl, Rl, Kc) + sizeof(int) * (size_t)(Kc + N);
   }
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   const int ncl = (int)(gridDim.x / G);
   const PlanDev& P = a.P;
   const int Kc = a.Kc, K = Kc - 1, Cl = a.Cl, Rl = a.Rl;
-  const int ClP = Cl | 1, RlP = Rl | 1;
+  const int ClP = Lay::pad(Cl), RlP = Lay::pad(Rl);
   const int tid = threadIdx.x;
   const int gi = tid / T, l = tid % T;
   const int lane = tid & 31;
