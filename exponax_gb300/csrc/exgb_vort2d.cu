@@ -204,10 +204,8 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
       cluster.sync();  // derived fields delivered
 
       // ================= row phase: local gather -> 2 IFFTs -> product -> paired FFT -> pushed to column owners
-      for (int r0 = 0; r0 < Rg; r0 += NG) {
-        const int r = r0 + gi;
-        const bool valid = r < Rg;
-        const int rr = valid ? r : 0;
+      // product u wx + v wy of local row rr in registers (lane l owns positions l + T j)
+      auto row_product = [&](int rr, float (&pj)[E]) {
         float2 z1[E], z2[E];
 #pragma unroll
         for (int j = 0; j < E; ++j) {
@@ -226,35 +224,60 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           z2[j] = pack_pair(WX, WY, ext, ro);
         }
         group_fft_x2<E, T, true>(z1, z2, l, tile, twl, gmask);
-        float pj[E];
 #pragma unroll
         for (int j = 0; j < E; ++j) pj[j] = fmaf(z1[j].x, z2[j].x, z1[j].y * z2[j].y);
-        float2 w[E];
+      };
+      // forward FFT of two rows packed as w = p_a + i p_b, unpacked and pushed to the column owners
+      auto push_pair = [&](float2 (&w)[E], int r) {
+        group_fft<E, T, false>(w, l, tile, twl, gmask);
+        const int xa = row0 + r;
 #pragma unroll
         for (int j = 0; j < E; ++j) {
-          const float other = __shfl_xor_sync(0xffffffffu, pj[j], T);
-          w[j] = make_float2(pj[j], other);
+          const float2 snd = w[E - 1 - j];
+          float2 rcv;
+          rcv.x = __shfl_sync(gmask, snd.x, (T - l) % T, T);
+          rcv.y = __shfl_sync(gmask, snd.y, (T - l) % T, T);
+          if (l == 0) rcv = w[(E - j) % E];
+          const int k = l + T * j;
+          if (k <= K) {
+            float2 A, B;
+            unpack_pair(w[j], rcv, A, B);
+            const int cm = colmap[k];
+            float2* dst = s_prodr[cm >> 16] + xa * ClP + (cm & 0xffff);
+            dst[0] = A;
+            if (r + 1 < Rg) dst[ClP] = B;
+          }
         }
-        if ((gi & 1) == 0 && valid) {
-          group_fft<E, T, false>(w, l, tile, twl, gmask);
-          const int xa = row0 + r;
+      };
+      if (Rg > NG) {
+        // more rows than groups: each group takes a pair of rows (2 product evaluations, 1 FFT),
+        // so no group waits through its neighbour's forward FFT
+        for (int r0 = 0; r0 < Rg; r0 += 2 * NG) {
+          const int r = r0 + 2 * gi;
+          if (r < Rg) {
+            float pa[E], pb[E];
+            row_product(r, pa);
+            row_product(r + 1 < Rg ? r + 1 : r, pb);
+            float2 w[E];
+#pragma unroll
+            for (int j = 0; j < E; ++j) w[j] = make_float2(pa[j], pb[j]);
+            push_pair(w, r);
+          }
+        }
+      } else {
+        // one row per group; neighbouring groups pair their rows through a warp shuffle
+        for (int r0 = 0; r0 < Rg; r0 += NG) {
+          const int r = r0 + gi;
+          const bool valid = r < Rg;
+          float pj[E];
+          row_product(valid ? r : 0, pj);
+          float2 w[E];
 #pragma unroll
           for (int j = 0; j < E; ++j) {
-            const float2 snd = w[E - 1 - j];
-            float2 rcv;
-            rcv.x = __shfl_sync(gmask, snd.x, (T - l) % T, T);
-            rcv.y = __shfl_sync(gmask, snd.y, (T - l) % T, T);
-            if (l == 0) rcv = w[(E - j) % E];
-            const int k = l + T * j;
-            if (k <= K) {
-              float2 A, B;
-              unpack_pair(w[j], rcv, A, B);
-              const int cm = colmap[k];
-              float2* dst = s_prodr[cm >> 16] + xa * ClP + (cm & 0xffff);
-              dst[0] = A;
-              if (r + 1 < Rg) dst[ClP] = B;
-            }
+            const float other = __shfl_xor_sync(0xffffffffu, pj[j], T);
+            w[j] = make_float2(pj[j], other);
           }
+          if ((gi & 1) == 0 && valid) push_pair(w, r);
         }
       }
       cluster.sync();  // product spectra delivered
@@ -283,12 +306,54 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           const int c = t / N, kx = t % N;
           uout[(int64_t)kx * M + col0 + c] = colbuf[kx * ClP + c];
         }
+      } else if (P.order == 2) {
+        // ETDRK2 (etdrk/_etdrk_2.py:91-102), four modes per thread with all loads issued first
+        const int total = ncols * N;
+        for (int t0 = tid; t0 < total; t0 += 4 * THREADS) {
+          float2 nv[4], x[4], y[4], e[4];
+          float cf[4];
+          int64_t o[4];
+          int sm_i[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int t = min(t0 + u * THREADS, total - 1);
+            const int c = t / N, kx = t - c * N;
+            o[u] = (int64_t)(col0 + c) * N + kx;
+            sm_i[u] = kx * ClP + c;
+            nv[u] = colbuf[sm_i[u]];
+            if (st == 0) {
+              x[u] = sb.U[o[u]];
+              e[u] = __ldg(P.E + o[u]);
+              cf[u] = __ldg(P.c[0] + o[u]);
+            } else {
+              x[u] = sb.S[o[u]];
+              y[u] = sb.N0[o[u]];
+              cf[u] = __ldg(P.c[1] + o[u]);
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (t0 + u * THREADS >= total) break;
+            if (st == 0) {
+              const float2 r = cadd(cmul(e[u], x[u]), cscale(nv[u], cf[u]));
+              sb.N0[o[u]] = nv[u];
+              sb.S[o[u]] = r;
+              colbuf[sm_i[u]] = r;
+            } else {
+              const float2 r = cadd(x[u], cscale(csub(nv[u], y[u]), cf[u]));
+              sb.U[o[u]] = r;
+              colbuf[sm_i[u]] = r;
+            }
+          }
+        }
       } else {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
           const int64_t o = (int64_t)(col0 + c) * N + kx;
           colbuf[kx * ClP + c] = stage_upd(P, sb, o, st, colbuf[kx * ClP + c]);
         }
+      }
+      if (!a.nonlinear_only) {
         if (last_of_step && a.project && col0 == 0 && ncols > 0) {
           // c2r projection of the step's physical round trip on ky = 0
           __syncthreads();
