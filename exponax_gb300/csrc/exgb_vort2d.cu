@@ -249,7 +249,10 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           }
         }
       };
-      if (Rg > NG) {
+      // At N = 128 every cluster size that fits gives a CTA at most one row per group, and the
+      // pair path below would only add register pressure, so it is compiled out there.
+      constexpr bool kRowPairs = (N != 128);
+      if (kRowPairs && Rg > NG) {
         // more rows than groups: each group takes a pair of rows (2 product evaluations, 1 FFT),
         // so no group waits through its neighbour's forward FFT
         for (int r0 = 0; r0 < Rg; r0 += 2 * NG) {
@@ -307,15 +310,17 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           uout[(int64_t)kx * M + col0 + c] = colbuf[kx * ClP + c];
         }
       } else if (P.order == 2) {
-        // ETDRK2 (etdrk/_etdrk_2.py:91-102), four modes per thread with all loads issued first
+        // ETDRK2 (etdrk/_etdrk_2.py:91-102), SB modes per thread with all loads issued first
+        // (2 at N = 256, where the row-pair path already fills the register budget)
+        constexpr int SB = (N == 256) ? 2 : 4;
         const int total = ncols * N;
-        for (int t0 = tid; t0 < total; t0 += 4 * THREADS) {
-          float2 nv[4], x[4], y[4], e[4];
-          float cf[4];
-          int64_t o[4];
-          int sm_i[4];
+        for (int t0 = tid; t0 < total; t0 += SB * THREADS) {
+          float2 nv[SB], x[SB], y[SB], e[SB];
+          float cf[SB];
+          int64_t o[SB];
+          int sm_i[SB];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < SB; ++u) {
             const int t = min(t0 + u * THREADS, total - 1);
             const int c = t / N, kx = t - c * N;
             o[u] = (int64_t)(col0 + c) * N + kx;
@@ -332,7 +337,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
             }
           }
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
+          for (int u = 0; u < SB; ++u) {
             if (t0 + u * THREADS >= total) break;
             if (st == 0) {
               const float2 r = cadd(cmul(e[u], x[u]), cscale(nv[u], cf[u]));
