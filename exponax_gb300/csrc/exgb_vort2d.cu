@@ -309,48 +309,6 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           const int c = t / N, kx = t % N;
           uout[(int64_t)kx * M + col0 + c] = colbuf[kx * ClP + c];
         }
-      } else if (P.order == 2) {
-        // ETDRK2 (etdrk/_etdrk_2.py:91-102), SB modes per thread with all loads issued first
-        // (2 at N = 256, where the row-pair path already fills the register budget)
-        constexpr int SB = (N == 256) ? 2 : 4;
-        const int total = ncols * N;
-        for (int t0 = tid; t0 < total; t0 += SB * THREADS) {
-          float2 nv[SB], x[SB], y[SB], e[SB];
-          float cf[SB];
-          int64_t o[SB];
-          int sm_i[SB];
-#pragma unroll
-          for (int u = 0; u < SB; ++u) {
-            const int t = min(t0 + u * THREADS, total - 1);
-            const int c = t / N, kx = t - c * N;
-            o[u] = (int64_t)(col0 + c) * N + kx;
-            sm_i[u] = kx * ClP + c;
-            nv[u] = colbuf[sm_i[u]];
-            if (st == 0) {
-              x[u] = sb.U[o[u]];
-              e[u] = __ldg(P.E + o[u]);
-              cf[u] = __ldg(P.c[0] + o[u]);
-            } else {
-              x[u] = sb.S[o[u]];
-              y[u] = sb.N0[o[u]];
-              cf[u] = __ldg(P.c[1] + o[u]);
-            }
-          }
-#pragma unroll
-          for (int u = 0; u < SB; ++u) {
-            if (t0 + u * THREADS >= total) break;
-            if (st == 0) {
-              const float2 r = cadd(cmul(e[u], x[u]), cscale(nv[u], cf[u]));
-              sb.N0[o[u]] = nv[u];
-              sb.S[o[u]] = r;
-              colbuf[sm_i[u]] = r;
-            } else {
-              const float2 r = cadd(x[u], cscale(csub(nv[u], y[u]), cf[u]));
-              sb.U[o[u]] = r;
-              colbuf[sm_i[u]] = r;
-            }
-          }
-        }
       } else {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
