@@ -136,3 +136,33 @@ def test_split_bf16_100_steps_against_fp32_and_fp64():
               f"fp32 oracle {eo32:.2e}; split-bf16 vs fp32 oracle {d:.2e}")
     assert res[1][3] < 1e-5
     assert res[n][3] < 1e-4
+
+
+def test_split_bf16_navier_stokes_rollout_and_switch_back():
+    """Plain NavierStokesVorticity (no forcing) on the tensor-core path: a 10-step physical rollout
+    (c2r projection between steps) within 1e-4 of the oracle, and switching the plan back to FP32
+    transforms reproduces the FP32 path."""
+    sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, 128, 0.01, diffusivity=1e-3)
+    so = o.NavierStokesVorticity(2, 2 * np.pi, 128, 0.01, diffusivity=1e-3)
+    u = _ics(3, seed0=40)
+    fp32 = ex.vmap(ex.rollout(sm, 10, include_init=True))(cu(u)).cpu().numpy()
+    sm.set_dft_precision("split_bf16")
+    tc = ex.vmap(ex.rollout(sm, 10, include_init=True))(cu(u)).cpu().numpy()
+    sm.plan.status()
+    for b in range(3):
+        want = o.rollout(so, 10, include_init=True)(u[b])
+        assert rel(tc[b], want) < 1e-4, b
+    sm.set_dft_precision("fp32")
+    again = ex.vmap(ex.rollout(sm, 10, include_init=True))(cu(u)).cpu().numpy()
+    np.testing.assert_array_equal(again, fp32)
+
+
+def test_split_bf16_batch_not_multiple_of_ctas():
+    """Batches smaller and larger than the persistent grid (152 CTAs) give the same per-sample result."""
+    sm = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 128, 0.01).set_dft_precision("split_bf16")
+    u = _ics(2, seed0=60)
+    small = ex.vmap(ex.repeat(sm, 3))(cu(u)).cpu().numpy()
+    big = np.concatenate([u] * 101)  # 202 samples
+    out = ex.vmap(ex.repeat(sm, 3))(cu(big)).cpu().numpy()
+    for rep in (0, 77, 100):
+        np.testing.assert_array_equal(out[2 * rep:2 * rep + 2], small)
