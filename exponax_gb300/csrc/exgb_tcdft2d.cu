@@ -79,8 +79,8 @@ constexpr uint32_t R_BYTES = 2 * TILE_B1 + 2 * TILE_A2;
 constexpr uint32_t PLANE = 48 * LD * 4;     // one float plane [k_full 0..47][k_half]
 constexpr uint32_t OFF_PM = OFF_R + R_BYTES;  // planes A+re, A+im, A-re, A-im
 constexpr uint32_t OFF_IL = OFF_PM + 4 * PLANE;  // 1 / (N^2 Lap) on the kept modes [k_full][k_half]
-constexpr uint32_t OFF_TAIL = OFF_IL + PLANE;     // 2 mbarriers (8 B each) and the TMEM base address (4 B)
-constexpr uint32_t SMEM_BYTES = OFF_TAIL + 24;
+constexpr uint32_t OFF_TAIL = OFF_IL + PLANE;     // mbarrier (8 B) and TMEM base address (4 B)
+constexpr uint32_t SMEM_BYTES = OFF_TAIL + 16;
 static_assert(2 * TILE_B3 <= R_BYTES && 2 * TILE_B4 <= R_BYTES, "region R too small");
 static_assert(48u * N * 8u <= R_BYTES, "nonlinear-term buffer must fit region R");
 static_assert(128 * KF * 2 - TILE_AF <= R_BYTES, "Af overflow rows must stay inside shared memory");
@@ -161,10 +161,8 @@ __device__ __forceinline__ void build_b1(unsigned char* hi, unsigned char* lo, c
 
 __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
   extern __shared__ __align__(128) unsigned char sm[];
-  // mbarrier A: full-axis inverse chains and the forward chains; mbarrier B: half-axis inverse chains
   uint64_t& s_mbar = *reinterpret_cast<uint64_t*>(sm + OFF_TAIL);
-  uint64_t& s_mbarB = *reinterpret_cast<uint64_t*>(sm + OFF_TAIL + 8);
-  uint32_t& s_tbase = *reinterpret_cast<uint32_t*>(sm + OFF_TAIL + 16);
+  uint32_t& s_tbase = *reinterpret_cast<uint32_t*>(sm + OFF_TAIL + 8);
   const PlanDev& P = a.P;
   const int K = min(P.kmax, KMAX);
   const int Kc = K + 1;
@@ -195,7 +193,6 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
   }
   if (tid == 0) {
     tc::mbar_init(&s_mbar, 1);
-    tc::mbar_init(&s_mbarB, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::fence_proxy_async();
@@ -213,8 +210,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
   const StageBufs sb = stage_bufs(a.scratch + (int64_t)blockIdx.x * a.scratch_stride, P.order, (int64_t)Kc * N);
   const uint32_t idI1 = tc::idesc_bf16(128, 96), idI2 = tc::idesc_bf16(128, 128);
   const uint32_t idF1 = tc::idesc_bf16(128, 128), idF2 = tc::idesc_bf16(128, 96);
-  uint32_t phase = 0, phaseB = 0;
-  bool pendA = false, pendB = false;  // a commit on the barrier has not been waited for
+  uint32_t phase = 0;
   bool bad = false;
 
   auto sync_for_mma = [&]() {
@@ -222,18 +218,13 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
     tc::fence_before_sync();
     __syncthreads();
   };
-  // wait for the pending phase of one barrier; on a timeout the phase stays pending (drained at exit)
-  auto wait_on = [&](uint64_t* bar, uint32_t& ph, bool& pend) -> bool {
-    const bool ok = tc::mbar_wait(bar, ph, WAIT_BUDGET);
+  auto wait_mma = [&]() -> bool {
+    const bool ok = tc::mbar_wait(&s_mbar, phase, WAIT_BUDGET);
+    phase ^= 1u;
     const int anybad = __syncthreads_or(!ok);
-    if (!anybad) {
-      ph ^= 1u;
-      pend = false;
-    }
     tc::fence_after_sync();
     return anybad == 0;
   };
-
   auto b1 = [&](int f) {
     unsigned char* h = rg + R_B1_HI;
     unsigned char* l = rg + R_B1_LO;
@@ -340,10 +331,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
     for (int qq = 0; qq < Q && !bad; ++qq) {
       const int st = qq % nst;
       const bool last_of_step = (st == nst - 1);
-      // ===== inverse transforms of the 4 derived fields; D2 of field f ends in TMEM slot f.
-      // The full-axis chain A(f+1) (barrier A) is issued before the half-axis operand of field f is
-      // built, and the half-axis chain B(f) (barrier B) before the next full-axis operand, so both
-      // kinds of MMA chain run under SIMT work; B1 / A2 are each reused once their chain has completed.
+      // ===== inverse transforms of the 4 derived fields; D2 of field f ends in TMEM slot f
       b1(0);
       sync_for_mma();
       if (tid == 0) {
@@ -351,34 +339,25 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
         tc::mma_split3(tmem, sAiH, sAiL, KI, sR + R_B1_HI, sR + R_B1_LO, KI, KI, idI1, false);
         tc::mma_commit(&s_mbar);
       }
-      pendA = true;
-      bad = !wait_on(&s_mbar, phase, pendA);
+      bad = !wait_mma();
       for (int f = 0; f < 4 && !bad; ++f) {
-        if (f < 3) {
-          b1(f + 1);  // B1 is free: A(f) has completed
-          sync_for_mma();
-          if (tid == 0) {
-            tc::fence_after_sync();
-            tc::mma_split3(tmem + 128u * (f + 1), sAiH, sAiL, KI, sR + R_B1_HI, sR + R_B1_LO, KI, KI, idI1, false);
-            tc::mma_commit(&s_mbar);
-          }
-          pendA = true;
-        }
-        if (f > 0) {
-          bad = !wait_on(&s_mbarB, phaseB, pendB);  // A2 is free: B(f-1) has completed
-          if (bad) break;
-        }
-        build_a2(f);  // D1(f) is complete: A(f) was waited for
+        build_a2(f);
         sync_for_mma();
         if (tid == 0) {
           tc::fence_after_sync();
           tc::mma_split3(tmem + 128u * f, sR + R_A2_HI, sR + R_A2_LO, KI, sAiH, sAiL, KI, KI, idI2, false);
-          tc::mma_commit(&s_mbarB);
         }
-        pendB = true;
-        if (f < 3) bad = !wait_on(&s_mbar, phase, pendA);  // D1(f+1) complete, B1 free again
+        if (f < 3) {
+          b1(f + 1);  // B1 is free (its MMA completed); overlaps the MMA above
+          sync_for_mma();
+          if (tid == 0) {
+            tc::fence_after_sync();
+            tc::mma_split3(tmem + 128u * (f + 1), sAiH, sAiL, KI, sR + R_B1_HI, sR + R_B1_LO, KI, KI, idI1, false);
+          }
+        }
+        if (tid == 0) tc::mma_commit(&s_mbar);
+        bad = !wait_mma();
       }
-      if (!bad) bad = !wait_on(&s_mbarB, phaseB, pendB);  // B(3): all four D2 complete
       if (bad) break;
 
       // ===== product u wx + v wy at (i, j) and (i, N-j) -> forward half-axis data (e | o)
@@ -418,8 +397,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
         tc::mma_split3(tmem, sAfH, sAfL, KF, sR, sR + TILE_B3, KF, KF, idF1, false);
         tc::mma_commit(&s_mbar);
       }
-      pendA = true;
-      bad = !wait_on(&s_mbar, phase, pendA);
+      bad = !wait_mma();
       if (bad) break;
 
       // ===== D3 rows (half modes: Re, -Im) -> forward full-axis data (e | o over the full axis)
@@ -451,8 +429,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
         tc::mma_split3(tmem + 128u, sAfH, sAfL, KF, sR, sR + TILE_B4, KF, KF, idF2, false);
         tc::mma_commit(&s_mbar);
       }
-      pendA = true;
-      bad = !wait_on(&s_mbar, phase, pendA);
+      bad = !wait_mma();
       if (bad) break;
 
       // ===== D4 -> nonlinear term at the kept modes (region R, B4 is no longer read)
@@ -593,8 +570,7 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
 
   if (bad) {
     // let any MMA still in flight finish before the tensor memory is released
-    if (pendA) tc::mbar_wait(&s_mbar, phase, WAIT_BUDGET);
-    if (pendB) tc::mbar_wait(&s_mbarB, phaseB, WAIT_BUDGET);
+    tc::mbar_wait(&s_mbar, phase ^ 1u, WAIT_BUDGET);
     if (tid == 0) atomicExch(a.status, EXGB_ETIMEOUT);
   }
   tc::fence_before_sync();
