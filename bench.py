@@ -142,13 +142,10 @@ def cpu_baseline(samples=None, nsteps=40):
 
 # ------------------------------------------------------------------ arms
 def dist_init():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    if ws > 1:
-        import torch.distributed as dist
+    """One process per GPU (torchrun); replicas over batch shards, no data-path collective."""
+    from exponax_gb300 import replicas
 
-        dist.init_process_group("nccl")
-    return rank, ws
+    return replicas.init("nccl")
 
 
 def run_reference(args, rank, ws):
@@ -187,7 +184,10 @@ def run_gb300(args, rank, ws):
     stream = torch.cuda.current_stream()
     sptr = _device.stream()
 
-    u0_host = make_ics(rank * BATCH, BATCH)  # this rank's shard of seeds
+    from exponax_gb300 import replicas
+
+    seeds = replicas.shard(BATCH, rank)  # this rank's contiguous shard of seeds
+    u0_host = make_ics(seeds.start, BATCH)
     u0 = torch.from_numpy(u0_host).cuda()
     uh0 = ex.fft(u0, num_spatial_dims=2)
     out_h = torch.empty_like(uh0)
@@ -218,13 +218,9 @@ def run_gb300(args, rank, ws):
         e1.record(stream)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
-    total_ms = float(np.sum(times))
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = replicas.max_over_ranks(float(np.sum(times)))
     ms_step = total_ms / args.steps
-    value = BATCH * ws * N * N * NSTEPS / (ms_step * 1e-3)
+    value = replicas.aggregate_throughput(BATCH * N * N * NSTEPS, ws, ms_step)
 
     # ---- e2e: public API, pinned host buffers, H2D + repeat + D2H inside the timed region
     pin_in = torch.from_numpy(u0_host).pin_memory()
@@ -248,12 +244,8 @@ def run_gb300(args, rank, ws):
         torch.cuda.synchronize()
         etimes.append(e0.elapsed_time(e1))
     clk = clocks.stop(local)
-    e_ms = float(np.sum(etimes)) / args.steps
-    if ws > 1:
-        t = torch.tensor([e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e_ms = float(t.item())
-    e2e = BATCH * ws * N * N * NSTEPS / (e_ms * 1e-3)
+    e_ms = replicas.max_over_ranks(float(np.sum(etimes)) / args.steps)
+    e2e = replicas.aggregate_throughput(BATCH * N * N * NSTEPS, ws, e_ms)
 
     # ---- roofline of the dominant kernel (vort2d_kernel: the only launch of fourier_run)
     peaks = {}
