@@ -45,10 +45,15 @@ struct V2Layout {
   static constexpr int NG = THREADS / T;
   static constexpr int TS = tile_stride<E, T>();
   // Exchange buffers are laid out so that consecutive lanes (consecutive positions of one
-  // transform) write consecutive addresses of the receiving CTA; the row strides (ClP, RlP) are
-  // padded so that the local column reads of one half-warp hit distinct banks: odd for groups
-  // of 16 lanes, = 2 (mod 16) for groups of 8 (two groups, on neighbouring rows, per half-warp).
-  __host__ __device__ static int pad(int v) { return T >= 16 ? (v | 1) : v + ((2 - v) & 15); }
+  // transform) write consecutive addresses of the receiving CTA, 16 bytes at a time:
+  //   derived fields  [pair][ky][row] x {field 2p, field 2p+1}   (float4 per entry)
+  //   product spectra [row/2][column] x {row even, row odd}       (float4 per row pair)
+  // The row strides are padded so that the local reads of one half-warp hit distinct banks:
+  // padC (product / stage-input buffer, 8-byte reads) odd for groups of 16 lanes and = 2 (mod 16)
+  // for groups of 8 (two groups, on neighbouring columns, per half-warp); padR (derived fields,
+  // 16-byte reads, one group per quarter-warp phase) odd.
+  __host__ __device__ static int padC(int v) { return T >= 16 ? (v | 1) : v + ((2 - v) & 15); }
+  __host__ __device__ static int padR(int v) { return v | 1; }
   // float2 offsets
   __host__ __device__ static size_t twl() { return 0; }
   __host__ __device__ static size_t tiles() { return N; }
@@ -56,8 +61,8 @@ struct V2Layout {
   // the product spectra received for the owned columns overwrite the stage input in place: the
   // stage input is consumed by the column inverse before the first cluster barrier of a stage
   __host__ __device__ static size_t prodr(int) { return colbuf(); }
-  __host__ __device__ static size_t mixr(int Cl) { return prodr(Cl) + (size_t)N * pad(Cl); }
-  __host__ __device__ static size_t maps(int Cl, int Rl, int Kc) { return mixr(Cl) + (size_t)4 * Kc * pad(Rl); }
+  __host__ __device__ static size_t mixr(int Cl) { return prodr(Cl) + (size_t)N * padC(Cl); }
+  __host__ __device__ static size_t maps(int Cl, int Rl, int Kc) { return mixr(Cl) + (size_t)4 * Kc * padR(Rl); }
   __host__ __device__ static size_t bytes(int Cl, int Rl, int Kc) {
     return sizeof(float2) * maps(Cl, Rl, Kc) + sizeof(int) * (size_t)(Kc + N);
   }
@@ -80,7 +85,9 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   const int ncl = (int)(gridDim.x / G);
   const PlanDev& P = a.P;
   const int Kc = a.Kc, K = Kc - 1, Cl = a.Cl, Rl = a.Rl;
-  const int ClP = Lay::pad(Cl), RlP = Lay::pad(Rl);
+  const int ClP = Lay::padC(Cl), RlP = Lay::padR(Rl);
+  // stage input / product spectra of row (or kx) x in owned column c: rows interleaved in pairs
+  auto cb = [ClP](int x, int c) { return ((x >> 1) * ClP + c) * 2 + (x & 1); };
   const int tid = threadIdx.x;
   const int gi = tid / T, l = tid % T;
   const int lane = tid & 31;
@@ -91,7 +98,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   float2* tile = sm + Lay::tiles() + (size_t)gi * TS;
   float2* colbuf = sm + Lay::colbuf();   // [kx][c]    owned columns (row stride ClP, shared with prodr)
   float2* prodr = sm + Lay::prodr(Cl);   // [x][c]     product spectra received for owned columns
-  float2* mixr = sm + Lay::mixr(Cl);     // [f][ky][r] derived fields received for owned rows (stride RlP)
+  float4* mixr = reinterpret_cast<float4*>(sm + Lay::mixr(Cl));  // [pair][ky][r] derived fields of owned rows
   int* colmap = reinterpret_cast<int*>(sm + Lay::maps(Cl, Rl, Kc));  // ky -> (owner << 16) | column
   int* rowmap = colmap + Kc;                                          // x  -> (owner << 16) | row
 
@@ -101,7 +108,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
   }
   for (int kk = tid; kk < Kc; kk += THREADS) colmap[kk] = ((kk / Cl) << 16) | (kk % Cl);
   for (int x = tid; x < N; x += THREADS) rowmap[x] = ((x / Rl) << 16) | (x % Rl);
-  __shared__ float2* s_mixr[16];
+  __shared__ float4* s_mixr[16];
   __shared__ float2* s_prodr[16];
   if (tid < G) {
     s_mixr[tid] = cluster.map_shared_rank(mixr, tid);
@@ -150,7 +157,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
     for (int t = tid; t < ncols * N; t += THREADS) {
       const int kx = t / ncols, c = t - kx * ncols;
       const float2 v = uin[(int64_t)kx * M + col0 + c];
-      colbuf[kx * ClP + c] = v;
+      colbuf[cb(kx, c)] = v;
       sb.U[(int64_t)(col0 + c) * N + kx] = v;
     }
     __syncthreads();
@@ -172,7 +179,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           const int ks = sgn_k<N>(kx);
           float2 r1 = make_float2(0.f, 0.f), r2 = r1;
           if (ks <= K && ks >= -K) {
-            const float2 w = colbuf[kx * ClP + c];
+            const float2 w = colbuf[cb(kx, c)];
             const float kxs = ksc * (float)ks;
             if (pr == 0) {
               const float lap = -(kxs * kxs + kys * kys);
@@ -200,14 +207,12 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           v2[j] = r2;
         }
         group_fft_x2<E, T, true>(v, v2, l, tile, twl, gmask);
-        const int f1 = 2 * pr, f2 = 2 * pr + 1;
 #pragma unroll
         for (int j = 0; j < E; ++j) {
           const int x = l + T * j;
           const int rm = rowmap[x];
           const int d = rm >> 16, xr = rm & 0xffff;
-          s_mixr[d][(f1 * Kc + ky) * RlP + xr] = v[j];
-          s_mixr[d][(f2 * Kc + ky) * RlP + xr] = v2[j];
+          s_mixr[d][(pr * Kc + ky) * RlP + xr] = make_float4(v[j].x, v[j].y, v2[j].x, v2[j].y);
         }
       }
       cluster.sync();  // derived fields delivered
@@ -224,10 +229,12 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           const bool ro = (k == 0) || (k == N / 2);
           float2 U = make_float2(0.f, 0.f), V = U, WX = U, WY = U;
           if (kk <= K) {
-            U = mixr[(0 * Kc + kk) * RlP + rr];
-            V = mixr[(1 * Kc + kk) * RlP + rr];
-            WX = mixr[(2 * Kc + kk) * RlP + rr];
-            WY = mixr[(3 * Kc + kk) * RlP + rr];
+            const float4 uv = mixr[(0 * Kc + kk) * RlP + rr];
+            const float4 wxy = mixr[(1 * Kc + kk) * RlP + rr];
+            U = make_float2(uv.x, uv.y);
+            V = make_float2(uv.z, uv.w);
+            WX = make_float2(wxy.x, wxy.y);
+            WY = make_float2(wxy.z, wxy.w);
           }
           z1[j] = pack_pair(U, V, ext, ro);
           z2[j] = pack_pair(WX, WY, ext, ro);
@@ -252,9 +259,12 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
             float2 A, B;
             unpack_pair(w[j], rcv, A, B);
             const int cm = colmap[k];
-            float2* dst = s_prodr[cm >> 16] + xa * ClP + (cm & 0xffff);
-            dst[0] = A;
-            if (r + 1 < Rg) dst[ClP] = B;
+            float2* dst = s_prodr[cm >> 16] + cb(xa, cm & 0xffff);  // xa is even: rows xa, xa + 1 adjacent
+            if (r + 1 < Rg) {
+              *reinterpret_cast<float4*>(dst) = make_float4(A.x, A.y, B.x, B.y);
+            } else {
+              dst[0] = A;
+            }
           }
         }
       };
@@ -299,7 +309,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
         const int ky = col0 + c;
         float2 v[E];
 #pragma unroll
-        for (int j = 0; j < E; ++j) v[j] = prodr[(l + T * j) * ClP + c];
+        for (int j = 0; j < E; ++j) v[j] = prodr[cb(l + T * j, c)];
         group_fft<E, T, false>(v, l, tile, twl, gmask);
 #pragma unroll
         for (int j = 0; j < E; ++j) {
@@ -308,7 +318,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           float2 nv = make_float2(0.f, 0.f);
           if (ks <= K && ks >= -K) nv = cscale(v[j], negb);
           if (ky == P.inj_mode && kx == 0) nv.x += P.inj_value;
-          colbuf[kx * ClP + c] = nv;
+          colbuf[cb(kx, c)] = nv;
         }
       }
       __syncthreads();
@@ -316,13 +326,13 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
       if (a.nonlinear_only) {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
-          uout[(int64_t)kx * M + col0 + c] = colbuf[kx * ClP + c];
+          uout[(int64_t)kx * M + col0 + c] = colbuf[cb(kx, c)];
         }
       } else {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
           const int64_t o = (int64_t)(col0 + c) * N + kx;
-          colbuf[kx * ClP + c] = stage_upd(P, sb, o, st, colbuf[kx * ClP + c]);
+          colbuf[cb(kx, c)] = stage_upd(P, sb, o, st, colbuf[cb(kx, c)]);
         }
       }
       if (!a.nonlinear_only) {
@@ -331,10 +341,10 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           __syncthreads();
           for (int kx = tid; kx <= N / 2; kx += THREADS) {
             const int kx2 = (N - kx) % N;
-            const float2 a1 = colbuf[kx * ClP], a2 = colbuf[kx2 * ClP];
+            const float2 a1 = colbuf[cb(kx, 0)], a2 = colbuf[cb(kx2, 0)];
             const float2 pv = make_float2(0.5f * (a1.x + a2.x), 0.5f * (a1.y - a2.y));
-            colbuf[kx * ClP] = pv;
-            colbuf[kx2 * ClP] = cconj(pv);
+            colbuf[cb(kx, 0)] = pv;
+            colbuf[cb(kx2, 0)] = cconj(pv);
             sb.U[kx] = pv;
             sb.U[kx2] = cconj(pv);
           }
@@ -409,8 +419,8 @@ static int v2_configure(exgb_plan* plan) {
   for (int G = 1; G <= 8; ++G) {
     if (wantG && wantG != G) continue;
     const int Cl = (Kc + G - 1) / G;
-    const int Rl = (N + G - 1) / G;
-    if (Rl < 2) continue;
+    const int Rl = 2 * ((N + 2 * G - 1) / (2 * G));  // even: row pairs never straddle two CTAs
+    if (Rl < 2 || (G - 1) * Rl >= N) continue;
     const size_t bytes = Lay::bytes(Cl, Rl, Kc);
     if (bytes > limit) continue;
     EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -442,7 +452,7 @@ static int v2_configure(exgb_plan* plan) {
     c.G = G;
     c.threads = THREADS;
     c.cols_per_cta = (Kc + G - 1) / G;
-    c.rows_per_cta = (N + G - 1) / G;
+    c.rows_per_cta = 2 * ((N + 2 * G - 1) / (2 * G));
     c.CB = Kc | 1;  // padded ky stride of the derived-field receive buffer
     c.RB = 0;
     c.mixed_in_smem = 1;
