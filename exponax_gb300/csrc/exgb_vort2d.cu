@@ -277,12 +277,28 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
         for (int r0 = 0; r0 < Rg; r0 += 2 * NG) {
           const int r = r0 + 2 * gi;
           if (r < Rg) {
-            float pa[E], pb[E];
-            row_product(r, pa);
-            row_product(r + 1 < Rg ? r + 1 : r, pb);
             float2 w[E];
+            {
+              float pa[E];
+              row_product(r, pa);
+              // park row r's product in row r's own (already consumed) derived-field slots, read by
+              // no other group, instead of holding it in registers through the second transform
 #pragma unroll
-            for (int j = 0; j < E; ++j) w[j] = make_float2(pa[j], pb[j]);
+              for (int q = 0; q < E / 4; ++q)
+                mixr[(q * T + l) * RlP + r] = make_float4(pa[4 * q], pa[4 * q + 1], pa[4 * q + 2], pa[4 * q + 3]);
+            }
+            {
+              float pb[E];
+              row_product(r + 1 < Rg ? r + 1 : r, pb);
+#pragma unroll
+              for (int q = 0; q < E / 4; ++q) {
+                const float4 pa4 = mixr[(q * T + l) * RlP + r];
+                w[4 * q] = make_float2(pa4.x, pb[4 * q]);
+                w[4 * q + 1] = make_float2(pa4.y, pb[4 * q + 1]);
+                w[4 * q + 2] = make_float2(pa4.z, pb[4 * q + 2]);
+                w[4 * q + 3] = make_float2(pa4.w, pb[4 * q + 3]);
+              }
+            }
             push_pair(w, r);
           }
         }
