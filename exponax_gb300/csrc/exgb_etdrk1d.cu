@@ -17,7 +17,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <type_traits>
 #include <vector>
 
 #include "exgb_internal.h"
@@ -173,25 +172,24 @@ __device__ __forceinline__ void stage_update(const PlanDev& P, const Bufs& b, in
 
 // One nonlinear evaluation of the m states X followed by the stage update
 // (stage >= 0) or a plain store of N^ into X_out (stage < 0).
-template <class Sync>
 __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m, int stage, float2* X_out,
-                        int tid, int nthr, const Sync& sync) {
+                        int tid, int nthr) {
   const int N = P.N, M = P.M;
   nl_pack(P, X, M, b.w0, m, tid, nthr);
-  sync();
+  __syncthreads();
   float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
   float2* other = (P.fft.npass & 1) ? b.w0 : b.w1;
-  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, P.tw, tid, nthr, sync);
+  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, P.tw, tid, nthr, BlockSync{});
   const bool zmf = P.gamma != 0.f && P.zero_mode_fix;
   nl_products(P, res, (float*)other, m, tid, nthr);
-  sync();
+  __syncthreads();
   if (zmf) {
     nl_reduce((const float*)other, b.sums, N, m, tid, nthr);
-    sync();
+    __syncthreads();
   }
   // forward: input in res, ping-pong with other
   float2* fres = (P.fft.npass & 1) ? other : res;
-  block_fft<false>(P.fft, res, other, LinMap{fres, N}, m, P.tw, tid, nthr, sync);
+  block_fft<false>(P.fft, res, other, LinMap{fres, N}, m, P.tw, tid, nthr, BlockSync{});
   for (int t = tid; t < m * M; t += nthr) {
     const int i = t / M, k = t - i * M;
     float2 nv = make_float2(0.f, 0.f);
@@ -209,13 +207,11 @@ __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m,
     if (stage < 0) X_out[t] = nv;
     else stage_update(P, b, i, k, stage, nv, M, 0);
   }
-  sync();
+  __syncthreads();
 }
 
 // Physical output of m states (pairs packed in one complex FFT).
-template <class Sync>
-__device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, int64_t inst_stride, int tid, int nthr,
-                          const Sync& sync) {
+__device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, int64_t inst_stride, int tid, int nthr) {
   const int N = P.N, M = P.M;
   const bool even = (N & 1) == 0;
   const int pairs = (m + 1) / 2;
@@ -230,48 +226,34 @@ __device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, in
     const float2 bb = ib < m ? b.U[ib * M + kk] : make_float2(0.f, 0.f);
     b.w0[t] = cscale(pack_pair(a, bb, ext, ro), invN);
   }
-  sync();
+  __syncthreads();
   float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
-  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, P.tw, tid, nthr, sync);
+  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, P.tw, tid, nthr, BlockSync{});
   for (int t = tid; t < pairs * N; t += nthr) {
     const int p = t / N, x = t - p * N;
     const float2 z = res[t];
     out[(int64_t)(2 * p) * inst_stride + x] = z.x;
     if (2 * p + 1 < m) out[(int64_t)(2 * p + 1) * inst_stride + x] = z.y;
   }
-  sync();
+  __syncthreads();
 }
 
-// A worker is W threads: the whole CTA (W = 256, block barriers) or one warp (W = 32, warp barriers;
-// up to 8 independent workers per CTA, each with its own queue slot and shared-memory slice of
-// worker_elems complex values).  Small transforms leave most of a CTA idle between block barriers,
-// so single-plan launches with N <= 512 use warp workers.
-constexpr int kMaxWorkers = 8;
-
-template <int W>
-__global__ void __launch_bounds__(256, W == 32 ? 2 : 4) etdrk1d_kernel(const Item1D* __restrict__ items, int n_items,
+__global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__ items, int n_items,
                                                       int* __restrict__ head, int nsteps, int mode, int project,
-                                                      int include_init, int64_t worker_elems) {
-  using Sync = std::conditional_t<W == 32, WarpSync, BlockSync>;
-  const Sync sync{};
-  extern __shared__ __align__(16) float2 sm_all[];
-  __shared__ PlanDev Ps_all[W == 32 ? kMaxWorkers : 1];
-  __shared__ int s_item_all[W == 32 ? kMaxWorkers : 1];
-  __shared__ float s_sums_all[W == 32 ? kMaxWorkers : 1][64];
-  const int wid = threadIdx.x / W;
-  const int tid = threadIdx.x % W, nthr = W;
-  float2* sm = sm_all + (int64_t)wid * worker_elems;
-  PlanDev& Ps = Ps_all[wid];
-  int& s_item = s_item_all[wid];
-  float* s_sums = s_sums_all[wid];
+                                                      int include_init, int T) {
+  extern __shared__ __align__(16) float2 sm[];
+  __shared__ PlanDev Ps;
+  __shared__ int s_item;
+  __shared__ float s_sums[64];
+  const int tid = threadIdx.x, nthr = blockDim.x;
   for (;;) {
     if (tid == 0) s_item = atomicAdd(head, 1);
-    sync();
+    __syncthreads();
     const int it = s_item;
     if (it >= n_items) break;
     const Item1D item = items[it];
     if (tid == 0) Ps = *item.plan;
-    sync();
+    __syncthreads();
     const PlanDev& P = Ps;
     const int N = P.N, M = P.M, m = item.m;
     // carve shared memory
@@ -314,9 +296,9 @@ __global__ void __launch_bounds__(256, W == 32 ? 2 : 4) etdrk1d_kernel(const Ite
           if (2 * p + 1 < m) o[(int64_t)(2 * p + 1) * item.out_stride + x] = bb;
         }
       }
-      sync();
+      __syncthreads();
       float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
-      block_fft<false>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, P.tw, tid, nthr, sync);
+      block_fft<false>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, P.tw, tid, nthr, BlockSync{});
       for (int t = tid; t < pairs * M; t += nthr) {
         const int p = t / M, k = t - p * M;
         float2 A, B;
@@ -331,7 +313,7 @@ __global__ void __launch_bounds__(256, W == 32 ? 2 : 4) etdrk1d_kernel(const Ite
         b.U[t] = uh[(int64_t)i * item.in_stride + k];
       }
     }
-    sync();
+    __syncthreads();
 
     // ---- time steps
     const int nstages = (P.order == 0 || P.kind == EXGB_NL_ZERO) ? 0 : P.order;
@@ -341,11 +323,11 @@ __global__ void __launch_bounds__(256, W == 32 ? 2 : 4) etdrk1d_kernel(const Ite
           const int k = t % M;
           b.U[t] = cmul(ldg2(P.E + k), b.U[t]);
         }
-        sync();
+        __syncthreads();
       } else {
         for (int s = 0; s < nstages; ++s) {
           const float2* X = (s == 0) ? b.U : (P.order == 4 && s == 1) ? b.S1 : b.S;
-          nl_eval(P, b, X, m, s, nullptr, tid, nthr, sync);
+          nl_eval(P, b, X, m, s, nullptr, tid, nthr);
         }
       }
       if (project) {
@@ -354,17 +336,17 @@ __global__ void __launch_bounds__(256, W == 32 ? 2 : 4) etdrk1d_kernel(const Ite
           b.U[i * M].y = 0.f;
           if ((N & 1) == 0) b.U[i * M + N / 2].y = 0.f;
         }
-        sync();
+        __syncthreads();
       }
       if (mode == MODE_TRAJ) {
         float* o = (float*)item.out + (int64_t)(step + include_init) * N;
-        emit_phys(P, b, m, o, item.out_stride, tid, nthr, sync);
+        emit_phys(P, b, m, o, item.out_stride, tid, nthr);
       }
     }
 
     // ---- final store
     if (mode == MODE_FINAL) {
-      emit_phys(P, b, m, (float*)item.out, item.out_stride, tid, nthr, sync);
+      emit_phys(P, b, m, (float*)item.out, item.out_stride, tid, nthr);
     } else if (mode == MODE_FOURIER) {
       float2* o = (float2*)item.out;
       for (int t = tid; t < m * M; t += nthr) {
@@ -372,7 +354,8 @@ __global__ void __launch_bounds__(256, W == 32 ? 2 : 4) etdrk1d_kernel(const Ite
         o[(int64_t)i * item.out_stride + k] = b.U[t];
       }
     }
-    sync();
+    __syncthreads();
+    (void)T;
   }
 }
 
@@ -401,7 +384,7 @@ __global__ void __launch_bounds__(256) nonlin1d_kernel(const Item1D* __restrict_
   }
   __syncthreads();
   // results go back into U (the pack step has consumed it before the epilogue)
-  nl_eval(P, b, b.U, m, -1, b.U, tid, nthr, BlockSync{});
+  nl_eval(P, b, b.U, m, -1, b.U, tid, nthr);
   float2* o = (float2*)item.out;
   for (int t = tid; t < m * M; t += nthr) {
     const int i = t / M, k = t - i * M;
@@ -436,7 +419,7 @@ static int choose_m(const PlanDev& P, int64_t batch, int sm_count, bool nonlin_o
 }
 
 static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStream_t st, int nsteps, int mode,
-                        int project, int include_init, int sm_count, bool nonlin_only, bool warp_workers = false) {
+                        int project, int include_init, int sm_count, bool nonlin_only) {
   if (items.empty()) return EXGB_OK;
   if (smem > (size_t)smem_limit() - 2048)
     return fail(EXGB_EUNSUPPORTED, "1D state does not fit in shared memory (N too large for this build)");
@@ -453,30 +436,14 @@ static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStrea
   if (nonlin_only) {
     EXGB_CUDA(cudaFuncSetAttribute(nonlin1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     nonlin1d_kernel<<<(unsigned)items.size(), 256, smem, st>>>((const Item1D*)ws, (int)items.size());
-  } else if (warp_workers) {
-    // one warp per worker, as many workers per CTA as spread the items over the SMs (<= 8)
-    const int64_t n = (int64_t)items.size();
-    const int fit = (int)std::max<int64_t>(1, ((int64_t)smem_limit() - 4096) / (int64_t)smem);
-    const int wpc = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)kMaxWorkers, (int64_t)fit,
-                                                                  (n + sm_count - 1) / sm_count}));
-    const size_t cta_smem = smem * wpc;
-    auto fn = etdrk1d_kernel<32>;
-    EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cta_smem));
-    int per_sm = 1;
-    EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * wpc, cta_smem));
-    per_sm = std::max(1, per_sm);
-    const int grid = (int)std::min<int64_t>((n + wpc - 1) / wpc, (int64_t)sm_count * per_sm);
-    fn<<<grid, 32 * wpc, cta_smem, st>>>((const Item1D*)ws, (int)n, head, nsteps, mode, project, include_init,
-                                         (int64_t)(smem / sizeof(float2)));
   } else {
-    auto fn = etdrk1d_kernel<256>;
-    EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    EXGB_CUDA(cudaFuncSetAttribute(etdrk1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;
-    EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem));
+    EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, etdrk1d_kernel, 256, smem));
     per_sm = std::max(1, per_sm);
     const int grid = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)sm_count * per_sm);
-    fn<<<grid, 256, smem, st>>>((const Item1D*)ws, (int)items.size(), head, nsteps, mode, project, include_init,
-                                (int64_t)(smem / sizeof(float2)));
+    etdrk1d_kernel<<<grid, 256, smem, st>>>((const Item1D*)ws, (int)items.size(), head, nsteps, mode, project,
+                                            include_init, 0);
   }
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
@@ -491,10 +458,7 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
   if (nonlinear_only) mode = MODE_NONLIN;
   else if (u0_phys) mode = emit_traj ? MODE_TRAJ : MODE_FINAL;
   else mode = MODE_FOURIER;
-  // warp workers for small transforms (a 256-thread CTA would idle between block barriers)
-  const bool warp_workers = !nonlinear_only && P.N <= 512;
   int m = choose_m(P, batch, plan->sm_count, nonlinear_only);
-  if (warp_workers) m = std::min(m, 2);
   if (plan->tune_items_per_cta > 0 && !nonlinear_only) {
     m = plan->tune_items_per_cta;
     while (m > 1 && smem_for(P, m, false) > (size_t)smem_limit() - 4096) --m;
@@ -525,7 +489,7 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
     items.push_back(it);
   }
   return launch_items(items, smem_for(P, m, nonlinear_only), st, nsteps, mode, project, include_init,
-                      plan->sm_count, nonlinear_only, warp_workers);
+                      plan->sm_count, nonlinear_only);
 }
 
 }  // namespace exgb
@@ -623,14 +587,13 @@ extern "C" int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, 
       (e = cudaMalloc(&q->d_head, sizeof(int))) != cudaSuccess ||
       (e = cudaMemcpy(q->d_items, sorted.data(), sizeof(Item1D) * sorted.size(), cudaMemcpyHostToDevice)) !=
           cudaSuccess ||
-      (e = cudaFuncSetAttribute(etdrk1d_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+      (e = cudaFuncSetAttribute(etdrk1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
           cudaSuccess) {
     exgb_queue_destroy(q);
     return cuda_fail(e, "exgb_queue_prepare");
   }
   int per_sm = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, etdrk1d_kernel<256>, 256, smem) != cudaSuccess)
-    per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, etdrk1d_kernel, 256, smem) != cudaSuccess) per_sm = 1;
   q->grid = (int)std::min<int64_t>((int64_t)sorted.size(), (int64_t)sm_count * std::max(1, per_sm));
   *out = q;
   return EXGB_OK;
@@ -640,8 +603,8 @@ extern "C" int exgb_queue_launch(exgb_queue* q, void* stream) {
   if (!q) return fail(EXGB_EINVAL, "NULL queue");
   cudaStream_t st = (cudaStream_t)stream;
   EXGB_CUDA(cudaMemsetAsync(q->d_head, 0, sizeof(int), st));
-  etdrk1d_kernel<256><<<q->grid, 256, q->smem, st>>>(q->d_items, q->n_items, q->d_head, q->nsteps, MODE_TRAJ, 1,
-                                                     q->include_init, (int64_t)(q->smem / sizeof(float2)));
+  etdrk1d_kernel<<<q->grid, 256, q->smem, st>>>(q->d_items, q->n_items, q->d_head, q->nsteps, MODE_TRAJ, 1,
+                                                q->include_init, 0);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }

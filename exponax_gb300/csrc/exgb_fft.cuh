@@ -183,10 +183,6 @@ __device__ __forceinline__ void stockham_pass(int R, const Src& src, const Dst& 
 }
 
 // Group barrier: whole block (id 0) or a named barrier over `nthr` threads.
-// one warp as the whole worker (warp-synchronous block_fft)
-struct WarpSync {
-  __device__ __forceinline__ void operator()() const { __syncwarp(); }
-};
 struct BlockSync {
   __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
