@@ -320,9 +320,7 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
       }
       cluster.sync();  // product spectra delivered
 
-      // ================= column forward FFT (local gather) -> N^; for ETDRK2 the stage update is
-      // fused here: each lane updates its own E modes from registers, 2 modes' loads in flight at once
-      const bool fused2 = !a.nonlinear_only && P.order == 2;
+      // ================= column forward FFT (local gather) -> raw N^ in colbuf
       for (int c = gi; c < ncols; c += NG) {
         const int ky = col0 + c;
         float2 v[E];
@@ -336,57 +334,17 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           float2 nv = make_float2(0.f, 0.f);
           if (ks <= K && ks >= -K) nv = cscale(v[j], negb);
           if (ky == P.inj_mode && kx == 0) nv.x += P.inj_value;
-          v[j] = nv;
-        }
-        if (fused2) {
-          // ETDRK2 (etdrk/_etdrk_2.py:91-102)
-          const int64_t ob = (int64_t)ky * N + l;
-#pragma unroll
-          for (int h = 0; h < E; h += 2) {
-            float2 x[2], y[2], e[2];
-            float cf[2];
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-              const int64_t o = ob + T * (h + u);
-              if (st == 0) {
-                x[u] = sb.U[o];
-                e[u] = __ldg(P.E + o);
-                cf[u] = __ldg(P.c[0] + o);
-              } else {
-                x[u] = sb.S[o];
-                y[u] = sb.N0[o];
-                cf[u] = __ldg(P.c[1] + o);
-              }
-            }
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-              const int j = h + u;
-              const int64_t o = ob + T * j;
-              float2 r;
-              if (st == 0) {
-                r = cadd(cmul(e[u], x[u]), cscale(v[j], cf[u]));
-                sb.N0[o] = v[j];
-                sb.S[o] = r;
-              } else {
-                r = cadd(x[u], cscale(csub(v[j], y[u]), cf[u]));
-                sb.U[o] = r;
-              }
-              colbuf[cb(l + T * j, c)] = r;
-            }
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < E; ++j) colbuf[cb(l + T * j, c)] = v[j];
+          colbuf[cb(kx, c)] = nv;
         }
       }
       __syncthreads();
-      // ================= output of the nonlinear term, or the stage update of the other orders
+      // ================= ETDRK stage update, all threads (latency-bound elementwise pass)
       if (a.nonlinear_only) {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
           uout[(int64_t)kx * M + col0 + c] = colbuf[cb(kx, c)];
         }
-      } else if (!fused2) {
+      } else {
         for (int t = tid; t < ncols * N; t += THREADS) {
           const int c = t / N, kx = t % N;
           const int64_t o = (int64_t)(col0 + c) * N + kx;
