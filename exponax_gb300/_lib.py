@@ -32,6 +32,8 @@ NL_VORTICITY_2D = 5
 NL_VORTICITY_2D_KOLMOGOROV = 6
 NL_PROJECTED_3D = 7
 NL_PROJECTED_3D_KOLMOGOROV = 8
+NL_CAHN_HILLIARD = 9
+NL_GRAY_SCOTT = 10
 
 
 class PlanDesc(ctypes.Structure):
@@ -59,6 +61,7 @@ class PlanDesc(ctypes.Structure):
         ("poly", ctypes.c_double * 8),
         ("injection_mode", ctypes.c_int32),
         ("injection_scale", ctypes.c_double),
+        ("reaction", ctypes.c_double * 2),
     ]
 
 

@@ -60,6 +60,9 @@ class Plan:
             d.poly[i] = float(c)
         d.injection_mode = int(nl.get("injection_mode", -1))
         d.injection_scale = float(nl.get("injection_scale", 0.0))
+        rx = list(nl.get("reaction", (0.0, 0.0)))
+        for i in range(2):
+            d.reaction[i] = float(rx[i])
         return d
 
     @property

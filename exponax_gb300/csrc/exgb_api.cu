@@ -244,28 +244,30 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   const bool nonlinear = d.order >= 1 && d.nonlin_kind != EXGB_NL_ZERO;
 
   // supported (D, kind) combinations of this build
-  if (d.order >= 1) {
-    if (D == 1) {
+  const bool staged = ndgen_handles(d);
+  if (d.order >= 1 && d.nonlin_kind != EXGB_NL_ZERO) {
+    if (d.nonlin_kind < EXGB_NL_ZERO || d.nonlin_kind > EXGB_NL_GRAY_SCOTT)
+      return fail(EXGB_EINVAL, "unknown nonlinear function");
+    if (staged) {
+      const int rc = ndgen_validate(d);
+      if (rc) return rc;
+    } else if (D == 1) {
       if (d.nonlin_kind > EXGB_NL_GENERAL)
-        return fail(EXGB_EUNSUPPORTED, "this nonlinear function needs num_spatial_dims == 2");
-      if (d.num_channels != 1) return fail(EXGB_EUNSUPPORTED, "1D plans have one channel");
-    } else if (D == 2) {
-      if (d.nonlin_kind != EXGB_NL_VORTICITY_2D && d.nonlin_kind != EXGB_NL_VORTICITY_2D_KOLMOGOROV &&
-          d.nonlin_kind != EXGB_NL_ZERO)
-        return fail(EXGB_EUNSUPPORTED, "2D plans support the vorticity-convection nonlinearity (and linear ETDRK)");
-      if (d.nonlin_kind != EXGB_NL_ZERO && d.num_channels != 1)
-        return fail(EXGB_ESHAPE, "vorticity formulation has one channel");
+        return fail(EXGB_EUNSUPPORTED, "this nonlinear function needs num_spatial_dims == 2 or 3");
+      if (d.num_channels != 1) return fail(EXGB_ESHAPE, "Number of channels in u_hat should match number of spatial dimensions");
+    } else if (d.nonlin_kind == EXGB_NL_VORTICITY_2D || d.nonlin_kind == EXGB_NL_VORTICITY_2D_KOLMOGOROV) {
+      if (D != 2) return fail(EXGB_EUNSUPPORTED, "vorticity convection needs num_spatial_dims == 2");
+      if (d.num_channels != 1) return fail(EXGB_ESHAPE, "vorticity formulation has one channel");
     } else {
-      if (d.nonlin_kind != EXGB_NL_PROJECTED_3D && d.nonlin_kind != EXGB_NL_PROJECTED_3D_KOLMOGOROV &&
-          d.nonlin_kind != EXGB_NL_ZERO)
-        return fail(EXGB_EUNSUPPORTED, "3D plans support the projected convection (and linear ETDRK)");
-      if (d.nonlin_kind != EXGB_NL_ZERO && d.num_channels != 3)
+      if (D != 3) return fail(EXGB_EUNSUPPORTED, "projected convection needs num_spatial_dims == 3");
+      if (d.num_channels != 3)
         return fail(EXGB_ESHAPE, "Number of channels in u_hat should match number of spatial dimensions");
     }
   }
 
   exgb_plan* p = new exgb_plan();
   p->desc = d;
+  p->staged = staged ? 1 : 0;
   p->desc.linear_operator = nullptr;  // host pointer not retained
   PlanDev& v = p->dev;
   std::memset(&v, 0, sizeof(v));
@@ -356,7 +358,8 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   for (int i = 0; i < D - 1; ++i) per *= (size_t)N;
   p->n_modes = per;
   const size_t nall = per * (size_t)v.lin_ch;
-  const bool transpose = (D == 2 && d.order >= 1);
+  const bool transpose = (D == 2 && d.order >= 1 && !staged);
+  p->tables_transposed = transpose ? 1 : 0;
   double2* d_L = nullptr;
   cudaError_t e;
   if ((e = cudaMalloc(&d_L, sizeof(double2) * nall)) != cudaSuccess ||
@@ -390,7 +393,7 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   v.Eh = p->d_Eh;
   for (int q = 0; q < 6; ++q) v.c[q] = p->d_c + (size_t)q * nall;
 
-  if (D == 2 && v.kind != EXGB_NL_ZERO) {
+  if (D == 2 && v.kind != EXGB_NL_ZERO && !staged) {
     rc = etdrk2d_configure(p);
     if (rc) {
       exgb_plan_destroy(p);
@@ -423,7 +426,7 @@ int exgb_plan_get_table(const exgb_plan* plan, int which, void* host_out, size_t
                                  : (const void*)(plan->d_c + (size_t)(which - 2) * nall);
   std::vector<char> tmp(need);
   EXGB_CUDA(cudaMemcpy(tmp.data(), src, need, cudaMemcpyDeviceToHost));
-  const bool transposed = plan->dev.D == 2 && plan->dev.order >= 1;
+  const bool transposed = plan->tables_transposed != 0;
   if (!transposed) {
     std::memcpy(host_out, tmp.data(), need);
     return EXGB_OK;
@@ -461,8 +464,8 @@ extern "C" int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int 
     return EXGB_OK;
   }
   if (kind == EXGB_TUNE_CLUSTER) {
-    if (plan->dev.D != 2 || plan->dev.kind == EXGB_NL_ZERO || plan->dev.order == 0)
-      return fail(EXGB_EUNSUPPORTED, "cluster size applies to 2D nonlinear plans");
+    if (plan->dev.D != 2 || plan->dev.kind == EXGB_NL_ZERO || plan->dev.order == 0 || plan->staged)
+      return fail(EXGB_EUNSUPPORTED, "cluster size applies to 2D vorticity plans");
     const int G = n > 0 ? values[0] : 0;
     if (G < 0 || G > 8) return fail(EXGB_EINVAL, "cluster size must be 1..8 (0 = automatic)");
     EXGB_CUDA(cudaDeviceSynchronize());
@@ -494,7 +497,8 @@ extern "C" int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int 
     return EXGB_OK;
   }
   if (kind == EXGB_TUNE_ITEMS_PER_CTA) {
-    if (plan->dev.D != 1) return fail(EXGB_EUNSUPPORTED, "items per CTA applies to 1D plans");
+    if (plan->dev.D != 1 || plan->staged)
+      return fail(EXGB_EUNSUPPORTED, "items per CTA applies to 1D single-channel plans");
     plan->tune_items_per_cta = n > 0 ? std::max(0, std::min(64, values[0])) : 0;
     return EXGB_OK;
   }

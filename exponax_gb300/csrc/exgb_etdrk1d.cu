@@ -512,7 +512,7 @@ static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps,
   for (int64_t i = 0; i < n_items;) {
     const exgb_plan* p = items[i].plan;
     if (!p || !items[i].u0 || !items[i].traj) return fail(EXGB_EINVAL, "work item with NULL plan or buffer");
-    if (p->dev.D != 1) return fail(EXGB_EUNSUPPORTED, "the work queue runs 1D plans");
+    if (p->dev.D != 1 || p->staged) return fail(EXGB_EUNSUPPORTED, "the work queue runs 1D single-channel plans");
     sm_count = p->sm_count;
     const int N = p->dev.N;
     const int mmax = std::min(64, std::max(1, 1024 / N));

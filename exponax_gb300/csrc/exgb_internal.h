@@ -79,6 +79,10 @@ struct exgb_plan {
   size_t tc_scratch_per_cta = 0;
   size_t tc_const_offset = 0;    // byte offset of the constant DFT tiles inside d_tc_scratch
   int* d_status = nullptr;       // device wait status of the tensor-core kernel (0 = ok)
+  // stepped by the staged N-D path (exgb_ndgen.cu) instead of a fused kernel
+  int staged = 0;
+  // 2D coefficient tables stored [lin_ch][ky][kx] (the fused 2D kernels' layout)
+  int tables_transposed = 0;
 };
 
 namespace exgb {
@@ -119,6 +123,10 @@ bool tcdft2d_supported(const exgb_plan* plan);
 int tcdft2d_configure(exgb_plan* plan);
 int tcdft2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                 int project, int nonlinear_only);
+bool ndgen_handles(const exgb_plan_desc& d);
+int ndgen_validate(const exgb_plan_desc& d);
+int ndgen_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
+              int project, int nonlinear_only);
 int etdrk0_apply(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                  int project);
 

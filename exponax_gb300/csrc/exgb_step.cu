@@ -1,5 +1,6 @@
 // exgb_step.cu -- stepping entry points of the C ABI: dispatch between the
-// fused 1D kernel, the 2D cluster kernel and the linear (ETDRK0) kernel, and
+// fused 1D kernel, the 2D cluster kernel, the 3D path, the staged N-D path
+// and the linear (ETDRK0) kernel, and
 // the physical-space wrappers (rfftn -> Fourier steps -> irfftn).
 #include <cuda_runtime.h>
 
@@ -71,9 +72,11 @@ static bool linear_only(const PlanDev& P) { return P.order == 0 || P.kind == EXG
 int steps3d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                 int project, int nonlinear_only);
 
-// Fourier-space multi-step for 2D and 3D plans.
+// Fourier-space multi-step for the plans without a fused 1D kernel: staged
+// N-D plans, 2D and 3D.
 static int fourier_steps_2d(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch,
                             int nsteps, int project) {
+  if (plan->staged) return ndgen_run(plan, st, in, out, batch, nsteps, project, 0);
   if (plan->dev.D == 3) return steps3d_run(plan, st, in, out, batch, nsteps, project, 0);
   if (linear_only(plan->dev)) return etdrk0_apply(plan, st, in, out, batch, nsteps, project);
   return etdrk2d_run(plan, st, in, out, batch, nsteps, project, 0);
@@ -105,7 +108,7 @@ int exgb_repeat_fourier(const exgb_plan* plan, void* stream, const void* u_hat0,
   if (!plan || !u_hat0 || !u_hat_out) return fail(EXGB_EINVAL, "NULL argument");
   if (batch < 0 || nsteps < 0) return fail(EXGB_EINVAL, "negative batch or nsteps");
   cudaStream_t st = (cudaStream_t)stream;
-  if (plan->dev.D == 1)
+  if (plan->dev.D == 1 && !plan->staged)
     return etdrk1d_run(plan, st, nullptr, (const float2*)u_hat0, nullptr, (float2*)u_hat_out, batch, nsteps, 0, 0, 0,
                        0);
   return fourier_steps_2d(plan, st, (const float2*)u_hat0, (float2*)u_hat_out, batch, nsteps, 0);
@@ -120,6 +123,7 @@ int exgb_nonlinear(const exgb_plan* plan, void* stream, const void* u_hat_in, vo
     EXGB_CUDA(cudaMemsetAsync(n_hat_out, 0, sizeof(float2) * hat_elems(P, batch), st));
     return EXGB_OK;
   }
+  if (plan->staged) return ndgen_run(plan, st, (const float2*)u_hat_in, (float2*)n_hat_out, batch, 0, 0, 1);
   if (P.D == 3) return steps3d_run(plan, st, (const float2*)u_hat_in, (float2*)n_hat_out, batch, 0, 0, 1);
   if (P.D == 1)
     return etdrk1d_run(plan, st, nullptr, (const float2*)u_hat_in, nullptr, (float2*)n_hat_out, batch, 0, 0, 0, 0,
@@ -132,7 +136,7 @@ int exgb_repeat(const exgb_plan* plan, void* stream, const float* u0, float* u_o
   if (batch < 0 || nsteps < 0) return fail(EXGB_EINVAL, "negative batch or nsteps");
   cudaStream_t st = (cudaStream_t)stream;
   const PlanDev& P = plan->dev;
-  if (P.D == 1) return etdrk1d_run(plan, st, u0, nullptr, u_out, nullptr, batch, nsteps, 1, 0, 0, 0);
+  if (P.D == 1 && !plan->staged) return etdrk1d_run(plan, st, u0, nullptr, u_out, nullptr, batch, nsteps, 1, 0, 0, 0);
   float2* hat = (float2*)workspace(sizeof(float2) * hat_elems(P, batch), 2);
   if (!hat) return fail(EXGB_ENOMEM, "workspace allocation failed");
   int rc = rfftn_impl(st, P.D, P.N, batch * P.C, u0, hat);
@@ -152,7 +156,7 @@ int exgb_rollout(const exgb_plan* plan, void* stream, const float* u0, float* tr
   if (batch < 0 || nsteps < 0) return fail(EXGB_EINVAL, "negative batch or nsteps");
   cudaStream_t st = (cudaStream_t)stream;
   const PlanDev& P = plan->dev;
-  if (P.D == 1)
+  if (P.D == 1 && !plan->staged)
     return etdrk1d_run(plan, st, u0, nullptr, traj, nullptr, batch, nsteps, 1, 1, include_init ? 1 : 0, 0);
   const int T = nsteps + (include_init ? 1 : 0);
   const size_t frame = phys_elems(P, 1);  // floats per sample

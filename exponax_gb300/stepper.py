@@ -425,3 +425,7 @@ class HyperDiffusion(_LinearStepper):
             lap = build_laplace_operator(d)
             return -self.hyper_diffusivity * lap * lap
         return -self.hyper_diffusivity * build_laplace_operator(d, order=4)
+
+
+# the reference's stepper sub-packages (stepper/generic, stepper/reaction)
+from . import generic, reaction  # noqa: E402

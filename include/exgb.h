@@ -52,6 +52,8 @@ extern "C" {
 #define EXGB_NL_VORTICITY_2D_KOLMOGOROV 6 /* VorticityConvection2dKolmogorov :102-182 */
 #define EXGB_NL_PROJECTED_3D 7       /* ProjectedConvection3d       _projected_convection.py:19-136 */
 #define EXGB_NL_PROJECTED_3D_KOLMOGOROV 8 /* ProjectedConvection3dKolmogorov :139-226 */
+#define EXGB_NL_CAHN_HILLIARD 9      /* CahnHilliardNonlinearFun    stepper/reaction/_cahn_hilliard.py:12-45 */
+#define EXGB_NL_GRAY_SCOTT 10        /* GrayScottNonlinearFun       stepper/reaction/_gray_scott.py:9-46 */
 
 typedef struct exgb_plan exgb_plan;
 
@@ -60,7 +62,7 @@ typedef struct exgb_plan exgb_plan;
  * complex128), the ETDRK order and contour parameters, and the nonlinear
  * function with its scalar parameters. */
 typedef struct {
-  int32_t num_spatial_dims;        /* D: 1 or 2 */
+  int32_t num_spatial_dims;        /* D: 1, 2 or 3 */
   int32_t num_points;              /* N (2^a 3^b 5^c) */
   int32_t num_channels;            /* C */
   int32_t order;                   /* ETDRK order 0..4 */
@@ -81,6 +83,7 @@ typedef struct {
   double poly[8];
   int32_t injection_mode;          /* Kolmogorov forcing mode k */
   double injection_scale;          /* Kolmogorov forcing amplitude */
+  double reaction[2];              /* Gray-Scott feed_rate, kill_rate */
 } exgb_plan_desc;
 
 /* One instance of an uneven batch (exgb_queue_rollout). */
