@@ -96,40 +96,14 @@ class RandomTruncatedFourierSeries:
     def __call__(self, num_points: int, *, key: int) -> np.ndarray:
         if self.num_spatial_dims == 1:
             u = RandomSineWaves1d(1, cutoff=self.cutoff)(num_points, key=key)[0]
-        elif self.num_spatial_dims == 2:
-            # same draws and modes as the general branch, summed by an inverse
-            # real FFT instead of mode by mode
-            rng = np.random.default_rng(key)
-            c, N = self.cutoff, num_points
-            H = np.zeros((N, N // 2 + 1), dtype=np.complex128)
-            for m in np.ndindex(2 * c + 1, 2 * c + 1):
-                kx, ky = m[0] - c, m[1] - c
-                if (kx, ky) == (0, 0) or ky < 0 or (ky == 0 and kx < 0):
-                    continue
-                a = rng.uniform(-1.0, 1.0)
-                phi = rng.uniform(0.0, 2 * np.pi)
-                z = 0.5 * a * np.exp(1j * phi) * N * N
-                H[kx % N, ky] += z
-                if ky == 0:
-                    H[(-kx) % N, 0] += np.conj(z)
-            u = np.fft.irfft2(H, s=(N, N))
         else:
-            rng = np.random.default_rng(key)
-            c = self.cutoff
-            x = np.arange(num_points) / num_points
-            grids = np.meshgrid(*([x] * self.num_spatial_dims), indexing="ij")
-            u = np.zeros((num_points,) * self.num_spatial_dims)
-            modes = [m for m in np.ndindex(*([2 * c + 1] * self.num_spatial_dims))]
-            for m in modes:
-                k = np.array(m) - c
-                # one representative of each +-k pair (last axis >= 0 half space)
-                nz = np.nonzero(k)[0]
-                if nz.size == 0 or k[nz[-1]] < 0:
-                    continue
-                a = rng.uniform(-1.0, 1.0)
-                phi = rng.uniform(0.0, 2 * np.pi)
-                arg = sum(2 * np.pi * k[d] * grids[d] for d in range(self.num_spatial_dims))
-                u += a * np.cos(arg + phi)
+            # one random cosine per +-k pair (the last nonzero component of k positive), drawn in
+            # mode order; summed by an inverse real FFT of the half-spectrum _draw lays out
+            idx, z = self._draw(num_points)(key)
+            D, N = self.num_spatial_dims, num_points
+            H = np.zeros(N ** (D - 1) * (N // 2 + 1), dtype=np.complex128)
+            np.add.at(H, idx, z)
+            u = np.fft.irfftn(H.reshape((N,) * (D - 1) + (N // 2 + 1,)), s=(N,) * D)
         u = u - u.mean()
         if self.max_one:
             u = u / np.max(np.abs(u))
