@@ -292,40 +292,53 @@ __device__ __forceinline__ int src_index_axis(int k_new, int n_new, int n_old, i
   return -1;
 }
 
+// signed wavenumber of index i on an fftfreq axis of n points
+__device__ __forceinline__ int fftfreq_k(int i, int n) { return (i <= (n - 1) / 2) ? i : i - n; }
+
+// true if a mode touches the Nyquist plane of an even n-point grid on any axis
+// (oddball_filter_mask, _spectral.py:345-400): |k| = n/2 on a leading axis or
+// k = n/2 on the last (rfftfreq) axis
+__device__ __forceinline__ bool on_nyquist(int D, const int (&k)[3], int kl, int n) {
+  if (kl >= n / 2) return true;
+  for (int a = 0; a < D - 1; ++a)
+    if (k[a] >= n / 2 || k[a] <= -n / 2) return true;
+  return false;
+}
+
 __global__ void resample_kernel(int D, int n_old, int n_new, int64_t count, const float2* __restrict__ in,
                                 float2* __restrict__ out, float scale, int zero_old_nyq, int zero_new_nyq) {
   const int Mo = n_old / 2 + 1, Mn = n_new / 2 + 1;
   const int nmin = min(n_old, n_new);
-  const int64_t per = (D == 1) ? Mn : (int64_t)n_new * Mn;
-  const int64_t per_old = (D == 1) ? Mo : (int64_t)n_old * Mo;
+  int64_t per = Mn, per_old = Mo;
+  for (int a = 0; a < D - 1; ++a) {
+    per *= n_new;
+    per_old *= n_old;
+  }
   const int64_t total = per * count;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = t / per;
-    const int64_t r = t - c * per;
-    int ky = (int)(r % Mn);
-    int kx = (D == 2) ? (int)(r / Mn) : 0;
-    float2 v = make_float2(0.f, 0.f);
-    bool ok = ky <= nmin / 2;
-    int sx = 0;
-    if (ok && D == 2) {
-      sx = src_index_axis(kx, n_new, n_old, nmin);
-      ok = sx >= 0;
+    int64_t r = t - c * per;
+    const int kl = (int)(r % Mn);  // last (rfftfreq) axis
+    r /= Mn;
+    // leading axes, innermost first: new index, old source index, signed wavenumbers
+    int kn[3] = {0, 0, 0}, ko[3] = {0, 0, 0};
+    int64_t src = kl;
+    int64_t stride = Mo;
+    bool ok = kl <= nmin / 2;
+    for (int a = D - 2; a >= 0 && ok; --a) {
+      const int i = (int)(r % n_new);
+      r /= n_new;
+      const int si = src_index_axis(i, n_new, n_old, nmin);
+      ok = si >= 0;
+      kn[a] = fftfreq_k(i, n_new);
+      ko[a] = fftfreq_k(si, n_old);
+      src += (int64_t)si * stride;
+      stride *= n_old;
     }
-    if (ok) {
-      // oddball masks: Nyquist of the old grid (upscaling) / new grid (downscaling)
-      if (zero_old_nyq) {
-        const int wy = ky;
-        const int wx = (D == 2) ? (sx <= n_old / 2 - 1 ? sx : sx - n_old) : 0;
-        if (wy >= n_old / 2 || (D == 2 && (wx >= n_old / 2 || wx <= -n_old / 2))) ok = false;
-      }
-      if (zero_new_nyq) {
-        const int wy = ky;
-        const int wx = (D == 2) ? (kx <= n_new / 2 - 1 ? kx : kx - n_new) : 0;
-        if (wy >= n_new / 2 || (D == 2 && (wx >= n_new / 2 || wx <= -n_new / 2))) ok = false;
-      }
-    }
-    if (ok) v = cscale(in[c * per_old + (int64_t)sx * Mo + ky], scale);
-    out[t] = v;
+    // oddball masks: Nyquist of the old grid (upscaling) / new grid (downscaling)
+    if (ok && zero_old_nyq && on_nyquist(D, ko, kl, n_old)) ok = false;
+    if (ok && zero_new_nyq && on_nyquist(D, kn, kl, n_new)) ok = false;
+    out[t] = ok ? cscale(in[c * per_old + src], scale) : make_float2(0.f, 0.f);
   }
 }
 
@@ -350,26 +363,34 @@ int exgb_irfftn(void* stream, int num_spatial_dims, int num_points, int64_t coun
 int exgb_map_between_resolutions(void* stream, int D, int n_old, int n_new, int64_t count, const float* in,
                                  float* out, int oddball_zero) {
   if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
-  if (D < 1 || D > 2) return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1 or 2 in this build");
+  if (D < 1 || D > 3) return fail(EXGB_EINVAL, "num_spatial_dims must be 1, 2 or 3");
+  if (n_old < 1 || n_new < 1 || count < 0) return fail(EXGB_EINVAL, "bad sizes");
   cudaStream_t st = (cudaStream_t)stream;
+  size_t pts_old = (size_t)n_old, pts_new = (size_t)n_new;  // grid points per field
+  size_t so = (size_t)(n_old / 2 + 1), sn = (size_t)(n_new / 2 + 1);  // modes per field
+  for (int d = 1; d < D; ++d) {
+    pts_old *= n_old;
+    pts_new *= n_new;
+    so *= n_old;
+    sn *= n_new;
+  }
   if (n_old == n_new) {
-    size_t bytes = sizeof(float) * (size_t)count * n_old * (D == 2 ? n_old : 1);
-    EXGB_CUDA(cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, st));
+    EXGB_CUDA(cudaMemcpyAsync(out, in, sizeof(float) * (size_t)count * pts_old, cudaMemcpyDeviceToDevice, st));
     return EXGB_OK;
   }
-  const int Mo = n_old / 2 + 1, Mn = n_new / 2 + 1;
-  const size_t so = (size_t)count * Mo * (D == 2 ? n_old : 1);
-  const size_t sn = (size_t)count * Mn * (D == 2 ? n_new : 1);
-  // slot 1 holds the old spectrum and later the 2D inverse intermediate
-  float2* a = (float2*)workspace(sizeof(float2) * std::max(so, sn), 1);
+  so *= (size_t)count;
+  sn *= (size_t)count;
+  // slot 1 holds the old spectrum; the new spectrum goes to slot 2 (irfftn_impl uses slot 0 for its
+  // intermediate in 2D and 3D)
+  float2* a = (float2*)workspace(sizeof(float2) * so, 1);
   if (!a) return fail(EXGB_ENOMEM, "workspace allocation failed");
   int rc = rfftn_impl(st, D, n_old, count, in, a);
   if (rc) return rc;
-  // the new spectrum must not overlap `a`: place it in slot 0
-  float2* b = (float2*)workspace(sizeof(float2) * std::max(sn, (size_t)count * n_new * Mn), 0);
+  float2* b = (float2*)workspace(sizeof(float2) * sn, 2);
   if (!b) return fail(EXGB_ENOMEM, "workspace allocation failed");
-  const double ratio = (double)n_new / (double)n_old;
-  const float scale = (float)(D == 2 ? ratio * ratio : ratio);
+  double ratio = 1.0;
+  for (int d = 0; d < D; ++d) ratio *= (double)n_new / (double)n_old;
+  const float scale = (float)ratio;
   const int zo = (n_new > n_old) && (n_old % 2 == 0) && oddball_zero;
   const int zn = (n_old > n_new) && (n_new % 2 == 0) && oddball_zero;
   const int64_t total = (int64_t)sn;
@@ -377,16 +398,7 @@ int exgb_map_between_resolutions(void* stream, int D, int n_old, int n_new, int6
   const unsigned blocks = (unsigned)std::min<int64_t>((total + th - 1) / th, 65535);
   resample_kernel<<<blocks, th, 0, st>>>(D, n_old, n_new, count, a, b, scale, zo, zn);
   EXGB_CUDA(cudaGetLastError());
-  const FftPlan* fp;
-  const float2* tw;
-  rc = get_tf(n_new, &fp, &tw);
-  if (rc) return rc;
-  if (D == 1) return launch_irfft1d(st, *fp, tw, count, b, out, 1.f / (float)n_new);
-  // 2D inverse: the column pass writes into slot 1 (the old spectrum is no longer needed)
-  float2* tmp = a;
-  rc = launch_cfft_axis(st, *fp, tw, true, count, (int64_t)n_new * Mn, Mn, Mn, b, tmp, 1.f);
-  if (rc) return rc;
-  return launch_irfft1d(st, *fp, tw, count * n_new, tmp, out, 1.f / ((float)n_new * (float)n_new));
+  return irfftn_impl(st, D, n_new, count, b, out);
 }
 
 }  // extern "C"

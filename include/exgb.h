@@ -216,7 +216,7 @@ int exgb_queue_destroy(exgb_queue* queue);
 int exgb_leray(void* stream, int num_spatial_dims, int num_points, double domain_extent, int64_t count,
                const void* in, void* out);
 
-/* map_between_resolutions (_interpolation.py:195-285) for D = 1, 2:
+/* map_between_resolutions (_interpolation.py:195-285) for D = 1, 2, 3:
  * spectral re-sampling of count = B*C fields from N_old to N_new points. */
 int exgb_map_between_resolutions(void* stream, int num_spatial_dims, int n_old, int n_new,
                                  int64_t count, const float* in, float* out, int oddball_zero);
@@ -238,12 +238,15 @@ int exgb_field_sums(void* stream, int64_t count, int64_t n, const float* a, cons
  *   complex fields pass 2n floats).
  * exgb_scatter_modes: zero count Fourier fields of field_elems complex64 each, then write
  *   vals[f * nmodes + m] at element idx[m] of field f (random-series initial conditions).
- * exgb_normalize_fields: per field of n floats subtract the mean (zero_mean) and divide by
- *   max |u| (max_one) (ic/_base_ic.py:18-32). */
+ * exgb_normalize_fields: per field of n floats subtract the mean (zero_mean), then divide by
+ *   the population standard deviation (std_one) or by max |u| (max_one) -- normalize_ic
+ *   (ic/_base_ic.py:18-32); std_one without zero_mean, or with max_one, is EXGB_EINVAL as
+ *   validate_normalization_options (ic/_base_ic.py:8-13) raises. */
 int exgb_axpy(void* stream, int64_t n, float alpha, const float* x, const float* y, float* out);
 int exgb_scatter_modes(void* stream, int64_t count, int64_t field_elems, int nmodes, const int64_t* idx,
                        const void* vals, void* hat);
-int exgb_normalize_fields(void* stream, int64_t count, int64_t n, float* u, int zero_mean, int max_one);
+int exgb_normalize_fields(void* stream, int64_t count, int64_t n, float* u, int zero_mean, int std_one,
+                          int max_one);
 
 /* Self-check of the tcgen05 tensor-core layer (no reference counterpart):
  * d (128 x n, FP32) = a (128 x k) . b (n x k)^T, device pointers, row-major.

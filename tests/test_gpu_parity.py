@@ -32,7 +32,7 @@ def host(t):
 # ------------------------------------------------------------------ transforms
 
 @pytest.mark.parametrize("D,N", [(1, 200), (1, 256), (1, 60), (1, 4096), (1, 45), (2, 60), (2, 64), (2, 128),
-                                 (2, 256)])
+                                 (2, 256), (3, 15), (3, 16), (3, 32), (3, 64)])
 def test_rfftn_irfftn_match_numpy(D, N):
     rng = np.random.default_rng(N + D)
     u = rng.standard_normal((3, 1) + (N,) * D).astype(np.float32)
@@ -308,6 +308,25 @@ def test_map_between_resolutions_matches_oracle():
         assert rel(got, o.map_between_resolutions(u, new)) < 1e-5
     u1 = _ic(1, 200, 2)
     assert rel(host(ex.map_between_resolutions(cu(u1), 50)), o.map_between_resolutions(u1, 50)) < 1e-5
+
+
+@pytest.mark.parametrize("D,old,news", [(1, 40, (25, 32, 64, 75)), (2, 32, (15, 20, 48, 64)),
+                                        (3, 16, (8, 12, 15, 24, 32)), (3, 15, (10, 16, 30))])
+@pytest.mark.parametrize("oddball_zero", [True, False])
+def test_map_between_resolutions_white_noise(D, old, news, oddball_zero):
+    """Non-bandlimited two-channel fields, so that the Nyquist planes (oddball masks) carry energy;
+    up- and downsampling, even and odd grids, 1D-3D.  Tolerance 1e-5 relative L2."""
+    rng = np.random.default_rng(5 + D)
+    u = rng.standard_normal((2,) + (old,) * D).astype(np.float32)
+    for new in news:
+        got = host(ex.map_between_resolutions(cu(u), new, oddball_zero=oddball_zero))
+        ref = o.map_between_resolutions(u, new, oddball_zero=oddball_zero)
+        assert got.shape == ref.shape
+        assert rel(got, ref) < 1e-5, (new, rel(got, ref))
+    batch = np.stack([u, 2 * u])
+    got = host(ex.interpolation.map_between_resolutions_batched(cu(batch), news[0], oddball_zero=oddball_zero))
+    ref = o.map_between_resolutions(u, news[0], oddball_zero=oddball_zero)
+    assert rel(got[1], 2 * ref) < 1e-5
 
 
 def test_errors_follow_the_reference():
