@@ -3,7 +3,7 @@
 //                         substep, reference _forced_stepper.py:64-65, :86-87)
 //   exgb_scatter_modes    zero `count` Fourier fields and write per-field
 //                         values at fixed mode positions (random-series ICs)
-//   exgb_normalize_fields subtract the mean and/or divide by max |u| per field
+//   exgb_normalize_fields subtract the mean, then divide by the standard deviation or by max |u|, per field
 //                         (reference ic/_base_ic.py:18-32, normalize_ic)
 #include <cuda_runtime.h>
 
@@ -31,8 +31,10 @@ __global__ void scatter_kernel(int64_t count, int64_t field_elems, int nmodes, c
   }
 }
 
-// one CTA per field: FP64 mean, then max |u - mean|, then the rescale
-__global__ void __launch_bounds__(256) normalize_kernel(int64_t n, float* u, int zero_mean, int max_one) {
+// one CTA per field: FP64 mean, then (std_one) the FP64 population standard deviation of u - mean or
+// (max_one) max |u - mean|, then the rescale -- normalize_ic (ic/_base_ic.py:18-32) in its order
+__global__ void __launch_bounds__(256) normalize_kernel(int64_t n, float* u, int zero_mean, int std_one,
+                                                        int max_one) {
   float* p = u + (int64_t)blockIdx.x * n;
   __shared__ double red[8];
   __shared__ float redf[8];
@@ -46,6 +48,22 @@ __global__ void __launch_bounds__(256) normalize_kernel(int64_t n, float* u, int
   double tot = 0.0;
   for (int i = 0; i < nw; ++i) tot += red[i];
   const float mean = zero_mean ? (float)(tot / (double)n) : 0.f;
+  __syncthreads();  // red is reused below
+  float inv = 1.f;
+  if (std_one) {
+    double q = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const double d = (double)(p[i] - mean);
+      q += d * d;
+    }
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    if (lane == 0) red[w] = q;
+    __syncthreads();
+    double qt = 0.0;
+    for (int i = 0; i < nw; ++i) qt += red[i];
+    const double sd = sqrt(qt / (double)n);
+    if (sd > 0.0) inv = (float)(1.0 / sd);
+  }
   float mx = 0.f;
   if (max_one)
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) mx = fmaxf(mx, fabsf(p[i] - mean));
@@ -54,7 +72,7 @@ __global__ void __launch_bounds__(256) normalize_kernel(int64_t n, float* u, int
   __syncthreads();
   float m = 0.f;
   for (int i = 0; i < nw; ++i) m = fmaxf(m, redf[i]);
-  const float inv = (max_one && m > 0.f) ? 1.f / m : 1.f;
+  if (max_one && m > 0.f) inv = 1.f / m;
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) p[i] = (p[i] - mean) * inv;
 }
 
@@ -87,11 +105,16 @@ extern "C" int exgb_scatter_modes(void* stream, int64_t count, int64_t field_ele
   return EXGB_OK;
 }
 
-extern "C" int exgb_normalize_fields(void* stream, int64_t count, int64_t n, float* u, int zero_mean, int max_one) {
+extern "C" int exgb_normalize_fields(void* stream, int64_t count, int64_t n, float* u, int zero_mean, int std_one,
+                                     int max_one) {
   if (!u) return fail(EXGB_EINVAL, "exgb_normalize_fields: NULL pointer");
   if (count < 0 || n <= 0) return fail(EXGB_EINVAL, "exgb_normalize_fields: bad size");
+  // validate_normalization_options (ic/_base_ic.py:8-13)
+  if (std_one && !zero_mean) return fail(EXGB_EINVAL, "Cannot have `zero_mean=False` and `std_one=True`.");
+  if (std_one && max_one) return fail(EXGB_EINVAL, "Cannot have `std_one=True` and `max_one=True`.");
   if (count == 0) return EXGB_OK;
-  normalize_kernel<<<(unsigned)count, 256, 0, (cudaStream_t)stream>>>(n, u, zero_mean, max_one);
+  if (count > 2147483647LL) return fail(EXGB_EINVAL, "exgb_normalize_fields: too many fields for one launch");
+  normalize_kernel<<<(unsigned)count, 256, 0, (cudaStream_t)stream>>>(n, u, zero_mean, std_one, max_one);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }

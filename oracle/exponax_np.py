@@ -1154,6 +1154,54 @@ def map_between_resolutions(state, new_num_points, *, oddball_zero=True):
     return ifft(new_hat, num_spatial_dims=D, num_points=new_num_points)
 
 
+def validate_normalization_options(*, zero_mean, std_one, max_one):
+    """ic/_base_ic.py:8-13"""
+    if not zero_mean and std_one:
+        raise ValueError("Cannot have `zero_mean=False` and `std_one=True`.")
+    if std_one and max_one:
+        raise ValueError("Cannot have `std_one=True` and `max_one=True`.")
+
+
+def normalize_ic(ic, *, zero_mean=True, std_one=False, max_one=False):
+    """ic/_base_ic.py:18-32: mean over all entries, then std (population) or max |u|."""
+    if zero_mean:
+        ic = ic - np.mean(ic)
+    if std_one:
+        ic = ic / np.std(ic)
+    if max_one:
+        ic = ic / np.max(np.abs(ic))
+    return ic
+
+
+def gaussian_random_field_from_noise(noise, *, num_spatial_dims, domain_extent=1.0, powerlaw_exponent=3.0,
+                                     zero_mean=True, std_one=False, max_one=False):
+    """ic/_gaussian_random_field.py:60-93 applied to a given white-noise field (1, N, ..., N):
+    rfftn, times |k|^(-p/2) of the scaled wavenumbers (1 at k = 0), irfftn, normalize_ic."""
+    D = num_spatial_dims
+    N = noise.shape[-1]
+    dtype = "float64" if noise.dtype == np.float64 else "float32"
+    noise_hat = fft(noise, num_spatial_dims=D)
+    k = build_scaled_wavenumbers(D, domain_extent, N, dtype=dtype)
+    knorm = np.linalg.norm(k, axis=0, keepdims=True)
+    with np.errstate(divide="ignore"):
+        amp = np.power(knorm, -powerlaw_exponent / 2.0)
+    amp = amp.reshape(-1)
+    amp[0] = 1.0
+    amp = amp.reshape(knorm.shape)
+    ic = ifft(noise_hat * amp, num_spatial_dims=D, num_points=N)
+    return normalize_ic(ic, zero_mean=zero_mean, std_one=std_one, max_one=max_one)
+
+
+def diffused_noise_from_noise(noise, *, num_spatial_dims, domain_extent=1.0, intensity=0.001, zero_mean=True,
+                              std_one=False, max_one=False):
+    """ic/_diffused_noise.py:60-76 applied to a given white-noise field: one Diffusion step of
+    dt = 1 with diffusivity = intensity, then normalize_ic."""
+    N = noise.shape[-1]
+    dtype = "float64" if noise.dtype == np.float64 else "float32"
+    st = Diffusion(num_spatial_dims, domain_extent, N, 1.0, diffusivity=intensity, dtype=dtype)
+    return normalize_ic(st(noise), zero_mean=zero_mean, std_one=std_one, max_one=max_one)
+
+
 def nRMSE(u_pred, u_ref, *, domain_extent=1.0):
     """metrics/_spatial.py:537-586 via spatial_norm(mode='normalized') :84-200:
     per-channel ratio of L2 norms, summed over channels."""
