@@ -118,9 +118,10 @@ def _oracle_worker(args):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(samples=None, nsteps=40):
+def cpu_baseline(samples=None, nsteps=NSTEPS):
     """NumPy oracle of the same workload on the host cores, one process per
-    sample (spawn), bounded sample of `samples` x `nsteps` sample-steps."""
+    sample (spawn), bounded sample of `samples` x `nsteps` sample-steps (by default one
+    sample per core, each the full 200-step trajectory of one initial condition)."""
     import multiprocessing as mp
 
     cores = os.cpu_count() or 1
@@ -157,7 +158,7 @@ def run_reference(args, rank, ws):
         cpu_baseline(samples=min(cores, 4), nsteps=2)
     vals = []
     for _ in range(args.steps):
-        vals.append(cpu_baseline(nsteps=20))
+        vals.append(cpu_baseline())
     v = float(np.median([x["value"] for x in vals]))
     base = dict(vals[0])
     base["value"] = v
