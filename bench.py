@@ -39,6 +39,11 @@ NU = 1e-3
 # algorithmic HBM bytes per DOF-step of ETDRK2 with the Fourier state
 # resident between steps: 6 passes over a complex64 half-spectrum
 BYTES_PER_DOF_STEP = 6 * 8 * (N // 2 + 1) / N
+# algorithmic FP32 transform flops per DOF-step of the fused kernel (5 n log2 n per complex length-n FFT):
+# per stage 4 inverse + 1 forward transforms of the K + 1 dealiased columns (K = 2/3 (N/2) - 1 = 84)
+# and 2 inverse + 1/2 forward (two rows packed) transforms per row; two stages per ETDRK2 step
+KEEP = int(2 / 3 * (N // 2)) - 1
+FFT_FLOPS_PER_DOF_STEP = 2 * (5 * (KEEP + 1) + 2.5 * N) * 5 * N * np.log2(N) / (N * N)
 
 
 def metric_name():
@@ -265,6 +270,15 @@ def run_gb300(args, rank, ws):
             if line.startswith("dram_bytes_per_launch="):
                 traffic = float(line.split("=")[1])
 
+    # the kernel keeps its stage buffers in L2 and shared memory, so the FP32 pipes bound it: transform
+    # flops against the nominal FP32 rate (152 SMs x 128 FMA lanes x 2) at the SM clock sampled under load
+    sm_mhz = float((clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0))
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_ach = FFT_FLOPS_PER_DOF_STEP * value / ws / 1e12  # per GPU
+    fp32 = {"achieved": fp32_ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": fp32_ach / fp32_peak,
+            "note": f"{FFT_FLOPS_PER_DOF_STEP:.0f} transform flop/DOF-step (5 n log2 n per complex FFT); "
+                    f"peak nominal at {sm_mhz:.0f} MHz"}
+
     if rank == 0:
         cpu = cpu_baseline() if ws == 1 and not args.no_cpu else None
         line = {"metric": metric_name(), "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
@@ -279,7 +293,8 @@ def run_gb300(args, rank, ws):
                              "frac": achieved / peak, "traffic": traffic,
                              "kernel": "vort2d_kernel<256,512>",
                              "note": f"algorithmic {BYTES_PER_DOF_STEP:.2f} B/DOF-step (ETDRK2, 6 complex64 "
-                                     f"half-spectrum passes) x {BATCH}x{N}^2x{NSTEPS} per launch; peak {peak_src}"},
+                                     f"half-spectrum passes) x {BATCH}x{N}^2x{NSTEPS} per launch; peak {peak_src}",
+                             "fp32": fp32},
                 "clocks": clk, "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     if ws > 1:
