@@ -11,7 +11,8 @@ Knobs (exgb_plan_tune):
     generic 2D kernel): every ordering of the factorisations of N into
     {8, 4, 2, 5, 3}, capped;
   * CTAs per cluster of the 2D register-FFT kernel: 1, 2, 4, 8 (those that fit);
-  * instances per work item of the 1D kernel.
+  * instances per work item of the 1D kernel;
+  * threads per CTA of the 1D kernel (searched after the two above).
 """
 
 from __future__ import annotations
@@ -63,10 +64,11 @@ def radix_candidates(n, cap=12):
 
 
 def get_tuning(plan):
-    buf = (ctypes.c_int * (KMAX + 3))()
-    check(load().exgb_plan_get_tuning(plan.handle, buf, KMAX + 3), "get_tuning")
+    buf = (ctypes.c_int * (KMAX + 5))()
+    check(load().exgb_plan_get_tuning(plan.handle, buf, KMAX + 5), "get_tuning")
     npass = buf[0]
-    return {"radices": [buf[1 + i] for i in range(npass)], "cluster": buf[1 + KMAX], "items_per_cta": buf[2 + KMAX]}
+    return {"radices": [buf[1 + i] for i in range(npass)], "cluster": buf[1 + KMAX], "items_per_cta": buf[2 + KMAX],
+            "threads": buf[4 + KMAX]}
 
 
 def _set(plan, kind, values):
@@ -139,6 +141,18 @@ def tune(stepper, *, batch=64, nsteps=10, repeats=3, use_cache=True, write_cache
                     _set(plan, 2, [m])
                 results.append(({"radices": list(rad), "items_per_cta": m},
                                 _time(plan, uh, out, batch, nsteps, repeats)))
+        if D == 1:
+            # threads per CTA for the best radix order / items per CTA found so far
+            fin = [r for r in results if np.isfinite(r[1])]
+            if fin:
+                base = min(fin, key=lambda r: r[1])[0]
+                _set(plan, 0, list(base["radices"]))
+                _set(plan, 2, [base["items_per_cta"]])
+                for t in (64, 128, 256):
+                    if _set(plan, 4, [t]) != EXGB_OK:
+                        continue
+                    results.append((dict(base, threads=t), _time(plan, uh, out, batch, nsteps, repeats)))
+                _set(plan, 4, [0])
     results = [r for r in results if np.isfinite(r[1])]
     best = min(results, key=lambda r: r[1])[0] if results else {}
     apply(stepper, best)
@@ -156,5 +170,7 @@ def apply(stepper, best):
         _set(plan, 0, list(best["radices"]))
     if "items_per_cta" in best:
         _set(plan, 2, [int(best["items_per_cta"])])
+    if "threads" in best:
+        _set(plan, 4, [int(best["threads"])])
     if "cluster" in best:
         _set(plan, 1, [int(best["cluster"])])

@@ -502,6 +502,14 @@ extern "C" int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int 
     plan->tune_items_per_cta = n > 0 ? std::max(0, std::min(64, values[0])) : 0;
     return EXGB_OK;
   }
+  if (kind == EXGB_TUNE_THREADS) {
+    if (plan->dev.D != 1 || plan->staged)
+      return fail(EXGB_EUNSUPPORTED, "threads per CTA applies to 1D single-channel plans");
+    const int t = n > 0 ? values[0] : 0;
+    if (t != 0 && t != 64 && t != 128 && t != 256) return fail(EXGB_EINVAL, "threads per CTA must be 64, 128 or 256 (0 = auto)");
+    plan->tune_threads_1d = t;
+    return EXGB_OK;
+  }
   return fail(EXGB_EINVAL, "unknown tuning kind");
 }
 
@@ -522,5 +530,6 @@ extern "C" int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n) {
   out[1 + kMaxPass] = plan->cfg2d.G;
   out[2 + kMaxPass] = plan->tune_items_per_cta;
   if (n >= 4 + kMaxPass) out[3 + kMaxPass] = plan->precision;
+  if (n >= 5 + kMaxPass) out[4 + kMaxPass] = plan->tune_threads_1d;
   return EXGB_OK;
 }

@@ -419,7 +419,7 @@ static int choose_m(const PlanDev& P, int64_t batch, int sm_count, bool nonlin_o
 }
 
 static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStream_t st, int nsteps, int mode,
-                        int project, int include_init, int sm_count, bool nonlin_only) {
+                        int project, int include_init, int sm_count, bool nonlin_only, int threads = 256) {
   if (items.empty()) return EXGB_OK;
   if (smem > (size_t)smem_limit() - 2048)
     return fail(EXGB_EUNSUPPORTED, "1D state does not fit in shared memory (N too large for this build)");
@@ -439,11 +439,11 @@ static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStrea
   } else {
     EXGB_CUDA(cudaFuncSetAttribute(etdrk1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;
-    EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, etdrk1d_kernel, 256, smem));
+    EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, etdrk1d_kernel, threads, smem));
     per_sm = std::max(1, per_sm);
     const int grid = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)sm_count * per_sm);
-    etdrk1d_kernel<<<grid, 256, smem, st>>>((const Item1D*)ws, (int)items.size(), head, nsteps, mode, project,
-                                            include_init, 0);
+    etdrk1d_kernel<<<grid, threads, smem, st>>>((const Item1D*)ws, (int)items.size(), head, nsteps, mode, project,
+                                                include_init, 0);
   }
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
@@ -488,8 +488,11 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
     }
     items.push_back(it);
   }
+  // 256 unless tuned: fewer threads measured slower for small latency-bound items (N = 200, one
+  // instance per CTA) and the autotuner picks 128 where it wins
+  const int threads = plan->tune_threads_1d > 0 ? plan->tune_threads_1d : 256;
   return launch_items(items, smem_for(P, m, nonlinear_only), st, nsteps, mode, project, include_init,
-                      plan->sm_count, nonlinear_only);
+                      plan->sm_count, nonlinear_only, threads);
 }
 
 }  // namespace exgb

@@ -73,6 +73,7 @@ struct exgb_plan {
   // autotuner overrides (0 = automatic choice)
   int tune_cluster = 0;          // 2D: CTAs per cluster
   int tune_items_per_cta = 0;    // 1D: instances per work item
+  int tune_threads_1d = 0;       // 1D: threads per CTA (0 = 256)
   // 2D vorticity transforms: 0 = FP32 register FFTs, 1 = split-BF16 tensor-core DFT
   int precision = 0;
   void* d_tc_scratch = nullptr;

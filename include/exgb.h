@@ -121,8 +121,11 @@ int exgb_plan_kmax(const exgb_plan* plan);
  *                           (1D kernel, transforms, generic 2D kernel)
  *   EXGB_TUNE_CLUSTER       values[0] = CTAs per cluster of the 2D kernel, 1..8 (0 = auto)
  *   EXGB_TUNE_ITEMS_PER_CTA values[0] = 1D instances per work item (0 = auto)
+ *   EXGB_TUNE_THREADS       values[0] = threads per CTA of the 1D kernel: 64, 128, 256
+ *                           (0 = default, 256)
  * exgb_plan_get_tuning writes npass, the kMaxPass (12) radix slots, the
- * cluster size and the items per CTA (n >= 15). */
+ * cluster size and the items per CTA (n >= 15), the precision (n >= 16) and
+ * the 1D threads per CTA (n >= 17). */
 #define EXGB_TUNE_RADICES 0
 #define EXGB_TUNE_CLUSTER 1
 #define EXGB_TUNE_ITEMS_PER_CTA 2
@@ -131,10 +134,11 @@ int exgb_plan_kmax(const exgb_plan* plan);
  *   EXGB_DFT_SPLIT_BF16  dense DFT contractions on the tcgen05 tensor cores in
  *                        split-BF16 form (hi.hi + hi.lo + lo.hi, FP32
  *                        accumulation); N = 128, dealiasing cutoff <= 47.
- * exgb_plan_get_tuning reports it after the items per CTA when n >= 16. */
+ * exgb_plan_get_tuning reports it after the items per CTA. */
 #define EXGB_TUNE_PRECISION 3
 #define EXGB_DFT_FP32 0
 #define EXGB_DFT_SPLIT_BF16 1
+#define EXGB_TUNE_THREADS 4
 int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int n);
 int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n);
 /* Synchronises the device and returns EXGB_ETIMEOUT if a bounded wait inside

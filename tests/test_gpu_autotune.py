@@ -72,3 +72,24 @@ def test_every_cluster_size_matches_oracle(n):
         ran.append(G)
     assert len(ran) >= 2, ran
     assert autotune._set(sm.plan, 1, [0]) == EXGB_OK
+
+
+@pytest.mark.parametrize("n,batch", [(200, 3), (64, 40), (1024, 2)])
+def test_1d_threads_per_cta_match_oracle(n, batch):
+    """Every threads-per-CTA setting of the 1D kernel (64, 128, 256 and the automatic choice) gives
+    the oracle's step within 1e-5 and the same 20-step rollout within 1e-4; other values are refused."""
+    from exponax_gb300._lib import EXGB_OK
+    sm = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, n, 0.1)
+    so = o.KuramotoSivashinskyConservative(1, 100.0, n, 0.1)
+    u = np.stack([ex.ic.RandomSineWaves1d(1, cutoff=5)(n, key=s) for s in range(batch)])
+    want1 = [so(u[b]) for b in range(batch)]
+    want20 = [o.rollout(so, 20, include_init=True)(u[b]) for b in range(batch)]
+    for t in (64, 128, 256, 0):
+        assert autotune._set(sm.plan, 4, [t]) == EXGB_OK
+        assert autotune.get_tuning(sm.plan)["threads"] == t
+        got = ex.vmap(sm)(torch.from_numpy(u).cuda()).cpu().numpy()
+        traj = ex.vmap(ex.rollout(sm, 20, include_init=True))(torch.from_numpy(u).cuda()).cpu().numpy()
+        for b in range(batch):
+            assert rel(got[b], want1[b]) < 1e-5, (t, b)
+            assert rel(traj[b], want20[b]) < 1e-4, (t, b)
+    assert autotune._set(sm.plan, 4, [96]) != EXGB_OK
