@@ -8,7 +8,7 @@ Drop-in surface for the reference's hot path: ``stepper.*`` (``__call__``,
 CUDA, C ABI in include/exgb.h); there is no CPU fallback.
 """
 
-from . import etdrk, ic, metrics, nonlin_fun, spectral, stepper
+from . import etdrk, ic, metrics, nonlin_fun, poisson, spectral, stepper
 from ._lib import ExgbError
 from ._utils import ForcedStepper, RepeatedStepper, make_grid, repeat, rollout, vmap
 from .interpolation import map_between_resolutions
@@ -32,6 +32,7 @@ __all__ = [
     "map_between_resolutions",
     "metrics",
     "nonlin_fun",
+    "poisson",
     "repeat",
     "rollout",
     "spectral",

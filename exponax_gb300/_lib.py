@@ -34,6 +34,7 @@ NL_PROJECTED_3D = 7
 NL_PROJECTED_3D_KOLMOGOROV = 8
 NL_CAHN_HILLIARD = 9
 NL_GRAY_SCOTT = 10
+NL_BELOUSOV_ZHABOTINSKY = 11
 
 
 class PlanDesc(ctypes.Structure):
@@ -105,6 +106,7 @@ SIGNATURES = [
     ("exgb_axpy", _I, [_VP, _I64, ctypes.c_float, _VP, _VP, _VP]),
     ("exgb_scatter_modes", _I, [_VP, _I64, _I64, _I, _VP, _VP, _VP]),
     ("exgb_normalize_fields", _I, [_VP, _I64, _I64, _VP, _I, _I, _I]),
+    ("exgb_mode_scale", _I, [_VP, _I64, _I64, _VP, _VP, _VP]),
     ("exgb_queue_prepare", _I, [ctypes.POINTER(WorkItem), _I64, _I32, _I32, ctypes.POINTER(_VP)]),
     ("exgb_queue_launch", _I, [_VP, _VP]),
     ("exgb_queue_destroy", _I, [_VP]),

@@ -246,7 +246,7 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   // supported (D, kind) combinations of this build
   const bool staged = ndgen_handles(d);
   if (d.order >= 1 && d.nonlin_kind != EXGB_NL_ZERO) {
-    if (d.nonlin_kind < EXGB_NL_ZERO || d.nonlin_kind > EXGB_NL_GRAY_SCOTT)
+    if (d.nonlin_kind < EXGB_NL_ZERO || d.nonlin_kind > EXGB_NL_BELOUSOV_ZHABOTINSKY)
       return fail(EXGB_EINVAL, "unknown nonlinear function");
     if (staged) {
       const int rc = ndgen_validate(d);

@@ -1,12 +1,13 @@
 // exgb_ndgen.cu -- staged ETDRK path for the nonlinearities that have no
 // fused kernel: the four convection variants, gradient norm, polynomial and
-// general nonlinearities in 2D and 3D, and the Cahn-Hilliard and Gray-Scott
-// reaction terms in 1D, 2D and 3D.
+// general nonlinearities in 2D and 3D, and the Cahn-Hilliard, Gray-Scott and
+// Belousov-Zhabotinsky reaction terms in 1D, 2D and 3D.
 //
 // Reference: nonlin_fun/_convection.py:104-231, _gradient_norm.py:68-101,
 // _polynomial.py:56-76, _general_nonlinear.py:99-119,
 // stepper/reaction/_cahn_hilliard.py:12-45 (CahnHilliardNonlinearFun),
 // stepper/reaction/_gray_scott.py:9-46 (GrayScottNonlinearFun),
+// stepper/reaction/_belousov_zhabotinsky.py:14-51 (BelousovZhabotinskyNonlinearFun),
 // nonlin_fun/_base.py:73-137 (pre-mask before every inverse transform,
 // post-mask after every forward transform), etdrk/_etdrk_1..4.py (stages).
 //
@@ -48,6 +49,7 @@ enum Op {
   OP_GENERAL,           // s0 F[u^2] + s1/2 (sum ik) F[u^2] + s2/2 F[|grad u|^2 - mean]
   OP_CAHN_HILLIARD,     // s Lap F[u^3]                         (_cahn_hilliard.py:31-45)
   OP_GRAY_SCOTT,        // F[f(1-u0) - u0 u1^2], F[-(f+k) u1 + u0 u1^2]  (_gray_scott.py:30-46)
+  OP_BZ,                // F[u0 + u1 - u0 u1 - u0^2], F[u2 - u1 - u0 u1], F[u0 - u2]  (_belousov_zhabotinsky.py:33-51)
 };
 
 struct Geo {
@@ -194,6 +196,13 @@ __global__ void pointwise_kernel(Geo g, Prog p, int64_t cb, const float* __restr
         f[0] = p.feed * (1.f - u0) - uvv;
         f[g.npts] = -(p.feed + p.kill) * u1 + uvv;
       } break;
+      case OP_BZ: {
+        const float u0 = in[0], u1 = in[1], u2 = in[2];
+        const float u01 = u0 * u1;
+        f[0] = u0 + u1 - u01 - u0 * u0;
+        f[g.npts] = u2 - u1 - u01;
+        f[2 * g.npts] = u0 - u2;
+      } break;
     }
   }
 }
@@ -317,6 +326,7 @@ bool ndgen_handles(const exgb_plan_desc& d) {
   switch (d.nonlin_kind) {
     case EXGB_NL_CAHN_HILLIARD:
     case EXGB_NL_GRAY_SCOTT:
+    case EXGB_NL_BELOUSOV_ZHABOTINSKY:
       return true;
     case EXGB_NL_CONVECTION:
     case EXGB_NL_GRADIENT_NORM:
@@ -331,7 +341,8 @@ bool ndgen_handles(const exgb_plan_desc& d) {
 // Channel rules of the reference's nonlinear functions, checked at plan creation.
 int ndgen_validate(const exgb_plan_desc& d) {
   const int C = d.num_channels, D = d.num_spatial_dims;
-  if (d.dealiasing_fraction < 0 && (d.nonlin_kind == EXGB_NL_CAHN_HILLIARD || d.nonlin_kind == EXGB_NL_GRAY_SCOTT))
+  if (d.dealiasing_fraction < 0 && (d.nonlin_kind == EXGB_NL_CAHN_HILLIARD || d.nonlin_kind == EXGB_NL_GRAY_SCOTT ||
+                                    d.nonlin_kind == EXGB_NL_BELOUSOV_ZHABOTINSKY))
     return fail(EXGB_EINVAL, "Nonlinear function was set up without dealiasing");
   switch (d.nonlin_kind) {
     case EXGB_NL_CONVECTION:
@@ -351,6 +362,9 @@ int ndgen_validate(const exgb_plan_desc& d) {
       return EXGB_OK;
     case EXGB_NL_GRAY_SCOTT:
       if (C != 2) return fail(EXGB_ESHAPE, "num_channels must be 2");
+      return EXGB_OK;
+    case EXGB_NL_BELOUSOV_ZHABOTINSKY:
+      if (C != 3) return fail(EXGB_ESHAPE, "num_channels must be 3");
       return EXGB_OK;
     default:
       return fail(EXGB_EUNSUPPORTED, "nonlinear function not handled by the staged path");
@@ -401,6 +415,10 @@ static Prog make_prog(const exgb_plan_desc& d) {
       p.op = OP_CAHN_HILLIARD;
       p.NI = p.NF = 1;
       p.s0 = b;
+      break;
+    case EXGB_NL_BELOUSOV_ZHABOTINSKY:
+      p.op = OP_BZ;
+      p.NI = p.NF = 3;
       break;
     default:  // Gray-Scott
       p.op = OP_GRAY_SCOTT;

@@ -5,6 +5,8 @@
 //                         values at fixed mode positions (random-series ICs)
 //   exgb_normalize_fields subtract the mean, then divide by the standard deviation or by max |u|, per field
 //                         (reference ic/_base_ic.py:18-32, normalize_ic)
+//   exgb_mode_scale       multiply Fourier fields by a per-mode complex table (Poisson.step_fourier,
+//                         reference _poisson.py:67-82)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -76,6 +78,14 @@ __global__ void __launch_bounds__(256) normalize_kernel(int64_t n, float* u, int
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) p[i] = (p[i] - mean) * inv;
 }
 
+// out[f][r] = table[r] * in[f][r] over count fields of `per` complex modes
+__global__ void mode_scale_kernel(int64_t count, int64_t per, const float2* __restrict__ table,
+                                  const float2* __restrict__ in, float2* __restrict__ out) {
+  const int64_t n = count * per;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = cmul(__ldg(table + i % per), in[i]);
+}
+
 int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 152 * 16); }
 
 }  // namespace
@@ -115,6 +125,17 @@ extern "C" int exgb_normalize_fields(void* stream, int64_t count, int64_t n, flo
   if (count == 0) return EXGB_OK;
   if (count > 2147483647LL) return fail(EXGB_EINVAL, "exgb_normalize_fields: too many fields for one launch");
   normalize_kernel<<<(unsigned)count, 256, 0, (cudaStream_t)stream>>>(n, u, zero_mean, std_one, max_one);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+extern "C" int exgb_mode_scale(void* stream, int64_t count, int64_t per, const void* table, const void* in,
+                               void* out) {
+  if (!table || !in || !out) return fail(EXGB_EINVAL, "exgb_mode_scale: NULL pointer");
+  if (count < 0 || per <= 0) return fail(EXGB_EINVAL, "exgb_mode_scale: bad size");
+  if (count == 0) return EXGB_OK;
+  mode_scale_kernel<<<grid_for(count * per), 256, 0, (cudaStream_t)stream>>>(
+      count, per, (const float2*)table, (const float2*)in, (float2*)out);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }

@@ -1,16 +1,19 @@
 """Reaction-diffusion steppers (exponax/stepper/reaction/*) on the GB300 ETDRK path.
 
 FisherKPP, AllenCahn and SwiftHohenberg use the polynomial nonlinearity;
-CahnHilliard and GrayScott bring their own nonlinear functions.  In 2D and 3D
-(and GrayScott's two species in 1D) they run on the staged N-D path of
-libexgb.so; the 1D single-species polynomial steppers on the fused 1D kernel.
+CahnHilliard, GrayScott and BelousovZhabotinsky bring their own nonlinear
+functions.  In 2D and 3D (and the multi-species steppers in 1D) they run on
+the staged N-D path of libexgb.so; the 1D single-species polynomial steppers
+on the fused 1D kernel.  BelousovZhabotinsky is defined but not exported by the
+reference (its module calls it experimental); it is importable from here as it
+is from the reference's module.
 """
 
 from __future__ import annotations
 
 import numpy as np
 
-from ._lib import NL_CAHN_HILLIARD, NL_GRAY_SCOTT
+from ._lib import NL_BELOUSOV_ZHABOTINSKY, NL_CAHN_HILLIARD, NL_GRAY_SCOTT
 from .nonlin_fun import BaseNonlinearFun, PolynomialNonlinearFun, _extent_from_derivative
 from .spectral import build_laplace_operator
 from .stepper import BaseStepper
@@ -56,6 +59,22 @@ class GrayScottNonlinearFun(BaseNonlinearFun):
     def _check_channels(self, C):
         if C != 2:
             raise ValueError("num_channels must be 2")
+        if self.dealiasing_mask is None:
+            raise ValueError("Nonlinear function was set up without dealiasing")
+
+
+class BelousovZhabotinskyNonlinearFun(BaseNonlinearFun):
+    """stepper/reaction/_belousov_zhabotinsky.py:14-51: three species,
+    F[u0 + u1 - u0 u1 - u0^2], F[u2 - u1 - u0 u1], F[u0 - u2] of the dealiased state."""
+
+    _kind = NL_BELOUSOV_ZHABOTINSKY
+
+    def __init__(self, num_spatial_dims, num_points, *, dealiasing_fraction):
+        super().__init__(num_spatial_dims, num_points, dealiasing_fraction=dealiasing_fraction)
+
+    def _check_channels(self, C):
+        if C != 3:
+            raise ValueError("num_channels must be 3")
         if self.dealiasing_mask is None:
             raise ValueError("Nonlinear function was set up without dealiasing")
 
@@ -148,6 +167,26 @@ class GrayScott(BaseStepper):
         return GrayScottNonlinearFun(self.num_spatial_dims, self.num_points,
                                      dealiasing_fraction=self.dealiasing_fraction, feed_rate=self.feed_rate,
                                      kill_rate=self.kill_rate)
+
+
+class BelousovZhabotinsky(BaseStepper):
+    """stepper/reaction/_belousov_zhabotinsky.py:54-118: three species with diffusivities
+    (nu0, nu1, nu2) times the Laplacian, the nonlinearity above, dealiasing 1/2 by default."""
+
+    def __init__(self, num_spatial_dims, domain_extent, num_points, dt, *, diffusivities=(1e-5, 2e-5, 1e-5),
+                 order=2, dealiasing_fraction=1 / 2, num_circle_points=16, circle_radius=1.0):
+        self.diffusivities = diffusivities
+        self.dealiasing_fraction = dealiasing_fraction
+        super().__init__(num_spatial_dims, domain_extent, num_points, dt, num_channels=3, order=order,
+                         num_circle_points=num_circle_points, circle_radius=circle_radius)
+
+    def _build_linear_operator(self, d):
+        lap = build_laplace_operator(d, order=2)
+        return np.concatenate([nu * lap for nu in self.diffusivities])
+
+    def _build_nonlinear_fun(self, d):
+        return BelousovZhabotinskyNonlinearFun(self.num_spatial_dims, self.num_points,
+                                               dealiasing_fraction=self.dealiasing_fraction)
 
 
 class SwiftHohenberg(BaseStepper):

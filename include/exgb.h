@@ -54,6 +54,7 @@ extern "C" {
 #define EXGB_NL_PROJECTED_3D_KOLMOGOROV 8 /* ProjectedConvection3dKolmogorov :139-226 */
 #define EXGB_NL_CAHN_HILLIARD 9      /* CahnHilliardNonlinearFun    stepper/reaction/_cahn_hilliard.py:12-45 */
 #define EXGB_NL_GRAY_SCOTT 10        /* GrayScottNonlinearFun       stepper/reaction/_gray_scott.py:9-46 */
+#define EXGB_NL_BELOUSOV_ZHABOTINSKY 11 /* BelousovZhabotinskyNonlinearFun stepper/reaction/_belousov_zhabotinsky.py:14-51 */
 
 typedef struct exgb_plan exgb_plan;
 
@@ -251,6 +252,11 @@ int exgb_scatter_modes(void* stream, int64_t count, int64_t field_elems, int nmo
                        const void* vals, void* hat);
 int exgb_normalize_fields(void* stream, int64_t count, int64_t n, float* u, int zero_mean, int std_one,
                           int max_one);
+/* exgb_mode_scale replaces Poisson.step_fourier (_poisson.py:67-82): out[f][r] = table[r] * in[f][r]
+ * for count Fourier fields of per complex64 modes; table is a device array of per complex64
+ * values (the Poisson solver passes -1/Lap^(order/2), 0 where the operator vanishes).  in and
+ * out may alias. */
+int exgb_mode_scale(void* stream, int64_t count, int64_t per, const void* table, const void* in, void* out);
 
 /* Self-check of the tcgen05 tensor-core layer (no reference counterpart):
  * d (128 x n, FP32) = a (128 x k) . b (n x k)^T, device pointers, row-major.

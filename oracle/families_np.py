@@ -57,6 +57,24 @@ class GrayScottNonlinearFun(BaseNonlinearFun):
         return self.fft(u_power)
 
 
+class BelousovZhabotinskyNonlinearFun(BaseNonlinearFun):
+    """stepper/reaction/_belousov_zhabotinsky.py:14-51"""
+
+    def __init__(self, num_spatial_dims, num_points, *, dealiasing_fraction, dtype="float32"):
+        super().__init__(num_spatial_dims, num_points, dealiasing_fraction=dealiasing_fraction, dtype=dtype)
+
+    def __call__(self, u_hat):
+        if u_hat.shape[0] != 3:
+            raise ValueError("num_channels must be 3")
+        u = self.ifft(self.dealias(u_hat))
+        u_power = np.stack([
+            u[0] + u[1] - u[0] * u[1] - u[0] ** 2,
+            u[2] - u[1] - u[0] * u[1],
+            u[0] - u[2],
+        ])
+        return self.fft(u_power)
+
+
 # --------------------------------------------------------------------------
 # reaction steppers
 # --------------------------------------------------------------------------
@@ -148,6 +166,25 @@ class GrayScott(BaseStepper):
         return GrayScottNonlinearFun(self.num_spatial_dims, self.num_points,
                                      dealiasing_fraction=self.dealiasing_fraction, feed_rate=self.feed_rate,
                                      kill_rate=self.kill_rate, dtype=self.dtype)
+
+
+class BelousovZhabotinsky(BaseStepper):
+    """stepper/reaction/_belousov_zhabotinsky.py:54-118: three species, L = (nu_i Lap)."""
+
+    def __init__(self, num_spatial_dims, domain_extent, num_points, dt, *, diffusivities=(1e-5, 2e-5, 1e-5), order=2,
+                 dealiasing_fraction=1 / 2, num_circle_points=16, circle_radius=1.0, dtype="float32"):
+        self.diffusivities = diffusivities
+        self.dealiasing_fraction = dealiasing_fraction
+        super().__init__(num_spatial_dims, domain_extent, num_points, dt, num_channels=3, order=order,
+                         num_circle_points=num_circle_points, circle_radius=circle_radius, dtype=dtype)
+
+    def _build_linear_operator(self, d):
+        lap = build_laplace_operator(d, order=2)
+        return np.concatenate([nu * lap for nu in self.diffusivities])
+
+    def _build_nonlinear_fun(self, d):
+        return BelousovZhabotinskyNonlinearFun(self.num_spatial_dims, self.num_points,
+                                               dealiasing_fraction=self.dealiasing_fraction, dtype=self.dtype)
 
 
 class SwiftHohenberg(BaseStepper):

@@ -18,6 +18,7 @@ REACTION = [
     ("CahnHilliard", (3, 2.0, 16, 0.001), dict(gamma=2e-3)),
     ("GrayScott", (2, 1.0, 32, 1.0), dict(feed_rate=0.03, kill_rate=0.05)),
     ("SwiftHohenberg", (2, 20.0, 32, 0.1), dict(critical_number=0.8)),
+    ("BelousovZhabotinsky", (2, 1.0, 32, 0.01), dict(diffusivities=(1e-3, 3e-3, 2e-3))),
 ]
 
 
@@ -41,6 +42,11 @@ def test_reaction_descriptors():
     assert fk.nonlinear_fun._nl_desc()["poly"] == (0.0, 0.0, -4.0)
     plan = gs.plan.desc()
     assert plan.nonlin_kind == 10 and tuple(plan.reaction) == (0.03, 0.05) and plan.num_channels == 2
+    bz = ex.stepper.reaction.BelousovZhabotinsky(1, 1.0, 64, 0.01)
+    d = bz.nonlinear_fun._nl_desc()
+    assert d["nonlin_kind"] == 11 and d["dealiasing_fraction"] == 0.5 and bz.num_channels == 3
+    with pytest.raises(ValueError, match="3"):
+        bz.nonlinear_fun._check_channels(2)
 
 
 GENERIC = [

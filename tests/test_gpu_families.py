@@ -1,6 +1,6 @@
 """Staged N-D path on the GPU against the oracle: the convection (four
 variants), gradient-norm, polynomial and general nonlinearities in 2D and 3D,
-the Cahn-Hilliard and Gray-Scott reaction terms in 1D/2D/3D, and the steppers
+the Cahn-Hilliard, Gray-Scott and Belousov-Zhabotinsky reaction terms in 1D/2D/3D, and the steppers
 built on them (Burgers / KS / KdV in 2D and 3D, the reaction-diffusion
 family, the generic General / Normalized / Difficulty steppers).
 
@@ -117,6 +117,8 @@ def _ic_for(name, D, N, C, key):
     if name == "GrayScott":
         blob = 0.5 * (1 + field(D, N, 1, key, cutoff=2)[0])
         return np.stack([1.0 - 0.5 * blob, 0.25 * blob]).astype(np.float32)
+    if name == "BelousovZhabotinsky":
+        return (0.5 + 0.4 * u).astype(np.float32)
     return u
 
 
@@ -155,6 +157,9 @@ REACTION = [
     ("CahnHilliard", 3, 16, dict(domain_extent=2 * np.pi, dt=0.001, gamma=1e-3), 20),
     ("GrayScott", 1, 128, dict(domain_extent=1.0, dt=0.5, diffusivity_1=2e-5, diffusivity_2=1e-5), 50),
     ("GrayScott", 2, 48, dict(domain_extent=1.0, dt=0.5, diffusivity_1=2e-5, diffusivity_2=1e-5), 50),
+    ("BelousovZhabotinsky", 1, 128, dict(domain_extent=1.0, dt=0.01), 50),
+    ("BelousovZhabotinsky", 2, 48, dict(domain_extent=1.0, dt=0.01, diffusivities=(1e-3, 2e-3, 1e-3)), 50),
+    ("BelousovZhabotinsky", 3, 16, dict(domain_extent=1.0, dt=0.01), 20),
 ]
 
 

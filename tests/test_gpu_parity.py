@@ -360,3 +360,35 @@ def test_queue_rollout_graph_capture_and_replay():
             got = host(tr)
             np.testing.assert_array_equal(got[0], u0)
             assert rel(got[1:], ref[1:]) < 1e-4
+
+
+# ------------------------------------------------------------------ Poisson (_poisson.py)
+
+@pytest.mark.parametrize("D,L,N", [(1, 1.0, 50), (2, 3.0, 25), (3, 3.0, 15)])
+def test_poisson_exact(D, L, N):
+    """tests/test_validation.py:214-292 on the GPU: sin products against the analytic solution, abs 1e-6."""
+    g = ex.make_grid(D, L, N)
+    k = 2 * np.pi / L
+    rhs = np.prod([np.sin(k * g[d:d + 1]) for d in range(D)], axis=0).astype(np.float32)
+    want = rhs / (D * k ** 2)
+    u = host(ex.poisson.Poisson(D, L, N)(cu(rhs)))
+    np.testing.assert_allclose(u, want, rtol=0, atol=1e-6)
+
+
+@pytest.mark.parametrize("D,N,order", [(1, 64, 2), (2, 48, 2), (2, 32, 4), (3, 16, 2)])
+def test_poisson_matches_oracle(D, N, order):
+    """Random right-hand sides (two channels, batched) against the oracle's Poisson: 1e-6 relative L2;
+    step_fourier alone, and the zero mean of the solution."""
+    rng = np.random.default_rng(D * 10 + order)
+    f = rng.standard_normal((3, 2) + (N,) * D).astype(np.float32)
+    pm = ex.poisson.Poisson(D, 2.0, N, order=order)
+    po = o.Poisson(D, 2.0, N, order=order)
+    got = host(pm.step(cu(f)))
+    for b in range(3):
+        assert rel(got[b], po(f[b])) < 1e-6, b
+        assert abs(float(got[b].mean())) < 1e-6
+    fh = o.fft(f[0], num_spatial_dims=D).astype(np.complex64)
+    gh = host(pm.step_fourier(cu(fh)))
+    assert rel(gh.view(np.float32), po.step_fourier(fh).astype(np.complex64).view(np.float32)) < 1e-6
+    with pytest.raises(ValueError):
+        pm(cu(f[0][..., :-1]))
