@@ -107,6 +107,7 @@ SIGNATURES = [
     ("exgb_scatter_modes", _I, [_VP, _I64, _I64, _I, _VP, _VP, _VP]),
     ("exgb_normalize_fields", _I, [_VP, _I64, _I64, _VP, _I, _I, _I]),
     ("exgb_mode_scale", _I, [_VP, _I64, _I64, _VP, _VP, _VP]),
+    ("exgb_mode_mix2", _I, [_VP, _I64, _I64, _VP, _VP, _VP, _I]),
     ("exgb_queue_prepare", _I, [ctypes.POINTER(WorkItem), _I64, _I32, _I32, ctypes.POINTER(_VP)]),
     ("exgb_queue_launch", _I, [_VP, _VP]),
     ("exgb_queue_destroy", _I, [_VP]),

@@ -7,6 +7,8 @@
 //                         (reference ic/_base_ic.py:18-32, normalize_ic)
 //   exgb_mode_scale       multiply Fourier fields by a per-mode complex table (Poisson.step_fourier,
 //                         reference _poisson.py:67-82)
+//   exgb_mode_mix2        per-mode real 2x2 map of two-channel Fourier fields, repeated (Wave,
+//                         reference stepper/_wave.py)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -86,6 +88,27 @@ __global__ void mode_scale_kernel(int64_t count, int64_t per, const float2* __re
     out[i] = cmul(__ldg(table + i % per), in[i]);
 }
 
+// Two-channel fields (h, v) per sample: (h, v) <- M(r) (h, v) nsteps times, M real [4][per] row-major
+// per mode (m00, m01, m10, m11), state in registers between steps
+__global__ void mode_mix2_kernel(int64_t count, int64_t per, const float* __restrict__ mat,
+                                 const float2* __restrict__ in, float2* __restrict__ out, int nsteps) {
+  const int64_t n = count * per;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / per, r = i - b * per;
+    const float m00 = __ldg(mat + r), m01 = __ldg(mat + per + r);
+    const float m10 = __ldg(mat + 2 * per + r), m11 = __ldg(mat + 3 * per + r);
+    const int64_t o = b * 2 * per + r;
+    float2 h = in[o], v = in[o + per];
+    for (int s = 0; s < nsteps; ++s) {
+      const float2 h2 = make_float2(fmaf(m00, h.x, m01 * v.x), fmaf(m00, h.y, m01 * v.y));
+      v = make_float2(fmaf(m10, h.x, m11 * v.x), fmaf(m10, h.y, m11 * v.y));
+      h = h2;
+    }
+    out[o] = h;
+    out[o + per] = v;
+  }
+}
+
 int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 152 * 16); }
 
 }  // namespace
@@ -136,6 +159,17 @@ extern "C" int exgb_mode_scale(void* stream, int64_t count, int64_t per, const v
   if (count == 0) return EXGB_OK;
   mode_scale_kernel<<<grid_for(count * per), 256, 0, (cudaStream_t)stream>>>(
       count, per, (const float2*)table, (const float2*)in, (float2*)out);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+extern "C" int exgb_mode_mix2(void* stream, int64_t count, int64_t per, const float* mat, const void* in, void* out,
+                              int nsteps) {
+  if (!mat || !in || !out) return fail(EXGB_EINVAL, "exgb_mode_mix2: NULL pointer");
+  if (count < 0 || per <= 0 || nsteps < 0) return fail(EXGB_EINVAL, "exgb_mode_mix2: bad size");
+  if (count == 0) return EXGB_OK;
+  mode_mix2_kernel<<<grid_for(count * per), 256, 0, (cudaStream_t)stream>>>(
+      count, per, mat, (const float2*)in, (float2*)out, nsteps);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }

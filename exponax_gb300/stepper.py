@@ -427,5 +427,96 @@ class HyperDiffusion(_LinearStepper):
         return -self.hyper_diffusivity * build_laplace_operator(d, order=4)
 
 
+class Wave(_LinearStepper):
+    """stepper/_wave.py:8-197: the wave equation h_tt = c^2 Lap h as the system (h, v = h_t), advanced
+    exactly.  The reference diagonalises per mode (w = i c |k| h, pos/neg = (w +- v)/sqrt(2), ETDRK0
+    factors exp(+-i c |k| dt)) and adds dt v to the mean of h.  Composed, one step is the real map
+      h' = cos(t) h + sin(t)/(c |k|) v,  v' = -c |k| sin(t) h + cos(t) v,  t = c |k| dt,
+    and h' = h + dt v, v' = v at k = 0.  It is built once in FP64 (from the float32 |k| the reference
+    uses) and applied on the device by exgb_mode_mix2, n steps per launch for repeat."""
+
+    def __init__(self, num_spatial_dims, domain_extent, num_points, dt, *, speed_of_sound=1.0):
+        from .spectral import build_scaled_wavenumbers
+
+        self.speed_of_sound = speed_of_sound
+        k = build_scaled_wavenumbers(num_spatial_dims, domain_extent, num_points).astype(np.float32)
+        self.wavenumber_norm = np.linalg.norm(k, axis=0, keepdims=True)
+        super().__init__(num_spatial_dims, domain_extent, num_points, dt, num_channels=2, order=0)
+        kn = self.wavenumber_norm.astype(np.float64).reshape(-1)
+        c = float(speed_of_sound)
+        th = c * kn * dt
+        safe = np.where(kn == 0, 1.0, c * kn)
+        m = np.stack([np.cos(th), np.where(kn == 0, dt, np.sin(th) / safe), -c * kn * np.sin(th), np.cos(th)])
+        self._mix = m.astype(np.float32)
+        self._mix_dev = None
+
+    def _build_linear_operator(self, d):
+        val = 1j * self.speed_of_sound * self.wavenumber_norm
+        return np.concatenate((val, -val), axis=0)
+
+    def _mix_table(self):
+        if self._mix_dev is None:
+            self._mix_dev = _device.torch().from_numpy(np.ascontiguousarray(self._mix)).cuda()
+        return self._mix_dev
+
+    def _apply(self, t_hat, B, n, out=None):
+        per = self._mix.shape[1]
+        out = _device.empty(t_hat.shape, "complex64") if out is None else out
+        check(load().exgb_mode_mix2(_device.stream(), B, per, _device.ptr(self._mix_table()), _device.ptr(t_hat),
+                                    _device.ptr(out), int(n)), "Wave")
+        return out
+
+    def _fourier(self, u_hat, n, batched):
+        t, back = _device.to_device(u_hat, "complex64")
+        ws = (2,) + wavenumber_shape(self.num_spatial_dims, self.num_points)
+        got = tuple(t.shape[1:]) if batched else tuple(t.shape)
+        if got != ws:
+            raise ValueError(f"Expected Fourier shape {ws}, got {got}")
+        return back(self._apply(t, t.shape[0] if batched else 1, n))
+
+    def step_fourier(self, u_hat):
+        return self._fourier(u_hat, 1, batched=False)
+
+    def _batched_step_fourier(self, u_hat):
+        return self._fourier(u_hat, 1, batched=True)
+
+    def _repeat_fourier(self, u_hat, n, batched):
+        return self._fourier(u_hat, n, batched)
+
+    def _phys_steps(self, u, n, batched):
+        from .spectral import fft, ifft
+
+        t, back, B = self._phys(u, batched)
+        D = self.num_spatial_dims
+        hat = fft(t, num_spatial_dims=D)
+        return ifft(self._apply(hat, B, n), num_spatial_dims=D, num_points=self.num_points), back
+
+    def _step(self, u, batched):
+        out, back = self._phys_steps(u, 1, batched)
+        return back(out)
+
+    def _repeat(self, u, n, batched):
+        # the map is real and even in k, so it keeps rfftn spectra Hermitian: the reference's
+        # per-step irfftn -> rfftn round trip changes nothing and the n steps run in one launch
+        out, back = self._phys_steps(u, n, batched)
+        return back(out)
+
+    def _rollout(self, u, n, include_init, batched):
+        from .spectral import fft, ifft
+
+        torch = _device.torch()
+        t, back, B = self._phys(u, batched)
+        D = self.num_spatial_dims
+        hat = fft(t, num_spatial_dims=D)
+        frames = [t] if include_init else []
+        for _ in range(n):
+            hat = self._apply(hat, B, 1)
+            frames.append(ifft(hat, num_spatial_dims=D, num_points=self.num_points))
+        if not frames:
+            shape = ((B,) if batched else ()) + (0,) + tuple(t.shape[1:] if batched else t.shape)
+            return back(_device.empty(shape, "float32"))
+        return back(torch.stack(frames, dim=1 if batched else 0).contiguous())
+
+
 # the reference's stepper sub-packages (stepper/generic, stepper/reaction)
 from . import generic, reaction  # noqa: E402

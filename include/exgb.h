@@ -257,6 +257,13 @@ int exgb_normalize_fields(void* stream, int64_t count, int64_t n, float* u, int 
  * values (the Poisson solver passes -1/Lap^(order/2), 0 where the operator vanishes).  in and
  * out may alias. */
 int exgb_mode_scale(void* stream, int64_t count, int64_t per, const void* table, const void* in, void* out);
+/* exgb_mode_mix2 replaces Wave.step_fourier (stepper/_wave.py:143-224) applied nsteps times: for
+ * count samples of two Fourier fields (h, v) of per complex64 modes each, (h, v) <- M (h, v) per
+ * mode, M a real 2x2 matrix given as mat[4][per] float32 on the device (m00, m01, m10, m11).  The
+ * Wave stepper passes its exact one-step map (the diagonalising transform, the ETDRK0 factors and
+ * the inverse transform composed; the mean mode's h += dt v folded in).  in and out may alias. */
+int exgb_mode_mix2(void* stream, int64_t count, int64_t per, const float* mat, const void* in, void* out,
+                   int nsteps);
 
 /* Self-check of the tcgen05 tensor-core layer (no reference counterpart):
  * d (128 x n, FP32) = a (128 x k) . b (n x k)^T, device pointers, row-major.

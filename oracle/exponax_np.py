@@ -1026,6 +1026,48 @@ class HyperDiffusion(_LinearStepper):
         return -self.hyper_diffusivity * build_laplace_operator(d, order=4)
 
 
+class Wave(_LinearStepper):
+    """stepper/_wave.py:8-197: h_tt = c^2 Lap h as the first-order system (h, v = h_t), stepped in the
+    diagonalising variables w = i c |k| h (|k| guarded to 1 at k = 0), pos/neg = (w +- v)/sqrt(2) with
+    the ETDRK0 factors exp(+-i c |k| dt), transformed back; the mean mode gets h += dt v."""
+
+    def __init__(self, num_spatial_dims, domain_extent, num_points, dt, *, speed_of_sound=1.0, dtype="float32"):
+        self.speed_of_sound = speed_of_sound
+        self.wavenumber_norm = np.linalg.norm(
+            build_scaled_wavenumbers(num_spatial_dims, domain_extent, num_points, dtype=dtype), axis=0, keepdims=True)
+        super().__init__(num_spatial_dims, domain_extent, num_points, dt, num_channels=2, order=0, dtype=dtype)
+
+    def _build_linear_operator(self, d):
+        val = 1j * self.speed_of_sound * self.wavenumber_norm
+        return np.concatenate((val, -val), axis=0)
+
+    def _guard(self):
+        return np.where(self.wavenumber_norm == 0, 1.0, self.wavenumber_norm).astype(self.wavenumber_norm.dtype)
+
+    def _forward_transform(self, u_hat):
+        """stepper/_wave.py:130-150"""
+        h_hat, v_hat = u_hat[0:1], u_hat[1:2]
+        w_hat = 1j * self.speed_of_sound * self._guard() * h_hat
+        pos = (1 / np.sqrt(2)) * (w_hat + v_hat)
+        neg = (1 / np.sqrt(2)) * (w_hat - v_hat)
+        return np.concatenate([pos, neg], axis=0).astype(self.cd)
+
+    def _inverse_transform(self, waves_hat):
+        """stepper/_wave.py:152-160"""
+        pos, neg = waves_hat[0:1], waves_hat[1:2]
+        w_hat = (1 / np.sqrt(2)) * (pos + neg)
+        v_hat = (1 / np.sqrt(2)) * (pos - neg)
+        h_hat = w_hat / (1j * self.speed_of_sound * self._guard())
+        return np.concatenate([h_hat, v_hat], axis=0).astype(self.cd)
+
+    def step_fourier(self, u_hat):
+        """stepper/_wave.py:175-197"""
+        nxt = self._inverse_transform(self._integrator.step_fourier(self._forward_transform(u_hat)))
+        dc = (0,) * self.num_spatial_dims
+        nxt[(0,) + dc] += self.dt * u_hat[(1,) + dc]
+        return nxt
+
+
 class Poisson:
     """_poisson.py:14-128: -inv(Lap^(order/2)) f with a zero mean mode."""
 

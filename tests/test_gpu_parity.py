@@ -392,3 +392,57 @@ def test_poisson_matches_oracle(D, N, order):
     assert rel(gh.view(np.float32), po.step_fourier(fh).astype(np.complex64).view(np.float32)) < 1e-6
     with pytest.raises(ValueError):
         pm(cu(f[0][..., :-1]))
+
+
+# ------------------------------------------------------------------ Wave (stepper/_wave.py)
+
+def _wave_ic(D, N, key):
+    g = ex.ic.RandomTruncatedFourierSeries(D, cutoff=3, max_one=True)
+    return np.concatenate([g(N, key=2 * key), 0.3 * g(N, key=2 * key + 1)]).astype(np.float32)
+
+
+@pytest.mark.parametrize("D,N,L,c,dt", [(1, 64, 2.0, 1.0, 0.01), (2, 32, 1.0, 2.0, 0.005), (3, 16, 3.0, 0.7, 0.05),
+                                        (2, 15, 1.0, 1.0, 0.01)])
+def test_wave_matches_oracle(D, N, L, c, dt):
+    """One step (1e-5), step_fourier (1e-5), 100 steps of repeat and a 20-step rollout (1e-4) against the
+    float32 oracle's diagonalised step; the 100-step error against the float64 oracle is asserted too."""
+    sm = ex.stepper.Wave(D, L, N, dt, speed_of_sound=c)
+    so = o.Wave(D, L, N, dt, speed_of_sound=c)
+    so64 = o.Wave(D, L, N, dt, speed_of_sound=c, dtype="float64")
+    u = np.stack([_wave_ic(D, N, k) for k in range(2)])
+    one = host(ex.vmap(sm)(cu(u)))
+    for b in range(2):
+        assert rel(one[b], so(u[b])) < 1e-5, b
+    uh = o.fft(u[0], num_spatial_dims=D).astype(np.complex64)
+    gh = host(sm.step_fourier(cu(uh)))
+    assert rel(gh.view(np.float32), so.step_fourier(uh).astype(np.complex64).view(np.float32)) < 1e-5
+    many = host(ex.vmap(ex.repeat(sm, 100))(cu(u)))
+    traj = host(ex.vmap(ex.rollout(sm, 20, include_init=True))(cu(u)))
+    for b in range(2):
+        assert rel(many[b], o.repeat(so, 100)(u[b])) < 1e-4, b
+        assert rel(many[b], o.repeat(so64, 100)(u[b].astype(np.float64))) < 1e-4, b
+        assert rel(traj[b], o.rollout(so, 20, include_init=True)(u[b])) < 1e-4, b
+    assert traj.shape == (2, 21, 2) + (N,) * D
+
+
+def test_wave_conserves_energy_and_drifts_the_mean():
+    """||v||^2 + c^2 ||grad h||^2 is invariant (exact step): within 3e-5 after 500 steps (the float32
+    one-step map alone drifts it by about 6e-6 here); the mean of h moves by dt * mean(v) per step
+    (the reference's mean-mode rule)."""
+    D, N, L, c, dt = 2, 48, 2.0, 1.5, 0.01
+    sm = ex.stepper.Wave(D, L, N, dt, speed_of_sound=c)
+    u = _wave_ic(D, N, 3)
+    u[1] += 0.25  # nonzero mean velocity
+
+    def energy(x):
+        xh = np.fft.rfftn(x.astype(np.float64), axes=(-2, -1))
+        k = np.linalg.norm(ex.spectral.build_scaled_wavenumbers(D, L, N), axis=0)
+        w = np.ones(xh.shape[-1])
+        w[1:-1] = 2.0  # rfft half-spectrum weights (N even)
+        dev = xh[1].copy()
+        dev[0, 0] = 0.0
+        return float(np.sum(w * (np.abs(dev) ** 2 + c ** 2 * k ** 2 * np.abs(xh[0]) ** 2)))
+
+    out = host(ex.repeat(sm, 500)(cu(u)))
+    assert abs(energy(out) - energy(u)) / energy(u) < 3e-5
+    assert abs(float(out[0].mean()) - (float(u[0].mean()) + 500 * dt * float(u[1].mean()))) < 1e-4

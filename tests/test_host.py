@@ -143,3 +143,18 @@ def test_ic_generators_are_seeded_and_normalised():
     s = ex.ic.RandomSineWaves1d(1, cutoff=5)(200, key=0)
     spec = np.abs(np.fft.rfft(s[0]))
     assert np.all(spec[6:] < 1e-3 * spec.max())
+
+
+def test_instantiate_linear_and_wave_steppers_without_a_gpu():
+    """tests/test_builtin_solvers.py:8-30: the linear steppers and Wave construct in 1D-3D on the host
+    (operators only; the device plan is made on first use).  Wave's exact one-step map is the identity
+    plus dt v at the mean mode and has unit determinant elsewhere."""
+    for D in (1, 2, 3):
+        for cls in (ex.stepper.Advection, ex.stepper.Diffusion, ex.stepper.AdvectionDiffusion,
+                    ex.stepper.Dispersion, ex.stepper.HyperDiffusion, ex.stepper.Wave):
+            cls(D, 10.0, 25, 0.1)
+    w = ex.stepper.Wave(2, 10.0, 25, 0.1, speed_of_sound=2.0)
+    m = w._mix.astype(np.float64)
+    np.testing.assert_allclose(m[:, 0], [1.0, 0.1, 0.0, 1.0])
+    np.testing.assert_allclose(m[0] * m[3] - m[1] * m[2], 1.0, atol=1e-6)
+
