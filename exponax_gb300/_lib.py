@@ -103,6 +103,8 @@ SIGNATURES = [
     ("exgb_tc_gemm_check", _I, [_VP, _I, _I, _VP, _VP, _VP, _I]),
     ("exgb_spectrum", _I, [_VP, _I, _I, _I64, _VP, _VP, _I, _I]),
     ("exgb_field_sums", _I, [_VP, _I64, _I64, _VP, _VP, _VP]),
+    ("exgb_field_pnorms", _I, [_VP, _I64, _I64, _VP, _VP, ctypes.c_float, _VP]),
+    ("exgb_fourier_pnorms", _I, [_VP, _I, _I, _I64, _VP, ctypes.c_float, ctypes.c_float, _I, _I, ctypes.c_float, _VP]),
     ("exgb_axpy", _I, [_VP, _I64, ctypes.c_float, _VP, _VP, _VP]),
     ("exgb_scatter_modes", _I, [_VP, _I64, _I64, _I, _VP, _VP, _VP]),
     ("exgb_normalize_fields", _I, [_VP, _I64, _I64, _VP, _I, _I, _I]),

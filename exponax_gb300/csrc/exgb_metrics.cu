@@ -1,7 +1,9 @@
 // exgb_metrics.cu -- evaluation kernels on device fields: the radially binned
-// power / amplitude spectrum (reference _spectral.py:866-1030, get_spectrum)
-// and the per-field sums behind nRMSE (metrics/_spatial.py:537-586) and
-// correlation (metrics/_correlation.py:33-60).
+// power / amplitude spectrum (reference _spectral.py:866-1030, get_spectrum),
+// the per-field sums behind nRMSE (metrics/_spatial.py:537-586) and
+// correlation (metrics/_correlation.py:33-60), and the p-norm aggregations of
+// the spatial, Fourier and H1 metric families (metrics/_spatial.py,
+// _fourier.py, _derivative.py).
 //
 // Spectrum of one field from its rfftn (N..., N/2+1 modes):
 //   power:      q = 0.5 * (|u^| / recon) * (|u^| / norm)
@@ -120,10 +122,124 @@ __global__ void __launch_bounds__(256) field_sums_kernel(int64_t n, const float*
   }
 }
 
+__device__ __forceinline__ float pow_abs(float x, float p) {
+  x = fabsf(x);
+  return p == 1.f ? x : p == 2.f ? x * x : powf(x, p);
+}
+
+__device__ __forceinline__ void block_sum3(double (&v)[3], double* red /* [3][8] */) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int q = 0; q < 3; ++q) {
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    if (lane == 0) red[q * 8 + w] = v[q];
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int i = 0; i < nw; ++i) t += red[threadIdx.x * 8 + i];
+    v[threadIdx.x] = t;
+  }
+}
+
+// One CTA per field of n floats: out[3 f + 0..2] = sum |a - b|^p, sum |a|^p, sum |b|^p
+// (b == nullptr: the difference is a itself and the last sum is 0) -- the aggregations behind
+// spatial_norm (metrics/_spatial.py:8-195), accumulated in FP64.
+__global__ void __launch_bounds__(256) field_pnorms_kernel(int64_t n, const float* __restrict__ a,
+                                                           const float* __restrict__ b, float p, double* out) {
+  __shared__ double red[24];
+  const float* fa = a + (int64_t)blockIdx.x * n;
+  const float* fb = b ? b + (int64_t)blockIdx.x * n : nullptr;
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const float x = fa[i];
+    const float y = fb ? fb[i] : 0.f;
+    v[0] += pow_abs(fb ? x - y : x, p);
+    v[1] += pow_abs(x, p);
+    v[2] += pow_abs(y, p);
+  }
+  block_sum3(v, red);
+  if (threadIdx.x < 3) out[3 * (int64_t)blockIdx.x + threadIdx.x] = v[threadIdx.x];
+}
+
+// One CTA per rfftn field (N..., N/2+1 modes): the sums of fourier_aggregator
+// (metrics/_fourier.py:15-140): coefficients with |c| < 1e-5 dropped, the band
+// low <= max_d |k_d| <= high kept (low_pass_filter_mask(low - 1) inverted, and
+// low_pass_filter_mask(high)), each |c|^p divided by the "reconstruction" scaling
+// (N^D, halved on the rfft-axis modes 0 < k < N/2).  With a derivative order a >= 0
+// the sum is split per axis d and weighted by |2 pi k_d / L|^(a p) (the magnitude of
+// (i k_d)^a); otherwise out has one sum per field.
+__global__ void __launch_bounds__(256) fourier_pnorms_kernel(int D, int N, int64_t per, const float2* __restrict__ hat,
+                                                             float p, float alpha, int use_deriv, int low, int high,
+                                                             float kscale, double* out) {
+  __shared__ double red[24];
+  const int M = N / 2 + 1;
+  const float2* h = hat + (int64_t)blockIdx.x * per;
+  double v[3] = {0.0, 0.0, 0.0};
+  double full = 1.0;
+  for (int d = 0; d < D; ++d) full *= (double)N;
+  for (int64_t r = threadIdx.x; r < per; r += blockDim.x) {
+    const float2 c = h[r];
+    const float m = sqrtf(c.x * c.x + c.y * c.y);
+    if (m < 1e-5f) continue;
+    int k[3] = {0, 0, 0};
+    const int kl = (int)(r % M);
+    k[D - 1] = kl;
+    int64_t rest = r / M;
+    for (int a = D - 2; a >= 0; --a) {
+      const int i = (int)(rest % N);
+      rest /= N;
+      k[a] = (i <= (N - 1) / 2) ? i : i - N;
+    }
+    int kmax = 0;
+    for (int a = 0; a < D; ++a) kmax = max(kmax, abs(k[a]));
+    if (kmax < low || kmax > high) continue;
+    const bool halve = kl != 0 && !((N % 2) == 0 && kl == N / 2);
+    const double base = (double)pow_abs(m, p) / (halve ? 0.5 * full : full);
+    if (!use_deriv) {
+      v[0] += base;
+    } else {
+      for (int a = 0; a < D; ++a) v[a] += base * (double)powf(kscale * (float)abs(k[a]), alpha * p);
+    }
+  }
+  block_sum3(v, red);
+  const int nout = use_deriv ? D : 1;
+  if (threadIdx.x < nout) out[(int64_t)blockIdx.x * nout + threadIdx.x] = v[threadIdx.x];
+}
+
 }  // namespace
 }  // namespace exgb
 
 using namespace exgb;
+
+extern "C" int exgb_field_pnorms(void* stream, int64_t count, int64_t n, const float* a, const float* b, float p,
+                                 double* out) {
+  if (!a || !out) return fail(EXGB_EINVAL, "exgb_field_pnorms: NULL pointer");
+  if (count < 0 || n < 0) return fail(EXGB_EINVAL, "exgb_field_pnorms: negative size");
+  if (!(p > 0.f)) return fail(EXGB_EINVAL, "exgb_field_pnorms: the exponent must be positive");
+  if (count == 0) return EXGB_OK;
+  field_pnorms_kernel<<<(unsigned)count, 256, 0, (cudaStream_t)stream>>>(n, a, b, p, out);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+extern "C" int exgb_fourier_pnorms(void* stream, int num_spatial_dims, int num_points, int64_t count,
+                                   const void* u_hat, float p, float derivative_order, int low, int high,
+                                   float domain_extent, double* out) {
+  const int D = num_spatial_dims, N = num_points;
+  if (!u_hat || !out) return fail(EXGB_EINVAL, "exgb_fourier_pnorms: NULL pointer");
+  if (D < 1 || D > 3 || N < 1) return fail(EXGB_ESHAPE, "exgb_fourier_pnorms: 1 to 3 axes of N >= 1 points");
+  if (count < 0) return fail(EXGB_EINVAL, "exgb_fourier_pnorms: negative count");
+  if (!(p > 0.f) || !(domain_extent > 0.f)) return fail(EXGB_EINVAL, "exgb_fourier_pnorms: bad exponent or extent");
+  if (count == 0) return EXGB_OK;
+  int64_t per = N / 2 + 1;
+  for (int d = 0; d < D - 1; ++d) per *= N;
+  const int use_deriv = derivative_order >= 0.f ? 1 : 0;
+  const float kscale = (float)(2.0 * 3.14159265358979323846 / (double)domain_extent);
+  fourier_pnorms_kernel<<<(unsigned)count, 256, 0, (cudaStream_t)stream>>>(
+      D, N, per, (const float2*)u_hat, p, use_deriv ? derivative_order : 0.f, use_deriv, low, high, kscale, out);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
 
 extern "C" int exgb_spectrum(void* stream, int num_spatial_dims, int num_points, int64_t count, const void* u_hat,
                              float* out, int power, int average) {

@@ -237,6 +237,18 @@ int exgb_map_between_resolutions(void* stream, int num_spatial_dims, int n_old, 
 int exgb_spectrum(void* stream, int num_spatial_dims, int num_points, int64_t count, const void* u_hat,
                   float* out, int power, int average);
 int exgb_field_sums(void* stream, int64_t count, int64_t n, const float* a, const float* b, double* out);
+/* The metric families of metrics/_spatial.py, _fourier.py and _derivative.py reduce to these sums
+ * (FP64), combined on the host:
+ * exgb_field_pnorms: count fields of n floats; out[3 f + 0..2] = sum |a - b|^p, sum |a|^p,
+ *   sum |b|^p (b may be NULL: the difference is a, the last sum 0) -- spatial_aggregator (:8-83).
+ * exgb_fourier_pnorms: count rfftn fields (N..., N/2+1) of D = 1..3 axes; the sums of
+ *   fourier_aggregator (_fourier.py:15-140): |c| < 1e-5 dropped, band low <= max_d |k_d| <= high,
+ *   |c|^p over the "reconstruction" scaling array; derivative_order < 0: one sum per field,
+ *   else D sums per field weighted by |2 pi k_d / domain_extent|^(derivative_order p). */
+int exgb_field_pnorms(void* stream, int64_t count, int64_t n, const float* a, const float* b, float p,
+                      double* out);
+int exgb_fourier_pnorms(void* stream, int num_spatial_dims, int num_points, int64_t count, const void* u_hat,
+                        float p, float derivative_order, int low, int high, float domain_extent, double* out);
 
 /* ---- helpers of the Python surface ----
  * exgb_axpy: out = x + alpha y over n floats (ForcedStepper, _forced_stepper.py:64-65, :86-87;

@@ -1258,6 +1258,134 @@ def nRMSE(u_pred, u_ref, *, domain_extent=1.0):
     return tot
 
 
+def spatial_aggregator(state_no_channel, *, num_spatial_dims=None, domain_extent=1.0, num_points=None,
+                       inner_exponent=2.0, outer_exponent=None):
+    """metrics/_spatial.py:8-83: (scale * sum |u|^p)^q, scale = (L/N)^D."""
+    if num_spatial_dims is None:
+        num_spatial_dims = state_no_channel.ndim
+    if num_points is None:
+        num_points = state_no_channel.shape[-1]
+    if outer_exponent is None:
+        outer_exponent = 1 / inner_exponent
+    scale = (domain_extent / num_points) ** num_spatial_dims
+    return (scale * np.sum(np.abs(state_no_channel) ** inner_exponent)) ** outer_exponent
+
+
+def spatial_norm(state, state_ref=None, *, mode="absolute", domain_extent=1.0, inner_exponent=2.0,
+                 outer_exponent=None):
+    """metrics/_spatial.py:86-195: per-channel aggregations (absolute / normalized / symmetric), summed."""
+    if state_ref is None:
+        if mode in ("normalized", "symmetric"):
+            raise ValueError(f"mode '{mode}' requires state_ref")
+        diff = state
+    else:
+        diff = state - state_ref
+    kw = dict(domain_extent=domain_extent, inner_exponent=inner_exponent, outer_exponent=outer_exponent)
+    dn = np.array([spatial_aggregator(d, **kw) for d in diff])
+    if mode == "normalized":
+        return np.sum(dn / np.array([spatial_aggregator(r, **kw) for r in state_ref]))
+    if mode == "symmetric":
+        sn = np.array([spatial_aggregator(x, **kw) for x in state])
+        rn = np.array([spatial_aggregator(r, **kw) for r in state_ref])
+        return np.sum(2 * dn / (sn + rn))
+    return np.sum(dn)
+
+
+def _spatial_metric(mode, p, q):
+    def metric(u_pred, u_ref=None, *, domain_extent=1.0):
+        return spatial_norm(u_pred, u_ref, mode=mode, domain_extent=domain_extent, inner_exponent=p,
+                            outer_exponent=q)
+    return metric
+
+
+# metrics/_spatial.py:198-634
+MAE = _spatial_metric("absolute", 1.0, 1.0)
+nMAE = _spatial_metric("normalized", 1.0, 1.0)
+sMAE = _spatial_metric("symmetric", 1.0, 1.0)
+MSE = _spatial_metric("absolute", 2.0, 1.0)
+nMSE = _spatial_metric("normalized", 2.0, 1.0)
+sMSE = _spatial_metric("symmetric", 2.0, 1.0)
+RMSE = _spatial_metric("absolute", 2.0, 0.5)
+sRMSE = _spatial_metric("symmetric", 2.0, 0.5)
+
+
+def fourier_aggregator(state_no_channel, *, num_spatial_dims=None, domain_extent=1.0, num_points=None,
+                       inner_exponent=2.0, outer_exponent=None, low=None, high=None, derivative_order=None):
+    """metrics/_fourier.py:15-140"""
+    if num_spatial_dims is None:
+        num_spatial_dims = state_no_channel.ndim
+    if num_points is None:
+        num_points = state_no_channel.shape[-1]
+    if outer_exponent is None:
+        outer_exponent = 1 / inner_exponent
+    dtype = "float64" if state_no_channel.dtype == np.float64 else "float32"
+    uh = fft(state_no_channel, num_spatial_dims=num_spatial_dims)
+    uh = np.where(np.abs(uh) < 1e-5, np.zeros_like(uh), uh)
+    if low is not None or high is not None:
+        low = 0 if low is None else low
+        high = (num_points // 2) + 1 if high is None else high
+        low_mask = low_pass_filter_mask(num_spatial_dims, num_points, cutoff=low - 1, dtype=dtype)
+        high_mask = low_pass_filter_mask(num_spatial_dims, num_points, cutoff=high, dtype=dtype)
+        uh = uh * (np.invert(low_mask) & high_mask)[0]
+    if derivative_order is not None:
+        d = build_derivative_operator(num_spatial_dims, domain_extent, num_points, dtype=dtype)
+        comps = uh * d ** derivative_order
+    else:
+        comps = uh[None]
+    recon = build_scaling_array(num_spatial_dims, num_points, mode="reconstruction", dtype=dtype)[0]
+    scale = (domain_extent / num_points) ** num_spatial_dims
+    return np.sum([(scale * np.sum(np.abs(c) ** inner_exponent / recon)) ** outer_exponent for c in comps])
+
+
+def fourier_norm(state, state_ref=None, *, mode="absolute", domain_extent=1.0, inner_exponent=2.0,
+                 outer_exponent=None, low=None, high=None, derivative_order=None):
+    """metrics/_fourier.py:143-235"""
+    if state_ref is None:
+        if mode == "normalized":
+            raise ValueError("mode 'normalized' requires state_ref")
+        diff = state
+    else:
+        diff = state - state_ref
+    kw = dict(domain_extent=domain_extent, inner_exponent=inner_exponent, outer_exponent=outer_exponent, low=low,
+              high=high, derivative_order=derivative_order)
+    dn = np.array([fourier_aggregator(x, **kw) for x in diff])
+    if mode == "normalized":
+        return np.sum(dn / np.array([fourier_aggregator(r, **kw) for r in state_ref]))
+    return np.sum(dn)
+
+
+def _fourier_metric(mode, p, q):
+    def metric(u_pred, u_ref=None, *, domain_extent=1.0, low=None, high=None, derivative_order=None):
+        return fourier_norm(u_pred, u_ref, mode=mode, domain_extent=domain_extent, inner_exponent=p,
+                            outer_exponent=q, low=low, high=high, derivative_order=derivative_order)
+    return metric
+
+
+# metrics/_fourier.py:238-592
+fourier_MAE = _fourier_metric("absolute", 1.0, 1.0)
+fourier_nMAE = _fourier_metric("normalized", 1.0, 1.0)
+fourier_MSE = _fourier_metric("absolute", 2.0, 1.0)
+fourier_nMSE = _fourier_metric("normalized", 2.0, 1.0)
+fourier_RMSE = _fourier_metric("absolute", 2.0, 0.5)
+fourier_nRMSE = _fourier_metric("normalized", 2.0, 0.5)
+
+
+def _h1(fm):
+    def metric(u_pred, u_ref=None, *, domain_extent=1.0, low=None, high=None):
+        kw = dict(domain_extent=domain_extent, low=low, high=high)
+        return fm(u_pred, u_ref, derivative_order=None, **kw) + fm(u_pred, u_ref, derivative_order=1, **kw)
+    return metric
+
+
+# metrics/_derivative.py:13-368: the Fourier metric plus that of the first derivative
+H1_MAE = _h1(fourier_MAE)
+H1_nMAE = _h1(fourier_nMAE)
+H1_MSE = _h1(fourier_MSE)
+H1_nMSE = _h1(fourier_nMSE)
+H1_RMSE = _h1(fourier_RMSE)
+H1_nRMSE = _h1(fourier_nRMSE)
+
+
 def correlation(u_pred, u_ref):
     """metrics/_correlation.py:33-60: channel-mean of normalised inner products."""
     vals = []

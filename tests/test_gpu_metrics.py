@@ -67,3 +67,62 @@ def test_nrmse_and_correlation():
     assert isinstance(metrics.nRMSE(pred, ref), float)
     mm = metrics.mean_metric(metrics.nRMSE, torch.from_numpy(pred[None]).cuda(), torch.from_numpy(ref[None]).cuda())
     assert abs(float(mm) - want_n) <= 1e-6 * want_n
+
+
+SPATIAL = ["MAE", "nMAE", "sMAE", "MSE", "nMSE", "sMSE", "RMSE", "nRMSE", "sRMSE"]
+FOURIER = ["fourier_MAE", "fourier_nMAE", "fourier_MSE", "fourier_nMSE", "fourier_RMSE", "fourier_nRMSE"]
+H1 = ["H1_MAE", "H1_nMAE", "H1_MSE", "H1_nMSE", "H1_RMSE", "H1_nRMSE"]
+
+
+def _pair(D, N, C, key):
+    rng = np.random.default_rng(key)
+    a = rng.standard_normal((C,) + (N,) * D).astype(np.float32)
+    b = (a + 0.3 * rng.standard_normal(a.shape)).astype(np.float32)
+    return a, b
+
+
+@pytest.mark.parametrize("D,N", [(1, 64), (2, 32), (3, 12)])
+def test_metric_families_match_oracle(D, N):
+    """Every spatial, Fourier and H1 metric (metrics/_spatial.py, _fourier.py, _derivative.py) on
+    two-channel random fields against the oracle: 1e-5 relative; also without a reference where the
+    metric allows it, with a band (low, high) and a derivative order, and on device tensors."""
+    a, b = _pair(D, N, 2, 10 * D)
+    for name in SPATIAL:
+        got, want = getattr(ex.metrics, name)(a, b, domain_extent=2.0), getattr(o, name)(a, b, domain_extent=2.0)
+        assert abs(got - want) <= 1e-5 * abs(want), (name, got, want)
+    for name in FOURIER + H1:
+        for kw in (dict(), dict(low=2, high=N // 4), dict(high=3)):
+            got = getattr(ex.metrics, name)(a, b, domain_extent=2.0, **kw)
+            want = getattr(o, name)(a, b, domain_extent=2.0, **kw)
+            assert abs(got - want) <= 1e-5 * abs(want), (name, kw, got, want)
+    for name in ("MAE", "MSE", "RMSE", "fourier_MAE", "fourier_MSE", "fourier_RMSE", "H1_MSE"):
+        got, want = getattr(ex.metrics, name)(a), getattr(o, name)(a)
+        assert abs(got - want) <= 1e-5 * abs(want), (name, got, want)
+    for order in (0, 1, 2, 1.5):
+        got = ex.metrics.fourier_nRMSE(a, b, derivative_order=order)
+        want = o.fourier_nRMSE(a, b, derivative_order=order)
+        assert abs(got - want) <= 1e-5 * abs(want), (order, got, want)
+    t = ex.metrics.sMSE(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda())
+    assert isinstance(t, torch.Tensor) and abs(float(t) - o.sMSE(a, b)) <= 1e-5 * o.sMSE(a, b)
+    for p in (1.0, 3.0):
+        got = ex.metrics.spatial_norm(a, b, mode="normalized", inner_exponent=p, outer_exponent=1 / p)
+        want = o.spatial_norm(a, b, mode="normalized", inner_exponent=p, outer_exponent=1 / p)
+        assert abs(got - want) <= 1e-5 * abs(want), (p, got, want)
+    with pytest.raises(ValueError):
+        ex.metrics.nMSE(a)
+
+
+def test_fourier_and_spatial_norms_agree_by_parseval():
+    """Size-independent property: the Fourier (R)MSE equals the spatial one (Parseval) for 256^2 fields."""
+    a, b = _pair(2, 256, 1, 3)
+    for fs, ss in (("fourier_MSE", "MSE"), ("fourier_nRMSE", "nRMSE")):
+        f, s = getattr(ex.metrics, fs)(a, b), getattr(ex.metrics, ss)(a, b)
+        assert abs(f - s) <= 1e-5 * abs(s), (fs, f, s)
+
+
+def test_mean_metric_over_a_batch():
+    a = np.stack([_pair(2, 32, 1, k)[0] for k in range(3)])
+    b = np.stack([_pair(2, 32, 1, k)[1] for k in range(3)])
+    got = ex.metrics.mean_metric(ex.metrics.nRMSE, a, b)
+    want = np.mean([o.nRMSE(a[i], b[i]) for i in range(3)])
+    assert abs(got - want) <= 1e-5 * want
