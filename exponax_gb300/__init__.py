@@ -11,7 +11,7 @@ CUDA, C ABI in include/exgb.h); there is no CPU fallback.
 from . import etdrk, ic, metrics, nonlin_fun, poisson, spectral, stepper
 from ._lib import ExgbError
 from ._utils import ForcedStepper, RepeatedStepper, make_grid, repeat, rollout, vmap
-from .interpolation import map_between_resolutions
+from .interpolation import FourierInterpolator, map_between_resolutions
 from .metrics import get_spectrum
 from .spectral import fft, ifft
 from .stepper import BaseStepper
@@ -22,6 +22,7 @@ __all__ = [
     "BaseStepper",
     "ExgbError",
     "ForcedStepper",
+    "FourierInterpolator",
     "RepeatedStepper",
     "etdrk",
     "fft",

@@ -96,6 +96,7 @@ SIGNATURES = [
     ("exgb_repeat_fourier_noalloc", _I, [_VP, _VP, _VP, _VP, _I64, _I32]),
     ("exgb_queue_rollout", _I, [ctypes.POINTER(WorkItem), _I64, _I32, _I32, _VP]),
     ("exgb_map_between_resolutions", _I, [_VP, _I, _I, _I, _I64, _VP, _VP, _I]),
+    ("exgb_fourier_interp", _I, [_VP, _I, _I, _I, _VP, ctypes.c_float, _I64, _VP, _VP]),
     ("exgb_leray", _I, [_VP, _I, _I, ctypes.c_double, _I64, _VP, _VP]),
     ("exgb_plan_tune", _I, [_VP, _I, ctypes.POINTER(_I), _I]),
     ("exgb_plan_get_tuning", _I, [_VP, ctypes.POINTER(_I), _I]),

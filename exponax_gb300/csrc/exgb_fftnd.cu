@@ -342,11 +342,77 @@ __global__ void resample_kernel(int D, int n_old, int n_new, int64_t count, cons
   }
 }
 
+// FourierInterpolator.__call__ (_interpolation.py:22-112) at P points: one warp per point,
+// u_c(x) = Re sum_modes c_scaled[c][mode] exp(i (k_0 x_0 + ... + k_{D-1} x_{D-1})) with the
+// scaled wavenumbers k_d = 2 pi n_d / L ('ij' grid, rfftfreq on the last axis).  The phase is
+// summed over the axes in FP32 in axis order and exp taken by sincosf, as the reference forms
+// exp(sum_d i k_d x_d); the per-lane partial sums are FP32, combined by a warp reduction.
+__global__ void __launch_bounds__(256) fourier_interp_kernel(int D, int N, int C, int64_t per,
+                                                             const float2* __restrict__ coef, float kscale,
+                                                             int64_t P, const float* __restrict__ x,
+                                                             float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t pt = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (pt >= P) return;  // whole warps exit together (P indexes warps)
+  const int M = N / 2 + 1;
+  float xs[3] = {0.f, 0.f, 0.f};
+  for (int d = 0; d < D; ++d) xs[d] = x[pt * D + d];
+  constexpr int kMaxC = 8;
+  for (int c0 = 0; c0 < C; c0 += kMaxC) {
+    const int nc = min(kMaxC, C - c0);
+    float acc[kMaxC];
+    for (int c = 0; c < kMaxC; ++c) acc[c] = 0.f;
+    for (int64_t r = lane; r < per; r += 32) {
+      int k[3] = {0, 0, 0};
+      k[D - 1] = (int)(r % M);
+      int64_t rest = r / M;
+      for (int a = D - 2; a >= 0; --a) {
+        const int i = (int)(rest % N);
+        rest /= N;
+        k[a] = (i <= (N - 1) / 2) ? i : i - N;
+      }
+      float th = 0.f;
+      for (int a = 0; a < D; ++a) th += (kscale * (float)k[a]) * xs[a];
+      float sn, cs;
+      sincosf(th, &sn, &cs);
+      for (int c = 0; c < nc; ++c) {
+        const float2 v = coef[(int64_t)(c0 + c) * per + r];
+        acc[c] += v.x * cs - v.y * sn;
+      }
+    }
+    for (int c = 0; c < nc; ++c) {
+      float v = acc[c];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) out[pt * C + c0 + c] = v;
+    }
+  }
+}
+
 }  // namespace exgb
 
 using namespace exgb;
 
 extern "C" {
+
+int exgb_fourier_interp(void* stream, int num_spatial_dims, int num_points, int num_channels, const void* coef,
+                        float domain_extent, int64_t num_queries, const float* x, float* out) {
+  const int D = num_spatial_dims, N = num_points, C = num_channels;
+  if (!coef || !x || !out) return fail(EXGB_EINVAL, "exgb_fourier_interp: NULL pointer");
+  if (D < 1 || D > 3 || N < 1 || C < 1) return fail(EXGB_ESHAPE, "exgb_fourier_interp: bad shape");
+  if (num_queries < 0 || !(domain_extent > 0.f)) return fail(EXGB_EINVAL, "exgb_fourier_interp: bad arguments");
+  if (num_queries == 0) return EXGB_OK;
+  int64_t per = N / 2 + 1;
+  for (int d = 0; d < D - 1; ++d) per *= N;
+  const float kscale = (float)(2.0 * 3.14159265358979323846 / (double)domain_extent);
+  const int64_t threads = num_queries * 32;
+  const int64_t blocks = (threads + 255) / 256;
+  if (blocks > 2147483647LL) return fail(EXGB_EINVAL, "exgb_fourier_interp: too many query points");
+  fourier_interp_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(D, N, C, per, (const float2*)coef, kscale,
+                                                                           num_queries, x, out);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
 
 int exgb_rfftn(void* stream, int num_spatial_dims, int num_points, int64_t count, const float* in, void* out) {
   if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");

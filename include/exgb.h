@@ -225,6 +225,12 @@ int exgb_leray(void* stream, int num_spatial_dims, int num_points, double domain
  * spectral re-sampling of count = B*C fields from N_old to N_new points. */
 int exgb_map_between_resolutions(void* stream, int num_spatial_dims, int n_old, int n_new,
                                  int64_t count, const float* in, float* out, int oddball_zero);
+/* exgb_fourier_interp replaces FourierInterpolator.__call__ (_interpolation.py:22-112) at
+ * num_queries points x (num_queries, D) float32: out (num_queries, C) = Re sum over the rfftn modes
+ * of coef[c][mode] exp(i k . x), k the scaled wavenumbers 2 pi n / domain_extent; coef (C, N...,
+ * N/2+1) complex64 is the rfftn of the state divided by the "reconstruction" scaling array. */
+int exgb_fourier_interp(void* stream, int num_spatial_dims, int num_points, int num_channels, const void* coef,
+                        float domain_extent, int64_t num_queries, const float* x, float* out);
 
 /* ---- evaluation ----
  * exgb_spectrum replaces get_spectrum (_spectral.py:866-1030) on count = B*C

@@ -1176,6 +1176,24 @@ class RepeatedStepper:
 # --------------------------------------------------------------------------
 
 
+class FourierInterpolator:
+    """_interpolation.py:22-112: Re sum (rfftn(state) / reconstruction scaling) exp(i k . x) per channel."""
+
+    def __init__(self, state, *, domain_extent=1.0):
+        self.num_spatial_dims = state.ndim - 1
+        self.num_points = state.shape[-1]
+        dtype = "float64" if state.dtype == np.float64 else "float32"
+        self.state_hat_scaled = fft(state, num_spatial_dims=self.num_spatial_dims) / build_scaling_array(
+            self.num_spatial_dims, self.num_points, mode="reconstruction", dtype=dtype)
+        self.wavenumbers = build_scaled_wavenumbers(self.num_spatial_dims, domain_extent, self.num_points, dtype=dtype)
+
+    def __call__(self, x):
+        D = self.num_spatial_dims
+        xb = np.asarray(x, dtype=self.wavenumbers.dtype).reshape((D,) + (1,) * D)
+        e = np.exp(np.sum(1j * self.wavenumbers * xb, axis=0))[None]
+        return np.real(np.sum((self.state_hat_scaled * e).reshape(self.state_hat_scaled.shape[0], -1), axis=1))
+
+
 def map_between_resolutions(state, new_num_points, *, oddball_zero=True):
     """_interpolation.py:195-285"""
     D = state.ndim - 1

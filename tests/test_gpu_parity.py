@@ -446,3 +446,32 @@ def test_wave_conserves_energy_and_drifts_the_mean():
     out = host(ex.repeat(sm, 500)(cu(u)))
     assert abs(energy(out) - energy(u)) / energy(u) < 3e-5
     assert abs(float(out[0].mean()) - (float(u[0].mean()) + 500 * dt * float(u[1].mean()))) < 1e-4
+
+
+# ------------------------------------------------------------------ FourierInterpolator (_interpolation.py)
+
+@pytest.mark.parametrize("D,N,L", [(1, 64, 2.0), (2, 32, 1.0), (2, 15, 3.0), (3, 12, 2 * np.pi)])
+def test_fourier_interpolator_matches_oracle(D, N, L):
+    """Random points of the domain, three channels of a smooth random field: within 5e-5 max|u| of the
+    float64 oracle (FP32 phases k.x up to pi N, as in the reference) and of the float32 oracle; at the
+    grid points the interpolant returns the grid values (1e-5 max|u|); one point and vmap agree."""
+    g = ex.ic.RandomTruncatedFourierSeries(D, cutoff=4, max_one=True)
+    u = np.concatenate([g(N, key=k) for k in range(3)]).astype(np.float32)
+    fi = ex.FourierInterpolator(cu(u), domain_extent=L)
+    fo64 = o.FourierInterpolator(u.astype(np.float64), domain_extent=L)
+    fo32 = o.FourierInterpolator(u, domain_extent=L)
+    pts = np.random.default_rng(D).uniform(0, L, (200, D)).astype(np.float32)
+    got = host(ex.vmap(fi)(cu(pts)))
+    assert got.shape == (200, 3)
+    want64 = np.stack([fo64(p.astype(np.float64)) for p in pts])
+    want32 = np.stack([fo32(p) for p in pts])
+    scale = float(np.abs(u).max())
+    assert np.abs(got - want64).max() < 5e-5 * scale
+    assert np.abs(got - want32).max() < 5e-5 * scale
+    one = host(fi(cu(pts[7])))
+    np.testing.assert_allclose(one, got[7], rtol=0, atol=1e-6 * scale)
+    grid = ex.make_grid(D, L, N).reshape(D, -1).T
+    sel = grid[:: max(1, grid.shape[0] // 100)]
+    at = host(ex.vmap(fi)(cu(np.ascontiguousarray(sel))))
+    flat = u.reshape(3, -1).T[:: max(1, grid.shape[0] // 100)]
+    assert np.abs(at - flat).max() < 1e-5 * scale
