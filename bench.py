@@ -60,9 +60,9 @@ def config(extra=None):
 
 
 def make_ics(b0, count):
-    from exponax_gb300.ic import RandomTruncatedFourierSeries
+    from exponax_gb300.ic import RandomAmplitudePhaseSeries
 
-    g = RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    g = RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
     return np.stack([g(N, key=s) for s in range(b0, b0 + count)])
 
 
@@ -475,7 +475,7 @@ def run_other(args, rank, ws):
         st = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, Nk, 0.01)
         if args.precision != "fp32":
             st.set_dft_precision(args.precision)
-        g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+        g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
         u0h = np.stack([g(Nk, key=s) for s in range(B)])
         uh = ex.fft(torch.from_numpy(u0h).cuda(), num_spatial_dims=2)
         out = torch.empty_like(uh)

@@ -35,8 +35,10 @@ __global__ void scatter_kernel(int64_t count, int64_t field_elems, int nmodes, c
   }
 }
 
-// one CTA per field: FP64 mean, then (std_one) the FP64 population standard deviation of u - mean or
-// (max_one) max |u - mean|, then the rescale -- normalize_ic (ic/_base_ic.py:18-32) in its order
+// one CTA per field: FP64 mean, then (std_one) the FP64 population standard deviation or (max_one)
+// max |u - mean|, then (u - mean) * scale with the mean subtracted only when zero_mean -- normalize_ic
+// (ic/_base_ic.py:18-32) in its order; std_one without zero_mean divides by the standard deviation
+// alone, as SineWaves1d does (ic/_sine_waves_1d.py:72-77)
 __global__ void __launch_bounds__(256) normalize_kernel(int64_t n, float* u, int zero_mean, int std_one,
                                                         int max_one) {
   float* p = u + (int64_t)blockIdx.x * n;
@@ -44,20 +46,21 @@ __global__ void __launch_bounds__(256) normalize_kernel(int64_t n, float* u, int
   __shared__ float redf[8];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double s = 0.0;
-  if (zero_mean)
+  if (zero_mean || std_one)
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += p[i];
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) red[w] = s;
   __syncthreads();
   double tot = 0.0;
   for (int i = 0; i < nw; ++i) tot += red[i];
-  const float mean = zero_mean ? (float)(tot / (double)n) : 0.f;
+  const float fmean = (float)(tot / (double)n);
+  const float mean = zero_mean ? fmean : 0.f;
   __syncthreads();  // red is reused below
   float inv = 1.f;
   if (std_one) {
     double q = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-      const double d = (double)(p[i] - mean);
+      const double d = (double)(p[i] - fmean);
       q += d * d;
     }
     for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
@@ -142,8 +145,6 @@ extern "C" int exgb_normalize_fields(void* stream, int64_t count, int64_t n, flo
                                      int max_one) {
   if (!u) return fail(EXGB_EINVAL, "exgb_normalize_fields: NULL pointer");
   if (count < 0 || n <= 0) return fail(EXGB_EINVAL, "exgb_normalize_fields: bad size");
-  // validate_normalization_options (ic/_base_ic.py:8-13)
-  if (std_one && !zero_mean) return fail(EXGB_EINVAL, "Cannot have `zero_mean=False` and `std_one=True`.");
   if (std_one && max_one) return fail(EXGB_EINVAL, "Cannot have `std_one=True` and `max_one=True`.");
   if (count == 0) return EXGB_OK;
   if (count > 2147483647LL) return fail(EXGB_EINVAL, "exgb_normalize_fields: too many fields for one launch");

@@ -47,7 +47,7 @@ def fine_coarse_trajectories(seeds, *, n_fine=512, n_coarse_grid=64, dt=0.001, r
     fine = stepper.KolmogorovFlowVorticity(2, 2 * np.pi, n_fine, dt, **KW)
     h = fine.plan.handle
     lib = load()
-    g = ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    g = ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
     out = torch.empty((len(seeds), n_coarse + 1, n_coarse_grid, n_coarse_grid), dtype=torch.float32, device="cuda")
     fine_ms = 0.0
     for b0 in range(0, len(seeds), batch):

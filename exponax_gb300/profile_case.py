@@ -39,7 +39,7 @@ def main():
         st = cls(2, 2 * np.pi, a.n, 0.01, order=a.order, **kw)
         if a.precision != "fp32":
             st.set_dft_precision(a.precision)
-        g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+        g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
     else:
         st = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, a.n, 0.1, order=a.order)
         g = ex.ic.RandomSineWaves1d(1, cutoff=5)

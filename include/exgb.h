@@ -262,9 +262,9 @@ int exgb_fourier_pnorms(void* stream, int num_spatial_dims, int num_points, int6
  * exgb_scatter_modes: zero count Fourier fields of field_elems complex64 each, then write
  *   vals[f * nmodes + m] at element idx[m] of field f (random-series initial conditions).
  * exgb_normalize_fields: per field of n floats subtract the mean (zero_mean), then divide by
- *   the population standard deviation (std_one) or by max |u| (max_one) -- normalize_ic
- *   (ic/_base_ic.py:18-32); std_one without zero_mean, or with max_one, is EXGB_EINVAL as
- *   validate_normalization_options (ic/_base_ic.py:8-13) raises. */
+ *   the population standard deviation (std_one) or by max |u - mean| (max_one) -- normalize_ic
+ *   (ic/_base_ic.py:18-32); std_one without zero_mean divides by the standard deviation without
+ *   centring (SineWaves1d, ic/_sine_waves_1d.py:72-77); std_one with max_one is EXGB_EINVAL. */
 int exgb_axpy(void* stream, int64_t n, float alpha, const float* x, const float* y, float* out);
 int exgb_scatter_modes(void* stream, int64_t count, int64_t field_elems, int nmodes, const int64_t* idx,
                        const void* vals, void* hat);

@@ -1233,6 +1233,21 @@ def normalize_ic(ic, *, zero_mean=True, std_one=False, max_one=False):
     return ic
 
 
+def truncated_fourier_series_from_noise(noise, *, num_spatial_dims, cutoff=5, offset=0.0, zero_mean=True,
+                                        std_one=False, max_one=False):
+    """ic/_truncated_fourier_series.py:65-100 on a given white-noise field (1, N, ..., N): rfftn, the
+    hypercube low-pass |k_d| <= cutoff, the first coefficient set to `offset`, irfftn, normalize_ic."""
+    D = num_spatial_dims
+    N = noise.shape[-1]
+    dtype = "float64" if noise.dtype == np.float64 else "float32"
+    hat = fft(noise, num_spatial_dims=D) * low_pass_filter_mask(D, N, cutoff=cutoff, axis_separate=True, dtype=dtype)
+    shape = hat.shape
+    hat = hat.reshape(-1)
+    hat[0] = offset
+    ic = ifft(hat.reshape(shape), num_spatial_dims=D, num_points=N)
+    return normalize_ic(ic, zero_mean=zero_mean, std_one=std_one, max_one=max_one)
+
+
 def gaussian_random_field_from_noise(noise, *, num_spatial_dims, domain_extent=1.0, powerlaw_exponent=3.0,
                                      zero_mean=True, std_one=False, max_one=False):
     """ic/_gaussian_random_field.py:60-93 applied to a given white-noise field (1, N, ..., N):

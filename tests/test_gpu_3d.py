@@ -30,7 +30,7 @@ def host(t):
 
 def velocity_ic(N, key, L=2 * np.pi):
     """Smooth random divergence-free velocity (3, N, N, N), float32."""
-    g = ex.ic.RandomTruncatedFourierSeries(3, cutoff=3, max_one=True)
+    g = ex.ic.RandomAmplitudePhaseSeries(3, cutoff=3, max_one=True)
     u = np.concatenate([g(N, key=3 * key + c) for c in range(3)], axis=0).astype(np.float64)
     d = o.build_derivative_operator(3, L, N, dtype="float64")
     P = o.Leray(3, N, derivative_operator=d, dtype="float64")

@@ -37,7 +37,7 @@ def test_tune_apply_cache_and_parity(case, tmp_path, monkeypatch):
     else:
         sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, 128, 0.01, diffusivity=1e-3)
         so = o.NavierStokesVorticity(2, 2 * np.pi, 128, 0.01, diffusivity=1e-3)
-        g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+        g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
         u = np.stack([g(128, key=s) for s in range(3)])
     res = autotune.tune(sm, batch=32, nsteps=4, repeats=2)
     assert not res["cached"] and res["best"] and len(res["timings_ms"]) >= 2
@@ -58,7 +58,7 @@ def test_every_cluster_size_matches_oracle(n):
     from exponax_gb300._lib import EXGB_OK
     sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
     so = o.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
-    g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
     u = np.stack([g(n, key=s) for s in range(3)])
     want = [so(u[b]) for b in range(3)]
     ran = []

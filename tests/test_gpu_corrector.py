@@ -107,7 +107,7 @@ def test_guard_trips_on_energetic_corrections():
     from exponax_gb300.learned import GuardedCorrectedStepper, PeriodicConvCorrector
 
     st = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.04)
-    g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
     u = torch.from_numpy(np.stack([g(64, key=s) for s in range(4)])).cuda()
     plain = ex.vmap(st)(u)
     quiet = PeriodicConvCorrector(64, seed=0, max_batch=4, out_scale=1e-6)

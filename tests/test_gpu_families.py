@@ -35,7 +35,7 @@ def host(t):
 
 
 def field(D, N, C, key, cutoff=4):
-    g = ex.ic.RandomTruncatedFourierSeries(D, cutoff=cutoff, max_one=True)
+    g = ex.ic.RandomAmplitudePhaseSeries(D, cutoff=cutoff, max_one=True)
     return np.concatenate([g(N, key=7 * key + c) for c in range(C)], axis=0).astype(np.float32)
 
 

@@ -31,7 +31,7 @@ def _case(name):
     else:
         args, kw = (2, 2 * np.pi, 64, 0.01), {"diffusivity": 1e-3}
         sm, so = ex.stepper.NavierStokesVorticity(*args, **kw), o.NavierStokesVorticity(*args, **kw)
-        u = np.stack([ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)(64, key=s) for s in range(3)])
+        u = np.stack([ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)(64, key=s) for s in range(3)])
     f = (0.5 * np.random.default_rng(7).standard_normal(u.shape)).astype(np.float32)
     return sm, so, u, f
 
@@ -78,10 +78,10 @@ def test_forced_rollout_matches_oracle(name, constant):
 
 @pytest.mark.parametrize("gen,N", [
     (ex.ic.RandomSineWaves1d(1, cutoff=5), 200),
-    (ex.ic.RandomTruncatedFourierSeries(1, cutoff=5), 128),
-    (ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True), 256),
-    (ex.ic.RandomTruncatedFourierSeries(2, cutoff=3), 60),
-    (ex.ic.RandomTruncatedFourierSeries(3, cutoff=2, max_one=True), 32),
+    (ex.ic.RandomAmplitudePhaseSeries(1, cutoff=5), 128),
+    (ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True), 256),
+    (ex.ic.RandomAmplitudePhaseSeries(2, cutoff=3), 60),
+    (ex.ic.RandomAmplitudePhaseSeries(3, cutoff=2, max_one=True), 32),
 ])
 def test_device_ics_match_host_generators(gen, N):
     keys = [0, 1, 17, 123456]
@@ -134,3 +134,23 @@ def test_normalize_ic_on_the_device():
         assert rel(got, o.normalize_ic(u, **kw)) < 1e-6, kw
     with pytest.raises(ValueError):
         ex.ic.normalize_ic(torch.from_numpy(u).cuda(), zero_mean=False, std_one=True)
+
+
+@pytest.mark.parametrize("gen,N", [
+    (ex.ic.RandomTruncatedFourierSeries(1, cutoff=5), 128),
+    (ex.ic.RandomTruncatedFourierSeries(2, cutoff=4, max_one=True), 64),
+    (ex.ic.RandomTruncatedFourierSeries(2, cutoff=3, std_one=True), 48),
+    (ex.ic.RandomTruncatedFourierSeries(3, cutoff=2, offset_range=(-1.0, 1.0)), 16),
+    (ex.ic.RandomSineWaves1d(1, cutoff=4, offset_range=(0.5, 1.0), max_one=True), 100),
+    (ex.ic.RandomSineWaves1d(1, cutoff=6, std_one=True), 64),
+])
+def test_device_ics_reference_recipes(gen, N):
+    """The reference's RandomTruncatedFourierSeries (low-pass-filtered white noise with an offset) and
+    RandomSineWaves1d with offset / std_one / max_one, built on the GPU from the host generator's draws:
+    within 1e-5 relative L2 of the host fields (both FP32 transforms)."""
+    keys = [0, 5, 77]
+    got = gen.device_batch(N, keys).cpu().numpy()
+    for i, k in enumerate(keys):
+        want = gen(N, key=k)
+        assert got[i].shape == want.shape
+        assert rel(got[i], want) < 1e-5, k

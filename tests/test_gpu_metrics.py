@@ -38,7 +38,7 @@ def test_get_spectrum_numpy_in_numpy_out_and_parseval():
     s = metrics.get_spectrum(u)
     assert isinstance(s, np.ndarray)
     # Parseval for a band-limited field (energy inside the Nyquist sphere)
-    g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5)
+    g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5)
     v = g(64, key=1)
     sv = metrics.get_spectrum(v)
     assert abs(float(sv.sum()) - 0.5 * float(np.mean(v.astype(np.float64) ** 2))) < 1e-5 * float(np.mean(v ** 2))

@@ -119,7 +119,7 @@ def test_vorticity_nonlinearity_matches_oracle(N, kolmogorov):
     else:
         fm = ex.nonlin_fun.VorticityConvection2d(2, N, derivative_operator=ex.spectral.build_derivative_operator(2, L, N), dealiasing_fraction=2 / 3)
         fo = o.VorticityConvection2d(2, N, derivative_operator=o.build_derivative_operator(2, L, N), dealiasing_fraction=2 / 3)
-    u = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)(N, key=2)
+    u = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)(N, key=2)
     uh = o.fft(u)
     got = host(fm(cu(uh)))
     want = fo(uh)
@@ -145,7 +145,7 @@ STEP_CASES = [
 def _ic(D, N, key):
     if D == 1:
         return ex.ic.RandomSineWaves1d(1, cutoff=5)(N, key=key)
-    return ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)(N, key=key)
+    return ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)(N, key=key)
 
 
 @pytest.mark.parametrize("name,cls,args,kw", STEP_CASES, ids=[c[0] for c in STEP_CASES])
@@ -397,7 +397,7 @@ def test_poisson_matches_oracle(D, N, order):
 # ------------------------------------------------------------------ Wave (stepper/_wave.py)
 
 def _wave_ic(D, N, key):
-    g = ex.ic.RandomTruncatedFourierSeries(D, cutoff=3, max_one=True)
+    g = ex.ic.RandomAmplitudePhaseSeries(D, cutoff=3, max_one=True)
     return np.concatenate([g(N, key=2 * key), 0.3 * g(N, key=2 * key + 1)]).astype(np.float32)
 
 
@@ -455,7 +455,7 @@ def test_fourier_interpolator_matches_oracle(D, N, L):
     """Random points of the domain, three channels of a smooth random field: within 5e-5 max|u| of the
     float64 oracle (FP32 phases k.x up to pi N, as in the reference) and of the float32 oracle; at the
     grid points the interpolant returns the grid values (1e-5 max|u|); one point and vmap agree."""
-    g = ex.ic.RandomTruncatedFourierSeries(D, cutoff=4, max_one=True)
+    g = ex.ic.RandomAmplitudePhaseSeries(D, cutoff=4, max_one=True)
     u = np.concatenate([g(N, key=k) for k in range(3)]).astype(np.float32)
     fi = ex.FourierInterpolator(cu(u), domain_extent=L)
     fo64 = o.FourierInterpolator(u.astype(np.float64), domain_extent=L)

@@ -64,7 +64,7 @@ def _kolmo(dtype="float32", n=128):
 
 
 def _ics(B, n=128, seed0=0):
-    g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
     return np.stack([g(n, key=seed0 + s) for s in range(B)])
 
 

@@ -133,7 +133,7 @@ def test_reference_errors_raised_at_construction():
 
 
 def test_ic_generators_are_seeded_and_normalised():
-    g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
     a = g(64, key=3)
     b = g(64, key=3)
     np.testing.assert_array_equal(a, b)

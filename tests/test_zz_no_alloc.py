@@ -27,7 +27,7 @@ def test_noalloc_matches_repeat_fourier_on_two_calls(N, order):
 
     lib = _lib.load()
     st = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, N, 0.01, diffusivity=1e-3, order=order)
-    g = ex.ic.RandomTruncatedFourierSeries(2, cutoff=5, max_one=True)
+    g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
     u0 = torch.from_numpy(np.stack([g(N, key=s) for s in range(24)])).cuda()
     uh = ex.fft(u0, num_spatial_dims=2)
     h = st.plan.handle
