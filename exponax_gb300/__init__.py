@@ -10,10 +10,12 @@ CUDA, C ABI in include/exgb.h); there is no CPU fallback.
 
 from . import etdrk, ic, metrics, nonlin_fun, poisson, spectral, stepper
 from ._lib import ExgbError
-from ._utils import ForcedStepper, RepeatedStepper, make_grid, repeat, rollout, vmap
+from ._utils import (ForcedStepper, RepeatedStepper, make_grid, repeat, rollout, stack_sub_trajectories, vmap,
+                     wrap_bc)
+from .ic import build_ic_set
 from .interpolation import FourierInterpolator, map_between_resolutions
 from .metrics import get_spectrum
-from .spectral import fft, ifft
+from .spectral import derivative, fft, ifft
 from .stepper import BaseStepper
 
 __version__ = "0.1.0"
@@ -24,6 +26,8 @@ __all__ = [
     "ForcedStepper",
     "FourierInterpolator",
     "RepeatedStepper",
+    "build_ic_set",
+    "derivative",
     "etdrk",
     "fft",
     "get_spectrum",
@@ -37,6 +41,8 @@ __all__ = [
     "repeat",
     "rollout",
     "spectral",
+    "stack_sub_trajectories",
     "stepper",
     "vmap",
+    "wrap_bc",
 ]

@@ -111,6 +111,8 @@ SIGNATURES = [
     ("exgb_normalize_fields", _I, [_VP, _I64, _I64, _VP, _I, _I, _I]),
     ("exgb_mode_scale", _I, [_VP, _I64, _I64, _VP, _VP, _VP]),
     ("exgb_mode_mix2", _I, [_VP, _I64, _I64, _VP, _VP, _VP, _I]),
+    ("exgb_spectral_derivative", _I, [_VP, _I, _I, _I64, _I, ctypes.c_float, _VP, _VP]),
+    ("exgb_make_incompressible", _I, [_VP, _I, _I, _I64, _VP, _VP]),
     ("exgb_queue_prepare", _I, [ctypes.POINTER(WorkItem), _I64, _I32, _I32, ctypes.POINTER(_VP)]),
     ("exgb_queue_launch", _I, [_VP, _VP]),
     ("exgb_queue_destroy", _I, [_VP]),

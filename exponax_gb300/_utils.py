@@ -28,6 +28,60 @@ def make_grid(num_spatial_dims: int, domain_extent: float, num_points: int, *, f
     return np.stack(np.meshgrid(*([g] * num_spatial_dims), indexing="ij")).astype(np.float32)
 
 
+def wrap_bc(u):
+    """_utils.py:65-89: a state (C, N, ..., N) padded periodically to (C, N+1, ..., N+1) (the first point
+    of every spatial axis repeated at its end), for plotting on closed grids."""
+    t = _device.torch()
+    if isinstance(u, t.Tensor):
+        out = u
+        for ax in range(1, u.ndim):
+            out = t.cat([out, out.narrow(ax, 0, 1)], dim=ax)
+        return out
+    u = np.asarray(u)
+    return np.pad(u, ((0, 0),) + ((0, 1),) * (u.ndim - 1), mode="wrap")
+
+
+def stack_sub_trajectories(trj, sub_len: int):
+    """_utils.py:257-313: all windows of sub_len consecutive time steps of a trajectory (n, ...) ->
+    (n - sub_len + 1, sub_len, ...); a tuple / list / dict of trajectories is mapped leaf by leaf
+    (all leaves must have the same number of time steps)."""
+    t = _device.torch()
+    leaves = []
+
+    def collect(x):
+        if isinstance(x, dict):
+            for v in x.values():
+                collect(v)
+        elif isinstance(x, (list, tuple)):
+            for v in x:
+                collect(v)
+        else:
+            leaves.append(x)
+
+    collect(trj)
+    steps = {int(x.shape[0]) for x in leaves}
+    if len(steps) != 1:
+        raise ValueError("All arrays in trj must have the same number of time steps in the leading axis")
+    n = steps.pop()
+    if sub_len > n:
+        raise ValueError("n must be smaller than or equal to the number of time steps in trj")
+
+    def windows(x):
+        if isinstance(x, t.Tensor):
+            return t.stack([x[i:i + sub_len] for i in range(n - sub_len + 1)])
+        x = np.asarray(x)
+        return np.stack([x[i:i + sub_len] for i in range(n - sub_len + 1)])
+
+    def rebuild(x):
+        if isinstance(x, dict):
+            return {k: rebuild(v) for k, v in x.items()}
+        if isinstance(x, (list, tuple)):
+            return type(x)(rebuild(v) for v in x)
+        return windows(x)
+
+    return rebuild(trj)
+
+
 class _Rollout:
     def __init__(self, stepper_fn, n, include_init):
         self.stepper_fn = stepper_fn

@@ -9,6 +9,9 @@
 //                         reference _poisson.py:67-82)
 //   exgb_mode_mix2        per-mode real 2x2 map of two-channel Fourier fields, repeated (Wave,
 //                         reference stepper/_wave.py)
+//   exgb_spectral_derivative, exgb_make_incompressible
+//                         spectral.derivative and spectral.make_incompressible in Fourier space
+//                         (reference _spectral.py:724-863)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -112,6 +115,65 @@ __global__ void mode_mix2_kernel(int64_t count, int64_t per, const float* __rest
   }
 }
 
+// signed integer wavenumbers of rfftn mode r of an (N..., N/2+1) field with D axes ('ij', rfftfreq last)
+__device__ __forceinline__ void mode_wavenumbers(int D, int N, int64_t r, int (&k)[3]) {
+  const int M = N / 2 + 1;
+  k[0] = k[1] = k[2] = 0;
+  k[D - 1] = (int)(r % M);
+  int64_t rest = r / M;
+  for (int a = D - 2; a >= 0; --a) {
+    const int i = (int)(rest % N);
+    rest /= N;
+    k[a] = (i <= (N - 1) / 2) ? i : i - N;
+  }
+}
+
+// (i k)^order u^ for every axis: out[f][d][r] = (i kscale k_d)^order in[f][r] (spectral.derivative,
+// reference _spectral.py:724-791); the integer power is taken by repeated multiplication
+__global__ void derivative_kernel(int D, int N, int64_t count, int64_t per, int order, float kscale,
+                                  const float2* __restrict__ in, float2* __restrict__ out) {
+  const int64_t n = count * per;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = i / per, r = i - f * per;
+    int k[3];
+    mode_wavenumbers(D, N, r, k);
+    const float2 u = in[i];
+    for (int d = 0; d < D; ++d) {
+      const float2 ik = make_float2(0.f, kscale * (float)k[d]);
+      float2 m = make_float2(1.f, 0.f);
+      for (int q = 0; q < order; ++q) m = cmul(m, ik);
+      out[(f * D + d) * per + r] = cmul(m, u);
+    }
+  }
+}
+
+// Leray projection of count samples of D velocity spectra (make_incompressible, _spectral.py:794-863):
+// div = sum_d i k_d u_d, p = div / Lap (1 / Lap taken as 1 where Lap = 0), u_d -= i k_d p
+__global__ void incompressible_kernel(int D, int N, int64_t count, int64_t per, float kscale,
+                                      const float2* __restrict__ in, float2* __restrict__ out) {
+  const int64_t n = count * per;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / per, r = i - b * per;
+    int k[3];
+    mode_wavenumbers(D, N, r, k);
+    float ks[3];
+    float lap = 0.f;
+    float2 div = make_float2(0.f, 0.f);
+    for (int d = 0; d < D; ++d) {
+      ks[d] = kscale * (float)k[d];
+      lap -= ks[d] * ks[d];
+      const float2 u = in[(b * D + d) * per + r];
+      div = cadd(div, make_float2(-ks[d] * u.y, ks[d] * u.x));
+    }
+    const float il = (lap == 0.f) ? 1.f : 1.f / lap;
+    const float2 pp = cscale(div, il);
+    for (int d = 0; d < D; ++d) {
+      const float2 u = in[(b * D + d) * per + r];
+      out[(b * D + d) * per + r] = csub(u, make_float2(-ks[d] * pp.y, ks[d] * pp.x));
+    }
+  }
+}
+
 int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 152 * 16); }
 
 }  // namespace
@@ -171,6 +233,43 @@ extern "C" int exgb_mode_mix2(void* stream, int64_t count, int64_t per, const fl
   if (count == 0) return EXGB_OK;
   mode_mix2_kernel<<<grid_for(count * per), 256, 0, (cudaStream_t)stream>>>(
       count, per, mat, (const float2*)in, (float2*)out, nsteps);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+static int64_t modes_per_field(int D, int N) {
+  int64_t per = N / 2 + 1;
+  for (int d = 0; d < D - 1; ++d) per *= N;
+  return per;
+}
+
+extern "C" int exgb_spectral_derivative(void* stream, int num_spatial_dims, int num_points, int64_t count,
+                                        int order, float domain_extent, const void* in, void* out) {
+  const int D = num_spatial_dims, N = num_points;
+  if (!in || !out) return fail(EXGB_EINVAL, "exgb_spectral_derivative: NULL pointer");
+  if (D < 1 || D > 3 || N < 1) return fail(EXGB_ESHAPE, "exgb_spectral_derivative: 1 to 3 axes of N >= 1 points");
+  if (count < 0 || order < 0 || !(domain_extent > 0.f)) return fail(EXGB_EINVAL, "exgb_spectral_derivative: bad arguments");
+  if (count == 0) return EXGB_OK;
+  const int64_t per = modes_per_field(D, N);
+  const float ks = (float)(2.0 * 3.14159265358979323846 / (double)domain_extent);
+  derivative_kernel<<<grid_for(count * per), 256, 0, (cudaStream_t)stream>>>(D, N, count, per, order, ks,
+                                                                             (const float2*)in, (float2*)out);
+  EXGB_CUDA(cudaGetLastError());
+  return EXGB_OK;
+}
+
+extern "C" int exgb_make_incompressible(void* stream, int num_spatial_dims, int num_points, int64_t count,
+                                        const void* in, void* out) {
+  const int D = num_spatial_dims, N = num_points;
+  if (!in || !out) return fail(EXGB_EINVAL, "exgb_make_incompressible: NULL pointer");
+  if (D < 1 || D > 3 || N < 1) return fail(EXGB_ESHAPE, "exgb_make_incompressible: 1 to 3 axes of N >= 1 points");
+  if (count < 0) return fail(EXGB_EINVAL, "exgb_make_incompressible: negative count");
+  if (count == 0) return EXGB_OK;
+  const int64_t per = modes_per_field(D, N);
+  // the projection does not depend on the domain extent: the reference evaluates it with L = 1
+  const float ks = (float)(2.0 * 3.14159265358979323846);
+  incompressible_kernel<<<grid_for(count * per), 256, 0, (cudaStream_t)stream>>>(D, N, count, per, ks,
+                                                                                 (const float2*)in, (float2*)out);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }

@@ -168,3 +168,65 @@ def ifft(field_hat, *, num_spatial_dims: int | None = None, num_points: int | No
     out = _device.empty(tuple(lead) + spatial_shape(D, N), "float32")
     check(load().exgb_irfftn(_device.stream(), D, N, count, _device.ptr(t), _device.ptr(out)), "ifft")
     return back(out)
+
+
+def derivative(field, domain_extent: float, *, order: int = 1, indexing: str = "ij"):
+    """spectral.derivative (_spectral.py:724-791) on the GPU: every axis' order-th spectral derivative of a
+    state (C, N, ..., N); (D, N, ...) for one channel, else (C, D, N, ...).  rfftn, the (i k_d)^order
+    multipliers (exgb_spectral_derivative), irfftn."""
+    if indexing != "ij":
+        raise NotImplementedError("only indexing='ij' is supported")
+    if int(order) != order or order < 0:
+        raise ValueError("order must be a non-negative integer")
+    t, back = _device.to_device(field, "float32")
+    C, D, N = t.shape[0], t.ndim - 1, t.shape[-1]
+    hat = fft(t, num_spatial_dims=D).contiguous()
+    dh = _device.empty((C, D) + wavenumber_shape(D, N), "complex64")
+    check(load().exgb_spectral_derivative(_device.stream(), D, N, C, int(order), float(domain_extent),
+                                          _device.ptr(hat), _device.ptr(dh)), "derivative")
+    out = ifft(dh, num_spatial_dims=D, num_points=N)
+    return back(out[0] if C == 1 else out)
+
+
+def make_incompressible(field, *, indexing: str = "ij"):
+    """spectral.make_incompressible (_spectral.py:794-863) on the GPU: the divergence-free part of a
+    velocity field (D, N, ..., N) (Leray projection; rfftn, exgb_make_incompressible, irfftn)."""
+    if indexing != "ij":
+        raise NotImplementedError("only indexing='ij' is supported")
+    t, back = _device.to_device(field, "float32")
+    D, N = t.ndim - 1, t.shape[-1]
+    if t.shape[0] != D:
+        raise ValueError(f"Expected the number of channels ({t.shape[0]}) to match the number of spatial "
+                         f"dimensions ({D}).")
+    hat = fft(t, num_spatial_dims=D).contiguous()
+    check(load().exgb_make_incompressible(_device.stream(), D, N, 1, _device.ptr(hat), _device.ptr(hat)),
+          "make_incompressible")
+    return back(ifft(hat, num_spatial_dims=D, num_points=N))
+
+
+def get_fourier_coefficients(state, *, scaling_compensation_mode: str | None = "coef_extraction", round=5,
+                             indexing: str = "ij"):
+    """spectral.get_fourier_coefficients (_spectral.py:1033-1172): rfftn of a state (C, N, ..., N) divided
+    by a scaling array (exgb_mode_scale) and rounded to `round` decimals (None: no rounding)."""
+    if indexing != "ij":
+        raise NotImplementedError("only indexing='ij' is supported")
+    t, back = _device.to_device(state, "float32")
+    D, N = t.ndim - 1, t.shape[-1]
+    hat = fft(t, num_spatial_dims=D).contiguous()
+    if scaling_compensation_mode is not None:
+        sc = build_scaling_array(D, N, mode=scaling_compensation_mode).reshape(-1)
+        table = _device.torch().from_numpy(np.ascontiguousarray((1.0 / sc).astype(np.complex64))).cuda()
+        check(load().exgb_mode_scale(_device.stream(), t.shape[0], table.numel(), _device.ptr(table),
+                                     _device.ptr(hat), _device.ptr(hat)), "get_fourier_coefficients")
+    if round is not None:
+        # round half to even of re and im at `round` decimals, as jnp.round does on complex arrays
+        torch = _device.torch()
+        hat = torch.complex(torch.round(hat.real, decimals=int(round)), torch.round(hat.imag, decimals=int(round)))
+    return back(hat)
+
+
+def get_spectrum(state, **kwargs):
+    """spectral.get_spectrum (_spectral.py:866-1030); see exponax_gb300.metrics.get_spectrum."""
+    from .metrics import get_spectrum as _gs
+
+    return _gs(state, **kwargs)

@@ -282,6 +282,16 @@ int exgb_mode_scale(void* stream, int64_t count, int64_t per, const void* table,
  * the inverse transform composed; the mean mode's h += dt v folded in).  in and out may alias. */
 int exgb_mode_mix2(void* stream, int64_t count, int64_t per, const float* mat, const void* in, void* out,
                    int nsteps);
+/* exgb_spectral_derivative replaces the Fourier-space part of spectral.derivative
+ * (_spectral.py:724-791): out (count, D, N..., N/2+1) = (i 2 pi k_d / domain_extent)^order times
+ * in (count, N..., N/2+1), complex64.
+ * exgb_make_incompressible replaces that of spectral.make_incompressible (_spectral.py:794-863):
+ * for count samples of D velocity spectra (count, D, N..., N/2+1), u_d - i k_d Lap^-1 (sum_j i k_j u_j)
+ * with 1/Lap taken as 1 at k = 0.  in and out may alias for the projection, not for the derivative. */
+int exgb_spectral_derivative(void* stream, int num_spatial_dims, int num_points, int64_t count, int order,
+                             float domain_extent, const void* in, void* out);
+int exgb_make_incompressible(void* stream, int num_spatial_dims, int num_points, int64_t count, const void* in,
+                             void* out);
 
 /* Self-check of the tcgen05 tensor-core layer (no reference counterpart):
  * d (128 x n, FP32) = a (128 x k) . b (n x k)^T, device pointers, row-major.

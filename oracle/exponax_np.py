@@ -193,6 +193,55 @@ def ifft(field_hat, *, num_spatial_dims=None, num_points=None):
     )
 
 
+def derivative(field, domain_extent, *, order=1):
+    """_spectral.py:724-791"""
+    C, D, N = field.shape[0], field.ndim - 1, field.shape[-1]
+    dtype = "float64" if field.dtype == np.float64 else "float32"
+    op = build_derivative_operator(D, domain_extent, N, dtype=dtype) ** order
+    fh = fft(field, num_spatial_dims=D)
+    dh = op * fh if C == 1 else fh[:, None] * op[None, ...]
+    return ifft(dh, num_spatial_dims=D, num_points=N)
+
+
+def make_incompressible(field):
+    """_spectral.py:794-863"""
+    D, N = field.ndim - 1, field.shape[-1]
+    if field.shape[0] != D:
+        raise ValueError("the number of channels must match the number of spatial dimensions")
+    dtype = "float64" if field.dtype == np.float64 else "float32"
+    d = build_derivative_operator(D, 1.0, N, dtype=dtype)
+    uh = fft(field, num_spatial_dims=D)
+    div = np.sum(d * uh, axis=0, keepdims=True)
+    lap = build_laplace_operator(d)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        inv = np.where(lap == 0, 1.0, 1.0 / lap)
+    return ifft(uh - d * (inv * div), num_spatial_dims=D, num_points=N)
+
+
+def get_fourier_coefficients(state, *, scaling_compensation_mode="coef_extraction", round=5):
+    """_spectral.py:1033-1172 (np.round: round half to even, like jnp.round)"""
+    dtype = "float64" if state.dtype == np.float64 else "float32"
+    hat = fft(state)
+    if scaling_compensation_mode is not None:
+        hat = hat / build_scaling_array(state.ndim - 1, state.shape[-1], mode=scaling_compensation_mode, dtype=dtype)
+    if round is not None:
+        hat = np.round(hat, round)
+    return hat
+
+
+def wrap_bc(u):
+    """_utils.py:65-89"""
+    return np.pad(u, ((0, 0),) + ((0, 1),) * (u.ndim - 1), mode="wrap")
+
+
+def stack_sub_trajectories(trj, sub_len):
+    """_utils.py:257-313 for one array trajectory (n, ...)."""
+    n = trj.shape[0]
+    if sub_len > n:
+        raise ValueError("n must be smaller than or equal to the number of time steps in trj")
+    return np.stack([trj[i:i + sub_len] for i in range(n - sub_len + 1)])
+
+
 def make_grid(num_spatial_dims, domain_extent, num_points, *, full=False, zero_centered=False, dtype="float32"):
     """_utils.py:10-62"""
     rd, _ = _dt(dtype)

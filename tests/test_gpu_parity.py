@@ -475,3 +475,55 @@ def test_fourier_interpolator_matches_oracle(D, N, L):
     at = host(ex.vmap(fi)(cu(np.ascontiguousarray(sel))))
     flat = u.reshape(3, -1).T[:: max(1, grid.shape[0] // 100)]
     assert np.abs(at - flat).max() < 1e-5 * scale
+
+
+# ------------------------------------------------------------------ spectral helpers (_spectral.py:724-1172)
+
+@pytest.mark.parametrize("D,N,C,order", [(1, 64, 1, 1), (1, 60, 2, 3), (2, 32, 1, 2), (2, 24, 2, 1), (3, 16, 3, 1)])
+def test_spectral_derivative_matches_oracle(D, N, C, order):
+    """spectral.derivative on random fields against the oracle (1e-5), and the exact derivative of a sine."""
+    rng = np.random.default_rng(D * 7 + order)
+    u = rng.standard_normal((C,) + (N,) * D).astype(np.float32)
+    got = host(ex.derivative(cu(u), 3.0, order=order))
+    want = o.derivative(u, 3.0, order=order)
+    assert got.shape == want.shape
+    assert rel(got, want) < 1e-5
+    g = ex.make_grid(D, 2.0, N)
+    s = np.sin(2 * np.pi / 2.0 * 2 * g[0:1]).astype(np.float32)
+    ds = host(ex.spectral.derivative(cu(s), 2.0, order=1))
+    np.testing.assert_allclose(ds[0], (2 * np.pi / 2.0 * 2) * np.cos(2 * np.pi / 2.0 * 2 * g[0]), atol=1e-4)
+
+
+@pytest.mark.parametrize("D,N", [(1, 32), (2, 32), (2, 25), (3, 16)])
+def test_make_incompressible(D, N):
+    """make_incompressible against the oracle (1e-5) and its size-independent property: the spectral
+    divergence of the result vanishes (relative to that of the input) and projecting twice changes nothing."""
+    u = np.random.default_rng(D).standard_normal((D,) + (N,) * D).astype(np.float32)
+    got = host(ex.spectral.make_incompressible(cu(u)))
+    assert rel(got, o.make_incompressible(u)) < 1e-5
+    # band-limited fields (no Nyquist energy, where the rfft derivative is not antisymmetric)
+    gen = ex.ic.RandomTruncatedFourierSeries(D, cutoff=N // 4)
+    v = np.concatenate([gen(N, key=10 + d) for d in range(D)]).astype(np.float32)
+    pv = host(ex.spectral.make_incompressible(cu(v)))
+    div = lambda f: sum(o.derivative(f[d:d + 1], 1.0)[d] for d in range(D))  # noqa: E731
+    if D > 1:  # in 1D only the (here zero) mean is divergence free
+        assert np.linalg.norm(div(pv.astype(np.float64))) < 1e-4 * np.linalg.norm(div(v.astype(np.float64)))
+        again = host(ex.spectral.make_incompressible(cu(pv)))
+        assert rel(again, pv) < 1e-5
+    with pytest.raises(ValueError):
+        ex.spectral.make_incompressible(cu(u[:1]) if D > 1 else cu(np.stack([u[0], u[0]])))
+
+
+@pytest.mark.parametrize("mode", ["coef_extraction", "reconstruction", "norm_compensation", None])
+def test_get_fourier_coefficients(mode):
+    """get_fourier_coefficients of a known cosine series: the coefficient-extraction amplitudes, and
+    agreement with the oracle (rounded to 5 decimals, so compare at 1e-5 absolute)."""
+    L, N = 2.0, 32
+    g = ex.make_grid(2, L, N)
+    u = (3 * np.cos(2 * np.pi / L * 2 * g[0:1]) + 0.5 * np.sin(2 * np.pi / L * 3 * g[1:2])).astype(np.float32)
+    got = host(ex.spectral.get_fourier_coefficients(cu(u), scaling_compensation_mode=mode))
+    want = o.get_fourier_coefficients(u, scaling_compensation_mode=mode)
+    np.testing.assert_allclose(got, want, atol=1e-5 if mode else 2e-3, rtol=0)
+    if mode == "coef_extraction":
+        assert abs(got[0, 2, 0].real - 3.0) < 1e-5 and abs(got[0, 0, 3].imag + 0.5) < 1e-5
+    assert np.asarray(ex.spectral.get_spectrum(u)).shape == (1, N // 2 + 1)

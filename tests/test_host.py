@@ -158,3 +158,18 @@ def test_instantiate_linear_and_wave_steppers_without_a_gpu():
     np.testing.assert_allclose(m[:, 0], [1.0, 0.1, 0.0, 1.0])
     np.testing.assert_allclose(m[0] * m[3] - m[1] * m[2], 1.0, atol=1e-6)
 
+
+
+def test_wrap_bc_and_sub_trajectories():
+    """_utils.py:65-89 and :257-313 against the oracle (host arrays), with a dict of trajectories."""
+    u = np.random.default_rng(0).standard_normal((2, 5, 4, 4)).astype(np.float32)
+    np.testing.assert_array_equal(ex.wrap_bc(u[0]), o.wrap_bc(u[0]))
+    assert ex.wrap_bc(u[0]).shape == (5, 5, 5)
+    trj = np.random.default_rng(1).standard_normal((7, 1, 8)).astype(np.float32)
+    np.testing.assert_array_equal(ex.stack_sub_trajectories(trj, 3), o.stack_sub_trajectories(trj, 3))
+    d = ex.stack_sub_trajectories({"u": trj, "v": (trj, 2 * trj)}, 4)
+    assert d["u"].shape == (4, 4, 1, 8) and d["v"][1].shape == (4, 4, 1, 8)
+    with pytest.raises(ValueError):
+        ex.stack_sub_trajectories(trj, 8)
+    with pytest.raises(ValueError):
+        ex.stack_sub_trajectories({"a": trj, "b": trj[:5]}, 2)
