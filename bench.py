@@ -146,6 +146,29 @@ def cpu_baseline(samples=None, nsteps=NSTEPS):
                       f"256^2 ETDRK2 problem, one spawn process per sample; slowest worker {wall:.2f} s"}
 
 
+# ------------------------------------------------------------------ float64 check (oracle as the checker)
+def _rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def fp64_check_ns256(st, ex, torch):
+    """Relative L2 of the GPU path against the float64 oracle (stand-in for a JAX float64 run) on the
+    first two initial conditions of the workload, after 1, 20 and 200 steps (outside any timed region)."""
+    from oracle import exponax_np as o
+
+    so = o.NavierStokesVorticity(2, 2 * np.pi, N, DT, diffusivity=NU, dtype="float64")
+    u0 = make_ics(0, 2)
+    got = ex.vmap(ex.rollout(st, NSTEPS))(torch.from_numpy(u0).cuda()).cpu().numpy()
+    errs = {}
+    refs = [o.rollout(so, NSTEPS)(u0[b].astype(np.float64)) for b in range(2)]
+    for nn in (1, 20, NSTEPS):
+        errs[f"rel_l2_vs_fp64_after_{nn}"] = max(_rel(got[b, nn - 1], refs[b][nn - 1]) for b in range(2))
+    errs["sample"] = "2 initial conditions, NumPy float64 oracle"
+    return errs
+
+
 # ------------------------------------------------------------------ arms
 def dist_init():
     """One process per GPU (torchrun); replicas over batch shards, no data-path collective."""
@@ -281,6 +304,7 @@ def run_gb300(args, rank, ws):
 
     if rank == 0:
         cpu = cpu_baseline() if ws == 1 and not args.no_cpu else None
+        fp64 = fp64_check_ns256(st, ex, torch) if ws == 1 and not args.no_cpu else None
         line = {"metric": metric_name(), "value": value, "unit": "DOF-steps/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded truncated Fourier series ICs)",
@@ -295,7 +319,7 @@ def run_gb300(args, rank, ws):
                              "note": f"algorithmic {BYTES_PER_DOF_STEP:.2f} B/DOF-step (ETDRK2, 6 complex64 "
                                      f"half-spectrum passes) x {BATCH}x{N}^2x{NSTEPS} per launch; peak {peak_src}",
                              "fp32": fp32},
-                "clocks": clk, "cpu_baseline": cpu}
+                "clocks": clk, "cpu_baseline": cpu, "fp64_check": fp64}
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.barrier()
@@ -427,6 +451,21 @@ def run_other(args, rank, ws):
             line["cpu_baseline"] = {"value": min(cores, B) * Nk * n / max(ts), "unit": "DOF-steps/s",
                                     "cores": min(cores, B), "kind": "port",
                                     "sample": f"NumPy oracle, {min(cores, B)} samples x {n}-step rollout, one process each"}
+            # float64 check: rel-L2 after 1 and 20 steps (chaotic case) and the time-averaged energy
+            # spectra of the last 100 steps (sum_k |E_gpu - E_fp64| / sum_k E_fp64)
+            from oracle import exponax_np as o
+
+            so = o.KuramotoSivashinskyConservative(1, 100.0, Nk, 0.1, dtype="float64")
+            got = roll(u0[:2]).cpu().numpy()
+            errs = {}
+            refs = [o.rollout(so, n, include_init=True)(u0h[b].astype(np.float64)) for b in range(2)]
+            for nn in (1, 20):
+                errs[f"rel_l2_vs_fp64_after_{nn}"] = max(_rel(got[b, nn], refs[b][nn]) for b in range(2))
+            spec = lambda tr: np.mean(np.abs(np.fft.rfft(tr[-100:, 0].astype(np.float64), axis=-1)) ** 2, axis=0)  # noqa
+            errs["energy_spectrum_rel_diff_last_100_steps"] = max(
+                float(np.sum(np.abs(spec(got[b]) - spec(refs[b]))) / np.sum(spec(refs[b]))) for b in range(2))
+            errs["sample"] = "2 initial conditions, NumPy float64 oracle"
+            line["fp64_check"] = errs
     elif args.workload == "uneven1d":
         from exponax_gb300.batching import QueueRollout, uneven_config3
 
@@ -468,6 +507,29 @@ def run_other(args, rank, ws):
             line["cpu_baseline"] = {"value": sum(r[1] for r in res) / max(r[0] for r in res), "unit": "DOF-steps/s",
                                     "cores": nproc, "kind": "port",
                                     "sample": f"NumPy oracle rollouts of the first 96 instances, {nproc} processes"}
+            # float64 check: the first instance of each PDE, 100-step trajectory after the graph replay
+            from oracle import exponax_np as o
+
+            q.replay()
+            torch.cuda.synchronize()
+            errs = {}
+            for i, (stp, u) in enumerate(instances):
+                name = type(stp).__name__
+                if f"{name}_rel_l2_vs_fp64_after_{n}" in errs:
+                    continue
+                if name == "Burgers":
+                    so = o.Burgers(1, 1.0, stp.num_points, 1e-3, diffusivity=0.01, dtype="float64")
+                elif name == "KortewegDeVries":
+                    so = o.KortewegDeVries(1, 20.0, stp.num_points, 0.01, dispersivity=1.0, hyper_diffusivity=0.01,
+                                           dtype="float64")
+                else:
+                    so = o.KuramotoSivashinskyConservative(1, 100.0, stp.num_points, 0.1, dtype="float64")
+                ref = o.rollout(so, n, include_init=True)(np.asarray(u, dtype=np.float64))
+                got = q.trajectories[i].cpu().numpy()
+                errs[f"{name}_rel_l2_vs_fp64_after_{n}"] = _rel(got[-1], ref[-1])
+                errs[f"{name}_N"] = int(stp.num_points)
+            errs["sample"] = "first instance of each PDE, NumPy float64 oracle"
+            line["fp64_check"] = errs
     elif args.workload == "kolmo128":
         from exponax_gb300 import _device, _lib
 
