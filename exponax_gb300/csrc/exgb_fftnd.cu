@@ -397,10 +397,10 @@ extern "C" {
 int exgb_fourier_interp(void* stream, int num_spatial_dims, int num_points, int num_channels, const void* coef,
                         float domain_extent, int64_t num_queries, const float* x, float* out) {
   const int D = num_spatial_dims, N = num_points, C = num_channels;
-  if (!coef || !x || !out) return fail(EXGB_EINVAL, "exgb_fourier_interp: NULL pointer");
   if (D < 1 || D > 3 || N < 1 || C < 1) return fail(EXGB_ESHAPE, "exgb_fourier_interp: bad shape");
   if (num_queries < 0 || !(domain_extent > 0.f)) return fail(EXGB_EINVAL, "exgb_fourier_interp: bad arguments");
   if (num_queries == 0) return EXGB_OK;
+  if (!coef || !x || !out) return fail(EXGB_EINVAL, "exgb_fourier_interp: NULL pointer");
   int64_t per = N / 2 + 1;
   for (int d = 0; d < D - 1; ++d) per *= N;
   const float kscale = (float)(2.0 * 3.14159265358979323846 / (double)domain_extent);
@@ -415,22 +415,25 @@ int exgb_fourier_interp(void* stream, int num_spatial_dims, int num_points, int 
 
 
 int exgb_rfftn(void* stream, int num_spatial_dims, int num_points, int64_t count, const float* in, void* out) {
-  if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
   if (count < 0) return fail(EXGB_EINVAL, "negative count");
+  if (count == 0) return EXGB_OK;
+  if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
   return rfftn_impl((cudaStream_t)stream, num_spatial_dims, num_points, count, in, (float2*)out);
 }
 
 int exgb_irfftn(void* stream, int num_spatial_dims, int num_points, int64_t count, const void* in, float* out) {
-  if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
   if (count < 0) return fail(EXGB_EINVAL, "negative count");
+  if (count == 0) return EXGB_OK;
+  if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
   return irfftn_impl((cudaStream_t)stream, num_spatial_dims, num_points, count, (const float2*)in, out);
 }
 
 int exgb_map_between_resolutions(void* stream, int D, int n_old, int n_new, int64_t count, const float* in,
                                  float* out, int oddball_zero) {
-  if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
   if (D < 1 || D > 3) return fail(EXGB_EINVAL, "num_spatial_dims must be 1, 2 or 3");
   if (n_old < 1 || n_new < 1 || count < 0) return fail(EXGB_EINVAL, "bad sizes");
+  if (count == 0) return EXGB_OK;
+  if (!in || !out) return fail(EXGB_EINVAL, "NULL pointer");
   cudaStream_t st = (cudaStream_t)stream;
   size_t pts_old = (size_t)n_old, pts_new = (size_t)n_new;  // grid points per field
   size_t so = (size_t)(n_old / 2 + 1), sn = (size_t)(n_new / 2 + 1);  // modes per field

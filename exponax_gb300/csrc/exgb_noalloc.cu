@@ -57,7 +57,7 @@ using namespace exgb;
 
 extern "C" int exgb_repeat_fourier_noalloc(const exgb_plan* plan, void* stream, const void* u_hat0,
                                            void* u_hat_out, int64_t batch, int32_t nsteps) {
-  if (!plan || !u_hat0 || !u_hat_out) return fail(EXGB_EINVAL, "NULL argument");
+  if (!plan) return fail(EXGB_EINVAL, "NULL argument");
   if (batch < 0 || nsteps < 0) return fail(EXGB_EINVAL, "negative batch or nsteps");
   if (plan->dev.D != 2 || plan->dev.kind == EXGB_NL_ZERO || plan->dev.order == 0 || plan->cfg2d.variant != 1)
     return fail(EXGB_EUNSUPPORTED,
@@ -66,6 +66,8 @@ extern "C" int exgb_repeat_fourier_noalloc(const exgb_plan* plan, void* stream, 
   if (need > kStaticScratchBytes)
     return fail(EXGB_EUNSUPPORTED, "this plan needs " + std::to_string(need) +
                                        " bytes of stage buffers per cluster, more than the 8 MiB static scratch");
+  if (batch == 0) return EXGB_OK;  // an empty batch touches no memory (its pointers may be NULL)
+  if (!u_hat0 || !u_hat_out) return fail(EXGB_EINVAL, "NULL argument");
   float2* scratch = nullptr;
   const int rc = static_scratch(&scratch);
   if (rc) return rc;

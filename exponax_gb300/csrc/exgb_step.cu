@@ -105,9 +105,17 @@ int exgb_step_fourier(const exgb_plan* plan, void* stream, const void* u_hat_in,
 
 int exgb_repeat_fourier(const exgb_plan* plan, void* stream, const void* u_hat0, void* u_hat_out, int64_t batch,
                         int32_t nsteps) {
-  if (!plan || !u_hat0 || !u_hat_out) return fail(EXGB_EINVAL, "NULL argument");
+  if (!plan) return fail(EXGB_EINVAL, "NULL argument");
   if (batch < 0 || nsteps < 0) return fail(EXGB_EINVAL, "negative batch or nsteps");
+  if (batch == 0) return EXGB_OK;  // an empty batch touches no memory (its pointers may be NULL)
+  if (!u_hat0 || !u_hat_out) return fail(EXGB_EINVAL, "NULL argument");
   cudaStream_t st = (cudaStream_t)stream;
+  if (nsteps == 0) {  // zero steps return the state itself, bit for bit
+    if (u_hat_out != u_hat0)
+      EXGB_CUDA(cudaMemcpyAsync(u_hat_out, u_hat0, sizeof(float2) * hat_elems(plan->dev, batch),
+                                cudaMemcpyDeviceToDevice, st));
+    return EXGB_OK;
+  }
   if (plan->dev.D == 1 && !plan->staged)
     return etdrk1d_run(plan, st, nullptr, (const float2*)u_hat0, nullptr, (float2*)u_hat_out, batch, nsteps, 0, 0, 0,
                        0);
@@ -115,8 +123,10 @@ int exgb_repeat_fourier(const exgb_plan* plan, void* stream, const void* u_hat0,
 }
 
 int exgb_nonlinear(const exgb_plan* plan, void* stream, const void* u_hat_in, void* n_hat_out, int64_t batch) {
-  if (!plan || !u_hat_in || !n_hat_out) return fail(EXGB_EINVAL, "NULL argument");
+  if (!plan) return fail(EXGB_EINVAL, "NULL argument");
   if (batch < 0) return fail(EXGB_EINVAL, "negative batch");
+  if (batch == 0) return EXGB_OK;
+  if (!u_hat_in || !n_hat_out) return fail(EXGB_EINVAL, "NULL argument");
   cudaStream_t st = (cudaStream_t)stream;
   const PlanDev& P = plan->dev;
   if (P.kind == EXGB_NL_ZERO || P.order == 0) {
@@ -132,10 +142,17 @@ int exgb_nonlinear(const exgb_plan* plan, void* stream, const void* u_hat_in, vo
 }
 
 int exgb_repeat(const exgb_plan* plan, void* stream, const float* u0, float* u_out, int64_t batch, int32_t nsteps) {
-  if (!plan || !u0 || !u_out) return fail(EXGB_EINVAL, "NULL argument");
+  if (!plan) return fail(EXGB_EINVAL, "NULL argument");
   if (batch < 0 || nsteps < 0) return fail(EXGB_EINVAL, "negative batch or nsteps");
+  if (batch == 0) return EXGB_OK;
+  if (!u0 || !u_out) return fail(EXGB_EINVAL, "NULL argument");
   cudaStream_t st = (cudaStream_t)stream;
   const PlanDev& P = plan->dev;
+  if (nsteps == 0) {  // zero steps return the state itself, bit for bit
+    if (u_out != u0)
+      EXGB_CUDA(cudaMemcpyAsync(u_out, u0, sizeof(float) * phys_elems(P, batch), cudaMemcpyDeviceToDevice, st));
+    return EXGB_OK;
+  }
   if (P.D == 1 && !plan->staged) return etdrk1d_run(plan, st, u0, nullptr, u_out, nullptr, batch, nsteps, 1, 0, 0, 0);
   float2* hat = (float2*)workspace(sizeof(float2) * hat_elems(P, batch), 2);
   if (!hat) return fail(EXGB_ENOMEM, "workspace allocation failed");
@@ -152,8 +169,10 @@ int exgb_step(const exgb_plan* plan, void* stream, const float* u_in, float* u_o
 
 int exgb_rollout(const exgb_plan* plan, void* stream, const float* u0, float* traj, int64_t batch, int32_t nsteps,
                  int32_t include_init) {
-  if (!plan || !u0 || !traj) return fail(EXGB_EINVAL, "NULL argument");
+  if (!plan) return fail(EXGB_EINVAL, "NULL argument");
   if (batch < 0 || nsteps < 0) return fail(EXGB_EINVAL, "negative batch or nsteps");
+  if (batch == 0) return EXGB_OK;
+  if (!u0 || !traj) return fail(EXGB_EINVAL, "NULL argument");
   cudaStream_t st = (cudaStream_t)stream;
   const PlanDev& P = plan->dev;
   if (P.D == 1 && !plan->staged)

@@ -182,9 +182,9 @@ int grid_for(int64_t n) { return (int)std::min<int64_t>((n + 255) / 256, 152 * 1
 using namespace exgb;
 
 extern "C" int exgb_axpy(void* stream, int64_t n, float alpha, const float* x, const float* y, float* out) {
-  if (!x || !y || !out) return fail(EXGB_EINVAL, "exgb_axpy: NULL pointer");
   if (n < 0) return fail(EXGB_EINVAL, "exgb_axpy: negative size");
   if (n == 0) return EXGB_OK;
+  if (!x || !y || !out) return fail(EXGB_EINVAL, "exgb_axpy: NULL pointer");
   axpy_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(n, alpha, x, y, out);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
@@ -205,10 +205,10 @@ extern "C" int exgb_scatter_modes(void* stream, int64_t count, int64_t field_ele
 
 extern "C" int exgb_normalize_fields(void* stream, int64_t count, int64_t n, float* u, int zero_mean, int std_one,
                                      int max_one) {
-  if (!u) return fail(EXGB_EINVAL, "exgb_normalize_fields: NULL pointer");
   if (count < 0 || n <= 0) return fail(EXGB_EINVAL, "exgb_normalize_fields: bad size");
   if (std_one && max_one) return fail(EXGB_EINVAL, "Cannot have `std_one=True` and `max_one=True`.");
   if (count == 0) return EXGB_OK;
+  if (!u) return fail(EXGB_EINVAL, "exgb_normalize_fields: NULL pointer");
   if (count > 2147483647LL) return fail(EXGB_EINVAL, "exgb_normalize_fields: too many fields for one launch");
   normalize_kernel<<<(unsigned)count, 256, 0, (cudaStream_t)stream>>>(n, u, zero_mean, std_one, max_one);
   EXGB_CUDA(cudaGetLastError());
@@ -217,9 +217,9 @@ extern "C" int exgb_normalize_fields(void* stream, int64_t count, int64_t n, flo
 
 extern "C" int exgb_mode_scale(void* stream, int64_t count, int64_t per, const void* table, const void* in,
                                void* out) {
-  if (!table || !in || !out) return fail(EXGB_EINVAL, "exgb_mode_scale: NULL pointer");
   if (count < 0 || per <= 0) return fail(EXGB_EINVAL, "exgb_mode_scale: bad size");
   if (count == 0) return EXGB_OK;
+  if (!table || !in || !out) return fail(EXGB_EINVAL, "exgb_mode_scale: NULL pointer");
   mode_scale_kernel<<<grid_for(count * per), 256, 0, (cudaStream_t)stream>>>(
       count, per, (const float2*)table, (const float2*)in, (float2*)out);
   EXGB_CUDA(cudaGetLastError());
@@ -228,9 +228,9 @@ extern "C" int exgb_mode_scale(void* stream, int64_t count, int64_t per, const v
 
 extern "C" int exgb_mode_mix2(void* stream, int64_t count, int64_t per, const float* mat, const void* in, void* out,
                               int nsteps) {
-  if (!mat || !in || !out) return fail(EXGB_EINVAL, "exgb_mode_mix2: NULL pointer");
   if (count < 0 || per <= 0 || nsteps < 0) return fail(EXGB_EINVAL, "exgb_mode_mix2: bad size");
   if (count == 0) return EXGB_OK;
+  if (!mat || !in || !out) return fail(EXGB_EINVAL, "exgb_mode_mix2: NULL pointer");
   mode_mix2_kernel<<<grid_for(count * per), 256, 0, (cudaStream_t)stream>>>(
       count, per, mat, (const float2*)in, (float2*)out, nsteps);
   EXGB_CUDA(cudaGetLastError());
@@ -246,10 +246,10 @@ static int64_t modes_per_field(int D, int N) {
 extern "C" int exgb_spectral_derivative(void* stream, int num_spatial_dims, int num_points, int64_t count,
                                         int order, float domain_extent, const void* in, void* out) {
   const int D = num_spatial_dims, N = num_points;
-  if (!in || !out) return fail(EXGB_EINVAL, "exgb_spectral_derivative: NULL pointer");
   if (D < 1 || D > 3 || N < 1) return fail(EXGB_ESHAPE, "exgb_spectral_derivative: 1 to 3 axes of N >= 1 points");
   if (count < 0 || order < 0 || !(domain_extent > 0.f)) return fail(EXGB_EINVAL, "exgb_spectral_derivative: bad arguments");
   if (count == 0) return EXGB_OK;
+  if (!in || !out) return fail(EXGB_EINVAL, "exgb_spectral_derivative: NULL pointer");
   const int64_t per = modes_per_field(D, N);
   const float ks = (float)(2.0 * 3.14159265358979323846 / (double)domain_extent);
   derivative_kernel<<<grid_for(count * per), 256, 0, (cudaStream_t)stream>>>(D, N, count, per, order, ks,
@@ -261,10 +261,10 @@ extern "C" int exgb_spectral_derivative(void* stream, int num_spatial_dims, int 
 extern "C" int exgb_make_incompressible(void* stream, int num_spatial_dims, int num_points, int64_t count,
                                         const void* in, void* out) {
   const int D = num_spatial_dims, N = num_points;
-  if (!in || !out) return fail(EXGB_EINVAL, "exgb_make_incompressible: NULL pointer");
   if (D < 1 || D > 3 || N < 1) return fail(EXGB_ESHAPE, "exgb_make_incompressible: 1 to 3 axes of N >= 1 points");
   if (count < 0) return fail(EXGB_EINVAL, "exgb_make_incompressible: negative count");
   if (count == 0) return EXGB_OK;
+  if (!in || !out) return fail(EXGB_EINVAL, "exgb_make_incompressible: NULL pointer");
   const int64_t per = modes_per_field(D, N);
   // the projection does not depend on the domain extent: the reference evaluates it with L = 1
   const float ks = (float)(2.0 * 3.14159265358979323846);

@@ -1,0 +1,96 @@
+"""Edge cases of the stepping and transform entry points on the GPU: empty batches (torch hands
+NULL data pointers for them), zero steps, zero states, in-place Fourier stepping, odd and
+non-power-of-two grids, and sizes the library refuses with an error instead of a launch."""
+
+import numpy as np
+import pytest
+
+import exponax_gb300 as ex
+from oracle import exponax_np as o
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _steppers():
+    return [
+        ex.stepper.KuramotoSivashinskyConservative(1, 100.0, 200, 0.1),   # fused 1D kernel
+        ex.stepper.NavierStokesVorticity(2, 2 * np.pi, 64, 0.01, diffusivity=1e-3),  # cluster kernel
+        ex.stepper.NavierStokesVorticity(2, 2 * np.pi, 45, 0.01, diffusivity=1e-3),  # generic 2D kernel
+        ex.stepper.Burgers(2, 2 * np.pi, 32, 0.01, diffusivity=0.05),     # staged N-D path
+        ex.stepper.NavierStokesVelocity(3, 2 * np.pi, 16, 0.01),          # 3D path
+        ex.stepper.Diffusion(2, 1.0, 32, 0.1),                            # ETDRK0
+        ex.stepper.Wave(2, 1.0, 32, 0.01),                                # per-mode 2x2 map
+    ]
+
+
+@pytest.mark.parametrize("idx", range(7))
+def test_empty_batches_and_zero_steps(idx):
+    sm = _steppers()[idx]
+    D, N, C = sm.num_spatial_dims, sm.num_points, sm.num_channels
+    shape = (C,) + (N,) * D
+    e = torch.empty((0,) + shape, dtype=torch.float32, device="cuda")
+    assert tuple(ex.vmap(sm)(e).shape) == (0,) + shape
+    assert tuple(ex.vmap(ex.repeat(sm, 4))(e).shape) == (0,) + shape
+    assert tuple(ex.vmap(ex.rollout(sm, 3, include_init=True))(e).shape) == (0, 4) + shape
+    eh = torch.empty((0, C) + (N,) * (D - 1) + (N // 2 + 1,), dtype=torch.complex64, device="cuda")
+    assert tuple(ex.vmap(sm.step_fourier)(eh).shape) == tuple(eh.shape)
+    assert tuple(ex.fft(e, num_spatial_dims=D).shape) == tuple(eh.shape)
+    assert tuple(ex.ifft(eh, num_spatial_dims=D, num_points=N).shape) == tuple(e.shape)
+    # zero steps return the state; rollout(0, include_init) is the initial state alone
+    u = torch.from_numpy(np.random.default_rng(idx).standard_normal((2,) + shape).astype(np.float32)).cuda()
+    np.testing.assert_array_equal(ex.vmap(ex.repeat(sm, 0))(u).cpu().numpy(), u.cpu().numpy())
+    r = ex.vmap(ex.rollout(sm, 0, include_init=True))(u)
+    assert tuple(r.shape) == (2, 1) + shape
+    np.testing.assert_array_equal(r[:, 0].cpu().numpy(), u.cpu().numpy())
+    # the zero state stays zero
+    z = torch.zeros((1,) + shape, dtype=torch.float32, device="cuda")
+    if not isinstance(sm, ex.stepper.Diffusion):
+        assert float(ex.vmap(ex.repeat(sm, 3))(z).abs().max()) == 0.0
+
+
+def test_empty_transforms_and_resampling():
+    e = torch.empty((0, 1, 32, 32), dtype=torch.float32, device="cuda")
+    assert tuple(ex.interpolation.map_between_resolutions_batched(e, 16).shape) == (0, 1, 16, 16)
+    assert tuple(ex.spectral.derivative(torch.zeros((1, 8, 8), device="cuda"), 1.0).shape) == (2, 8, 8)
+
+
+@pytest.mark.parametrize("kind", ["ks1d", "ns64"])
+def test_in_place_fourier_stepping(kind):
+    """exgb_repeat_fourier with the output buffer equal to the input buffer (the header allows aliasing)."""
+    from exponax_gb300 import _device, _lib
+
+    if kind == "ks1d":
+        sm = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, 200, 0.1)
+        so = o.KuramotoSivashinskyConservative(1, 100.0, 200, 0.1)
+        u = np.stack([ex.ic.RandomSineWaves1d(1)(200, key=k) for k in range(3)])
+    else:
+        sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, 64, 0.01, diffusivity=1e-3)
+        so = o.NavierStokesVorticity(2, 2 * np.pi, 64, 0.01, diffusivity=1e-3)
+        u = np.stack([ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)(64, key=k) for k in range(3)])
+    D = sm.num_spatial_dims
+    uh = ex.fft(torch.from_numpy(u).cuda(), num_spatial_dims=D).contiguous()
+    _lib.check(_lib.load().exgb_repeat_fourier(sm.plan.handle, _device.stream(), uh.data_ptr(), uh.data_ptr(), 3, 5))
+    got = ex.ifft(uh, num_spatial_dims=D, num_points=sm.num_points).cpu().numpy()
+    for b in range(3):
+        assert rel(got[b], o.repeat(so, 5)(u[b])) < 1e-5, b
+
+
+def test_sizes_the_library_refuses():
+    """N that is not 2^a 3^b 5^c, and a 1D grid larger than one CTA's shared memory, raise instead of
+    launching; the library stays usable afterwards."""
+    with pytest.raises(ValueError):
+        ex.vmap(ex.stepper.Burgers(1, 1.0, 77, 0.01))(torch.zeros((1, 1, 77), device="cuda"))
+    big = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, 2 ** 16, 0.1)
+    with pytest.raises((ValueError, ex.ExgbError)):
+        ex.vmap(big)(torch.zeros((1, 1, 2 ** 16), device="cuda"))
+    sm = ex.stepper.Burgers(1, 1.0, 64, 0.01)
+    u = ex.ic.RandomSineWaves1d(1)(64, key=1)
+    assert rel(sm(torch.from_numpy(u).cuda()).cpu().numpy(), o.Burgers(1, 1.0, 64, 0.01)(u)) < 1e-5
