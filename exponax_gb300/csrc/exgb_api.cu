@@ -64,6 +64,7 @@ bool make_fft_plan(int n, FftPlan* p) {
   if (p->npass == 0) {  // n == 1: identity (one trivial radix-... pass is not needed)
     return false;
   }
+  fft_plan_finalize(p);
   return true;
 }
 
@@ -460,6 +461,7 @@ extern "C" int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int 
     if (prod != plan->dev.N) return fail(EXGB_EINVAL, "radices must multiply to N");
     plan->dev.fft.npass = n;
     for (int i = 0; i < n; ++i) plan->dev.fft.radix[i] = values[i];
+    fft_plan_finalize(&plan->dev.fft);
     EXGB_CUDA(cudaMemcpy(plan->d_dev, &plan->dev, sizeof(PlanDev), cudaMemcpyHostToDevice));
     return EXGB_OK;
   }

@@ -170,6 +170,14 @@ __device__ __forceinline__ void stage_update(const PlanDev& P, const Bufs& b, in
   }
 }
 
+// The plan's device constants into shared memory, all threads copying 4-byte words.
+__device__ __forceinline__ void copy_plan(PlanDev* dst, const PlanDev* __restrict__ src, int tid, int nthr) {
+  static_assert(sizeof(PlanDev) % 4 == 0, "PlanDev is copied as 4-byte words");
+  int* d = reinterpret_cast<int*>(dst);
+  const int* s = reinterpret_cast<const int*>(src);
+  for (int i = tid; i < (int)(sizeof(PlanDev) / 4); i += nthr) d[i] = s[i];
+}
+
 // One nonlinear evaluation of the m states X followed by the stage update
 // (stage >= 0) or a plain store of N^ into X_out (stage < 0).
 __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m, int stage, float2* X_out,
@@ -252,7 +260,7 @@ __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__
     const int it = s_item;
     if (it >= n_items) break;
     const Item1D item = items[it];
-    if (tid == 0) Ps = *item.plan;
+    copy_plan(&Ps, item.plan, tid, nthr);
     __syncthreads();
     const PlanDev& P = Ps;
     const int N = P.N, M = P.M, m = item.m;
@@ -368,7 +376,7 @@ __global__ void __launch_bounds__(256) nonlin1d_kernel(const Item1D* __restrict_
   const int it = blockIdx.x;
   if (it >= n_items) return;
   const Item1D item = items[it];
-  if (tid == 0) Ps = *item.plan;
+  copy_plan(&Ps, item.plan, tid, nthr);
   __syncthreads();
   const PlanDev& P = Ps;
   const int N = P.N, M = P.M, m = item.m;

@@ -26,7 +26,39 @@ struct FftPlan {
   int n;
   int npass;
   int radix[kMaxPass];
+  // per pass, set by fft_plan_finalize: butterflies per sequence (n / R), product of the earlier
+  // radices (Ns), twiddle-table step ((n / R) / Ns), and FP32 reciprocals of the first two for the
+  // quotient estimate of fdiv
+  int nb[kMaxPass];
+  int ns[kMaxPass];
+  int step[kMaxPass];
+  float rnb[kMaxPass];
+  float rns[kMaxPass];
 };
+
+// Host: fill the per-pass constants of a plan whose n, npass and radix[] are set.
+inline void fft_plan_finalize(FftPlan* p) {
+  int Ns = 1;
+  for (int i = 0; i < p->npass; ++i) {
+    const int R = p->radix[i];
+    p->nb[i] = p->n / R;
+    p->ns[i] = Ns;
+    p->step[i] = (p->n / R) / Ns;
+    p->rnb[i] = (float)(1.0 / (double)p->nb[i]);
+    p->rns[i] = (float)(1.0 / (double)Ns);
+    Ns *= R;
+  }
+}
+
+// t / d for 0 <= t < 2^24 and d >= 1, with rd = (float)(1 / d): the FP32 product is within 1 of the
+// quotient there, so one correction step makes it exact (a dependent chain of a few instructions
+// instead of the ~20 of an integer division by a runtime divisor)
+__device__ __forceinline__ int fdiv(int t, int d, float rd) {
+  int q = __float2int_rz(__int2float_rn(t) * rd);
+  const int r = t - q * d;
+  q += (r >= d) - (r < 0);
+  return q;
+}
 
 // ---------------------------------------------------------------- complex helpers
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -135,15 +167,12 @@ struct LinMap {
 
 // ---------------------------------------------------------------- one pass
 template <int R, bool INV, class Src, class Dst>
-__device__ __forceinline__ void stockham_bfly(const Src& src, const Dst& dst, int s, int j, int n, int Ns,
-                                              const float2* __restrict__ tw) {
-  const int stride = n / R;
+__device__ __forceinline__ void stockham_bfly(const Src& src, const Dst& dst, int s, int j, int k, int stride,
+                                              int Ns, int step, const float2* __restrict__ tw) {
   float2 v[R];
 #pragma unroll
   for (int r = 0; r < R; ++r) v[r] = src(s, j + r * stride);
-  const int k = j % Ns;
   if (Ns > 1) {
-    const int step = stride / Ns;
 #pragma unroll
     for (int r = 1; r < R; ++r) {
       float2 w = tw[r * k * step];
@@ -157,19 +186,23 @@ __device__ __forceinline__ void stockham_bfly(const Src& src, const Dst& dst, in
   for (int r = 0; r < R; ++r) dst(s, base + r * Ns) = v[r];
 }
 
+// One radix-R pass over `count` sequences: nb = n / R butterflies per sequence, Ns the product of
+// the earlier radices, step = nb / Ns, rnb / rns the FP32 reciprocals of nb / Ns (FftPlan).
 template <bool INV, class Src, class Dst>
-__device__ __forceinline__ void stockham_pass(int R, const Src& src, const Dst& dst, int count, int n, int Ns,
-                                              const float2* __restrict__ tw, int tid, int nthr) {
-  const int nb = n / R;
+__device__ __forceinline__ void stockham_pass(int R, const Src& src, const Dst& dst, int count, int nb, int Ns,
+                                              int step, float rnb, float rns, const float2* __restrict__ tw,
+                                              int tid, int nthr) {
   const int total = nb * count;
+  const bool fast = total < (1 << 24);  // fdiv's exact range (uniform across the block)
   switch (R) {
-#define EXGB_PASS_CASE(RR)                                        \
-  case RR:                                                        \
-    for (int t = tid; t < total; t += nthr) {                     \
-      const int s = t / nb;                                       \
-      const int j = t - s * nb;                                   \
-      stockham_bfly<RR, INV>(src, dst, s, j, n, Ns, tw);          \
-    }                                                             \
+#define EXGB_PASS_CASE(RR)                                                      \
+  case RR:                                                                      \
+    for (int t = tid; t < total; t += nthr) {                                   \
+      const int s = fast ? fdiv(t, nb, rnb) : t / nb;                           \
+      const int j = t - s * nb;                                                 \
+      const int k = j - (fast ? fdiv(j, Ns, rns) : j / Ns) * Ns;                \
+      stockham_bfly<RR, INV>(src, dst, s, j, k, nb, Ns, step, tw);              \
+    }                                                                           \
     break;
     EXGB_PASS_CASE(2)
     EXGB_PASS_CASE(3)
@@ -207,9 +240,11 @@ __device__ void block_fft(const FftPlan& p, float2* buf0, float2* buf1, const Ou
   for (int pass = 0; pass < p.npass; ++pass) {
     const int R = p.radix[pass];
     if (pass == p.npass - 1) {
-      stockham_pass<INV>(R, LinMap{src, n}, out, count, n, Ns, tw, tid, nthr);
+      stockham_pass<INV>(R, LinMap{src, n}, out, count, p.nb[pass], Ns, p.step[pass], p.rnb[pass], p.rns[pass], tw,
+                         tid, nthr);
     } else {
-      stockham_pass<INV>(R, LinMap{src, n}, LinMap{dst, n}, count, n, Ns, tw, tid, nthr);
+      stockham_pass<INV>(R, LinMap{src, n}, LinMap{dst, n}, count, p.nb[pass], Ns, p.step[pass], p.rnb[pass],
+                         p.rns[pass], tw, tid, nthr);
     }
     sync();
     Ns *= R;
