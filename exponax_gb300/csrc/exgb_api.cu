@@ -275,6 +275,7 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   v.D = D;
   v.N = N;
   v.M = M;
+  v.rN = (float)(1.0 / (double)N);
   v.C = d.num_channels;
   v.order = d.order;
   v.kind = nonlinear ? d.nonlin_kind : EXGB_NL_ZERO;

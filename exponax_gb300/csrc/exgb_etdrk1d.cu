@@ -178,26 +178,88 @@ __device__ __forceinline__ void copy_plan(PlanDev* dst, const PlanDev* __restric
   for (int i = tid; i < (int)(sizeof(PlanDev) / 4); i += nthr) d[i] = s[i];
 }
 
+// First-pass source of the inverse transform of a nonlinear evaluation: element k of sequence i is
+// what nl_pack would have stored (mask u^ + i mask ik u^, Hermitian extension, 1/N), computed from X.
+struct PackSrc {
+  const PlanDev* P;
+  const float2* X;
+  int sx;
+  __device__ __forceinline__ float2 operator()(int i, int k) const {
+    const int N = P->N, M = P->M;
+    const bool ext = k >= M;
+    const int kk = ext ? N - k : k;
+    const bool ro = (k == 0) || ((N & 1) == 0 && k == N / 2);
+    float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+    if (kk <= P->kmax) {
+      a = X[i * sx + kk];
+      if (P->needs_ux) {
+        const float ks = P->kscale * (float)kk;
+        b = make_float2(-ks * a.y, ks * a.x);
+      }
+    }
+    return cscale(pack_pair(a, b, ext, ro), P->rN);
+  }
+};
+
+// Last-pass sink of that inverse transform: the physical value z = u + i u_x at x of sequence i
+// becomes (u^2, q) as nl_products computes it, stored at res[i N + x].
+struct ProductOut {
+  const PlanDev* P;
+  float2* res;
+  struct Ref {
+    const PlanDev* P;
+    float2* p;
+    __device__ __forceinline__ void operator=(float2 z) const {
+      const float u = z.x, ux = z.y;
+      float q = 0.f;
+      if (P->beta != 0.f) q = fmaf(P->beta * u, ux, q);
+      if (P->gamma != 0.f) q = fmaf(P->gamma * ux, ux, q);
+      if (P->npoly > 0) {
+        float pw = 1.f, acc = 0.f;
+        for (int c = 0; c < P->npoly; ++c) {
+          acc = fmaf(P->poly[c], pw, acc);
+          pw *= u;
+        }
+        q += acc;
+      }
+      *p = make_float2(u * u, q);
+    }
+  };
+  __device__ __forceinline__ Ref operator()(int i, int x) const { return Ref{P, res + i * P->N + x}; }
+};
+
 // One nonlinear evaluation of the m states X followed by the stage update
 // (stage >= 0) or a plain store of N^ into X_out (stage < 0).
+// fuse: pack fused into the first inverse pass and the products into the last (fewer barrier phases;
+// the throughput choice when several work items share an SM).  Otherwise each elementwise step is a
+// phase of its own spread over all threads (the latency choice for one small item per SM).
+template <bool fuse>
 __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m, int stage, float2* X_out,
                         int tid, int nthr) {
   const int N = P.N, M = P.M;
-  nl_pack(P, X, M, b.w0, m, tid, nthr);
-  __syncthreads();
-  float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
-  float2* other = (P.fft.npass & 1) ? b.w0 : b.w1;
-  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, P.tw, tid, nthr, BlockSync{});
   const bool zmf = P.gamma != 0.f && P.zero_mode_fix;
-  nl_products(P, res, (float*)other, m, tid, nthr);
-  __syncthreads();
-  if (zmf) {
-    nl_reduce((const float*)other, b.sums, N, m, tid, nthr);
+  float2 *res, *other;
+  if (fuse && !zmf) {  // compile-time fuse: each kernel carries one of the two paths
+    res = io_result_buf(P.fft, b.w0, b.w1);
+    other = (res == b.w0) ? b.w1 : b.w0;
+    block_fft_io<true>(P.fft, PackSrc{&P, X, M}, b.w0, b.w1, ProductOut{&P, res}, m, P.tw, tid, nthr, BlockSync{});
+  } else {
+    // separate pack and product phases (the zero-mode fix also needs u_x^2 in a buffer of its own)
+    nl_pack(P, X, M, b.w0, m, tid, nthr);
     __syncthreads();
+    res = (P.fft.npass & 1) ? b.w1 : b.w0;
+    other = (P.fft.npass & 1) ? b.w0 : b.w1;
+    block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, P.tw, tid, nthr, BlockSync{});
+    nl_products(P, res, (float*)other, m, tid, nthr);
+    __syncthreads();
+    if (zmf) {
+      nl_reduce((const float*)other, b.sums, N, m, tid, nthr);
+      __syncthreads();
+    }
   }
-  // forward: input in res, ping-pong with other
-  float2* fres = (P.fft.npass & 1) ? other : res;
-  block_fft<false>(P.fft, res, other, LinMap{fres, N}, m, P.tw, tid, nthr, BlockSync{});
+  // forward: input in res, passes ping-pong other <-> res
+  float2* fres = io_result_buf(P.fft, other, res);
+  block_fft_io<false>(P.fft, LinMap{res, N}, other, res, LinMap{fres, N}, m, P.tw, tid, nthr, BlockSync{});
   for (int t = tid; t < m * M; t += nthr) {
     const int i = t / M, k = t - i * M;
     float2 nv = make_float2(0.f, 0.f);
@@ -218,21 +280,58 @@ __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m,
   __syncthreads();
 }
 
-// Physical output of m states (pairs packed in one complex FFT).
-__device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, int64_t inst_stride, int tid, int nthr) {
-  const int N = P.N, M = P.M;
-  const bool even = (N & 1) == 0;
-  const int pairs = (m + 1) / 2;
-  const float invN = 1.f / (float)N;
-  for (int t = tid; t < pairs * N; t += nthr) {
-    const int p = t / N, k = t - p * N;
+// First-pass source of the trajectory output: instances 2p and 2p+1 packed as one complex sequence.
+struct EmitSrc {
+  const PlanDev* P;
+  const float2* U;
+  int m;
+  __device__ __forceinline__ float2 operator()(int p, int k) const {
+    const int N = P->N, M = P->M;
     const bool ext = k >= M;
     const int kk = ext ? N - k : k;
-    const bool ro = (k == 0) || (even && k == N / 2);
+    const bool ro = (k == 0) || ((N & 1) == 0 && k == N / 2);
     const int ia = 2 * p, ib = 2 * p + 1;
-    const float2 a = b.U[ia * M + kk];
-    const float2 bb = ib < m ? b.U[ib * M + kk] : make_float2(0.f, 0.f);
-    b.w0[t] = cscale(pack_pair(a, bb, ext, ro), invN);
+    const float2 a = U[ia * M + kk];
+    const float2 bb = ib < m ? U[ib * M + kk] : make_float2(0.f, 0.f);
+    return cscale(pack_pair(a, bb, ext, ro), P->rN);
+  }
+};
+
+// Last-pass sink of the trajectory output: the real and imaginary parts are the two instances' values.
+struct EmitOut {
+  float* out;
+  int64_t stride;
+  int m;
+  struct Ref {
+    float* a;
+    float* b;
+    __device__ __forceinline__ void operator=(float2 z) const {
+      *a = z.x;
+      if (b) *b = z.y;
+    }
+  };
+  __device__ __forceinline__ Ref operator()(int p, int x) const {
+    float* a = out + (int64_t)(2 * p) * stride + x;
+    return Ref{a, (2 * p + 1 < m) ? a + stride : nullptr};
+  }
+};
+
+// Physical output of m states (pairs packed in one complex FFT); with `fuse` the pack is the first
+// pass's source and the global stores the last pass's sink, else each is a phase of its own.
+template <bool fuse>
+__device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, int64_t inst_stride, int tid,
+                          int nthr) {
+  const int pairs = (m + 1) / 2;
+  if constexpr (fuse) {
+    block_fft_io<true>(P.fft, EmitSrc{&P, b.U, m}, b.w0, b.w1, EmitOut{out, inst_stride, m}, pairs, P.tw, tid,
+                       nthr, BlockSync{});
+    return;
+  }
+  const int N = P.N;
+  const EmitSrc src{&P, b.U, m};
+  for (int t = tid; t < pairs * N; t += nthr) {
+    const int p = t / N, k = t - p * N;
+    b.w0[t] = src(p, k);
   }
   __syncthreads();
   float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
@@ -246,9 +345,10 @@ __device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, in
   __syncthreads();
 }
 
+template <bool FUSE>
 __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__ items, int n_items,
                                                       int* __restrict__ head, int nsteps, int mode, int project,
-                                                      int include_init, int T) {
+                                                      int include_init) {
   extern __shared__ __align__(16) float2 sm[];
   __shared__ PlanDev Ps;
   __shared__ int s_item;
@@ -335,7 +435,7 @@ __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__
       } else {
         for (int s = 0; s < nstages; ++s) {
           const float2* X = (s == 0) ? b.U : (P.order == 4 && s == 1) ? b.S1 : b.S;
-          nl_eval(P, b, X, m, s, nullptr, tid, nthr);
+          nl_eval<FUSE>(P, b, X, m, s, nullptr, tid, nthr);
         }
       }
       if (project) {
@@ -348,13 +448,13 @@ __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__
       }
       if (mode == MODE_TRAJ) {
         float* o = (float*)item.out + (int64_t)(step + include_init) * N;
-        emit_phys(P, b, m, o, item.out_stride, tid, nthr);
+        emit_phys<FUSE>(P, b, m, o, item.out_stride, tid, nthr);
       }
     }
 
     // ---- final store
     if (mode == MODE_FINAL) {
-      emit_phys(P, b, m, (float*)item.out, item.out_stride, tid, nthr);
+      emit_phys<FUSE>(P, b, m, (float*)item.out, item.out_stride, tid, nthr);
     } else if (mode == MODE_FOURIER) {
       float2* o = (float2*)item.out;
       for (int t = tid; t < m * M; t += nthr) {
@@ -363,7 +463,6 @@ __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__
       }
     }
     __syncthreads();
-    (void)T;
   }
 }
 
@@ -392,7 +491,7 @@ __global__ void __launch_bounds__(256) nonlin1d_kernel(const Item1D* __restrict_
   }
   __syncthreads();
   // results go back into U (the pack step has consumed it before the epilogue)
-  nl_eval(P, b, b.U, m, -1, b.U, tid, nthr);
+  nl_eval<false>(P, b, b.U, m, -1, b.U, tid, nthr);
   float2* o = (float2*)item.out;
   for (int t = tid; t < m * M; t += nthr) {
     const int i = t / M, k = t - i * M;
@@ -445,13 +544,17 @@ static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStrea
     EXGB_CUDA(cudaFuncSetAttribute(nonlin1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     nonlin1d_kernel<<<(unsigned)items.size(), 256, smem, st>>>((const Item1D*)ws, (int)items.size());
   } else {
-    EXGB_CUDA(cudaFuncSetAttribute(etdrk1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // more work items than SMs: throughput-bound, the fused elementwise steps pay; otherwise each SM
+    // runs one item at latency and the separate all-thread phases are shorter
+    const bool fuse = (int64_t)items.size() > (int64_t)sm_count;
+    auto kern = fuse ? etdrk1d_kernel<true> : etdrk1d_kernel<false>;
+    EXGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;
-    EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, etdrk1d_kernel, threads, smem));
+    EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
     per_sm = std::max(1, per_sm);
     const int grid = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)sm_count * per_sm);
-    etdrk1d_kernel<<<grid, threads, smem, st>>>((const Item1D*)ws, (int)items.size(), head, nsteps, mode, project,
-                                                include_init, 0);
+    kern<<<grid, threads, smem, st>>>((const Item1D*)ws, (int)items.size(), head, nsteps, mode, project,
+                                      include_init);
   }
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
@@ -563,6 +666,7 @@ struct exgb_queue {
   int n_items = 0;
   size_t smem = 0;
   int grid = 1;
+  int sm_count = 1;
   int nsteps = 0;
   int include_init = 0;
 };
@@ -593,18 +697,20 @@ extern "C" int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, 
   q->smem = smem;
   q->nsteps = nsteps;
   q->include_init = include_init ? 1 : 0;
+  q->sm_count = sm_count;
+  // the fused kernel variant when the queue holds more items than there are SMs (see launch_items)
+  auto kern = q->n_items > q->sm_count ? etdrk1d_kernel<true> : etdrk1d_kernel<false>;
   cudaError_t e;
   if ((e = cudaMalloc(&q->d_items, sizeof(Item1D) * sorted.size())) != cudaSuccess ||
       (e = cudaMalloc(&q->d_head, sizeof(int))) != cudaSuccess ||
       (e = cudaMemcpy(q->d_items, sorted.data(), sizeof(Item1D) * sorted.size(), cudaMemcpyHostToDevice)) !=
           cudaSuccess ||
-      (e = cudaFuncSetAttribute(etdrk1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-          cudaSuccess) {
+      (e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess) {
     exgb_queue_destroy(q);
     return cuda_fail(e, "exgb_queue_prepare");
   }
   int per_sm = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, etdrk1d_kernel, 256, smem) != cudaSuccess) per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess) per_sm = 1;
   q->grid = (int)std::min<int64_t>((int64_t)sorted.size(), (int64_t)sm_count * std::max(1, per_sm));
   *out = q;
   return EXGB_OK;
@@ -614,8 +720,8 @@ extern "C" int exgb_queue_launch(exgb_queue* q, void* stream) {
   if (!q) return fail(EXGB_EINVAL, "NULL queue");
   cudaStream_t st = (cudaStream_t)stream;
   EXGB_CUDA(cudaMemsetAsync(q->d_head, 0, sizeof(int), st));
-  etdrk1d_kernel<<<q->grid, 256, q->smem, st>>>(q->d_items, q->n_items, q->d_head, q->nsteps, MODE_TRAJ, 1,
-                                                q->include_init, 0);
+  auto kern = q->n_items > q->sm_count ? etdrk1d_kernel<true> : etdrk1d_kernel<false>;
+  kern<<<q->grid, 256, q->smem, st>>>(q->d_items, q->n_items, q->d_head, q->nsteps, MODE_TRAJ, 1, q->include_init);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }

@@ -254,6 +254,46 @@ __device__ void block_fft(const FftPlan& p, float2* buf0, float2* buf1, const Ou
   }
 }
 
+// Full FFT of `count` sequences whose first pass reads through the functor `in` (operator()(s, k)
+// returning element k of sequence s) and whose last pass writes through `out`, so that an
+// elementwise step before and after the transform costs no pass of its own.  Intermediate passes
+// ping-pong b0 <-> b1 (pass p writes b0 for even p, b1 for odd p); `out` must not alias the source
+// of the last pass (b0 if npass is even, b1 if npass > 1 is odd; `in` if npass == 1).  A barrier
+// follows every pass.
+template <bool INV, class In, class Out, class Sync>
+__device__ void block_fft_io(const FftPlan& p, const In& in, float2* b0, float2* b1, const Out& out, int count,
+                             const float2* __restrict__ tw, int tid, int nthr, const Sync& sync) {
+  const int n = p.n;
+  int Ns = 1;
+  for (int pass = 0; pass < p.npass; ++pass) {
+    const int R = p.radix[pass];
+    const bool last = pass == p.npass - 1;
+    float2* dst = (pass & 1) ? b1 : b0;
+    if (pass == 0) {
+      if (last)
+        stockham_pass<INV>(R, in, out, count, p.nb[0], Ns, p.step[0], p.rnb[0], p.rns[0], tw, tid, nthr);
+      else
+        stockham_pass<INV>(R, in, LinMap{dst, n}, count, p.nb[0], Ns, p.step[0], p.rnb[0], p.rns[0], tw, tid,
+                           nthr);
+    } else {
+      float2* src = (pass & 1) ? b0 : b1;
+      if (last)
+        stockham_pass<INV>(R, LinMap{src, n}, out, count, p.nb[pass], Ns, p.step[pass], p.rnb[pass], p.rns[pass],
+                           tw, tid, nthr);
+      else
+        stockham_pass<INV>(R, LinMap{src, n}, LinMap{dst, n}, count, p.nb[pass], Ns, p.step[pass], p.rnb[pass],
+                           p.rns[pass], tw, tid, nthr);
+    }
+    sync();
+    Ns *= R;
+  }
+}
+
+// Where block_fft_io's last pass writes when `out` is a LinMap over one of b0 / b1.
+__host__ __device__ __forceinline__ float2* io_result_buf(const FftPlan& p, float2* b0, float2* b1) {
+  return ((p.npass - 1) & 1) ? b1 : b0;
+}
+
 // Buffer that holds the result when the input starts in buf0 and the last
 // pass writes through a LinMap over the returned buffer.
 __host__ __device__ __forceinline__ float2* result_buf(const FftPlan& p, float2* buf0, float2* buf1) {

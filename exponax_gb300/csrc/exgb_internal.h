@@ -18,6 +18,7 @@ struct PlanDev {
   int D, N, M, C, order, kind;
   int kmax;        // largest |k| kept by the dealiasing mask on every axis
   int lin_ch;      // 1 or C coefficient sets
+  float rN;        // 1/N in FP32 (the c2r scaling of the 1D kernel's packed inverse transforms)
   FftPlan fft;     // length-N complex FFT
   const float2* tw;  // N twiddles exp(-2 pi i k / N)
   // Coefficient tables.  1D: [lin_ch][M].  2D: [lin_ch][ky][kx] (ky-major).
