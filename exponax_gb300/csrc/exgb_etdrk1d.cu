@@ -516,7 +516,7 @@ static int smem_limit() {
 
 // Items for `batch` instances of one plan, m instances per item.
 static int choose_m(const PlanDev& P, int64_t batch, int sm_count, bool nonlin_only) {
-  int m = std::max(1, 1024 / P.N);
+  int m = std::max(1, 2048 / P.N);  // instances per item up to m N = 2048 (as the work queue)
   // spread small batches over the SMs first
   const int64_t per_sm = (batch + 2 * sm_count - 1) / (2 * (int64_t)sm_count);
   m = (int)std::max<int64_t>(1, std::min<int64_t>(m, per_sm));
@@ -629,7 +629,7 @@ static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps,
     if (p->dev.D != 1 || p->staged) return fail(EXGB_EUNSUPPORTED, "the work queue runs 1D single-channel plans");
     sm_count = p->sm_count;
     const int N = p->dev.N;
-    const int mmax = std::min(64, std::max(1, 1024 / N));
+    const int mmax = std::min(64, std::max(1, 2048 / N));  // 2048 / N measured best (1024: -8 %, 4096: -22 %)
     int m = 1;
     while (m < mmax && i + m < n_items && items[i + m].plan == p &&
            items[i + m].u0 == items[i].u0 + (int64_t)m * N && items[i + m].traj == items[i].traj + (int64_t)m * T * N)
