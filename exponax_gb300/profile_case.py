@@ -2,11 +2,15 @@
 
     python -m exponax_gb300.profile_case --dims 2 --n 256 --batch 32 --steps 10 --reps 3
     python -m exponax_gb300.profile_case --dims 2 --n 128 --kolmogorov --precision split_bf16
+    python -m exponax_gb300.profile_case --uneven 600 --steps 100 --reps 3
 
 Builds the stepper (NavierStokesVorticity in 2D, KuramotoSivashinsky-
 Conservative in 1D), creates device-resident Fourier states and launches
 ``repeat_fourier`` --reps times (one fused-kernel launch each), then
-synchronises.  Prints the CUDA-event time per launch.
+synchronises.  Prints the CUDA-event time per launch.  With --uneven K it
+instead builds the first K instances of the uneven 1D batch (Burgers / KdV /
+KS-conservative, N in {128 .. 4096}), captures their work-queue rollout in a
+CUDA graph and replays it --reps times.
 """
 
 from __future__ import annotations
@@ -26,12 +30,29 @@ def main():
     ap.add_argument("--order", type=int, default=2)
     ap.add_argument("--kolmogorov", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split_bf16"])
+    ap.add_argument("--uneven", type=int, default=0, help="instances of the uneven 1D work-queue batch")
     a = ap.parse_args()
 
     import torch
 
     import exponax_gb300 as ex
     from exponax_gb300 import _device, _lib
+
+    if a.uneven:
+        from exponax_gb300.batching import QueueRollout, uneven_config3
+
+        instances, _ = uneven_config3(a.uneven, a.steps, seed=0)
+        q = QueueRollout(instances, a.steps, include_init=True)
+        q.capture()
+        for _ in range(a.reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            q.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            print(f"uneven queue ({a.uneven} instances, {a.steps} steps): {e0.elapsed_time(e1):.3f} ms")
+        return
 
     if a.dims == 2:
         cls = ex.stepper.KolmogorovFlowVorticity if a.kolmogorov else ex.stepper.NavierStokesVorticity
