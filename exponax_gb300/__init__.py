@@ -8,7 +8,7 @@ Drop-in surface for the reference's hot path: ``stepper.*`` (``__call__``,
 CUDA, C ABI in include/exgb.h); there is no CPU fallback.
 """
 
-from . import etdrk, ic, metrics, nonlin_fun, poisson, spectral, stepper
+from . import etdrk, graphs, ic, metrics, nonlin_fun, poisson, spectral, stepper
 from ._lib import ExgbError
 from ._utils import (ForcedStepper, RepeatedStepper, make_grid, repeat, rollout, stack_sub_trajectories, vmap,
                      wrap_bc)
@@ -31,6 +31,7 @@ __all__ = [
     "etdrk",
     "fft",
     "get_spectrum",
+    "graphs",
     "ic",
     "ifft",
     "make_grid",

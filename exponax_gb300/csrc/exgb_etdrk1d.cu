@@ -528,6 +528,14 @@ static int choose_m(const PlanDev& P, int64_t batch, int sm_count, bool nonlin_o
 static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStream_t st, int nsteps, int mode,
                         int project, int include_init, int sm_count, bool nonlin_only, int threads = 256) {
   if (items.empty()) return EXGB_OK;
+  {
+    // the item list below is copied from host memory that is gone when a captured graph replays
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+      return fail(EXGB_EUNSUPPORTED,
+                  "1D stepping through the per-call entry points cannot be captured in a CUDA graph (its work list "
+                  "is copied from host memory); capture exgb_queue_launch of an exgb_queue_prepare'd queue instead");
+  }
   if (smem > (size_t)smem_limit() - 2048)
     return fail(EXGB_EUNSUPPORTED, "1D state does not fit in shared memory (N too large for this build)");
   // items + queue head in one workspace region (slot 2+: keep the transform slots free)

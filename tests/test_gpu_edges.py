@@ -124,3 +124,39 @@ def test_1d_batches_larger_than_the_gpu(name, order):
         assert rel(one[b], so(u[b])) < 1e-5, b
         assert rel(traj[b], o.rollout(so, 10, include_init=True)(u[b])) < 1e-4, b
     assert rel(traj[:3], small) < 1e-6
+
+
+@pytest.mark.parametrize("kind", ["ks1d", "ch1d", "ns2d", "burgers2d", "wave2d"])
+@pytest.mark.parametrize("trajectory", [True, False])
+def test_graph_rollout_replays_the_eager_result(kind, trajectory):
+    """GraphRollout (rollouts captured as CUDA graphs): two replays with different initial states equal
+    the eager vmap(rollout) / vmap(repeat) results within 1e-6 (the same kernels; in 1D the work queue
+    may pair other instances in the packed output transform, which changes the last bit)."""
+    if kind == "ks1d":
+        sm = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, 200, 0.1)
+        mk = lambda k: ex.ic.RandomSineWaves1d(1)(200, key=k)  # noqa: E731
+    elif kind == "ch1d":
+        sm = ex.stepper.reaction.CahnHilliard(1, 2 * np.pi, 64, 0.001, gamma=1e-3)
+        mk = lambda k: ex.ic.RandomSineWaves1d(1)(64, key=k)  # noqa: E731
+    elif kind == "ns2d":
+        sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, 64, 0.01, diffusivity=1e-3)
+        mk = lambda k: ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)(64, key=k)  # noqa: E731
+    elif kind == "burgers2d":
+        sm = ex.stepper.Burgers(2, 2 * np.pi, 32, 0.01, diffusivity=0.05)
+        g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=3, max_one=True)
+        mk = lambda k: np.concatenate([g(32, key=2 * k), g(32, key=2 * k + 1)])  # noqa: E731
+    else:
+        sm = ex.stepper.Wave(2, 1.0, 32, 0.01)
+        g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=3, max_one=True)
+        mk = lambda k: np.concatenate([g(32, key=2 * k), 0.3 * g(32, key=2 * k + 1)])  # noqa: E731
+    B, n = 3, 7
+    gr = ex.graphs.GraphRollout(sm, n, B, include_init=True, trajectory=trajectory)
+    eager = ex.vmap(ex.rollout(sm, n, include_init=True)) if trajectory else ex.vmap(ex.repeat(sm, n))
+    for base in (0, 10):
+        u = torch.from_numpy(np.stack([mk(base + b) for b in range(B)]).astype(np.float32)).cuda()
+        got = gr(u).clone()
+        want = eager(u)
+        assert tuple(got.shape) == tuple(want.shape)
+        np.testing.assert_allclose(got.cpu().numpy(), want.cpu().numpy(), rtol=0, atol=1e-6)
+    with pytest.raises(ValueError):
+        gr(torch.zeros((B + 1,) + gr.shape[1:], device="cuda"))
