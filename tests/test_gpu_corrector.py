@@ -120,3 +120,27 @@ def test_guard_trips_on_energetic_corrections():
     out = gs(u)
     assert int(gs.last_tripped.sum()) == 4
     assert torch.equal(out, plain)
+
+
+def test_trained_corrector_beats_the_plain_coarse_stepper():
+    """The learned part's gain, end to end on the GPU at small scale: Kolmogorov flow (nu 1e-3, drag
+    0.1, forcing k = 4) solved at 128^2 (dt 0.002, 3000-step spin-up) and downsampled to 64^2 every 8
+    fine steps; 64 trajectories x 30 pairs train the corrector (20 epochs, the project's BF16 kernels
+    and Adam); on 16 held-out seeds the guarded corrected 64^2 stepper (dt 0.016) has at most 0.85x
+    the relative L2 error of the plain 64^2 stepper after 1, 10 and 30 coarse steps (measured about
+    0.72x, 0.78x, 0.76x)."""
+    import exponax_gb300 as ex
+    from exponax_gb300 import kolmogorov_experiment as ke
+    from exponax_gb300.learned import PeriodicConvCorrector
+
+    kw = dict(n_fine=128, n_coarse_grid=64, dt=0.002, ratio=8, spinup=3000, n_coarse=30)
+    train_data, _ = ke.fine_coarse_trajectories(list(range(1000, 1064)), **kw)
+    eval_data, _ = ke.fine_coarse_trajectories(list(range(5000, 5016)), **kw)
+    coarse = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.016, **ke.KW)
+    net = PeriodicConvCorrector(H=64, seed=0, max_batch=128)
+    hist = ke.train(net, coarse, train_data, epochs=20, batch=128)
+    assert hist[-1] < 0.7 * hist[0]
+    res = ke.evaluate(eval_data, coarse, net)
+    plain, learned = res["plain"][0], res["learned"][0]
+    for t in (1, 10, 30):
+        assert learned[t] < 0.85 * plain[t], (t, learned[t], plain[t])
