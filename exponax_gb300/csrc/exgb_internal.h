@@ -132,4 +132,18 @@ int ndgen_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* 
 int etdrk0_apply(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                  int project);
 
+// FP32 sum with Kahan compensation per thread (the thread's running sum carries its rounding error);
+// device reductions combine the per-thread results by a pairwise warp/block tree.  About 1e-7 relative
+// for the metric and normalisation sums, as the reference's FP32 reductions; the GPU keeps FP64 for
+// the phi-coefficient contour integrals only.
+struct KahanSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+
 }  // namespace exgb

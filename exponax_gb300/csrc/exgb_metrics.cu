@@ -93,33 +93,45 @@ __global__ void spectrum_average_kernel(int64_t n, float* sums, const int* count
   if (i < n) sums[i] = counts[i] ? sums[i] / (float)counts[i] : nanf("");
 }
 
-// per field: sum (a-b)^2, sum b^2, sum a b, sum a^2 in FP64 (one CTA per field, block reduction)
+// Block sum of K per-thread values (K <= 4, blockDim.x <= 256); thread k < K gets the total of value k.
+template <int K>
+__device__ __forceinline__ void block_sum(float (&v)[K], float* red /* [K][8] */) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    if (lane == 0) red[q * 8 + w] = v[q];
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    KahanSum t;
+    for (int i = 0; i < nw; ++i) t.add(red[threadIdx.x * 8 + i]);
+#pragma unroll
+    for (int q = 0; q < K; ++q)
+      if (q == (int)threadIdx.x) v[q] = t.s;
+  }
+}
+
+// per field: sum (a-b)^2, sum b^2, sum a b, sum a^2 (one CTA per field)
 __global__ void __launch_bounds__(256) field_sums_kernel(int64_t n, const float* __restrict__ a,
                                                          const float* __restrict__ b, double* out) {
   const float* pa = a + (int64_t)blockIdx.x * n;
   const float* pb = b + (int64_t)blockIdx.x * n;
-  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  KahanSum s[4];
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-    const double x = pa[i], y = pb[i];
-    s[0] += (x - y) * (x - y);
-    s[1] += y * y;
-    s[2] += x * y;
-    s[3] += x * x;
+    const float x = pa[i], y = pb[i];
+    const float d = x - y;
+    s[0].add(d * d);
+    s[1].add(y * y);
+    s[2].add(x * y);
+    s[3].add(x * x);
   }
-  __shared__ double red[4][8];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ float red[4 * 8];
+  float v[4] = {s[0].s, s[1].s, s[2].s, s[3].s};
+  block_sum<4>(v, red);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    double v = s[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[k][w] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < 4) {
-    double v = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) v += red[threadIdx.x][i];
-    out[(int64_t)blockIdx.x * 4 + threadIdx.x] = v;
-  }
+  for (int q = 0; q < 4; ++q)
+    if (q == (int)threadIdx.x) out[(int64_t)blockIdx.x * 4 + q] = (double)v[q];
 }
 
 __device__ __forceinline__ float pow_abs(float x, float p) {
@@ -127,38 +139,27 @@ __device__ __forceinline__ float pow_abs(float x, float p) {
   return p == 1.f ? x : p == 2.f ? x * x : powf(x, p);
 }
 
-__device__ __forceinline__ void block_sum3(double (&v)[3], double* red /* [3][8] */) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int q = 0; q < 3; ++q) {
-    for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
-    if (lane == 0) red[q * 8 + w] = v[q];
-  }
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    double t = 0.0;
-    for (int i = 0; i < nw; ++i) t += red[threadIdx.x * 8 + i];
-    v[threadIdx.x] = t;
-  }
-}
-
 // One CTA per field of n floats: out[3 f + 0..2] = sum |a - b|^p, sum |a|^p, sum |b|^p
 // (b == nullptr: the difference is a itself and the last sum is 0) -- the aggregations behind
 // spatial_norm (metrics/_spatial.py:8-195), accumulated in FP64.
 __global__ void __launch_bounds__(256) field_pnorms_kernel(int64_t n, const float* __restrict__ a,
                                                            const float* __restrict__ b, float p, double* out) {
-  __shared__ double red[24];
+  __shared__ float red[3 * 8];
   const float* fa = a + (int64_t)blockIdx.x * n;
   const float* fb = b ? b + (int64_t)blockIdx.x * n : nullptr;
-  double v[3] = {0.0, 0.0, 0.0};
+  KahanSum s[3];
   for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
     const float x = fa[i];
     const float y = fb ? fb[i] : 0.f;
-    v[0] += pow_abs(fb ? x - y : x, p);
-    v[1] += pow_abs(x, p);
-    v[2] += pow_abs(y, p);
+    s[0].add(pow_abs(fb ? x - y : x, p));
+    s[1].add(pow_abs(x, p));
+    s[2].add(pow_abs(y, p));
   }
-  block_sum3(v, red);
-  if (threadIdx.x < 3) out[3 * (int64_t)blockIdx.x + threadIdx.x] = v[threadIdx.x];
+  float v[3] = {s[0].s, s[1].s, s[2].s};
+  block_sum<3>(v, red);
+#pragma unroll
+  for (int q = 0; q < 3; ++q)
+    if (q == (int)threadIdx.x) out[3 * (int64_t)blockIdx.x + q] = (double)v[q];
 }
 
 // One CTA per rfftn field (N..., N/2+1 modes): the sums of fourier_aggregator
@@ -171,12 +172,12 @@ __global__ void __launch_bounds__(256) field_pnorms_kernel(int64_t n, const floa
 __global__ void __launch_bounds__(256) fourier_pnorms_kernel(int D, int N, int64_t per, const float2* __restrict__ hat,
                                                              float p, float alpha, int use_deriv, int low, int high,
                                                              float kscale, double* out) {
-  __shared__ double red[24];
+  __shared__ float red[3 * 8];
   const int M = N / 2 + 1;
   const float2* h = hat + (int64_t)blockIdx.x * per;
-  double v[3] = {0.0, 0.0, 0.0};
-  double full = 1.0;
-  for (int d = 0; d < D; ++d) full *= (double)N;
+  KahanSum s[3];
+  float full = 1.f;
+  for (int d = 0; d < D; ++d) full *= (float)N;
   for (int64_t r = threadIdx.x; r < per; r += blockDim.x) {
     const float2 c = h[r];
     const float m = sqrtf(c.x * c.x + c.y * c.y);
@@ -194,16 +195,18 @@ __global__ void __launch_bounds__(256) fourier_pnorms_kernel(int D, int N, int64
     for (int a = 0; a < D; ++a) kmax = max(kmax, abs(k[a]));
     if (kmax < low || kmax > high) continue;
     const bool halve = kl != 0 && !((N % 2) == 0 && kl == N / 2);
-    const double base = (double)pow_abs(m, p) / (halve ? 0.5 * full : full);
+    const float base = pow_abs(m, p) / (halve ? 0.5f * full : full);
     if (!use_deriv) {
-      v[0] += base;
+      s[0].add(base);
     } else {
-      for (int a = 0; a < D; ++a) v[a] += base * (double)powf(kscale * (float)abs(k[a]), alpha * p);
+      for (int a = 0; a < D; ++a) s[a].add(base * powf(kscale * (float)abs(k[a]), alpha * p));
     }
   }
-  block_sum3(v, red);
+  float v[3] = {s[0].s, s[1].s, s[2].s};
+  block_sum<3>(v, red);
   const int nout = use_deriv ? D : 1;
-  if (threadIdx.x < nout) out[(int64_t)blockIdx.x * nout + threadIdx.x] = v[threadIdx.x];
+  for (int q = 0; q < 3; ++q)
+    if (q == (int)threadIdx.x && q < nout) out[(int64_t)blockIdx.x * nout + q] = (double)v[q];
 }
 
 }  // namespace

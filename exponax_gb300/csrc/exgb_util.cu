@@ -38,41 +38,41 @@ __global__ void scatter_kernel(int64_t count, int64_t field_elems, int nmodes, c
   }
 }
 
-// one CTA per field: FP64 mean, then (std_one) the FP64 population standard deviation or (max_one)
+// one CTA per field: the mean, then (std_one) the population standard deviation or (max_one)
 // max |u - mean|, then (u - mean) * scale with the mean subtracted only when zero_mean -- normalize_ic
 // (ic/_base_ic.py:18-32) in its order; std_one without zero_mean divides by the standard deviation
-// alone, as SineWaves1d does (ic/_sine_waves_1d.py:72-77)
+// alone, as SineWaves1d does (ic/_sine_waves_1d.py:72-77).  FP32 sums with Kahan compensation.
+__device__ __forceinline__ float block_total(float v, float* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  KahanSum t;
+  for (int i = 0; i < nw; ++i) t.add(red[i]);
+  __syncthreads();  // red may be reused by the caller
+  return t.s;
+}
+
 __global__ void __launch_bounds__(256) normalize_kernel(int64_t n, float* u, int zero_mean, int std_one,
                                                         int max_one) {
   float* p = u + (int64_t)blockIdx.x * n;
-  __shared__ double red[8];
+  __shared__ float red[8];
   __shared__ float redf[8];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  double s = 0.0;
+  KahanSum s;
   if (zero_mean || std_one)
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += p[i];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) red[w] = s;
-  __syncthreads();
-  double tot = 0.0;
-  for (int i = 0; i < nw; ++i) tot += red[i];
-  const float fmean = (float)(tot / (double)n);
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s.add(p[i]);
+  const float fmean = block_total(s.s, red) / (float)n;
   const float mean = zero_mean ? fmean : 0.f;
-  __syncthreads();  // red is reused below
   float inv = 1.f;
   if (std_one) {
-    double q = 0.0;
+    KahanSum q;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-      const double d = (double)(p[i] - fmean);
-      q += d * d;
+      const float d = p[i] - fmean;
+      q.add(d * d);
     }
-    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
-    if (lane == 0) red[w] = q;
-    __syncthreads();
-    double qt = 0.0;
-    for (int i = 0; i < nw; ++i) qt += red[i];
-    const double sd = sqrt(qt / (double)n);
-    if (sd > 0.0) inv = (float)(1.0 / sd);
+    const float sd = sqrtf(block_total(q.s, red) / (float)n);
+    if (sd > 0.f) inv = 1.f / sd;
   }
   float mx = 0.f;
   if (max_one)
