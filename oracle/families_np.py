@@ -5,7 +5,8 @@ only ``tests/`` may import it; the product package never does.
 
 Follows exponax 0.2.0:
   stepper/reaction/_fisher_kpp.py, _allen_cahn.py, _cahn_hilliard.py,
-  _gray_scott.py, _swift_hohenberg.py (each stepper and its nonlinear function);
+  _gray_scott.py, _swift_hohenberg.py, _belousov_zhabotinsky.py (each stepper
+  and its nonlinear function);
   stepper/generic/_linear.py, _convection.py, _gradient_norm.py,
   _polynomial.py, _nonlinear.py, _vorticity_convection.py, _utils.py
   (General / Normalized / Difficulty steppers and the coefficient algebra).
