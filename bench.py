@@ -233,8 +233,10 @@ def run_gb300(args, rank, ws):
         torch.distributed.barrier()
 
     # ---- value: device-resident inputs, the fused 2D kernel (1 launch per bench step)
-    clocks = ClockSampler(os.path.join(ROOT, "gpurun_out", f"bench_clocks_r{rank}.csv")
-                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/bench_clocks_r{rank}.csv")
+    import tempfile
+
+    clocks = ClockSampler(os.path.join(os.environ.get("EXGB_CLOCKS_DIR", tempfile.gettempdir()),
+                                       f"bench_clocks_r{rank}.csv"))
     clocks.start()
     times = []
     for _ in range(args.steps):
