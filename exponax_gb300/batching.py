@@ -95,7 +95,7 @@ class QueueRollout:
 
 
 def uneven_config3(num_instances=3000, nsteps=100, seed=0):
-    """The uneven 1D batch of the benchmark configuration: a seeded
+    """The uneven 1D benchmark batch: a seeded
     multinomial over Burgers (L=1, nu=0.01, dt=1e-3), KdV (L=20, dispersion 1,
     hyper-diffusion 0.01, dt=0.01) and KS-conservative (L=100, dt=0.1), N
     uniform over {128, ..., 4096}, sine-series ICs (cutoff 5) per seed.

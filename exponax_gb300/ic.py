@@ -11,9 +11,9 @@ build their fields on the GPU (``device_batch``, ``build_ic_set(device=True)``,
 discontinuities) are evaluated on the host grid as the reference evaluates them
 on its grid.
 
-``RandomAmplitudePhaseSeries`` is the benchmark configurations' recipe (random
+``RandomAmplitudePhaseSeries`` is the benchmark workloads' recipe (random
 amplitudes U(-1, 1) and phases U(0, 2 pi) of the modes |k_d| <= cutoff), which
-the configurations call a "random truncated Fourier series"; the reference's
+the benchmark descriptions call a "random truncated Fourier series"; the reference's
 ``RandomTruncatedFourierSeries`` is low-pass-filtered white noise and is
 provided under its own name with its own recipe.
 """
@@ -185,7 +185,7 @@ class RandomSineWaves1d(BaseRandomICGenerator):
 
 
 class RandomAmplitudePhaseSeries:
-    """The benchmark configurations' "random truncated Fourier series": one cosine per +-k pair of the
+    """The benchmark workloads' "random truncated Fourier series": one cosine per +-k pair of the
     modes |k_d| <= cutoff on every axis (the hypercube of ic/_truncated_fourier_series.py's low-pass)
     with amplitude U(-1, 1) and phase U(0, 2 pi), zero mean, optionally rescaled to max |u| = 1
     (normalize_ic, ic/_base_ic.py:18-32).  In 1D it is RandomSineWaves1d's series."""
