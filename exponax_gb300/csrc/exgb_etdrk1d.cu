@@ -107,6 +107,7 @@ struct Bufs {
   float2 *U, *S1, *S, *N0, *N1, *N2;
   float2 *w0, *w1;
   float* sums;
+  const float2* tw;  // the item's twiddles: a shared-memory copy when it fits, else the plan's global table
 };
 
 // Stage epilogue: combine the fresh nonlinear value nv at mode k of instance
@@ -242,14 +243,14 @@ __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m,
   if (fuse && !zmf) {  // compile-time fuse: each kernel carries one of the two paths
     res = io_result_buf(P.fft, b.w0, b.w1);
     other = (res == b.w0) ? b.w1 : b.w0;
-    block_fft_io<true>(P.fft, PackSrc{&P, X, M}, b.w0, b.w1, ProductOut{&P, res}, m, P.tw, tid, nthr, BlockSync{});
+    block_fft_io<true>(P.fft, PackSrc{&P, X, M}, b.w0, b.w1, ProductOut{&P, res}, m, b.tw, tid, nthr, BlockSync{});
   } else {
     // separate pack and product phases (the zero-mode fix also needs u_x^2 in a buffer of its own)
     nl_pack(P, X, M, b.w0, m, tid, nthr);
     __syncthreads();
     res = (P.fft.npass & 1) ? b.w1 : b.w0;
     other = (P.fft.npass & 1) ? b.w0 : b.w1;
-    block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, P.tw, tid, nthr, BlockSync{});
+    block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, b.tw, tid, nthr, BlockSync{});
     nl_products(P, res, (float*)other, m, tid, nthr);
     __syncthreads();
     if (zmf) {
@@ -259,7 +260,7 @@ __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m,
   }
   // forward: input in res, passes ping-pong other <-> res
   float2* fres = io_result_buf(P.fft, other, res);
-  block_fft_io<false>(P.fft, LinMap{res, N}, other, res, LinMap{fres, N}, m, P.tw, tid, nthr, BlockSync{});
+  block_fft_io<false>(P.fft, LinMap{res, N}, other, res, LinMap{fres, N}, m, b.tw, tid, nthr, BlockSync{});
   for (int t = tid; t < m * M; t += nthr) {
     const int i = t / M, k = t - i * M;
     float2 nv = make_float2(0.f, 0.f);
@@ -323,7 +324,7 @@ __device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, in
                           int nthr) {
   const int pairs = (m + 1) / 2;
   if constexpr (fuse) {
-    block_fft_io<true>(P.fft, EmitSrc{&P, b.U, m}, b.w0, b.w1, EmitOut{out, inst_stride, m}, pairs, P.tw, tid,
+    block_fft_io<true>(P.fft, EmitSrc{&P, b.U, m}, b.w0, b.w1, EmitOut{out, inst_stride, m}, pairs, b.tw, tid,
                        nthr, BlockSync{});
     return;
   }
@@ -335,7 +336,7 @@ __device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, in
   }
   __syncthreads();
   float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
-  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, P.tw, tid, nthr, BlockSync{});
+  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, b.tw, tid, nthr, BlockSync{});
   for (int t = tid; t < pairs * N; t += nthr) {
     const int p = t / N, x = t - p * N;
     const float2 z = res[t];
@@ -348,7 +349,7 @@ __device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, in
 template <bool FUSE>
 __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__ items, int n_items,
                                                       int* __restrict__ head, int nsteps, int mode, int project,
-                                                      int include_init) {
+                                                      int include_init, int smem_bytes) {
   extern __shared__ __align__(16) float2 sm[];
   __shared__ PlanDev Ps;
   __shared__ int s_item;
@@ -387,7 +388,16 @@ __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__
     b.w0 = q;
     q += m * N;
     b.w1 = q;
+    q += m * N;
     b.sums = s_sums;
+    // the twiddles go into the dynamic shared memory left over by this item (the launch reserves the
+    // largest item's footprint, or room for them); the copy is complete at the barrier below
+    if ((size_t)(q - sm + N) * sizeof(float2) <= (size_t)smem_bytes) {
+      for (int i = tid; i < N; i += nthr) q[i] = __ldg(P.tw + i);
+      b.tw = q;
+    } else {
+      b.tw = P.tw;
+    }
 
     // ---- load initial state
     if (mode == MODE_TRAJ || mode == MODE_FINAL) {
@@ -406,7 +416,7 @@ __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__
       }
       __syncthreads();
       float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
-      block_fft<false>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, P.tw, tid, nthr, BlockSync{});
+      block_fft<false>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, b.tw, tid, nthr, BlockSync{});
       for (int t = tid; t < pairs * M; t += nthr) {
         const int p = t / M, k = t - p * M;
         float2 A, B;
@@ -484,6 +494,7 @@ __global__ void __launch_bounds__(256) nonlin1d_kernel(const Item1D* __restrict_
   b.w0 = sm + m * M;
   b.w1 = b.w0 + m * N;
   b.sums = s_sums;
+  b.tw = P.tw;
   const float2* uh = (const float2*)item.in;
   for (int t = tid; t < m * M; t += nthr) {
     const int i = t / M, k = t - i * M;
@@ -562,7 +573,7 @@ static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStrea
     per_sm = std::max(1, per_sm);
     const int grid = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)sm_count * per_sm);
     kern<<<grid, threads, smem, st>>>((const Item1D*)ws, (int)items.size(), head, nsteps, mode, project,
-                                      include_init);
+                                      include_init, (int)smem);
   }
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
@@ -610,8 +621,11 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
   // 256 unless tuned: fewer threads measured slower for small latency-bound items (N = 200, one
   // instance per CTA) and the autotuner picks 128 where it wins
   const int threads = plan->tune_threads_1d > 0 ? plan->tune_threads_1d : 256;
-  return launch_items(items, smem_for(P, m, nonlinear_only), st, nsteps, mode, project, include_init,
-                      plan->sm_count, nonlinear_only, threads);
+  // room for a shared-memory copy of the twiddles when it does not cost occupancy headroom beyond the limit
+  size_t smem = smem_for(P, m, nonlinear_only);
+  if (!nonlinear_only && smem + sizeof(float2) * (size_t)P.N <= (size_t)smem_limit() - 4096)
+    smem += sizeof(float2) * (size_t)P.N;
+  return launch_items(items, smem, st, nsteps, mode, project, include_init, plan->sm_count, nonlinear_only, threads);
 }
 
 }  // namespace exgb
@@ -729,7 +743,8 @@ extern "C" int exgb_queue_launch(exgb_queue* q, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   EXGB_CUDA(cudaMemsetAsync(q->d_head, 0, sizeof(int), st));
   auto kern = q->n_items > q->sm_count ? etdrk1d_kernel<true> : etdrk1d_kernel<false>;
-  kern<<<q->grid, 256, q->smem, st>>>(q->d_items, q->n_items, q->d_head, q->nsteps, MODE_TRAJ, 1, q->include_init);
+  kern<<<q->grid, 256, q->smem, st>>>(q->d_items, q->n_items, q->d_head, q->nsteps, MODE_TRAJ, 1, q->include_init,
+                                      (int)q->smem);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }
