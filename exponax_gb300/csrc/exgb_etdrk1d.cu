@@ -347,9 +347,10 @@ __device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, in
 }
 
 template <bool FUSE>
-__global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__ items, int n_items,
+__global__ void __launch_bounds__(256, 3) etdrk1d_kernel(const Item1D* __restrict__ items, int n_items,
                                                       int* __restrict__ head, int nsteps, int mode, int project,
-                                                      int include_init, int smem_bytes) {
+                                                      int include_init, int smem_bytes, float2* gstate,
+                                                      int64_t gstate_stride) {
   extern __shared__ __align__(16) float2 sm[];
   __shared__ PlanDev Ps;
   __shared__ int s_item;
@@ -365,9 +366,13 @@ __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__
     __syncthreads();
     const PlanDev& P = Ps;
     const int N = P.N, M = P.M, m = item.m;
-    // carve shared memory
+    // carve shared memory: the ETDRK state buffers and the two work buffers when the item fits in the
+    // launch's reservation; otherwise the state buffers live in this CTA's global slot (L2-resident)
+    // and only the work buffers in shared memory (the work queue reserves what keeps 3 CTAs per SM)
     Bufs b;
-    float2* q = sm;
+    const size_t state_elems = (size_t)nbuf_for_order(P.order) * m * M, work_elems = 2 * (size_t)m * N;
+    const bool local = (state_elems + work_elems) * sizeof(float2) <= (size_t)smem_bytes;
+    float2* q = local ? sm : gstate + (int64_t)blockIdx.x * gstate_stride;
     b.U = q;
     q += m * M;
     b.S1 = b.S = b.N0 = b.N1 = b.N2 = nullptr;
@@ -385,6 +390,7 @@ __global__ void __launch_bounds__(256) etdrk1d_kernel(const Item1D* __restrict__
       b.N1 = q; q += m * M;
       b.N2 = q; q += m * M;
     }
+    if (!local) q = sm;
     b.w0 = q;
     q += m * N;
     b.w1 = q;
@@ -537,7 +543,8 @@ static int choose_m(const PlanDev& P, int64_t batch, int sm_count, bool nonlin_o
 }
 
 static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStream_t st, int nsteps, int mode,
-                        int project, int include_init, int sm_count, bool nonlin_only, int threads = 256) {
+                        int project, int include_init, int sm_count, bool nonlin_only, int threads = 256,
+                        size_t gstate_bytes = 0) {
   if (items.empty()) return EXGB_OK;
   {
     // the item list below is copied from host memory that is gone when a captured graph replays
@@ -572,8 +579,13 @@ static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStrea
     EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
     per_sm = std::max(1, per_sm);
     const int grid = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)sm_count * per_sm);
+    float2* gstate = nullptr;
+    if (gstate_bytes) {
+      gstate = (float2*)workspace(gstate_bytes * (size_t)grid, 6);
+      if (!gstate) return fail(EXGB_ENOMEM, "workspace allocation failed");
+    }
     kern<<<grid, threads, smem, st>>>((const Item1D*)ws, (int)items.size(), head, nsteps, mode, project,
-                                      include_init, (int)smem);
+                                      include_init, (int)smem, gstate, (int64_t)(gstate_bytes / sizeof(float2)));
   }
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
@@ -636,14 +648,20 @@ namespace exgb {
 
 // Groups consecutive instances of the same plan with evenly strided buffers
 // into items of up to m instances and sorts the items longest first.
+// Shared memory one queue CTA reserves when that keeps 3 CTAs of 256 threads per SM; items whose full
+// footprint is larger keep their ETDRK state buffers in a per-CTA global slot (see etdrk1d_kernel).
+constexpr size_t kQueueSmemCap = 72 * 1024;
+
 static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps, int include_init,
-                       std::vector<Item1D>& sorted, size_t& smem, int& sm_count) {
+                       std::vector<Item1D>& sorted, size_t& smem, int& sm_count, size_t& gstate_bytes) {
   if (n_items < 0 || (n_items > 0 && !items)) return fail(EXGB_EINVAL, "bad work item list");
   if (nsteps < 0) return fail(EXGB_EINVAL, "nsteps must be >= 0");
   const int T = nsteps + (include_init ? 1 : 0);
   std::vector<Item1D> its;
   std::vector<double> cost;
   smem = 0;
+  gstate_bytes = 0;
+  size_t full_max = 0;
   sm_count = 0;
   for (int64_t i = 0; i < n_items;) {
     const exgb_plan* p = items[i].plan;
@@ -666,8 +684,19 @@ static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps,
     its.push_back(it);
     const double lg = std::log2((double)N);
     cost.push_back((double)m * N * lg * (p->dev.order + 1));
-    smem = std::max(smem, smem_for(p->dev, m, false));
+    full_max = std::max(full_max, smem_for(p->dev, m, false));
+    const size_t full = smem_for(p->dev, m, false), work = sizeof(float2) * 2 * (size_t)m * N;
+    if (full <= kQueueSmemCap) {
+      smem = std::max(smem, full);
+    } else {
+      smem = std::max(smem, work);
+      gstate_bytes = std::max(gstate_bytes, full - work);
+    }
     i += m;
+  }
+  if (smem > kQueueSmemCap) {  // some item's work buffers alone exceed the cap: reserve full footprints
+    smem = full_max;
+    gstate_bytes = 0;
   }
   std::vector<size_t> idx(its.size());
   for (size_t k = 0; k < idx.size(); ++k) idx[k] = k;
@@ -687,6 +716,8 @@ struct exgb_queue {
   int* d_head = nullptr;
   int n_items = 0;
   size_t smem = 0;
+  float2* d_gstate = nullptr;  // per-CTA global slots for the state buffers of the largest items
+  size_t gstate_bytes = 0;     // per CTA
   int grid = 1;
   int sm_count = 1;
   int nsteps = 0;
@@ -697,11 +728,12 @@ extern "C" int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, 
                                   int32_t include_init, void* stream) {
   if (n_items == 0) return EXGB_OK;
   std::vector<Item1D> sorted;
-  size_t smem = 0;
+  size_t smem = 0, gstate_bytes = 0;
   int sm_count = 0;
-  const int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count);
+  const int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count, gstate_bytes);
   if (rc) return rc;
-  return launch_items(sorted, smem, (cudaStream_t)stream, nsteps, MODE_TRAJ, 1, include_init, sm_count, false);
+  return launch_items(sorted, smem, (cudaStream_t)stream, nsteps, MODE_TRAJ, 1, include_init, sm_count, false, 256,
+                      gstate_bytes);
 }
 
 extern "C" int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, int32_t nsteps, int32_t include_init,
@@ -710,13 +742,14 @@ extern "C" int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, 
   *out = nullptr;
   if (n_items < 1) return fail(EXGB_EINVAL, "empty work item list");
   std::vector<Item1D> sorted;
-  size_t smem = 0;
+  size_t smem = 0, gstate_bytes = 0;
   int sm_count = 0;
-  int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count);
+  int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count, gstate_bytes);
   if (rc) return rc;
   exgb_queue* q = new exgb_queue();
   q->n_items = (int)sorted.size();
   q->smem = smem;
+  q->gstate_bytes = gstate_bytes;
   q->nsteps = nsteps;
   q->include_init = include_init ? 1 : 0;
   q->sm_count = sm_count;
@@ -734,6 +767,10 @@ extern "C" int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, 
   int per_sm = 1;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem) != cudaSuccess) per_sm = 1;
   q->grid = (int)std::min<int64_t>((int64_t)sorted.size(), (int64_t)sm_count * std::max(1, per_sm));
+  if (gstate_bytes && (e = cudaMalloc(&q->d_gstate, gstate_bytes * (size_t)q->grid)) != cudaSuccess) {
+    exgb_queue_destroy(q);
+    return cuda_fail(e, "exgb_queue_prepare");
+  }
   *out = q;
   return EXGB_OK;
 }
@@ -744,7 +781,7 @@ extern "C" int exgb_queue_launch(exgb_queue* q, void* stream) {
   EXGB_CUDA(cudaMemsetAsync(q->d_head, 0, sizeof(int), st));
   auto kern = q->n_items > q->sm_count ? etdrk1d_kernel<true> : etdrk1d_kernel<false>;
   kern<<<q->grid, 256, q->smem, st>>>(q->d_items, q->n_items, q->d_head, q->nsteps, MODE_TRAJ, 1, q->include_init,
-                                      (int)q->smem);
+                                      (int)q->smem, q->d_gstate, (int64_t)(q->gstate_bytes / sizeof(float2)));
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }
@@ -753,6 +790,7 @@ extern "C" int exgb_queue_destroy(exgb_queue* q) {
   if (!q) return EXGB_OK;
   cudaFree(q->d_items);
   cudaFree(q->d_head);
+  cudaFree(q->d_gstate);
   delete q;
   return EXGB_OK;
 }
