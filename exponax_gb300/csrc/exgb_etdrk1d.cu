@@ -516,6 +516,10 @@ __global__ void __launch_bounds__(256) nonlin1d_kernel(const Item1D* __restrict_
   }
 }
 
+// Shared memory a 1D CTA reserves when that keeps 3 CTAs of 256 threads per SM; items whose full
+// footprint is larger keep their ETDRK state buffers in a per-CTA global slot (see etdrk1d_kernel).
+constexpr size_t kQueueSmemCap = 72 * 1024;
+
 static size_t smem_for(const PlanDev& P, int m, bool nonlin_only) {
   const int nb = nonlin_only ? 1 : nbuf_for_order(P.order);
   return sizeof(float2) * (size_t)m * ((size_t)nb * P.M + 2 * (size_t)P.N);
@@ -633,11 +637,20 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
   // 256 unless tuned: fewer threads measured slower for small latency-bound items (N = 200, one
   // instance per CTA) and the autotuner picks 128 where it wins
   const int threads = plan->tune_threads_1d > 0 ? plan->tune_threads_1d : 256;
-  // room for a shared-memory copy of the twiddles when it does not cost occupancy headroom beyond the limit
-  size_t smem = smem_for(P, m, nonlinear_only);
-  if (!nonlinear_only && smem + sizeof(float2) * (size_t)P.N <= (size_t)smem_limit() - 4096)
-    smem += sizeof(float2) * (size_t)P.N;
-  return launch_items(items, smem, st, nsteps, mode, project, include_init, plan->sm_count, nonlinear_only, threads);
+  // shared memory: as the work queue, at most kQueueSmemCap per CTA (3 CTAs per SM) when the items'
+  // work buffers fit in it -- the state buffers then go to per-CTA global slots -- plus a copy of the
+  // twiddles when that still fits
+  size_t smem = smem_for(P, m, nonlinear_only), gstate_bytes = 0;
+  if (!nonlinear_only) {
+    const size_t work = sizeof(float2) * 2 * (size_t)m * P.N, tw = sizeof(float2) * (size_t)P.N;
+    if (smem > kQueueSmemCap && work <= kQueueSmemCap) {
+      gstate_bytes = smem - work;
+      smem = work;
+    }
+    if (smem + tw <= kQueueSmemCap) smem += tw;
+  }
+  return launch_items(items, smem, st, nsteps, mode, project, include_init, plan->sm_count, nonlinear_only, threads,
+                      gstate_bytes);
 }
 
 }  // namespace exgb
@@ -648,10 +661,6 @@ namespace exgb {
 
 // Groups consecutive instances of the same plan with evenly strided buffers
 // into items of up to m instances and sorts the items longest first.
-// Shared memory one queue CTA reserves when that keeps 3 CTAs of 256 threads per SM; items whose full
-// footprint is larger keep their ETDRK state buffers in a per-CTA global slot (see etdrk1d_kernel).
-constexpr size_t kQueueSmemCap = 72 * 1024;
-
 static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps, int include_init,
                        std::vector<Item1D>& sorted, size_t& smem, int& sm_count, size_t& gstate_bytes) {
   if (n_items < 0 || (n_items > 0 && !items)) return fail(EXGB_EINVAL, "bad work item list");
