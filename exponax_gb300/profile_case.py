@@ -31,6 +31,8 @@ def main():
     ap.add_argument("--kolmogorov", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split_bf16"])
     ap.add_argument("--uneven", type=int, default=0, help="instances of the uneven 1D work-queue batch")
+    ap.add_argument("--pde", default="", choices=["", "burgers", "grayscott"],
+                    help="2D/3D Burgers or Gray-Scott on the staged N-D path instead of the vorticity / KS steppers")
     a = ap.parse_args()
 
     import torch
@@ -54,7 +56,16 @@ def main():
             print(f"uneven queue ({a.uneven} instances, {a.steps} steps): {e0.elapsed_time(e1):.3f} ms")
         return
 
-    if a.dims == 2:
+    if a.pde == "burgers":
+        st = ex.stepper.Burgers(a.dims, 2 * np.pi, a.n, 0.01, diffusivity=0.05, order=a.order)
+        g = ex.ic.RandomAmplitudePhaseSeries(a.dims, cutoff=4, max_one=True)
+    elif a.pde == "grayscott":
+        st = ex.stepper.reaction.GrayScott(a.dims, 1.0, a.n, 0.5, order=a.order)
+        g = ex.ic.RandomAmplitudePhaseSeries(a.dims, cutoff=2, max_one=True)
+    elif a.dims == 3:
+        st = ex.stepper.NavierStokesVelocity(3, 2 * np.pi, a.n, 0.01, order=a.order)
+        g = ex.ic.RandomAmplitudePhaseSeries(3, cutoff=3, max_one=True)
+    elif a.dims == 2:
         cls = ex.stepper.KolmogorovFlowVorticity if a.kolmogorov else ex.stepper.NavierStokesVorticity
         kw = {} if a.kolmogorov else {"diffusivity": 1e-3}
         st = cls(2, 2 * np.pi, a.n, 0.01, order=a.order, **kw)
@@ -64,7 +75,11 @@ def main():
     else:
         st = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, a.n, 0.1, order=a.order)
         g = ex.ic.RandomSineWaves1d(1, cutoff=5)
-    u0 = torch.from_numpy(np.stack([g(a.n, key=s) for s in range(a.batch)])).cuda()
+    C = st.num_channels
+    u0 = torch.from_numpy(np.stack([np.concatenate([g(a.n, key=C * s + c) for c in range(C)])
+                                    for s in range(a.batch)])).cuda()
+    if a.pde == "grayscott":
+        u0 = torch.stack([1.0 - 0.25 * (1 + u0[:, 0]), 0.25 * (1 + u0[:, 1])], dim=1).contiguous()
     uh = ex.fft(u0, num_spatial_dims=a.dims)
     out = torch.empty_like(uh)
     lib = _lib.load()
@@ -77,7 +92,7 @@ def main():
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
-        dofs = a.batch * a.n**a.dims * a.steps
+        dofs = a.batch * st.num_channels * a.n**a.dims * a.steps  # channels x grid points
         print(f"repeat_fourier: {ms:.3f} ms, {dofs / ms * 1e3:.3e} DOF-steps/s")
 
 
