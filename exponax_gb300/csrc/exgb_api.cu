@@ -477,7 +477,7 @@ extern "C" int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int 
     const int old = plan->tune_cluster;
     plan->tune_cluster = G;
     int rc = etdrk2d_configure(plan);
-    if (rc || (G && (plan->cfg2d.variant != 1 || plan->cfg2d.G != G))) {
+    if (rc || (G && plan->cfg2d.G != G)) {
       cudaFree(plan->d_scratch);
       plan->d_scratch = nullptr;
       plan->tune_cluster = old;

@@ -12,7 +12,7 @@
 //
 // Work split inside a cluster of G CTAs:
 //   * CTA g owns masked columns [g*Cl, min(Kc, (g+1)*Cl)) and physical rows
-//     [g*Rl, (g+1)*Rl), Rl = N/G.
+//     [g*Rl, min(N, (g+1)*Rl)), Rl = ceil(N/G) (the last CTA may own fewer).
 //   * Column phase (per owned column, in batches of CB columns):
 //       forward FFT along kx of the dealiased product (gathered from the
 //       row owners' shared memory), -b scaling + forcing, ETDRK stage update
@@ -188,6 +188,7 @@ __global__ void __launch_bounds__(512, 1) etdrk2d_kernel(const Args2D a) {
   const int col0 = g * Cl;
   const int ncols = max(0, min(Kc, col0 + Cl) - col0);
   const int row0 = g * Rl;
+  const int myRl = max(0, min(Rl, N - row0));
   const float invNN = 1.f / ((float)N * (float)N);
   const float negb = -P.conv_scale;
   const int nst = a.nonlinear_only ? 1 : P.order;
@@ -268,8 +269,8 @@ __global__ void __launch_bounds__(512, 1) etdrk2d_kernel(const Args2D a) {
       cluster.sync();  // mixed complete
 
       // ---------------- row phase
-      for (int rb0 = 0; rb0 < Rl; rb0 += RB) {
-        const int nr = min(RB, Rl - rb0);
+      for (int rb0 = 0; rb0 < myRl; rb0 += RB) {
+        const int nr = min(RB, myRl - rb0);
         for (int t = tid; t < nr * N; t += nthr) {
           const int r = t / N, k = t - r * N;
           const int x = row0 + rb0 + r;
@@ -464,35 +465,74 @@ int etdrk2d_configure(exgb_plan* plan) {
   const size_t limit = (size_t)lim - 1024;  // static shared memory headroom
   const int threads = N >= 128 ? 512 : 256;
   if (N > 2 * threads) return fail(EXGB_EUNSUPPORTED, "N too large for the 2D kernel in this build");
+  // Candidates: cluster size G (the autotuner's choice, else EXGB_CLUSTER, else 1..8; a CTA owns
+  // ceil(N/G) rows), columns (CB) and rows (RB) per transform batch (EXGB_2D_CB / EXGB_2D_RB, else
+  // about twelve, eight or four points per thread per transform), mixed fields in distributed
+  // shared memory or in a per-cluster global buffer.  The kernel waits at a block barrier after
+  // every radix pass, so larger batches amortise the barriers: at 512^2 (Kolmogorov, 20 steps, per
+  // sample and CTA-wave) twelve points per thread cost 0.70x and eight 0.75x the time of four; 256
+  // threads instead of 512 were slower.  Choice: mixed fields in shared memory when any candidate
+  // fits so, then the most SMs kept busy (co-resident clusters x G from the occupancy query, at
+  // most the SM count) weighted by that batch efficiency, ties to the smaller cluster.
+  const char* envG = getenv("EXGB_CLUSTER");
+  const int wantG = plan->tune_cluster > 0 ? plan->tune_cluster : (envG ? atoi(envG) : 0);
+  const char* envCB = getenv("EXGB_2D_CB");
+  const char* envRB = getenv("EXGB_2D_RB");
+  const int wantCB = envCB ? atoi(envCB) : 0;
+  const int wantRB = envRB ? atoi(envRB) : 0;
+  // the opt-in maximum (every generic 2D plan launches this kernel with its own footprint)
+  EXGB_CUDA(cudaFuncSetAttribute(etdrk2d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
   bool found = false;
+  double best = -1.0;
   for (int mis = 1; mis >= 0 && !found; --mis) {
-    for (int G : {1, 2, 4, 8}) {
-      if (N % G || (N / G) < 2) continue;
-      const int Cl = (Kc + G - 1) / G;
-      const int Rl = N / G;
-      int CB = std::max(1, std::min(Cl, (threads * 4) / (4 * N)));
-      int RB = std::max(2, std::min(Rl, (threads * 4) / (2 * N)));
-      RB += RB & 1;
-      const size_t wlen = std::max((size_t)4 * CB * N, (size_t)2 * RB * N);
-      size_t words = (size_t)N + (size_t)Rl * Kc + (size_t)CB * N + 2 * wlen;
-      if (mis) words += (size_t)4 * N * Cl;
-      const size_t bytes = words * sizeof(float2);
-      if (bytes <= limit) {
-        c.G = G;
-        c.threads = threads;
-        c.cols_per_cta = Cl;
-        c.rows_per_cta = Rl;
-        c.CB = CB;
-        c.RB = RB;
-        c.mixed_in_smem = mis;
-        c.smem_bytes = bytes;
-        found = true;
-        break;
+    for (int pts : {12, 8, 4}) {
+      const double eff = pts == 12 ? 1.42 : pts == 8 ? 1.34 : 1.0;
+      for (int G = 1; G <= 8; ++G) {
+        if (wantG && wantG != G) continue;
+        const int Rl = (N + G - 1) / G;
+        if (Rl < 2 || (G - 1) * Rl >= N) continue;
+        const int Cl = (Kc + G - 1) / G;
+        int CB = std::max(1, std::min(Cl, wantCB > 0 ? wantCB : (threads * pts) / (4 * N)));
+        int RB = std::max(2, std::min(Rl, wantRB > 0 ? wantRB : (threads * pts) / (2 * N)));
+        RB += RB & 1;
+        const size_t wlen = std::max((size_t)4 * CB * N, (size_t)2 * RB * N);
+        size_t words = (size_t)N + (size_t)Rl * Kc + (size_t)CB * N + 2 * wlen;
+        if (mis) words += (size_t)4 * N * Cl;
+        const size_t bytes = words * sizeof(float2);
+        if (bytes > limit) continue;
+        cudaLaunchConfig_t q = {};
+        cudaLaunchAttribute qa[1];
+        qa[0].id = cudaLaunchAttributeClusterDimension;
+        qa[0].val.clusterDim.x = G;
+        qa[0].val.clusterDim.y = 1;
+        qa[0].val.clusterDim.z = 1;
+        q.gridDim = dim3(G * plan->sm_count, 1, 1);
+        q.blockDim = dim3(threads, 1, 1);
+        q.dynamicSmemBytes = bytes;
+        q.attrs = qa;
+        q.numAttrs = 1;
+        int nq = 0;
+        if (cudaOccupancyMaxActiveClusters(&nq, (void*)etdrk2d_kernel, &q) != cudaSuccess || nq <= 0) {
+          cudaGetLastError();
+          continue;
+        }
+        const double score = (double)std::min(nq * G, plan->sm_count) * eff;
+        if (score > best * (1.0 + 1e-9)) {
+          best = score;
+          c.G = G;
+          c.threads = threads;
+          c.cols_per_cta = Cl;
+          c.rows_per_cta = Rl;
+          c.CB = CB;
+          c.RB = RB;
+          c.mixed_in_smem = mis;
+          c.smem_bytes = bytes;
+          found = true;
+        }
       }
     }
   }
   if (!found) return fail(EXGB_EUNSUPPORTED, "2D configuration does not fit in shared memory");
-  EXGB_CUDA(cudaFuncSetAttribute(etdrk2d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)c.smem_bytes));
   // co-resident clusters
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];

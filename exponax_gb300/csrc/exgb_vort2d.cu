@@ -473,7 +473,9 @@ static int v2_configure(exgb_plan* plan) {
     c.RB = 0;
     c.mixed_in_smem = 1;
     c.smem_bytes = bestBytes;
-    EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bestBytes));
+    // the opt-in maximum, not this plan's size: plans of the same N with other cluster sizes share
+    // the kernel and launch with their own (larger or smaller) footprint
+    EXGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
     c.clusters = bestN;
     const int nb = P.order <= 1 ? 1 : P.order == 2 ? 3 : P.order == 3 ? 4 : 6;
     c.scratch_per_cluster = (size_t)nb * Kc * N;

@@ -259,6 +259,43 @@ def test_ns_256_config_short_rollout():
             assert rel(traj[b, t], ref[t]) < 1e-5 * (t + 1)
 
 
+@pytest.mark.parametrize("cluster", [0, 4, 6, 8])
+def test_kolmogorov_512_generic_cluster_kernel(cluster):
+    """Kolmogorov flow 512^2 runs on the generic 2D cluster kernel (its derived fields
+    go through L2): 3 ETDRK2 steps within 1e-5 of the oracle, at the automatic cluster
+    size and at 4, 6 (rows split 86 x 5 + 82) and 8 CTAs per cluster."""
+    from exponax_gb300 import autotune
+
+    N = 512
+    sm = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, N, 0.001)
+    so = o.KolmogorovFlowVorticity(2, 2 * np.pi, N, 0.001)
+    if cluster:
+        assert autotune._set(sm.plan, 1, [cluster]) == 0
+        assert autotune.get_tuning(sm.plan)["cluster"] == cluster
+    u0 = np.stack([_ic(2, N, s) for s in range(3)])
+    got = host(ex.vmap(ex.repeat(sm, 3))(cu(u0)))
+    for b in range(3):
+        assert rel(got[b], o.repeat(so, 3)(u0[b])) < 1e-5
+
+
+@pytest.mark.parametrize("cluster", [0, 2, 4, 7])
+def test_generic_2d_kernel_uneven_row_split(cluster):
+    """N = 45 on the generic 2D kernel with cluster sizes that do not divide N (rows per
+    CTA 23/22, 12 x 3 + 9, 7 x 6 + 3): 5 ETDRK2 steps of NS vorticity within 1e-5."""
+    from exponax_gb300 import autotune
+
+    N = 45
+    sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, N, 0.01, diffusivity=1e-3)
+    so = o.NavierStokesVorticity(2, 2 * np.pi, N, 0.01, diffusivity=1e-3)
+    if cluster:
+        assert autotune._set(sm.plan, 1, [cluster]) == 0
+        assert autotune.get_tuning(sm.plan)["cluster"] == cluster
+    u0 = np.stack([_ic(2, N, s) for s in range(4)])
+    got = host(ex.vmap(ex.repeat(sm, 5))(cu(u0)))
+    for b in range(4):
+        assert rel(got[b], o.repeat(so, 5)(u0[b])) < 1e-5
+
+
 def test_repeated_stepper_stays_in_fourier_space():
     sm = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.01)
     so = o.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.01)
