@@ -10,7 +10,8 @@ Knobs (exgb_plan_tune):
   * radix order of the length-N Stockham FFT (1D kernel, transforms,
     generic 2D kernel): every ordering of the factorisations of N into
     {8, 4, 2, 5, 3}, capped;
-  * CTAs per cluster of the 2D register-FFT kernel: 1, 2, 4, 8 (those that fit);
+  * CTAs per cluster of the 2D cluster kernels: 1..8 (those that fit; for the
+    generic kernel searched after its radix order);
   * instances per work item of the 1D kernel;
   * threads per CTA of the 1D kernel (searched after the two above).
 """
@@ -153,6 +154,17 @@ def tune(stepper, *, batch=64, nsteps=10, repeats=3, use_cache=True, write_cache
                         continue
                     results.append((dict(base, threads=t), _time(plan, uh, out, batch, nsteps, repeats)))
                 _set(plan, 4, [0])
+        if D == 2 and cfg["cluster"] > 0 and stepper.order > 0:
+            # generic 2D cluster kernel: cluster size for the best radix order found so far
+            fin = [r for r in results if np.isfinite(r[1])]
+            if fin:
+                base = min(fin, key=lambda r: r[1])[0]
+                _set(plan, 0, list(base["radices"]))
+                for G in range(1, 9):
+                    if _set(plan, 1, [G]) != EXGB_OK:
+                        continue
+                    results.append((dict(base, cluster=G), _time(plan, uh, out, batch, nsteps, repeats)))
+                _set(plan, 1, [0])
     results = [r for r in results if np.isfinite(r[1])]
     best = min(results, key=lambda r: r[1])[0] if results else {}
     apply(stepper, best)

@@ -120,7 +120,8 @@ int exgb_plan_kmax(const exgb_plan* plan);
  * which times candidates on the device and caches the winner):
  *   EXGB_TUNE_RADICES       values = radix order of the length-N Stockham FFT
  *                           (1D kernel, transforms, generic 2D kernel)
- *   EXGB_TUNE_CLUSTER       values[0] = CTAs per cluster of the 2D kernel, 1..8 (0 = auto)
+ *   EXGB_TUNE_CLUSTER       values[0] = CTAs per cluster of the 2D vorticity kernels
+ *                           (register-FFT and generic), 1..8 (0 = auto)
  *   EXGB_TUNE_ITEMS_PER_CTA values[0] = 1D instances per work item (0 = auto)
  *   EXGB_TUNE_THREADS       values[0] = threads per CTA of the 1D kernel: 64, 128, 256
  *                           (0 = default, 256)

@@ -27,7 +27,7 @@ def test_radix_candidates_multiply_to_n():
             assert int(np.prod(c)) == n
 
 
-@pytest.mark.parametrize("case", ["ks1d", "ns2d"])
+@pytest.mark.parametrize("case", ["ks1d", "ns2d", "ns2d_generic"])
 def test_tune_apply_cache_and_parity(case, tmp_path, monkeypatch):
     monkeypatch.setenv("EXGB_AUTOTUNE_CACHE", str(tmp_path / "cache.json"))
     if case == "ks1d":
@@ -35,12 +35,17 @@ def test_tune_apply_cache_and_parity(case, tmp_path, monkeypatch):
         so = o.KuramotoSivashinskyConservative(1, 100.0, 200, 0.1)
         u = np.stack([ex.ic.RandomSineWaves1d(1, cutoff=5)(200, key=s) for s in range(3)])
     else:
-        sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, 128, 0.01, diffusivity=1e-3)
-        so = o.NavierStokesVorticity(2, 2 * np.pi, 128, 0.01, diffusivity=1e-3)
+        n = 128 if case == "ns2d" else 96
+        sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
+        so = o.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
         g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
-        u = np.stack([g(128, key=s) for s in range(3)])
+        u = np.stack([g(n, key=s) for s in range(3)])
     res = autotune.tune(sm, batch=32, nsteps=4, repeats=2)
     assert not res["cached"] and res["best"] and len(res["timings_ms"]) >= 2
+    if case == "ns2d_generic":
+        # radix orders first, then every cluster size for the best of them
+        assert "cluster" in res["best"] and "radices" in res["best"]
+        assert autotune.get_tuning(sm.plan)["cluster"] == res["best"]["cluster"]
     cache = json.load(open(tmp_path / "cache.json"))
     assert res["key"] in cache
     got = ex.vmap(sm)(torch.from_numpy(u).cuda()).cpu().numpy()
@@ -50,11 +55,12 @@ def test_tune_apply_cache_and_parity(case, tmp_path, monkeypatch):
     assert again["cached"] and again["best"] == res["best"]
 
 
-@pytest.mark.parametrize("n", [64, 128, 256])
+@pytest.mark.parametrize("n", [64, 128, 256, 96, 512])
 def test_every_cluster_size_matches_oracle(n):
-    """The register-FFT 2D kernel with each cluster size 1..8 that fits (rows split unevenly when
-    G does not divide N): one ETDRK2 step within 1e-5 of the oracle; sizes that do not fit are
-    refused with EXGB_EUNSUPPORTED and leave the plan usable."""
+    """The 2D cluster kernels (register FFTs at N = 64 / 128 / 256, the generic kernel at 96 and
+    512) with each cluster size 1..8 that fits (rows split unevenly when G does not divide N): one
+    ETDRK2 step within 1e-5 of the oracle; sizes that do not fit are refused with
+    EXGB_EUNSUPPORTED and leave the plan usable."""
     from exponax_gb300._lib import EXGB_OK
     sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
     so = o.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
