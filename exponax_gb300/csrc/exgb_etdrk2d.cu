@@ -271,23 +271,40 @@ __global__ void __launch_bounds__(512, 1) etdrk2d_kernel(const Args2D a) {
       // ---------------- row phase
       for (int rb0 = 0; rb0 < myRl; rb0 += RB) {
         const int nr = min(RB, myRl - rb0);
-        for (int t = tid; t < nr * N; t += nthr) {
-          const int r = t / N, k = t - r * N;
-          const int x = row0 + rb0 + r;
-          const bool ext = k >= M;
-          const int kk = ext ? N - k : k;
-          const bool ro = (k == 0) || (even && k == N / 2);
-          float2 U = make_float2(0.f, 0.f), V = U, WX = U, WY = U;
-          if (kk <= K) {
-            const int og = kk / Cl, c = kk - og * Cl;
-            const float2* mb = s_mixed[og];
-            U = mb[(0 * N + x) * Cl + c];
-            V = mb[(1 * N + x) * Cl + c];
-            WX = mb[(2 * N + x) * Cl + c];
-            WY = mb[(3 * N + x) * Cl + c];
+        // gather, four elements per thread in flight: all loads (L2 or DSMEM) first, then the
+        // shared-memory stores, so the loads of later elements do not wait behind earlier stores
+        const int tot = nr * N;
+        for (int t0 = tid; t0 < tot; t0 += 4 * nthr) {
+          float2 L[4][4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int t = t0 + u * nthr;
+            L[u][0] = L[u][1] = L[u][2] = L[u][3] = make_float2(0.f, 0.f);
+            if (t < tot) {
+              const int r = t / N, k = t - r * N;
+              const int x = row0 + rb0 + r;
+              const int kk = k >= M ? N - k : k;
+              if (kk <= K) {
+                const int og = kk / Cl, c = kk - og * Cl;
+                const float2* mb = s_mixed[og];
+                L[u][0] = mb[(0 * N + x) * Cl + c];
+                L[u][1] = mb[(1 * N + x) * Cl + c];
+                L[u][2] = mb[(2 * N + x) * Cl + c];
+                L[u][3] = mb[(3 * N + x) * Cl + c];
+              }
+            }
           }
-          w0[(2 * r) * N + k] = pack_pair(U, V, ext, ro);
-          w0[(2 * r + 1) * N + k] = pack_pair(WX, WY, ext, ro);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int t = t0 + u * nthr;
+            if (t < tot) {
+              const int r = t / N, k = t - r * N;
+              const bool ext = k >= M;
+              const bool ro = (k == 0) || (even && k == N / 2);
+              w0[(2 * r) * N + k] = pack_pair(L[u][0], L[u][1], ext, ro);
+              w0[(2 * r + 1) * N + k] = pack_pair(L[u][2], L[u][3], ext, ro);
+            }
+          }
         }
         __syncthreads();
         float2* res = result_buf(P.fft, w0, w1);
@@ -323,10 +340,29 @@ __global__ void __launch_bounds__(512, 1) etdrk2d_kernel(const Args2D a) {
       for (int cb0 = 0; cb0 < ncols; cb0 += CB) {
         const int nc = min(CB, ncols - cb0);
         // gather the product columns (ky fixed, all x) from the row owners
-        for (int t = tid; t < nc * N; t += nthr) {
-          const int x = t / nc, c = t - x * nc;
-          const int og = x / Rl, xr = x - og * Rl;
-          w0[c * N + x] = s_prod[og][xr * Kc + col0 + cb0 + c];
+        {
+          const int tot = nc * N;
+          for (int t0 = tid; t0 < tot; t0 += 4 * nthr) {
+            float2 L[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int t = t0 + u * nthr;
+              L[u] = make_float2(0.f, 0.f);
+              if (t < tot) {
+                const int x = t / nc, c = t - x * nc;
+                const int og = x / Rl, xr = x - og * Rl;
+                L[u] = s_prod[og][xr * Kc + col0 + cb0 + c];
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const int t = t0 + u * nthr;
+              if (t < tot) {
+                const int x = t / nc, c = t - x * nc;
+                w0[c * N + x] = L[u];
+              }
+            }
+          }
         }
         __syncthreads();
         float2* res = result_buf(P.fft, w0, w1);
