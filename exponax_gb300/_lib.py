@@ -100,6 +100,7 @@ SIGNATURES = [
     ("exgb_leray", _I, [_VP, _I, _I, ctypes.c_double, _I64, _VP, _VP]),
     ("exgb_plan_tune", _I, [_VP, _I, ctypes.POINTER(_I), _I]),
     ("exgb_plan_get_tuning", _I, [_VP, ctypes.POINTER(_I), _I]),
+    ("exgb_plan_fused_launches", _I, [_VP, ctypes.c_int64, ctypes.POINTER(_I)]),
     ("exgb_plan_status", _I, [_VP]),
     ("exgb_tc_gemm_check", _I, [_VP, _I, _I, _VP, _VP, _VP, _I]),
     ("exgb_spectrum", _I, [_VP, _I, _I, _I64, _VP, _VP, _I, _I]),

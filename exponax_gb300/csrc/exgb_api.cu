@@ -218,6 +218,7 @@ int exgb_plan_destroy(exgb_plan* plan) {
   cudaFree(plan->d_Eh);
   cudaFree(plan->d_c);
   cudaFree(plan->d_scratch);
+  cudaFree(plan->d_scratch_tail);
   cudaFree(plan->d_tc_scratch);
   cudaFree(plan->d_status);
   delete plan;
@@ -522,6 +523,19 @@ extern "C" int exgb_plan_status(const exgb_plan* plan) {
   int h = 0;
   EXGB_CUDA(cudaMemcpy(&h, plan->d_status, sizeof(int), cudaMemcpyDeviceToHost));
   if (h) return fail(h, "a bounded device wait of the tensor-core kernel gave up");
+  return EXGB_OK;
+}
+
+extern "C" int exgb_plan_fused_launches(const exgb_plan* plan, int64_t batch, int* launches) {
+  if (!plan || !launches) return fail(EXGB_EINVAL, "null plan or output");
+  if (batch < 0) return fail(EXGB_EINVAL, "negative batch");
+  const PlanDev& P = plan->dev;
+  int n = 0;
+  if (batch > 0 && P.D == 2 && P.kind != EXGB_NL_ZERO && P.order > 0 && !plan->staged) {
+    if (plan->precision == 1 || plan->cfg2d.variant != 1) n = 1;
+    else n = vort2d_launches(plan, batch);
+  }
+  *launches = n;
   return EXGB_OK;
 }
 

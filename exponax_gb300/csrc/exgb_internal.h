@@ -70,6 +70,11 @@ struct exgb_plan {
   exgb::Plan2DConfig cfg2d{};
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
+  // 2D register-FFT kernel, automatic cluster choice only: a second configuration with larger
+  // clusters (fewer rows per CTA, so a shorter wave) for the samples of a partial last wave;
+  // G = 0 when unused
+  exgb::Plan2DConfig cfg2d_tail{};
+  void* d_scratch_tail = nullptr;
   int sm_count = 0;
   // autotuner overrides (0 = automatic choice)
   int tune_cluster = 0;          // 2D: CTAs per cluster
@@ -119,6 +124,7 @@ int etdrk2d_run(const exgb_plan* plan, cudaStream_t st, const float2* u_hat_in, 
                 int nsteps, int project, int nonlinear_only);
 int etdrk2d_configure(exgb_plan* plan);
 int vort2d_configure(exgb_plan* plan);
+int vort2d_launches(const exgb_plan* plan, int64_t batch);
 int vort2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                int project, int nonlinear_only);
 bool tcdft2d_supported(const exgb_plan* plan);

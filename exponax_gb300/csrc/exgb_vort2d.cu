@@ -432,6 +432,11 @@ static int v2_configure(exgb_plan* plan) {
   auto fn = vort2d_kernel<N, THREADS>;
   int bestG = 0, bestN = 0, bestSM = -1;
   size_t bestBytes = 0;
+  int candN[9] = {0};
+  size_t candBytes[9] = {0};
+  cudaFree(plan->d_scratch_tail);
+  plan->d_scratch_tail = nullptr;
+  plan->cfg2d_tail = Plan2DConfig{};
   for (int G = 1; G <= 8; ++G) {
     if (wantG && wantG != G) continue;
     const int Cl = (Kc + G - 1) / G;
@@ -456,6 +461,8 @@ static int v2_configure(exgb_plan* plan) {
       cudaGetLastError();
       ncl = std::max(1, plan->sm_count / G);
     }
+    candN[G] = ncl;
+    candBytes[G] = bytes;
     if (ncl * G > bestSM) {
       bestSM = ncl * G;
       bestG = G;
@@ -481,15 +488,33 @@ static int v2_configure(exgb_plan* plan) {
     c.scratch_per_cluster = (size_t)nb * Kc * N;
     plan->scratch_bytes = sizeof(float2) * c.scratch_per_cluster * (size_t)bestN;
     EXGB_CUDA(cudaMalloc(&plan->d_scratch, plan->scratch_bytes));
+    // Partial last wave (N = 256): its samples run on the largest cluster size that fits, whose CTAs
+    // own fewer rows and columns, so the wave ends sooner than one of the main configuration.
+    int tG = 0;
+    if (!wantG && N >= 256)
+      for (int g2 = 8; g2 > G; --g2)
+        if (candN[g2] > 0) {
+          tG = g2;
+          break;
+        }
+    if (tG) {
+      Plan2DConfig& t = plan->cfg2d_tail;
+      t = c;
+      t.G = tG;
+      t.cols_per_cta = (Kc + tG - 1) / tG;
+      t.rows_per_cta = 2 * ((N + 2 * tG - 1) / (2 * tG));
+      t.smem_bytes = candBytes[tG];
+      t.clusters = candN[tG];
+      EXGB_CUDA(cudaMalloc(&plan->d_scratch_tail, sizeof(float2) * t.scratch_per_cluster * (size_t)t.clusters));
+    }
     return EXGB_OK;
   }
   return EXGB_EUNSUPPORTED;
 }
 
 template <int N, int THREADS>
-static int v2_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
-                  int project, int nonlinear_only) {
-  const Plan2DConfig& c = plan->cfg2d;
+static int v2_launch(const exgb_plan* plan, const Plan2DConfig& c, void* scratch, cudaStream_t st, const float2* in,
+                     float2* out, int64_t batch, int nsteps, int project, int nonlinear_only) {
   ArgsV2 a;
   a.P = plan->dev;
   a.G = c.G;
@@ -504,7 +529,7 @@ static int v2_run(const exgb_plan* plan, cudaStream_t st, const float2* in, floa
   a.nsteps = nsteps;
   a.project = project;
   a.nonlinear_only = nonlinear_only;
-  a.scratch = (float2*)plan->d_scratch;
+  a.scratch = (float2*)scratch;
   a.scratch_stride = (int64_t)c.scratch_per_cluster;
   const int ncl = (int)std::min<int64_t>(c.clusters, batch);
   cudaLaunchConfig_t cfg = {};
@@ -521,6 +546,40 @@ static int v2_run(const exgb_plan* plan, cudaStream_t st, const float2* in, floa
   cfg.numAttrs = 1;
   EXGB_CUDA(cudaLaunchKernelEx(&cfg, vort2d_kernel<N, THREADS>, a));
   return EXGB_OK;
+}
+
+// Samples of the main configuration's partial last wave (when the tail configuration holds them
+// all in one wave) go to a second launch with the tail configuration, on the same stream.
+static int64_t v2_main_part(const exgb_plan* plan, int64_t batch) {
+  const Plan2DConfig& c = plan->cfg2d;
+  const Plan2DConfig& t = plan->cfg2d_tail;
+  if (t.G <= 0 || !plan->d_scratch_tail || c.clusters <= 0) return batch;
+  const int64_t r = batch % c.clusters;
+  return (r > 0 && r <= t.clusters) ? batch - r : batch;
+}
+
+template <int N, int THREADS>
+static int v2_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
+                  int project, int nonlinear_only) {
+  const int64_t bm = v2_main_part(plan, batch);
+  if (bm > 0) {
+    const int rc = v2_launch<N, THREADS>(plan, plan->cfg2d, plan->d_scratch, st, in, out, bm, nsteps, project,
+                                         nonlinear_only);
+    if (rc) return rc;
+  }
+  if (bm < batch) {
+    const int64_t off = bm * (int64_t)N * (N / 2 + 1);
+    return v2_launch<N, THREADS>(plan, plan->cfg2d_tail, plan->d_scratch_tail, st, in + off, out + off, batch - bm,
+                                 nsteps, project, nonlinear_only);
+  }
+  return EXGB_OK;
+}
+
+// Kernel launches one call of the register-FFT kernel makes for `batch` samples.
+int vort2d_launches(const exgb_plan* plan, int64_t batch) {
+  if (batch <= 0) return 0;
+  const int64_t bm = v2_main_part(plan, batch);
+  return (bm > 0 ? 1 : 0) + (bm < batch ? 1 : 0);
 }
 
 // Returns EXGB_EUNSUPPORTED when this N has no register-FFT variant.

@@ -143,6 +143,12 @@ int exgb_plan_kmax(const exgb_plan* plan);
 #define EXGB_TUNE_THREADS 4
 int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int n);
 int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n);
+/* Kernel launches of the fused 2D stepping kernel that one exgb_repeat_fourier
+ * (or exgb_step_fourier) call makes for `batch` samples, written to *launches:
+ * 1, or 2 when the register-FFT kernel runs the samples of a partial last wave
+ * on its tail configuration (larger clusters); 0 for plans without a fused 2D
+ * kernel.  No reference counterpart (launch accounting for benchmarks). */
+int exgb_plan_fused_launches(const exgb_plan* plan, int64_t batch, int* launches);
 /* Synchronises the device and returns EXGB_ETIMEOUT if a bounded wait inside
  * the tensor-core kernel of this plan gave up (its outputs are then invalid). */
 int exgb_plan_status(const exgb_plan* plan);

@@ -296,6 +296,33 @@ def test_generic_2d_kernel_uneven_row_split(cluster):
         assert rel(got[b], o.repeat(so, 5)(u0[b])) < 1e-5
 
 
+def test_ns256_partial_last_wave_on_tail_configuration():
+    """NS vorticity 256^2 with one more sample than the co-resident clusters: the main launch runs
+    a full wave and the extra sample runs in a second launch on larger clusters (the fused-launch
+    count says 2); every sample within 1e-5 of the oracle after 3 steps."""
+    import ctypes
+
+    from exponax_gb300 import _lib
+
+    N = 256
+    sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, N, 0.01, diffusivity=1e-3)
+    so = o.NavierStokesVorticity(2, 2 * np.pi, N, 0.01, diffusivity=1e-3)
+    lib, h, cnt = _lib.load(), sm.plan.handle, ctypes.c_int(0)
+
+    def launches(b):
+        assert lib.exgb_plan_fused_launches(h, b, ctypes.byref(cnt)) == 0
+        return cnt.value
+
+    assert launches(0) == 0 and launches(1) == 1
+    two = [b for b in range(2, 80) if launches(b) == 2]
+    assert two, "N = 256 has a tail configuration"
+    B = two[0]
+    u0 = np.stack([_ic(2, N, s % 7) * np.float32(1.0 + 0.01 * s) for s in range(B)]).astype(np.float32)
+    got = host(ex.vmap(ex.repeat(sm, 3))(cu(u0)))
+    for b in range(B):
+        assert rel(got[b], o.repeat(so, 3)(u0[b])) < 1e-5, b
+
+
 def test_repeated_stepper_stays_in_fourier_space():
     sm = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.01)
     so = o.KolmogorovFlowVorticity(2, 2 * np.pi, 64, 0.01)
