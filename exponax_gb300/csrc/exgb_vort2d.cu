@@ -489,7 +489,9 @@ static int v2_configure(exgb_plan* plan) {
     plan->scratch_bytes = sizeof(float2) * c.scratch_per_cluster * (size_t)bestN;
     EXGB_CUDA(cudaMalloc(&plan->d_scratch, plan->scratch_bytes));
     // Partial last wave (N = 256): its samples run on the largest cluster size that fits, whose CTAs
-    // own fewer rows and columns, so the wave ends sooner than one of the main configuration.
+    // own fewer rows and columns, so the wave ends sooner than one of the main configuration.  At
+    // N = 128 (Kolmogorov, batch 1024: 13 waves of 76 clusters of 2 plus 36 samples) the 36 samples
+    // on clusters of 4 took as long as a wave of 2 (36.38 against 36.32 ms), so 128 keeps one launch.
     int tG = 0;
     if (!wantG && N >= 256)
       for (int g2 = 8; g2 > G; --g2)
