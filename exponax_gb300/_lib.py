@@ -23,6 +23,9 @@ EXGB_ENOMEM = -7
 EXGB_EUNSUPPORTED = -8
 EXGB_ENOTIMPL = -9
 
+# exgb_plan_tune knob of the tensor-core kernel's timeout path (tests only)
+EXGB_TUNE_WAIT_BUDGET = 5
+
 NL_ZERO = 0
 NL_CONVECTION = 1
 NL_GRADIENT_NORM = 2

@@ -500,6 +500,12 @@ extern "C" int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int 
     plan->precision = 1;
     return EXGB_OK;
   }
+  if (kind == EXGB_TUNE_WAIT_BUDGET) {
+    const long long v = n > 0 ? values[0] : 0;
+    if (v < 0) return fail(EXGB_EINVAL, "wait budget must be >= 0 (0 = the normal budget)");
+    plan->tc_first_wait_budget = v;
+    return EXGB_OK;
+  }
   if (kind == EXGB_TUNE_ITEMS_PER_CTA) {
     if (plan->dev.D != 1 || plan->staged)
       return fail(EXGB_EUNSUPPORTED, "items per CTA applies to 1D single-channel plans");
@@ -522,7 +528,11 @@ extern "C" int exgb_plan_status(const exgb_plan* plan) {
   if (!plan->d_status) return EXGB_OK;
   int h = 0;
   EXGB_CUDA(cudaMemcpy(&h, plan->d_status, sizeof(int), cudaMemcpyDeviceToHost));
-  if (h) return fail(h, "a bounded device wait of the tensor-core kernel gave up");
+  if (h) {
+    // read and clear: a later call reports only the waits that gave up after this one
+    EXGB_CUDA(cudaMemset(plan->d_status, 0, sizeof(int)));
+    return fail(h, "a bounded device wait of the tensor-core kernel gave up");
+  }
   return EXGB_OK;
 }
 

@@ -51,7 +51,7 @@ struct Plan2DConfig {
   int variant;   // 0: generic Stockham kernel, 1: register-FFT kernel (compile-time N)
   size_t smem_bytes;
   int clusters;       // persistent clusters launched
-  size_t scratch_per_cluster;  // bytes of global scratch per cluster
+  size_t scratch_per_cluster;  // float2 elements of global scratch per cluster
 };
 
 }  // namespace exgb
@@ -86,6 +86,9 @@ struct exgb_plan {
   size_t tc_scratch_per_cta = 0;
   size_t tc_const_offset = 0;    // byte offset of the constant DFT tiles inside d_tc_scratch
   int* d_status = nullptr;       // device wait status of the tensor-core kernel (0 = ok)
+  // clock cycles of the tensor-core kernel's first MMA-completion wait per launch (0 = the normal
+  // budget); set only by tests, through EXGB_TUNE_WAIT_BUDGET, to make that wait run out
+  long long tc_first_wait_budget = 0;
   // stepped by the staged N-D path (exgb_ndgen.cu) instead of a fused kernel
   int staged = 0;
   // 2D coefficient tables stored [lin_ch][ky][kx] (the fused 2D kernels' layout)

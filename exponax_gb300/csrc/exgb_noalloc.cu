@@ -17,8 +17,6 @@
 // concurrently) race on the array and must be serialised by the caller.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "exgb_internal.h"
 
 namespace exgb {
@@ -31,23 +29,17 @@ constexpr size_t kStaticScratchElems = kStaticScratchBytes / sizeof(float2);
 
 static __device__ __align__(256) float2 g_static_scratch[kStaticScratchElems];
 
-// Device address of g_static_scratch, looked up once per device (with that
-// device current) on the first call made on it.
-static std::mutex g_static_mu;
-static float2* g_static_ptr[64] = {nullptr};
-
+// Device address of g_static_scratch on the current device.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up with
+// that device current.  It is looked up on every call (a cheap runtime query),
+// so a context torn down and re-created (cudaDeviceReset) never leaves a stale
+// address behind; the first call on a device also loads the module there,
+// which is why that first call should come before any stream capture.
 static int static_scratch(float2** out) {
-  int dev = 0;
-  EXGB_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(EXGB_EUNSUPPORTED, "device index out of range for the static scratch table");
-  std::lock_guard<std::mutex> lk(g_static_mu);
-  if (!g_static_ptr[dev]) {
-    float2* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_static_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_static_scratch)");
-    g_static_ptr[dev] = p;
-  }
-  *out = g_static_ptr[dev];
+  float2* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_static_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_static_scratch)");
+  *out = p;
   return EXGB_OK;
 }
 
@@ -62,6 +54,12 @@ extern "C" int exgb_repeat_fourier_noalloc(const exgb_plan* plan, void* stream, 
   if (plan->dev.D != 2 || plan->dev.kind == EXGB_NL_ZERO || plan->dev.order == 0 || plan->cfg2d.variant != 1)
     return fail(EXGB_EUNSUPPORTED,
                 "exgb_repeat_fourier_noalloc runs 2D vorticity plans with N in {64, 128, 256} and ETDRK order >= 1");
+  // The split-BF16 tensor-core kernel keeps its operands in plan-owned scratch; this entry point
+  // runs only the FP32 register-FFT kernel, so a plan switched to split-BF16 is refused rather than
+  // silently stepped with other arithmetic than exgb_repeat_fourier would use.
+  if (plan->precision != EXGB_DFT_FP32)
+    return fail(EXGB_EUNSUPPORTED,
+                "exgb_repeat_fourier_noalloc runs FP32 transforms only; this plan is set to split-BF16");
   const size_t need = plan->cfg2d.scratch_per_cluster * sizeof(float2);
   if (need > kStaticScratchBytes)
     return fail(EXGB_EUNSUPPORTED, "this plan needs " + std::to_string(need) +

@@ -201,12 +201,24 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
 }
 // Wait until the phase with the given parity has completed; gives up after
-// `budget` clock cycles and returns false.
+// `budget` clock cycles and returns false.  Each round first probes without
+// blocking (test_wait) and checks the budget, then makes a potentially
+// suspending try_wait (which returns by itself after a system time limit), so
+// even a budget of a few cycles is honoured.
 __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, long long budget) {
   const uint32_t a = smem_u32(mbar);
   const long long t0 = clock64();
   while (true) {
     uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > budget) return false;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
@@ -215,7 +227,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, long 
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
-    if (clock64() - t0 > budget) return false;
   }
 }
 

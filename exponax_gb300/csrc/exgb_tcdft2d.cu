@@ -99,6 +99,7 @@ struct Args {
   int64_t scratch_stride;
   const uint4* consts;
   int* status;
+  long long first_wait_budget;  // budget of the launch's first MMA-completion wait
 };
 
 __device__ __forceinline__ float rcp_approx(float x) {
@@ -218,8 +219,10 @@ __global__ void __launch_bounds__(THREADS, 1) tcdft2d_kernel(const Args a) {
     tc::fence_before_sync();
     __syncthreads();
   };
+  bool first_wait = true;
   auto wait_mma = [&]() -> bool {
-    const bool ok = tc::mbar_wait(&s_mbar, phase, WAIT_BUDGET);
+    const bool ok = tc::mbar_wait(&s_mbar, phase, first_wait ? a.first_wait_budget : WAIT_BUDGET);
+    first_wait = false;
     phase ^= 1u;
     const int anybad = __syncthreads_or(!ok);
     tc::fence_after_sync();
@@ -682,6 +685,7 @@ int tcdft2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2
   a.scratch_stride = (int64_t)plan->tc_scratch_per_cta;
   a.consts = reinterpret_cast<const uint4*>((const unsigned char*)plan->d_tc_scratch + plan->tc_const_offset);
   a.status = plan->d_status;
+  a.first_wait_budget = plan->tc_first_wait_budget > 0 ? plan->tc_first_wait_budget : tcd::WAIT_BUDGET;
   const int grid = (int)std::min<int64_t>(batch, plan->sm_count);
   tcd::tcdft2d_kernel<<<grid, tcd::THREADS, tcd::SMEM_BYTES, st>>>(a);
   EXGB_CUDA(cudaGetLastError());

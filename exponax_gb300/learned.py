@@ -22,8 +22,11 @@ import ctypes
 
 import numpy as np
 
-from . import _device
+from . import _device, ic, stepper
 from ._lib import check, load
+from ._utils import rollout, vmap
+from .interpolation import map_between_resolutions_batched
+from .spectral import fft, ifft
 
 C = 48
 NMID = 4
@@ -247,9 +250,6 @@ class GuardedCorrectedStepper:
 
     def step(self, u):
         """u: (B, 1, H, 64) -> (B, 1, H, 64)."""
-        from ._utils import vmap
-        from .spectral import fft
-
         torch = _device.torch()
         lib = _lib()
         plain = vmap(self.coarse)(u)
@@ -264,3 +264,119 @@ class GuardedCorrectedStepper:
         return corrected
 
     __call__ = step
+
+
+# ---- training data, training and evaluation of the corrector (2D Kolmogorov flow) ----
+
+KW = dict(diffusivity=1e-3, drag=-0.1, injection_mode=4, injection_scale=1.0)
+
+
+def _events():
+    torch = _device.torch()
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def fine_coarse_trajectories(seeds, *, n_fine=512, n_coarse_grid=64, dt=0.001, ratio=8, spinup=1000, n_coarse=200,
+                             batch=256):
+    """Downsampled fine trajectories (len(seeds), n_coarse + 1, n_coarse_grid, n_coarse_grid) on the GPU, and
+    the GPU milliseconds of the post-spin-up fine steps."""
+    torch = _device.torch()
+    fine = stepper.KolmogorovFlowVorticity(2, 2 * np.pi, n_fine, dt, **KW)
+    h = fine.plan.handle
+    lib = load()
+    g = ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
+    out = torch.empty((len(seeds), n_coarse + 1, n_coarse_grid, n_coarse_grid), dtype=torch.float32, device="cuda")
+    fine_ms = 0.0
+    for b0 in range(0, len(seeds), batch):
+        sb = seeds[b0:b0 + batch]
+        B = len(sb)
+        u0 = torch.from_numpy(np.stack([g(n_fine, key=int(s)) for s in sb])).cuda()
+        uh = fft(u0, num_spatial_dims=2)
+        tmp = torch.empty_like(uh)
+        check(lib.exgb_repeat_fourier(h, _device.stream(), uh.data_ptr(), tmp.data_ptr(), B, spinup), "spin-up")
+        uh, tmp = tmp, uh
+        for t in range(n_coarse + 1):
+            if t > 0:
+                e0, e1 = _events()
+                e0.record()
+                check(lib.exgb_repeat_fourier(h, _device.stream(), uh.data_ptr(), tmp.data_ptr(), B, ratio), "fine")
+                e1.record()
+                uh, tmp = tmp, uh
+                torch.cuda.synchronize()
+                fine_ms += e0.elapsed_time(e1)
+            phys = ifft(uh, num_spatial_dims=2, num_points=n_fine)  # (B, 1, N, N)
+            out[b0:b0 + B, t] = map_between_resolutions_batched(phys, n_coarse_grid)[:, 0]
+    return out, fine_ms
+
+
+def train(net, coarse, data, *, epochs=4, batch=256, lr=1e-3, seed=0, log=None):
+    """data: (T, n_coarse + 1, H, W) coarse snapshots."""
+    torch = _device.torch()
+    T, S, H, W = data.shape
+    x = data[:, :-1].reshape(-1, 1, H, W)
+    y = data[:, 1:].reshape(-1, H, W)
+    v = torch.empty_like(x)
+    for i in range(0, x.shape[0], 4096):
+        v[i:i + 4096] = vmap(coarse)(x[i:i + 4096])
+    v = v.reshape(-1, H, W)
+    net.in_scale = float(1.0 / v.std())
+    net.out_scale = float((y - v).std())
+    rng = np.random.default_rng(seed)
+    n = v.shape[0]
+    hist = []
+    for ep in range(epochs):
+        perm = torch.from_numpy(rng.permutation(n)).cuda()
+        tot, cnt = 0.0, 0
+        for i in range(0, n - batch + 1, batch):
+            idx = perm[i:i + batch]
+            loss = net.train_step(v[idx], y[idx], lr=lr)
+            if (i // batch) % 50 == 0:
+                tot += float(loss)
+                cnt += 1
+        hist.append(tot / max(cnt, 1))
+        if log:
+            log(f"epoch {ep}: mean loss {hist[-1]:.3e} (normalised by out_scale^2: {hist[-1] / net.out_scale ** 2:.3e})")
+    return hist
+
+
+def evaluate(ref, coarse, net, *, kg=16, thresh=0.05):
+    """ref: (B, S, H, W) downsampled fine trajectories.  Returns metrics and GPU ms."""
+    torch = _device.torch()
+    B, S, H, W = ref.shape
+    u0 = ref[:, 0:1].contiguous()  # (B, 1, H, W)
+    roll = vmap(rollout(coarse, S - 1, include_init=True))
+    e0, e1 = _events()
+    e0.record()
+    plain = roll(u0)[:, :, 0]  # (B, S, H, W)
+    e1.record()
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    gs = GuardedCorrectedStepper(coarse, net, kg=kg, thresh=thresh)
+    learned = torch.empty_like(ref)
+    learned[:, 0] = ref[:, 0]
+    u = u0
+    trips = 0
+    e0, e1 = _events()
+    e0.record()
+    for t in range(1, S):
+        u = gs(u)
+        learned[:, t] = u[:, 0]
+        trips += gs.last_tripped.sum()
+    e1.record()
+    torch.cuda.synchronize()
+    learned_ms = e0.elapsed_time(e1)
+
+    def metrics(pred):
+        d = (pred - ref).reshape(B, S, -1)
+        r = ref.reshape(B, S, -1)
+        rel = (d.norm(dim=2) / r.norm(dim=2)).mean(dim=0)  # per step, mean over seeds
+        p = pred.reshape(B, S, -1)
+        corr = ((p * r).sum(dim=2) / (p.norm(dim=2) * r.norm(dim=2))).mean(dim=0)
+        below = (corr < 0.8).nonzero()
+        ct = int(below[0, 0]) if below.numel() else S - 1
+        return rel.cpu().numpy(), corr.cpu().numpy(), ct
+
+    rp, cp, ctp = metrics(plain)
+    rl, cl, ctl = metrics(learned)
+    return {"plain": (rp, cp, ctp), "learned": (rl, cl, ctl), "plain_ms": plain_ms, "learned_ms": learned_ms,
+            "guard_trips": int(trips), "guard_checks": int(B * (S - 1))}

@@ -141,6 +141,13 @@ int exgb_plan_kmax(const exgb_plan* plan);
 #define EXGB_DFT_FP32 0
 #define EXGB_DFT_SPLIT_BF16 1
 #define EXGB_TUNE_THREADS 4
+/* EXGB_TUNE_WAIT_BUDGET values[0] = clock cycles allowed to the first
+ * MMA-completion wait of each launch of the split-BF16 tensor-core kernel
+ * (0 = the normal budget of about 2 s).  For tests of the timeout path only:
+ * a budget of a few cycles makes that wait give up while its MMAs are still
+ * in flight; the kernel then waits for them with the normal budget, releases
+ * its tensor memory and reports EXGB_ETIMEOUT through exgb_plan_status. */
+#define EXGB_TUNE_WAIT_BUDGET 5
 int exgb_plan_tune(exgb_plan* plan, int kind, const int* values, int n);
 int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n);
 /* Kernel launches of the fused 2D stepping kernel that one exgb_repeat_fourier
@@ -150,7 +157,8 @@ int exgb_plan_get_tuning(const exgb_plan* plan, int* out, int n);
  * kernel.  No reference counterpart (launch accounting for benchmarks). */
 int exgb_plan_fused_launches(const exgb_plan* plan, int64_t batch, int* launches);
 /* Synchronises the device and returns EXGB_ETIMEOUT if a bounded wait inside
- * the tensor-core kernel of this plan gave up (its outputs are then invalid). */
+ * the tensor-core kernel of this plan gave up since the last call (the
+ * outputs of that launch are then invalid); the status is cleared on read. */
 int exgb_plan_status(const exgb_plan* plan);
 
 /* ---- spectral transforms ----
@@ -191,15 +199,17 @@ int exgb_rollout(const exgb_plan* plan, void* stream, const float* u0, float* tr
                  int32_t nsteps, int32_t include_init);
 
 /* Same result as exgb_repeat_fourier for 2D vorticity plans (N in {64, 128,
- * 256}, ETDRK order >= 1), for callers that cannot allocate device memory
- * where they step (e.g. inside a framework's custom call that may only use
- * the buffers it is given).  No counterpart in the reference.  Calls no
- * cudaMalloc/cudaFree: the stage buffers live in an 8 MiB file-scope device
- * array that every GPU loading the library keeps until exit; plans needing
- * more than 8 MiB per cluster are rejected with EXGB_EUNSUPPORTED.  The
- * first call on a device looks up the array's address (make it before any
- * stream capture).  All calls share the array: calls that overlap on the
- * GPU race and must be serialised by the caller. */
+ * 256}, ETDRK order >= 1, FP32 transforms), for callers that cannot allocate
+ * device memory where they step (e.g. inside a framework's custom call that
+ * may only use the buffers it is given).  No counterpart in the reference.
+ * Calls no cudaMalloc/cudaFree: the stage buffers live in an 8 MiB
+ * file-scope device array that every GPU loading the library keeps until
+ * exit; plans needing more than 8 MiB per cluster, and plans switched to
+ * EXGB_DFT_SPLIT_BF16, are rejected with EXGB_EUNSUPPORTED.  Every call
+ * looks up the array's address on the current device; the first call on a
+ * device also loads the module there (make it before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
 int exgb_repeat_fourier_noalloc(const exgb_plan* plan, void* stream, const void* u_hat0, void* u_hat_out,
                                 int64_t batch, int32_t nsteps);
 

@@ -1,8 +1,8 @@
 """Run one stepping workload for profiling (e.g. under ncu).
 
-    python -m exponax_gb300.profile_case --dims 2 --n 256 --batch 32 --steps 10 --reps 3
-    python -m exponax_gb300.profile_case --dims 2 --n 128 --kolmogorov --precision split_bf16
-    python -m exponax_gb300.profile_case --uneven 600 --steps 100 --reps 3
+    python profile_case.py --dims 2 --n 256 --batch 32 --steps 10 --reps 3
+    python profile_case.py --dims 2 --n 128 --kolmogorov --precision split_bf16
+    python profile_case.py --uneven 600 --steps 100 --reps 3
 
 Builds the stepper (NavierStokesVorticity in 2D, KuramotoSivashinsky-
 Conservative in 1D), creates device-resident Fourier states and launches

@@ -130,7 +130,7 @@ def test_trained_corrector_beats_the_plain_coarse_stepper():
     the relative L2 error of the plain 64^2 stepper after 1, 10 and 30 coarse steps (measured about
     0.72x, 0.78x, 0.76x)."""
     import exponax_gb300 as ex
-    from exponax_gb300 import kolmogorov_experiment as ke
+    from exponax_gb300 import learned as ke
     from exponax_gb300.learned import PeriodicConvCorrector
 
     kw = dict(n_fine=128, n_coarse_grid=64, dt=0.002, ratio=8, spinup=3000, n_coarse=30)

@@ -166,3 +166,30 @@ def test_split_bf16_batch_not_multiple_of_ctas():
     out = ex.vmap(ex.repeat(sm, 3))(cu(big)).cpu().numpy()
     for rep in (0, 77, 100):
         np.testing.assert_array_equal(out[2 * rep:2 * rep + 2], small)
+
+
+def test_bounded_wait_runs_out_and_reports_timeout():
+    """The timeout path of the tensor-core kernel's bounded device waits, with no fault: a test-only
+    knob gives the first MMA-completion wait of each launch a budget of 2 clock cycles, so it gives up
+    while its MMAs are in flight.  The kernel then drains them with the normal budget, releases its
+    tensor memory and sets the status word: exgb_plan_status returns EXGB_ETIMEOUT (and clears it),
+    the context stays usable, and with the normal budget restored the next call matches the oracle
+    within 1e-5 after one step."""
+    from exponax_gb300 import _lib, autotune
+
+    lib = load()
+    N = 128
+    sm = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, N, 0.01).set_dft_precision("split_bf16")
+    so = o.KolmogorovFlowVorticity(2, 2 * np.pi, N, 0.01)
+    u0 = np.stack([ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)(N, key=s) for s in range(4)])
+    assert autotune._set(sm.plan, _lib.EXGB_TUNE_WAIT_BUDGET, [2]) == 0
+    ex.vmap(sm)(cu(u0))
+    torch.cuda.synchronize()
+    assert lib.exgb_plan_status(sm.plan.handle) == _lib.EXGB_ETIMEOUT
+    assert b"gave up" in lib.exgb_last_error()
+    assert lib.exgb_plan_status(sm.plan.handle) == 0  # cleared on read
+    assert autotune._set(sm.plan, _lib.EXGB_TUNE_WAIT_BUDGET, [0]) == 0
+    got = ex.vmap(sm)(cu(u0)).cpu().numpy()
+    sm.plan.status()
+    for b in range(4):
+        assert rel(got[b], so(u0[b])) < 1e-5

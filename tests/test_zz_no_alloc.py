@@ -51,3 +51,23 @@ def test_noalloc_rejects_plans_it_cannot_serve():
     rc = lib.exgb_repeat_fourier_noalloc(st.plan.handle, _device.stream(), uh.data_ptr(), uh.data_ptr(), 1, 1)
     assert rc == _lib.EXGB_EUNSUPPORTED
     assert b"2D vorticity" in lib.exgb_last_error()
+
+
+def test_noalloc_refuses_a_plan_switched_to_split_bf16():
+    """The entry point runs FP32 transforms only: a plan switched to the
+    split-BF16 tensor-core DFT is refused instead of being stepped with other
+    arithmetic than exgb_repeat_fourier uses for it."""
+    import exponax_gb300 as ex
+    from exponax_gb300 import _device, _lib
+
+    lib = _lib.load()
+    st = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, 128, 0.01).set_dft_precision("split_bf16")
+    uh = torch.zeros((2, 1, 128, 65), dtype=torch.complex64, device="cuda")
+    rc = lib.exgb_repeat_fourier_noalloc(st.plan.handle, _device.stream(), uh.data_ptr(), uh.data_ptr(), 2, 1)
+    assert rc == _lib.EXGB_EUNSUPPORTED
+    assert b"split-BF16" in lib.exgb_last_error()
+    st.set_dft_precision("fp32")
+    out = torch.full_like(uh, float("nan"))
+    _lib.check(lib.exgb_repeat_fourier_noalloc(st.plan.handle, _device.stream(), uh.data_ptr(), out.data_ptr(), 2, 1))
+    torch.cuda.synchronize()
+    assert torch.isfinite(torch.view_as_real(out)).all()
