@@ -233,9 +233,12 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
     return fail(EXGB_EUNSUPPORTED, "num_spatial_dims must be 1, 2 or 3");
   if (d.order < 0 || d.order > 4)
     return fail(EXGB_ENOTIMPL, "Order " + std::to_string(d.order) + " not implemented.");
-  if (!factorable(d.num_points))
-    return fail(EXGB_ENOTFACTORABLE, "num_points must be a product of 2, 3 and 5 (got " +
-                                         std::to_string(d.num_points) + ")");
+  if (d.num_points < 2) return fail(EXGB_EINVAL, "num_points must be >= 2");
+  {
+    // every N the transforms take: 2^a 3^b 5^c (any length in 1D), other N through Bluestein
+    const int trc = transform_supported(d.num_points);
+    if (trc) return trc;
+  }
   if (d.num_channels < 1) return fail(EXGB_ESHAPE, "num_channels must be >= 1");
   if (d.linear_operator_channels != 1 && d.linear_operator_channels != d.num_channels)
     return fail(EXGB_ESHAPE, "linear operator must have 1 or num_channels channels");
@@ -245,8 +248,18 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   const int D = d.num_spatial_dims, N = d.num_points, M = N / 2 + 1;
   const bool nonlinear = d.order >= 1 && d.nonlin_kind != EXGB_NL_ZERO;
 
-  // supported (D, kind) combinations of this build
-  const bool staged = ndgen_handles(d);
+  // supported (D, kind) combinations of this build.  The fused kernels take N = 2^a 3^b 5^c (1D: one
+  // instance in one CTA's shared memory; 2D vorticity: N <= 1024); other sizes of the 1D
+  // nonlinearities and of 2D vorticity are stepped by the staged path on the general transforms.
+  const bool smooth = factorable(d.num_points);
+  bool staged = ndgen_handles(d);
+  if (!staged && d.order >= 1 && d.nonlin_kind != EXGB_NL_ZERO && ndgen_can(d)) {
+    if (d.num_spatial_dims == 1 && d.nonlin_kind <= EXGB_NL_GENERAL)
+      staged = !smooth || !etdrk1d_fits(d.num_points, d.order);
+    else if (d.num_spatial_dims == 2 &&
+             (d.nonlin_kind == EXGB_NL_VORTICITY_2D || d.nonlin_kind == EXGB_NL_VORTICITY_2D_KOLMOGOROV))
+      staged = !smooth || d.num_points > 1024;
+  }
   if (d.order >= 1 && d.nonlin_kind != EXGB_NL_ZERO) {
     if (d.nonlin_kind < EXGB_NL_ZERO || d.nonlin_kind > EXGB_NL_BELOUSOV_ZHABOTINSKY)
       return fail(EXGB_EINVAL, "unknown nonlinear function");
@@ -290,16 +303,21 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
     cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev);
   }
 
-  if (!make_fft_plan(N, &v.fft)) {
-    exgb_plan_destroy(p);
-    return fail(EXGB_ENOTFACTORABLE, "cannot build an FFT plan for N=" + std::to_string(N));
+  // length-N plan and twiddles of the fused kernels (N = 2^a 3^b 5^c); the staged, 3D and
+  // linear paths go through the general transforms instead
+  int rc = EXGB_OK;
+  if (smooth) {
+    if (!make_fft_plan(N, &v.fft)) {
+      exgb_plan_destroy(p);
+      return fail(EXGB_ENOTFACTORABLE, "cannot build an FFT plan for N=" + std::to_string(N));
+    }
+    rc = build_twiddles(N, &p->d_tw);
+    if (rc) {
+      exgb_plan_destroy(p);
+      return rc;
+    }
+    v.tw = p->d_tw;
   }
-  int rc = build_twiddles(N, &p->d_tw);
-  if (rc) {
-    exgb_plan_destroy(p);
-    return rc;
-  }
-  v.tw = p->d_tw;
 
   // nonlinear parameters
   const float b = (float)d.scale;

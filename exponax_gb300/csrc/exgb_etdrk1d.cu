@@ -535,6 +535,16 @@ static int smem_limit() {
   return lim;
 }
 
+bool etdrk1d_fits(int N, int order) {
+  PlanDev P{};
+  P.N = N;
+  P.M = N / 2 + 1;
+  P.order = order;
+  const size_t lim = (size_t)smem_limit() - 4096;
+  const size_t work = sizeof(float2) * 2 * (size_t)N;
+  return smem_for(P, 1, true) <= lim && (smem_for(P, 1, false) <= lim || work <= kQueueSmemCap);
+}
+
 // Items for `batch` instances of one plan, m instances per item.
 static int choose_m(const PlanDev& P, int64_t batch, int sm_count, bool nonlin_only) {
   int m = std::max(1, 2048 / P.N);  // instances per item up to m N = 2048 (as the work queue)
@@ -675,7 +685,9 @@ static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps,
   for (int64_t i = 0; i < n_items;) {
     const exgb_plan* p = items[i].plan;
     if (!p || !items[i].u0 || !items[i].traj) return fail(EXGB_EINVAL, "work item with NULL plan or buffer");
-    if (p->dev.D != 1 || p->staged) return fail(EXGB_EUNSUPPORTED, "the work queue runs 1D single-channel plans");
+    if (p->dev.D != 1 || p->staged || p->dev.fft.n == 0 || !etdrk1d_fits(p->dev.N, p->dev.order))
+      return fail(EXGB_EUNSUPPORTED,
+                  "the work queue runs 1D single-channel plans of N = 2^a 3^b 5^c that fit in one CTA");
     sm_count = p->sm_count;
     const int N = p->dev.N;
     const int mmax = std::min(64, std::max(1, 2048 / N));  // 2048 / N measured best (1024: -8 %, 4096: -22 %)

@@ -135,6 +135,12 @@ int tcdft2d_configure(exgb_plan* plan);
 int tcdft2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                 int project, int nonlinear_only);
 bool ndgen_handles(const exgb_plan_desc& d);
+bool ndgen_can(const exgb_plan_desc& d);
+// 0 when rfftn / irfftn take transforms of length n on this device (any n with a prime factor
+// above 5 up to the Bluestein limit, 2^a 3^b 5^c of any length in 1D), else an EXGB_E* code
+int transform_supported(int n);
+// does the fused 1D kernel hold one instance of N points at this ETDRK order in shared memory?
+bool etdrk1d_fits(int N, int order);
 int ndgen_validate(const exgb_plan_desc& d);
 int ndgen_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
               int project, int nonlinear_only);

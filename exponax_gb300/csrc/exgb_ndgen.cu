@@ -50,6 +50,8 @@ enum Op {
   OP_CAHN_HILLIARD,     // s Lap F[u^3]                         (_cahn_hilliard.py:31-45)
   OP_GRAY_SCOTT,        // F[f(1-u0) - u0 u1^2], F[-(f+k) u1 + u0 u1^2]  (_gray_scott.py:30-46)
   OP_BZ,                // F[u0 + u1 - u0 u1 - u0^2], F[u2 - u1 - u0 u1], F[u0 - u2]  (_belousov_zhabotinsky.py:33-51)
+  OP_VORT,              // -b F[u w_x + v w_y], (u, v) = (d_y, -d_x) Lap^-1 w  (_vorticity_convection.py:78-99),
+                        // + the Kolmogorov injection at (0, k)               (_vorticity_convection.py:166-176)
 };
 
 struct Geo {
@@ -127,6 +129,18 @@ __global__ void derive_kernel(Geo g, Prog p, int64_t cb, const float2* __restric
         w[0] = u;
         for (int j = 0; j < g.D; ++j) w[(1 + j) * g.per] = times_i(d[j], u);
       } break;
+      case OP_VORT: {
+        // stream function psi = w / Lap with 1/Lap = 1 at k = 0; u = i k_y psi, v = -i k_x psi,
+        // w_x = i k_x w, w_y = i k_y w (k_x the leading axis, k_y the rfft axis)
+        const float2 wv = m ? x[0] : z;
+        const float lap = -(d[0] * d[0] + d[1] * d[1]);
+        const float il = lap != 0.f ? 1.f / lap : 1.f;
+        const float2 psi = cscale(wv, il);
+        w[0] = times_i(d[1], psi);
+        w[g.per] = times_i(-d[0], psi);
+        w[2 * g.per] = times_i(d[0], wv);
+        w[3 * g.per] = times_i(d[1], wv);
+      } break;
       default:  // the masked state itself, one spectrum per channel
         for (int c = 0; c < g.C; ++c) w[c * g.per] = m ? x[c * g.per] : z;
         break;
@@ -196,6 +210,9 @@ __global__ void pointwise_kernel(Geo g, Prog p, int64_t cb, const float* __restr
         f[0] = p.feed * (1.f - u0) - uvv;
         f[g.npts] = -(p.feed + p.kill) * u1 + uvv;
       } break;
+      case OP_VORT:
+        f[0] = fmaf(in[0], in[2], in[1] * in[3]);
+        break;
       case OP_BZ: {
         const float u0 = in[0], u1 = in[1], u2 = in[2];
         const float u01 = u0 * u1;
@@ -263,11 +280,12 @@ __global__ void combine_kernel(PlanDev P, Geo g, Prog p, int64_t cb, const float
         case OP_CAHN_HILLIARD:
           nv[0] = cscale(h[0], p.s0 * lap);
           break;
-        default:  // -b F[.] (non-conservative convection) or F[.] (polynomial, Gray-Scott): scale s0
+        default:  // -b F[.] (non-conservative convection, vorticity) or F[.] (polynomial, Gray-Scott): scale s0
           for (int c = 0; c < g.C; ++c) nv[c] = cscale(h[c * g.per], p.s0);
           break;
       }
     }
+    if (p.op == OP_VORT && k[0] == 0 && k[1] == P.inj_mode) nv[0].x += P.inj_value;
     const int64_t base = b * g.C * g.per + r;
     if (stage < 0) {
       for (int c = 0; c < g.C; ++c) nout[base + c * g.per] = nv[c];
@@ -321,6 +339,28 @@ using namespace ndg;
 
 // Does the staged path step this plan?  (The fused kernels cover the 1D
 // single-channel nonlinearities, 2D vorticity and 3D projected convection.)
+// Can the staged path step this plan?  Besides the plans it always takes, it steps the 1D
+// nonlinearities and 2D vorticity at the sizes the fused kernels do not cover (a prime factor above
+// 5, or a grid longer than one CTA's shared memory holds).
+bool ndgen_can(const exgb_plan_desc& d) {
+  if (d.order < 1 || d.nonlin_kind == EXGB_NL_ZERO) return false;
+  switch (d.nonlin_kind) {
+    case EXGB_NL_CONVECTION:
+    case EXGB_NL_GRADIENT_NORM:
+    case EXGB_NL_POLYNOMIAL:
+    case EXGB_NL_GENERAL:
+    case EXGB_NL_CAHN_HILLIARD:
+    case EXGB_NL_GRAY_SCOTT:
+    case EXGB_NL_BELOUSOV_ZHABOTINSKY:
+      return true;
+    case EXGB_NL_VORTICITY_2D:
+    case EXGB_NL_VORTICITY_2D_KOLMOGOROV:
+      return d.num_spatial_dims == 2;
+    default:
+      return false;
+  }
+}
+
 bool ndgen_handles(const exgb_plan_desc& d) {
   if (d.order < 1 || d.nonlin_kind == EXGB_NL_ZERO) return false;
   switch (d.nonlin_kind) {
@@ -365,6 +405,11 @@ int ndgen_validate(const exgb_plan_desc& d) {
       return EXGB_OK;
     case EXGB_NL_BELOUSOV_ZHABOTINSKY:
       if (C != 3) return fail(EXGB_ESHAPE, "num_channels must be 3");
+      return EXGB_OK;
+    case EXGB_NL_VORTICITY_2D:
+    case EXGB_NL_VORTICITY_2D_KOLMOGOROV:
+      if (D != 2) return fail(EXGB_EUNSUPPORTED, "vorticity convection needs num_spatial_dims == 2");
+      if (C != 1) return fail(EXGB_ESHAPE, "vorticity formulation has one channel");
       return EXGB_OK;
     default:
       return fail(EXGB_EUNSUPPORTED, "nonlinear function not handled by the staged path");
@@ -419,6 +464,13 @@ static Prog make_prog(const exgb_plan_desc& d) {
     case EXGB_NL_BELOUSOV_ZHABOTINSKY:
       p.op = OP_BZ;
       p.NI = p.NF = 3;
+      break;
+    case EXGB_NL_VORTICITY_2D:
+    case EXGB_NL_VORTICITY_2D_KOLMOGOROV:
+      p.op = OP_VORT;
+      p.NI = 4;
+      p.NF = 1;
+      p.s0 = -b;
       break;
     default:  // Gray-Scott
       p.op = OP_GRAY_SCOTT;

@@ -54,9 +54,37 @@ __global__ void etdrk0_2d_kernel(const float2* __restrict__ E, int transposed, i
   }
 }
 
+// ETDRK0 for 1D fields of N/2+1 modes: u^ <- E u^, nsteps times; the c2r projection keeps the real
+// part of the k = 0 and (N even) k = N/2 modes.  One thread per mode.
+__global__ void etdrk0_1d_kernel(const float2* __restrict__ E, int N, int lin_ch, int C, int64_t batch,
+                                 const float2* in, float2* out, int nsteps, int project) {
+  const int M = N / 2 + 1;
+  const int64_t total = (int64_t)M * C * batch;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t field = t / M;
+    const int k = (int)(t - field * M);
+    const int lc = lin_ch == 1 ? 0 : (int)(field % C);
+    const float2 e = E[(int64_t)lc * M + k];
+    const bool proj = project && (k == 0 || ((N & 1) == 0 && k == N / 2));
+    float2 v = in[t];
+    for (int s = 0; s < nsteps; ++s) {
+      v = cmul(e, v);
+      if (proj) v.y = 0.f;
+    }
+    out[t] = v;
+  }
+}
+
 int etdrk0_apply(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                  int project) {
   const PlanDev& P = plan->dev;
+  if (P.D == 1) {
+    const int64_t total = (int64_t)P.M * P.C * batch;
+    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)plan->sm_count * 16));
+    etdrk0_1d_kernel<<<blocks, 256, 0, st>>>(P.E, P.N, P.lin_ch, P.C, batch, in, out, nsteps, project);
+    EXGB_CUDA(cudaGetLastError());
+    return EXGB_OK;
+  }
   const int transposed = (P.D == 2 && P.order >= 1) ? 1 : 0;
   const int64_t total = (int64_t)(P.N / 2 + 1) * (P.N / 2 + 1) * P.C * batch;
   if (total <= 0) return EXGB_OK;
@@ -68,6 +96,13 @@ int etdrk0_apply(const exgb_plan* plan, cudaStream_t st, const float2* in, float
 }
 
 static bool linear_only(const PlanDev& P) { return P.order == 0 || P.kind == EXGB_NL_ZERO; }
+
+// 1D plans stepped by the fused 1D kernel: N = 2^a 3^b 5^c and one instance fits in a CTA's shared
+// memory (the other 1D plans run on the staged path or, when linear, on etdrk0_1d_kernel)
+static bool fused1d(const exgb_plan* plan) {
+  const PlanDev& P = plan->dev;
+  return P.D == 1 && !plan->staged && P.fft.n > 0 && etdrk1d_fits(P.N, P.order);
+}
 
 int steps3d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* out, int64_t batch, int nsteps,
                 int project, int nonlinear_only);
@@ -116,7 +151,7 @@ int exgb_repeat_fourier(const exgb_plan* plan, void* stream, const void* u_hat0,
                                 cudaMemcpyDeviceToDevice, st));
     return EXGB_OK;
   }
-  if (plan->dev.D == 1 && !plan->staged)
+  if (fused1d(plan))
     return etdrk1d_run(plan, st, nullptr, (const float2*)u_hat0, nullptr, (float2*)u_hat_out, batch, nsteps, 0, 0, 0,
                        0);
   return fourier_steps_2d(plan, st, (const float2*)u_hat0, (float2*)u_hat_out, batch, nsteps, 0);
@@ -135,7 +170,7 @@ int exgb_nonlinear(const exgb_plan* plan, void* stream, const void* u_hat_in, vo
   }
   if (plan->staged) return ndgen_run(plan, st, (const float2*)u_hat_in, (float2*)n_hat_out, batch, 0, 0, 1);
   if (P.D == 3) return steps3d_run(plan, st, (const float2*)u_hat_in, (float2*)n_hat_out, batch, 0, 0, 1);
-  if (P.D == 1)
+  if (fused1d(plan))
     return etdrk1d_run(plan, st, nullptr, (const float2*)u_hat_in, nullptr, (float2*)n_hat_out, batch, 0, 0, 0, 0,
                        1);
   return etdrk2d_run(plan, st, (const float2*)u_hat_in, (float2*)n_hat_out, batch, 0, 0, 1);
@@ -153,7 +188,7 @@ int exgb_repeat(const exgb_plan* plan, void* stream, const float* u0, float* u_o
       EXGB_CUDA(cudaMemcpyAsync(u_out, u0, sizeof(float) * phys_elems(P, batch), cudaMemcpyDeviceToDevice, st));
     return EXGB_OK;
   }
-  if (P.D == 1 && !plan->staged) return etdrk1d_run(plan, st, u0, nullptr, u_out, nullptr, batch, nsteps, 1, 0, 0, 0);
+  if (fused1d(plan)) return etdrk1d_run(plan, st, u0, nullptr, u_out, nullptr, batch, nsteps, 1, 0, 0, 0);
   float2* hat = (float2*)workspace(sizeof(float2) * hat_elems(P, batch), 2);
   if (!hat) return fail(EXGB_ENOMEM, "workspace allocation failed");
   int rc = rfftn_impl(st, P.D, P.N, batch * P.C, u0, hat);
@@ -175,7 +210,7 @@ int exgb_rollout(const exgb_plan* plan, void* stream, const float* u0, float* tr
   if (!u0 || !traj) return fail(EXGB_EINVAL, "NULL argument");
   cudaStream_t st = (cudaStream_t)stream;
   const PlanDev& P = plan->dev;
-  if (P.D == 1 && !plan->staged)
+  if (fused1d(plan))
     return etdrk1d_run(plan, st, u0, nullptr, traj, nullptr, batch, nsteps, 1, 1, include_init ? 1 : 0, 0);
   const int T = nsteps + (include_init ? 1 : 0);
   const size_t frame = phys_elems(P, 1);  // floats per sample

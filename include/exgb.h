@@ -34,7 +34,7 @@ extern "C" {
 #define EXGB_OK 0
 #define EXGB_EINVAL (-1)          /* bad argument (NULL pointer, bad enum) */
 #define EXGB_ESHAPE (-2)          /* shape / channel / dimension mismatch */
-#define EXGB_ENOTFACTORABLE (-3)  /* N has a prime factor other than 2, 3, 5 */
+#define EXGB_ENOTFACTORABLE (-3)  /* N has a prime factor above 5 and is too long for the Bluestein transform */
 #define EXGB_ECUDA (-4)           /* a CUDA runtime call failed */
 #define EXGB_ETIMEOUT (-5)        /* a bounded device wait gave up */
 #define EXGB_EGUARD (-6)          /* spectral-energy / non-finite guard tripped */
@@ -64,7 +64,7 @@ typedef struct exgb_plan exgb_plan;
  * function with its scalar parameters. */
 typedef struct {
   int32_t num_spatial_dims;        /* D: 1, 2 or 3 */
-  int32_t num_points;              /* N (2^a 3^b 5^c) */
+  int32_t num_points;              /* N >= 2 (prime factors above 5 through Bluestein) */
   int32_t num_channels;            /* C */
   int32_t order;                   /* ETDRK order 0..4 */
   double domain_extent;            /* L */

@@ -83,19 +83,6 @@ def test_in_place_fourier_stepping(kind):
         assert rel(got[b], o.repeat(so, 5)(u[b])) < 1e-5, b
 
 
-def test_sizes_the_library_refuses():
-    """N that is not 2^a 3^b 5^c, and a 1D grid larger than one CTA's shared memory, raise instead of
-    launching; the library stays usable afterwards."""
-    with pytest.raises(ValueError):
-        ex.vmap(ex.stepper.Burgers(1, 1.0, 77, 0.01))(torch.zeros((1, 1, 77), device="cuda"))
-    big = ex.stepper.KuramotoSivashinskyConservative(1, 100.0, 2 ** 16, 0.1)
-    with pytest.raises((ValueError, ex.ExgbError)):
-        ex.vmap(big)(torch.zeros((1, 1, 2 ** 16), device="cuda"))
-    sm = ex.stepper.Burgers(1, 1.0, 64, 0.01)
-    u = ex.ic.RandomSineWaves1d(1)(64, key=1)
-    assert rel(sm(torch.from_numpy(u).cuda()).cpu().numpy(), o.Burgers(1, 1.0, 64, 0.01)(u)) < 1e-5
-
-
 @pytest.mark.parametrize("name,order", [("KuramotoSivashinskyConservative", 2), ("Burgers", 1), ("Burgers", 3),
                                         ("KuramotoSivashinsky", 2), ("KortewegDeVries", 4), ("FisherKPP", 2)])
 def test_1d_batches_larger_than_the_gpu(name, order):

@@ -397,9 +397,8 @@ def test_errors_follow_the_reference():
     sm = ex.stepper.Burgers(1, 1.0, 64, 0.01)
     with pytest.raises(ValueError):
         sm(cu(np.zeros((2, 64), np.float32)))
-    bad = ex.stepper.Burgers(1, 1.0, 14, 0.01)  # 14 = 2 * 7 cannot be planned
-    with pytest.raises(ValueError):
-        bad(cu(np.zeros((1, 14), np.float32)))
+    with pytest.raises(ValueError):  # prime, too long for the Bluestein transform of one CTA
+        ex.stepper.Burgers(1, 1.0, 7919, 0.01)(cu(np.zeros((1, 7919), np.float32)))
 
 
 def test_queue_rollout_graph_capture_and_replay():

@@ -48,9 +48,11 @@ def test_null_arguments_are_rejected_without_touching_the_gpu():
     assert b"NULL" in lib.exgb_last_error()
     d = _lib.PlanDesc()
     d.num_spatial_dims = 1
-    d.num_points = 14  # 2 * 7: not a product of 2, 3, 5
+    d.num_points = 1
     d.order = 2
     d.num_channels = 1
+    assert lib.exgb_plan_create(ctypes.byref(d), ctypes.byref(h)) == _lib.EXGB_EINVAL
+    d.num_points = 7919  # prime, too long for the Bluestein transform of one CTA
     assert lib.exgb_plan_create(ctypes.byref(d), ctypes.byref(h)) == _lib.EXGB_ENOTFACTORABLE
     d.num_points = 16
     d.order = 5
