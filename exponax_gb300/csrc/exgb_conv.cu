@@ -9,9 +9,10 @@
 // input/output fields are float32 (B, H, 64).  Weights W[tap][co][ci],
 // tap = (dy+1)*3 + (dx+1), periodic wrap in both directions.
 //
-// * conv48_mma_kernel: 48 -> 48 channels as an implicit GEMM on the tensor
-//   cores (mma.sync m16n8k16, bf16 x bf16 -> f32): a CTA computes 4 rows x
-//   64 columns x 48 output channels from a shared-memory halo tile; the
+// * conv48_tc_kernel: 48 -> 48 channels as an implicit GEMM on the tcgen05
+//   tensor cores (kind::f16, bf16 x bf16 -> FP32 in tensor memory): a tile
+//   is 2 rows x 64 columns x 48 output channels, its operands read by
+//   shared-memory descriptors from shifted copies of the input rows; the
 //   epilogue adds the bias and applies GELU (forward) or multiplies by
 //   GELU'(pre) of the layer below (backward-data, with flipped weights).
 // * conv_in1 / conv_out1: the 1 -> 48 and 48 -> 1 layers (SIMT).
@@ -22,142 +23,379 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "exgb_internal.h"
+#include "exgb_tc.cuh"
 
 namespace exgb {
 
 constexpr int kC = 48;     // hidden channels
 constexpr int kW = 64;     // grid width (columns)
-constexpr int kCP = 56;    // padded channel stride in shared memory (bank-conflict free)
-constexpr int kTR = 4;     // output rows per CTA
 
-__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks & Gimpel, "Gaussian Error Linear Units", 2016):
+//   gelu(x) = x / 2 (1 + tanh(u)),  u = sqrt(2 / pi) (x + 0.044715 x^3),
+// with the hardware tanh (tanh.approx.f32, relative error about 2^-11, below the bf16 rounding of
+// the activations); gelu'(x) = (1 + t) / 2 + x / 2 (1 - t^2) sqrt(2 / pi) (1 + 3 0.044715 x^2).
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kGeluA = 0.79788456080286536f;            // sqrt(2 / pi)
+constexpr float kGeluB = 0.79788456080286536f * 0.044715f;
+__device__ __forceinline__ float gelu_f(float x) {
+  const float t = tanh_hw(x * fmaf(kGeluB, x * x, kGeluA));
+  const float h = 0.5f * x;
+  return fmaf(h, t, h);
+}
 __device__ __forceinline__ float gelu_d(float x) {
-  const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
-  return cdf + x * pdf;
+  const float x2 = x * x;
+  const float t = tanh_hw(x * fmaf(kGeluB, x2, kGeluA));
+  const float du = fmaf(3.f * kGeluB, x2, kGeluA);
+  return fmaf(0.5f * x * du, fmaf(-t, t, 1.f), fmaf(0.5f, t, 0.5f));
 }
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                         uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
+// 48 -> 48 channels as an implicit GEMM on the tcgen05 tensor cores.  A tile is 2 output rows x 64
+// columns = 128 pixels (M = 128) x 48 output channels (N = 48); K = 9 taps x 48 input channels, 27
+// MMAs of K = 16 issued by one thread with the FP32 accumulator in tensor memory.
+//
+// Operand A of tap (dy, dx) is read straight from a shared-memory copy of the 4 input rows the tile
+// needs, with no im2col: the copy for horizontal shift dx holds x[y][(c + dx) mod 64] at pixel slot
+// q = 64 r + c (r the halo row, the periodic wrap applied while copying), stored K-major without
+// swizzle as 8-channel chunks: (q, channel) at chunk * 4096 + q * 16 + (channel % 8) * 2.  Rows of
+// the A operand (pixels) are 16 bytes apart inside and across core matrices (stride byte offset
+// 128), chunks 4096 bytes apart (leading byte offset), so the 128 pixels of output rows (oy, oy+1)
+// under tap (dy, dx) are the 128 consecutive slots from q = 64 (1 + dy) of copy dx: one descriptor.
+// Operand B is W[tap][co][ci] in the K-major layout of exgb_tc.cuh.
+//
+// Warp roles, handing tiles over through mbarriers (every wait clock-bounded; a wait that gives up
+// raises a CTA-wide abort flag and the status word read by exgb_conv_status):
+//   warps 0-3   copy a tile's input rows into one of two stages (cp.async), then arrive on full[s]
+//   warp 12     waits full[s] and accumulator a free, issues the 27 MMAs, commits to empty[s] and
+//               accfull[a]
+//   warps 4-11  wait accfull[a], read the accumulator (warp w: TMEM lanes 32 (w % 4).., 24 channels),
+//               free it, apply bias and GELU (or GELU' for the backward pass), stage the tile's outputs
+//               in shared memory -- they form the 12 KB the tile occupies contiguously in global
+//               memory -- and one thread writes them with a bulk copy
+namespace ctc {
+constexpr int kProducerWarps = 4, kEpilogueWarps = 8;
+constexpr int kMmaWarp = kProducerWarps + kEpilogueWarps;      // 12
+constexpr int kThreads = 32 * (kMmaWarp + 1);                  // 416
+constexpr int kProducerThreads = 32 * kProducerWarps;
+constexpr int kEpilogueThreads = 32 * kEpilogueWarps;
+constexpr int kHaloRows = 4;                                   // 2 output rows + 1 above + 1 below
+constexpr uint32_t kSlots = kHaloRows * kW;                    // 256 pixel slots per copy
+constexpr uint32_t kChunkStride = kSlots * 16;                 // 4096 B between 8-channel chunks
+constexpr uint32_t kCopyBytes = (kC / 8) * kChunkStride;       // 24576 B per shifted copy
+constexpr uint32_t kStageBytes = 3 * kCopyBytes;               // dx = -1, 0, +1
+constexpr uint32_t kTapBytes = kC * kC * 2;                    // 4608 B of weights per tap
+constexpr uint32_t kWBytes = 9 * kTapBytes;
+constexpr uint32_t kOutBytes = 2 * kW * kC * 2;                // 12288 B: one tile of bf16 outputs
+constexpr uint32_t kOffW = 2 * kStageBytes;
+constexpr uint32_t kOffOut = kOffW + kWBytes;                  // staged `post` (forward) or result (backward)
+constexpr uint32_t kOffOut2 = kOffOut + kOutBytes;             // staged `pre` (forward before a backward pass)
+constexpr uint32_t kOffBar = kOffOut2 + kOutBytes;             // 9 mbarriers
+constexpr uint32_t kSmemBytes = kOffBar + 9 * 8;
+constexpr uint32_t kAccCols = 64;                              // accumulator a at TMEM column 64 a
+constexpr int kItems = (int)kSlots * (kC / 8) / kProducerThreads;  // (slot, chunk) copies per producer per tile
+constexpr long long kWaitBudget = 4000000000LL;                // clock cycles (~2 s)
+static_assert(kItems * kProducerThreads == (int)kSlots * (kC / 8), "whole copy items per producer thread");
+static_assert(kSmemBytes + 1024 <= 227 * 1024, "conv tile does not fit in shared memory");
+static_assert(kStageBytes % 16 == 0 && kWBytes % 16 == 0 && kOutBytes % 16 == 0, "16-byte aligned regions");
+}  // namespace ctc
 
-// mode 0: forward  out_pre = conv(x) + bias, out_post = gelu(out_pre)
-// mode 1: backward data  out_pre (= dPre of the layer below) = conv_flipped(x = dPre) * gelu'(aux = pre below)
-__global__ void __launch_bounds__(256, 2) conv48_mma_kernel(const __nv_bfloat16* __restrict__ x, int H,
-                                                           const __nv_bfloat16* __restrict__ w,
-                                                           const float* __restrict__ bias, int mode,
-                                                           const __nv_bfloat16* __restrict__ aux,
-                                                           __nv_bfloat16* __restrict__ out_pre,
-                                                           __nv_bfloat16* __restrict__ out_post) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __nv_bfloat16* xs = reinterpret_cast<__nv_bfloat16*>(smem_raw);           // (kTR+2) x (kW+2) x kCP
-  __nv_bfloat16* ws = xs + (kTR + 2) * (kW + 2) * kCP;                        // 9 x kC x kCP
-  const int tiles_per_img = H / kTR;
-  const int b = blockIdx.x / tiles_per_img;
-  const int y0 = (blockIdx.x % tiles_per_img) * kTR;
-  const int tid = threadIdx.x;
+__device__ int g_conv_status;  // EXGB_ETIMEOUT after a bounded wait of the conv kernel gave up
 
-  // weights -> smem (9 * 48 rows of 48 ci, 16-byte chunks)
-  for (int t = tid; t < 9 * kC * (kC / 8); t += 256) {
-    const int row = t / (kC / 8), ch = t % (kC / 8);
-    *reinterpret_cast<uint4*>(ws + row * kCP + ch * 8) = *reinterpret_cast<const uint4*>(w + row * kC + ch * 8);
+// Copy items of producer thread p, fixed for every tile: item i of the 256 x 6 (slot, chunk) pairs in
+// blocks of 8 slots x 6 chunks, so the 8 threads of a shared-memory store phase write 8 consecutive
+// slots of one chunk (distinct banks) and a warp reads whole 64-byte runs of 4 chunks per pixel.
+struct CopyItems {
+  int src[ctc::kItems];        // element offset inside an input row: column * 48 + chunk * 8
+  int row[ctc::kItems];        // halo row 0..3
+  uint32_t dst[ctc::kItems];   // byte offset in a stage of copy dx = -1 (low 16 bits) and 0 (high 16 bits)
+  uint32_t dst2[ctc::kItems];  // byte offset of copy dx = +1
+};
+
+__device__ __forceinline__ void conv_items(int p, CopyItems& c) {
+#pragma unroll
+  for (int k = 0; k < ctc::kItems; ++k) {
+    const int i = p + ctc::kProducerThreads * k;
+    const int blk = i / 48, rem = i - blk * 48;
+    const int ch = rem >> 3, q = blk * 8 + (rem & 7);
+    const int r = q >> 6, gx = q & (kW - 1);
+    c.src[k] = gx * kC + ch * 8;
+    c.row[k] = r;
+    // copy dx holds x[.][(c + dx) mod 64] at column c, so input column gx lands at c = gx - dx
+    uint32_t o[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      o[d] = (uint32_t)d * ctc::kCopyBytes + (uint32_t)ch * ctc::kChunkStride +
+             (uint32_t)(r * kW + ((gx - (d - 1)) & (kW - 1))) * 16u;
+    c.dst[k] = o[0] | (o[1] << 16);
+    c.dst2[k] = o[2];
   }
-  // halo tile -> smem, periodic wrap
+}
+
+// Copy the 4 input rows of tile `tile` (rows y0 - 1 .. y0 + 2, periodic inside the image) into the
+// three shifted copies with 16-byte cp.async (L1-allocating, so the three copies of a chunk read
+// global memory once), as one commit group.
+__device__ __forceinline__ void conv_load_tile(const __nv_bfloat16* __restrict__ x, int H, int tile,
+                                               uint32_t stage_saddr, const CopyItems& c) {
+  const int tiles_per_img = H / 2;
+  const int b = tile / tiles_per_img, y0 = (tile - b * tiles_per_img) * 2;
   const __nv_bfloat16* xb = x + (size_t)b * H * kW * kC;
-  for (int t = tid; t < (kTR + 2) * (kW + 2) * (kC / 8); t += 256) {
-    const int ch = t % (kC / 8);
-    const int pix = t / (kC / 8);
-    const int r = pix / (kW + 2), c = pix % (kW + 2);
-    const int gy = (y0 + r - 1 + H) % H, gx = (c - 1 + kW) % kW;
-    *reinterpret_cast<uint4*>(xs + pix * kCP + ch * 8) =
-        *reinterpret_cast<const uint4*>(xb + ((size_t)gy * kW + gx) * kC + ch * 8);
+  int rows[ctc::kHaloRows];
+#pragma unroll
+  for (int r = 0; r < ctc::kHaloRows; ++r) {
+    const int gy = y0 + r - 1;
+    rows[r] = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
   }
-  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < ctc::kItems; ++k) {
+    int gy = rows[0];
+#pragma unroll
+    for (int r = 1; r < ctc::kHaloRows; ++r) gy = c.row[k] == r ? rows[r] : gy;
+    const __nv_bfloat16* src = xb + (size_t)gy * kW * kC + c.src[k];
+    const uint32_t d0 = stage_saddr + (c.dst[k] & 0xFFFFu), d1 = stage_saddr + (c.dst[k] >> 16),
+                   d2 = stage_saddr + c.dst2[k];
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d0), "l"(src) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d1), "l"(src) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d2), "l"(src) : "memory");
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_but_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
-  const int warp = tid >> 5, lane = tid & 31;
-  const int g = lane >> 2, tig = lane & 3;
-  float acc[2][6][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 6; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(tc::smem_u32(mbar))
+               : "memory");
+}
+// named barrier over the epilogue warps only
+__device__ __forceinline__ void epilogue_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(ctc::kEpilogueThreads) : "memory");
+}
 
-  // this warp: pixels [warp*32, warp*32+32) of the 4 x 64 tile
-  int prow[2][2], pcol[2][2];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int p = warp * 32 + i * 16 + g + 8 * h;
-      prow[i][h] = p / kW;
-      pcol[i][h] = p % kW;
-    }
+// bulk copy of `bytes` (multiple of 16) from shared to global memory, tracked by the bulk-group counter
+__device__ __forceinline__ void bulk_store(void* gdst, uint32_t ssrc, uint32_t bytes) {
+  asm volatile(
+      "{\n\t.reg .u64 g;\n\tcvta.to.global.u64 g, %0;\n\t"
+      "cp.async.bulk.global.shared::cta.bulk_group [g], [%1], %2;\n\t}\n" ::"l"(gdst),
+      "r"(ssrc), "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the sources of every committed bulk copy have been read (their shared memory may be rewritten)
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// every committed bulk copy has completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
+__device__ __forceinline__ void conv_issue(uint32_t stage_saddr, uint32_t w_saddr, uint32_t d_tmem) {
+  const uint32_t idesc = tc::idesc_bf16(128, kC);
 #pragma unroll 1
   for (int tap = 0; tap < 9; ++tap) {
     const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const uint32_t a0 = stage_saddr + (uint32_t)(dx + 1) * ctc::kCopyBytes + (uint32_t)((1 + dy) * kW) * 16u;
 #pragma unroll
-    for (int kc = 0; kc < kC / 16; ++kc) {
-      uint32_t a[2][4];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int sp = (prow[i][h] + 1 + dy) * (kW + 2) + (pcol[i][h] + 1 + dx);
-          const __nv_bfloat16* src = xs + sp * kCP + kc * 16 + tig * 2;
-          a[i][h] = *reinterpret_cast<const uint32_t*>(src);
-          a[i][2 + h] = *reinterpret_cast<const uint32_t*>(src + 8);
-        }
-      }
-      // register order of the A fragment: {row g, k 0-7}, {row g+8, k 0-7}, {row g, k 8-15}, {row g+8, k 8-15}
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        const __nv_bfloat16* wsrc = ws + (tap * kC + j * 8 + g) * kCP + kc * 16 + tig * 2;
-        const uint32_t b0 = *reinterpret_cast<const uint32_t*>(wsrc);
-        const uint32_t b1 = *reinterpret_cast<const uint32_t*>(wsrc + 8);
-#pragma unroll
-        for (int i = 0; i < 2; ++i) mma_bf16(acc[i][j], a[i][0], a[i][1], a[i][2], a[i][3], b0, b1);
-      }
+    for (int s = 0; s < kC / 16; ++s) {
+      const uint64_t ad = tc::smem_desc(a0 + (uint32_t)s * 2u * ctc::kChunkStride, ctc::kChunkStride, 128u);
+      const uint64_t bd = tc::kmaj_desc(w_saddr + (uint32_t)tap * ctc::kTapBytes, kC, s);
+      tc::mma_bf16(d_tmem, ad, bd, idesc, (tap | s) != 0 ? 1u : 0u);
     }
   }
-
-  // epilogue: C fragment {row g, cols 2tig, 2tig+1}, {row g+8, same cols}
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int p = warp * 32 + i * 16 + g + 8 * h;
-      const size_t o = (((size_t)b * H + y0 + p / kW) * kW + (p % kW)) * kC;
-#pragma unroll
-      for (int j = 0; j < 6; ++j) {
-        const int co = j * 8 + tig * 2;
-        float v0 = acc[i][j][2 * h], v1 = acc[i][j][2 * h + 1];
-        if (mode == 0) {
-          v0 += bias[co];
-          v1 += bias[co + 1];
-          *reinterpret_cast<__nv_bfloat162*>(out_pre + o + co) = __floats2bfloat162_rn(v0, v1);
-          *reinterpret_cast<__nv_bfloat162*>(out_post + o + co) = __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
-        } else {
-          const __nv_bfloat162 pr = *reinterpret_cast<const __nv_bfloat162*>(aux + o + co);
-          v0 *= gelu_d(__bfloat162float(pr.x));
-          v1 *= gelu_d(__bfloat162float(pr.y));
-          *reinterpret_cast<__nv_bfloat162*>(out_pre + o + co) = __floats2bfloat162_rn(v0, v1);
-        }
-      }
-    }
 }
 
-// 1 -> 48 forward: pre = conv(x) + b, post = gelu(pre).  One thread per pixel.
+// mode 0: forward  out_post = gelu(conv(x) + bias), and out_pre = conv(x) + bias unless out_pre is NULL
+// mode 1: backward data  out_pre (= dPre of the layer below) = conv_flipped(x = dPre) * gelu'(aux = pre below)
+__global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __nv_bfloat16* __restrict__ x, int B, int H,
+                                                                  const __nv_bfloat16* __restrict__ w,
+                                                                  const float* __restrict__ bias, int mode,
+                                                                  const __nv_bfloat16* __restrict__ aux,
+                                                                  __nv_bfloat16* __restrict__ out_pre,
+                                                                  __nv_bfloat16* __restrict__ out_post) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_abort;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + ctc::kOffBar);
+  uint64_t* full = bars;          // [2] stage s holds its tile's rows (producer arrivals)
+  uint64_t* empty = bars + 2;     // [2] the MMAs that read stage s have completed
+  uint64_t* accfull = bars + 4;   // [2] accumulator a holds a finished tile
+  uint64_t* accempty = bars + 6;  // [2] the epilogue has read accumulator a
+  uint64_t* drain = bars + 8;     // every MMA of this CTA has completed (before the TMEM is released)
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int ntiles = B * (H / 2);
+  const uint32_t sbase = tc::smem_u32(smem);
+  const uint32_t wsaddr = sbase + ctc::kOffW;
+  // outputs of the forward pass go to out_post (and out_pre), of the backward pass to out_pre
+  __nv_bfloat16* out_a = mode == 0 ? out_post : out_pre;
+  __nv_bfloat16* out_b = mode == 0 ? out_pre : nullptr;
+
+  // weights -> K-major tiles, one per tap (consecutive threads: consecutive output channels)
+  for (int t = tid; t < 9 * kC * (kC / 8); t += ctc::kThreads) {
+    const int co = t % kC, rest = t / kC;  // rest = tap * 6 + chunk
+    const int ch = rest % (kC / 8), tap = rest / (kC / 8);
+    *reinterpret_cast<uint4*>(smem + ctc::kOffW + tap * ctc::kTapBytes + tc::kmaj_chunk(co, ch, kC)) =
+        *reinterpret_cast<const uint4*>(w + ((size_t)tap * kC + co) * kC + ch * 8);
+  }
+  if (warp == ctc::kMmaWarp) {
+    tc::tmem_alloc(&s_tmem, 2 * ctc::kAccCols);
+    tc::tmem_relinquish();
+  }
+  if (tid == 0) {
+    s_abort = 0;
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(full + i, ctc::kProducerThreads);
+      tc::mbar_init(empty + i, 1);
+      tc::mbar_init(accfull + i, 1);
+      tc::mbar_init(accempty + i, ctc::kEpilogueThreads);
+    }
+    tc::mbar_init(drain, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  // a wait that gives up: raise the abort flag (every role then leaves its loop at its next check)
+  auto give_up = [&]() {
+    atomicExch(&s_abort, 1);
+    atomicExch(&g_conv_status, EXGB_ETIMEOUT);
+  };
+  auto aborted = [&]() { return *reinterpret_cast<volatile int*>(&s_abort) != 0; };
+
+  if (warp < ctc::kProducerWarps) {
+    // ---------------- producers: tile i of this CTA goes to stage i & 1
+    CopyItems items;
+    conv_items(tid, items);
+    int i = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      const int s = i & 1;
+      const uint32_t par = ((uint32_t)(i >> 1) & 1u) ^ 1u;  // the first use of a stage passes at once
+      if (!tc::mbar_wait(empty + s, par, ctc::kWaitBudget)) { give_up(); break; }
+      if (aborted()) break;
+      conv_load_tile(x, H, tile, sbase + (uint32_t)s * ctc::kStageBytes, items);
+      cp_async_wait_all();
+      tc::fence_proxy_async();  // the copies -> visible to the tensor core (async proxy)
+      mbar_arrive(full + s);
+    }
+  } else if (warp == ctc::kMmaWarp) {
+    // ---------------- MMA issuer (lane 0)
+    if (lane == 0) {
+      int i = 0;
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+        const int s = i & 1, a = i & 1;
+        const uint32_t par = (uint32_t)(i >> 1) & 1u;
+        if (!tc::mbar_wait(full + s, par, ctc::kWaitBudget)) { give_up(); break; }
+        if (!tc::mbar_wait(accempty + a, par ^ 1u, ctc::kWaitBudget)) { give_up(); break; }
+        if (aborted()) break;
+        tc::fence_after_sync();
+        conv_issue(sbase + (uint32_t)s * ctc::kStageBytes, wsaddr, tmem + (uint32_t)a * ctc::kAccCols);
+        tc::mma_commit(empty + s);
+        tc::mma_commit(accfull + a);
+      }
+      // one more commit tracks every MMA issued above: after it arrives none is in flight
+      tc::mma_commit(drain);
+      if (!tc::mbar_wait(drain, 0u, ctc::kWaitBudget)) give_up();
+    }
+    __syncwarp();
+  } else {
+    // ---------------- epilogue: warp w reads TMEM lanes 32 (w % 4) + lane = pixel m, 24 channels
+    constexpr int kCg = kC / 2;
+    const int ew = warp - ctc::kProducerWarps;
+    const int m = 32 * (warp & 3) + lane;
+    const int c0 = kCg * (ew >> 2);
+    const bool leader = ew == 0 && lane == 0;
+    float bv[kCg];
+#pragma unroll
+    for (int j = 0; j < kCg; ++j) bv[j] = mode == 0 ? bias[c0 + j] : 0.f;
+    const uint32_t stg = (uint32_t)(m * kC + c0) * 2u;  // byte offset of this thread's outputs in a staged tile
+    int i = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      const int a = i & 1;
+      const uint32_t par = (uint32_t)(i >> 1) & 1u;
+      const bool ok = tc::mbar_wait(accfull + a, par, ctc::kWaitBudget);
+      if (!ok) give_up();
+      if (!ok || aborted()) break;
+      tc::fence_after_sync();
+      const uint32_t ta = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)a * ctc::kAccCols + (uint32_t)c0;
+      float v[kCg];
+      {
+        float a8[8], b8[8], c8[8];
+        tc::tmem_ld8x2(ta, ta + 8u, a8, b8);
+        tc::tmem_ld8(ta + 16u, c8);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          v[j] = a8[j];
+          v[8 + j] = b8[j];
+          v[16 + j] = c8[j];
+        }
+      }
+      tc::fence_before_sync();
+      mbar_arrive(accempty + a);  // accumulator a may be overwritten by the MMAs of tile i + 2
+      uint32_t ra[kCg / 2], rb[kCg / 2];
+      if (mode == 0) {
+#pragma unroll
+        for (int j = 0; j < kCg / 2; ++j) {
+          const float v0 = v[2 * j] + bv[2 * j], v1 = v[2 * j + 1] + bv[2 * j + 1];
+          const __nv_bfloat162 p = __floats2bfloat162_rn(v0, v1);
+          const __nv_bfloat162 g = __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
+          rb[j] = *reinterpret_cast<const uint32_t*>(&p);
+          ra[j] = *reinterpret_cast<const uint32_t*>(&g);
+        }
+      } else {
+        // pixel m of this tile: 128 * tile + m in the batch (tiles are consecutive row pairs)
+        const size_t o = ((size_t)tile * 128 + m) * kC + c0;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          const uint4 pr = *reinterpret_cast<const uint4*>(aux + o + 8 * q);
+          const uint32_t prw[4] = {pr.x, pr.y, pr.z, pr.w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const __nv_bfloat162 pp = *reinterpret_cast<const __nv_bfloat162*>(&prw[j]);
+            const float v0 = v[8 * q + 2 * j] * gelu_d(__bfloat162float(pp.x));
+            const float v1 = v[8 * q + 2 * j + 1] * gelu_d(__bfloat162float(pp.y));
+            const __nv_bfloat162 r = __floats2bfloat162_rn(v0, v1);
+            ra[4 * q + j] = *reinterpret_cast<const uint32_t*>(&r);
+          }
+        }
+      }
+      if (leader) bulk_wait_read();  // the previous tile's staged outputs have left shared memory
+      epilogue_sync();
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        *reinterpret_cast<uint4*>(smem + ctc::kOffOut + stg + 16 * q) =
+            make_uint4(ra[4 * q], ra[4 * q + 1], ra[4 * q + 2], ra[4 * q + 3]);
+        if (out_b)
+          *reinterpret_cast<uint4*>(smem + ctc::kOffOut2 + stg + 16 * q) =
+              make_uint4(rb[4 * q], rb[4 * q + 1], rb[4 * q + 2], rb[4 * q + 3]);
+      }
+      tc::fence_proxy_async();  // staged outputs -> visible to the bulk copy
+      epilogue_sync();
+      if (leader) {
+        const size_t off = (size_t)tile * (ctc::kOutBytes / 2);  // in bf16 elements
+        bulk_store(out_a + off, sbase + ctc::kOffOut, ctc::kOutBytes);
+        if (out_b) bulk_store(out_b + off, sbase + ctc::kOffOut2, ctc::kOutBytes);
+        bulk_commit();
+      }
+    }
+    if (leader) bulk_wait_all();
+  }
+
+  // every MMA this CTA issued has completed (drain barrier above) before the tensor memory is released
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == ctc::kMmaWarp) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 2 * ctc::kAccCols);
+  }
+}
+
+// 1 -> 48 forward: pre = conv(x) + b, post = gelu(pre).  One thread per (pixel, 8-channel chunk):
+// the six threads of a pixel share its 9 input values through L1, and a warp stores 512 contiguous
+// bytes per output.  `pre` may be NULL (inference: no backward pass follows).
 __global__ void conv_in1_kernel(const float* __restrict__ x, int B, int H, const float* __restrict__ w,
                                 const float* __restrict__ bias, __nv_bfloat16* __restrict__ pre,
                                 __nv_bfloat16* __restrict__ post) {
@@ -165,86 +403,125 @@ __global__ void conv_in1_kernel(const float* __restrict__ x, int B, int H, const
   for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];  // [tap][co]
   for (int t = threadIdx.x; t < kC; t += blockDim.x) wsm[9 * kC + t] = bias[t];
   __syncthreads();
-  const int64_t n = (int64_t)B * H * kW;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t n = (int64_t)B * H * kW * (kC / 8);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t / (kC / 8);
+    const int cg = (int)(t - p * (kC / 8));
     const int64_t b = p / (H * kW);
-    const int r = (int)(p % (H * kW));
+    const int r = (int)(p - b * H * kW);
     const int y = r / kW, xx = r % kW;
     float v[9];
 #pragma unroll
     for (int tap = 0; tap < 9; ++tap) {
-      const int gy = (y + tap / 3 - 1 + H) % H, gx = (xx + tap % 3 - 1 + kW) % kW;
-      v[tap] = x[(b * H + gy) * kW + gx];
+      int gy = y + tap / 3 - 1;
+      gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+      const int gx = (xx + tap % 3 - 1) & (kW - 1);
+      v[tap] = __ldg(x + (b * H + gy) * kW + gx);
     }
-    for (int co = 0; co < kC; co += 2) {
+    uint32_t hp[4], hq[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int co = cg * 8 + 2 * j;
       float s0 = wsm[9 * kC + co], s1 = wsm[9 * kC + co + 1];
 #pragma unroll
       for (int tap = 0; tap < 9; ++tap) {
         s0 = fmaf(wsm[tap * kC + co], v[tap], s0);
         s1 = fmaf(wsm[tap * kC + co + 1], v[tap], s1);
       }
-      *reinterpret_cast<__nv_bfloat162*>(pre + p * kC + co) = __floats2bfloat162_rn(s0, s1);
-      *reinterpret_cast<__nv_bfloat162*>(post + p * kC + co) = __floats2bfloat162_rn(gelu_f(s0), gelu_f(s1));
+      const __nv_bfloat162 a = __floats2bfloat162_rn(s0, s1);
+      const __nv_bfloat162 g = __floats2bfloat162_rn(gelu_f(s0), gelu_f(s1));
+      hp[j] = *reinterpret_cast<const uint32_t*>(&a);
+      hq[j] = *reinterpret_cast<const uint32_t*>(&g);
     }
+    if (pre) *reinterpret_cast<uint4*>(pre + t * 8) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
+    *reinterpret_cast<uint4*>(post + t * 8) = make_uint4(hq[0], hq[1], hq[2], hq[3]);
   }
 }
 
-// 48 -> 1 forward: out = base + scale * (conv(h) + b).  One thread per pixel.
+// 48 -> 1 forward: out = base + scale * (conv(h) + b).  Four threads per pixel, 12 channels each
+// (three 8-byte loads per tap, so a warp reads 8 whole 96-byte pixels per tap), partial sums
+// combined by two warp shuffles.
 __global__ void conv_out1_kernel(const __nv_bfloat16* __restrict__ h, int B, int H, const float* __restrict__ w,
                                  const float* __restrict__ bias, const float* __restrict__ base, float scale,
                                  float* __restrict__ out) {
   __shared__ float wsm[9 * kC];
   for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];  // [tap][ci]
   __syncthreads();
-  const int64_t n = (int64_t)B * H * kW;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t n = (int64_t)B * H * kW * 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // whole warps run the same number of iterations (n is a multiple of 4 and the shuffles stay in quads)
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t - (threadIdx.x & 31) < n; t += stride) {
+    const bool live = t < n;
+    const int64_t p = live ? t >> 2 : 0;
+    const int j = (int)(t & 3);
     const int64_t b = p / (H * kW);
-    const int r = (int)(p % (H * kW));
+    const int r = (int)(p - b * H * kW);
     const int y = r / kW, xx = r % kW;
-    float s = bias[0];
-#pragma unroll 1
+    float s = 0.f;
+#pragma unroll 3
     for (int tap = 0; tap < 9; ++tap) {
-      const int gy = (y + tap / 3 - 1 + H) % H, gx = (xx + tap % 3 - 1 + kW) % kW;
-      const __nv_bfloat16* src = h + ((b * H + gy) * kW + gx) * kC;
-      for (int ci = 0; ci < kC; ci += 2) {
-        const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(src + ci));
-        s = fmaf(wsm[tap * kC + ci], f.x, s);
-        s = fmaf(wsm[tap * kC + ci + 1], f.y, s);
+      int gy = y + tap / 3 - 1;
+      gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+      const int gx = (xx + tap % 3 - 1) & (kW - 1);
+      const uint2* src = reinterpret_cast<const uint2*>(h + ((b * H + gy) * kW + gx) * kC + 12 * j);
+      const float* wt = wsm + tap * kC + 12 * j;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        const uint2 u = __ldg(src + q);
+        const float2 f0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+        const float2 f1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+        s = fmaf(wt[4 * q], f0.x, s);
+        s = fmaf(wt[4 * q + 1], f0.y, s);
+        s = fmaf(wt[4 * q + 2], f1.x, s);
+        s = fmaf(wt[4 * q + 3], f1.y, s);
       }
     }
-    out[p] = (base ? base[p] : 0.f) + scale * s;
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (live && j == 0) out[p] = (base ? base[p] : 0.f) + scale * (s + bias[0]);
   }
 }
 
 // backward of the 48 -> 1 layer w.r.t. its input, times GELU'(pre):
-// dpre[p][ci] = gelu'(pre[p][ci]) * sum_tap w[tap][ci] * dout[p - shift(tap)]
+// dpre[p][ci] = gelu'(pre[p][ci]) * sum_tap w[tap][ci] * dout[p - shift(tap)].  One thread per
+// (pixel, 8-channel chunk), coalesced 16-byte loads and stores.
 __global__ void conv_out1_bwd_data_kernel(const float* __restrict__ dout, int B, int H, const float* __restrict__ w,
                                           const __nv_bfloat16* __restrict__ pre, __nv_bfloat16* __restrict__ dpre) {
   __shared__ float wsm[9 * kC];
   for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];
   __syncthreads();
-  const int64_t n = (int64_t)B * H * kW;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t n = (int64_t)B * H * kW * (kC / 8);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = t / (kC / 8);
+    const int cg = (int)(t - p * (kC / 8));
     const int64_t b = p / (H * kW);
-    const int r = (int)(p % (H * kW));
+    const int r = (int)(p - b * H * kW);
     const int y = r / kW, xx = r % kW;
     float g[9];
 #pragma unroll
     for (int tap = 0; tap < 9; ++tap) {
-      const int gy = (y - (tap / 3 - 1) + H) % H, gx = (xx - (tap % 3 - 1) + kW) % kW;
-      g[tap] = dout[(b * H + gy) * kW + gx];
+      int gy = y - (tap / 3 - 1);
+      gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+      const int gx = (xx - (tap % 3 - 1)) & (kW - 1);
+      g[tap] = __ldg(dout + (b * H + gy) * kW + gx);
     }
-    for (int ci = 0; ci < kC; ci += 2) {
+    const uint4 pr = *reinterpret_cast<const uint4*>(pre + t * 8);
+    const uint32_t prw[4] = {pr.x, pr.y, pr.z, pr.w};
+    uint32_t res[4];
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int ci = cg * 8 + 2 * jj;
       float s0 = 0.f, s1 = 0.f;
 #pragma unroll
       for (int tap = 0; tap < 9; ++tap) {
         s0 = fmaf(wsm[tap * kC + ci], g[tap], s0);
         s1 = fmaf(wsm[tap * kC + ci + 1], g[tap], s1);
       }
-      const float2 pr = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(pre + p * kC + ci));
-      *reinterpret_cast<__nv_bfloat162*>(dpre + p * kC + ci) =
-          __floats2bfloat162_rn(s0 * gelu_d(pr.x), s1 * gelu_d(pr.y));
+      const float2 pf = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&prw[jj]));
+      const __nv_bfloat162 rr = __floats2bfloat162_rn(s0 * gelu_d(pf.x), s1 * gelu_d(pf.y));
+      res[jj] = *reinterpret_cast<const uint32_t*>(&rr);
     }
+    *reinterpret_cast<uint4*>(dpre + t * 8) = make_uint4(res[0], res[1], res[2], res[3]);
   }
 }
 
@@ -464,23 +741,48 @@ extern "C" {
 
 int exgb_conv48(void* stream, const void* x, int B, int H, const void* w, const float* bias, int mode,
                 const void* aux, void* out_pre, void* out_post) {
-  if (!x || !w || !out_pre || H % kTR || (mode == 0 && (!bias || !out_post)) || (mode == 1 && !aux))
-    return fail(EXGB_EINVAL, "exgb_conv48: bad arguments (H must be a multiple of 4)");
-  const size_t smem = sizeof(__nv_bfloat16) * ((size_t)(kTR + 2) * (kW + 2) * kCP + (size_t)9 * kC * kCP);
-  EXGB_CUDA(cudaFuncSetAttribute(conv48_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const unsigned grid = (unsigned)B * (H / kTR);
-  conv48_mma_kernel<<<grid, 256, smem, (cudaStream_t)stream>>>(
-      (const __nv_bfloat16*)x, H, (const __nv_bfloat16*)w, bias, mode, (const __nv_bfloat16*)aux,
+  if (!x || !w || B < 0 || H < 2 || H % 2 || (mode == 0 && (!bias || !out_post)) ||
+      (mode == 1 && (!aux || !out_pre)) || (mode != 0 && mode != 1))
+    return fail(EXGB_EINVAL, "exgb_conv48: bad arguments (H must be even)");
+  if (B == 0) return EXGB_OK;
+  static int sm_count[64] = {0};
+  int dev = 0;
+  EXGB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(EXGB_EUNSUPPORTED, "device index out of range");
+  if (!sm_count[dev]) {
+    EXGB_CUDA(cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev));
+    EXGB_CUDA(cudaFuncSetAttribute(conv48_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)ctc::kSmemBytes));
+  }
+  const int64_t ntiles = (int64_t)B * (H / 2);
+  if (ntiles > 2147483647LL) return fail(EXGB_EINVAL, "exgb_conv48: too many tiles");
+  const unsigned grid = (unsigned)std::min<int64_t>(ntiles, sm_count[dev]);
+  conv48_tc_kernel<<<grid, ctc::kThreads, ctc::kSmemBytes, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)x, B, H, (const __nv_bfloat16*)w, bias, mode, (const __nv_bfloat16*)aux,
       (__nv_bfloat16*)out_pre, (__nv_bfloat16*)out_post);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }
 
+// Synchronises the device; EXGB_ETIMEOUT if a bounded wait of the tensor-core conv kernel gave up
+// since the last call (its outputs are then invalid).  The status is cleared on read.
+int exgb_conv_status(void) {
+  int h = 0;
+  EXGB_CUDA(cudaMemcpyFromSymbol(&h, g_conv_status, sizeof(int)));
+  if (h) {
+    const int zero = 0;
+    EXGB_CUDA(cudaMemcpyToSymbol(g_conv_status, &zero, sizeof(int)));
+    return fail(h, "a bounded device wait of the tensor-core conv kernel gave up");
+  }
+  return EXGB_OK;
+}
+
 int exgb_conv_in1(void* stream, const float* x, int B, int H, const float* w, const float* bias, void* pre,
                   void* post) {
-  if (!x || !w || !bias || !pre || !post) return fail(EXGB_EINVAL, "NULL argument");
-  const int64_t n = (int64_t)B * H * kW;
-  conv_in1_kernel<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(x, B, H, w, bias, (__nv_bfloat16*)pre,
+  if (!x || !w || !bias || !post || B < 0 || H < 1) return fail(EXGB_EINVAL, "NULL argument or bad shape");
+  if ((int64_t)B * H == 0) return EXGB_OK;
+  if ((int64_t)B * H > 2147483647LL) return fail(EXGB_EINVAL, "too many rows");
+  conv_in1_kernel<<<blocks_for((int64_t)B * H * kW * (kC / 8)), 256, 0, (cudaStream_t)stream>>>(x, B, H, w, bias, (__nv_bfloat16*)pre,
                                                                    (__nv_bfloat16*)post);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
@@ -488,9 +790,10 @@ int exgb_conv_in1(void* stream, const float* x, int B, int H, const float* w, co
 
 int exgb_conv_out1(void* stream, const void* h, int B, int H, const float* w, const float* bias, const float* base,
                    float scale, float* out) {
-  if (!h || !w || !bias || !out) return fail(EXGB_EINVAL, "NULL argument");
-  const int64_t n = (int64_t)B * H * kW;
-  conv_out1_kernel<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)h, B, H, w, bias, base,
+  if (!h || !w || !bias || !out || B < 0 || H < 1) return fail(EXGB_EINVAL, "NULL argument or bad shape");
+  if ((int64_t)B * H == 0) return EXGB_OK;
+  if ((int64_t)B * H > 2147483647LL) return fail(EXGB_EINVAL, "too many rows");
+  conv_out1_kernel<<<blocks_for((int64_t)B * H * kW * 4), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)h, B, H, w, bias, base,
                                                                     scale, out);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
@@ -498,7 +801,7 @@ int exgb_conv_out1(void* stream, const void* h, int B, int H, const float* w, co
 
 int exgb_conv_out1_bwd_data(void* stream, const float* dout, int B, int H, const float* w, const void* pre,
                             void* dpre) {
-  const int64_t n = (int64_t)B * H * kW;
+  const int64_t n = (int64_t)B * H * kW * (kC / 8);
   conv_out1_bwd_data_kernel<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(dout, B, H, w, (const __nv_bfloat16*)pre,
                                                                              (__nv_bfloat16*)dpre);
   EXGB_CUDA(cudaGetLastError());

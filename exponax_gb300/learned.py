@@ -3,11 +3,11 @@
 A small periodic convolutional residual network corrects every coarse
 (64^2, dt = 0.04) ETDRK2 step:  u_{n+1} = v + out_scale * NN(in_scale * v),
 v = coarse_step(u_n).  Network: 3x3 periodic convolutions 1 -> 48 -> 48 x 4
--> 1 with GELU (six layers, ~84 k parameters), BF16 weights and
-activations, FP32 accumulation; the 48 -> 48 layers run on the tensor cores
-(exgb_conv48).  Training (Adam, lr 1e-3, mean squared error against the
-downsampled fine solution) and inference use only the kernels of
-libexgb.so.  A spectral-energy guard replaces a corrected state by the plain
+-> 1 with GELU in its tanh form (six layers, ~84 k parameters), BF16 weights and
+activations, FP32 accumulation; the 48 -> 48 layers (forward and
+backward-data) run on the tcgen05 tensor cores (exgb_conv48).  Training
+(Adam, lr 1e-3, mean squared error against the downsampled fine solution)
+and inference use only the kernels of libexgb.so.  A spectral-energy guard replaces a corrected state by the plain
 coarse state when the correction puts too much energy above |k| > kg or is
 not finite.
 
@@ -47,6 +47,7 @@ def _lib():
             "exgb_cast_weights": [V, V, I64, V, V, I],
             "exgb_mse": [V, V, V, I64, F, V, V, I],
             "exgb_guard": [V, V, V, I, I, I, F, V, V, V],
+            "exgb_conv_status": [],
         }
         for name, args in sigs.items():
             fn = getattr(lib, name)
@@ -69,8 +70,8 @@ class PeriodicConvCorrector:
                  out_scale: float = 1.0):
         torch = _device.torch()
         _device.require_cuda()
-        if H % 4:
-            raise ValueError("grid height must be a multiple of 4")
+        if H % 2:
+            raise ValueError("grid height must be even")
         self.H, self.Wd = H, 64
         self.in_scale, self.out_scale = float(in_scale), float(out_scale)
         self.max_batch = int(max_batch)
@@ -153,8 +154,9 @@ class PeriodicConvCorrector:
         return out
 
     # ------------------------------------------------------------------ forward / backward
-    def forward(self, v, out=None):
-        """v: (B, H, 64) float32 CUDA tensor -> corrected state (B, H, 64)."""
+    def forward(self, v, out=None, keep=False):
+        """v: (B, H, 64) float32 CUDA tensor -> corrected state (B, H, 64).  keep: also store the
+        pre-activations that a following backward pass needs (inference skips those writes)."""
         torch = _device.torch()
         lib = _lib()
         s = _device.stream()
@@ -166,10 +168,10 @@ class PeriodicConvCorrector:
         H = self.H
         torch.mul(v.reshape(-1), self.in_scale, out=self.x0[:B * H * 64])
         check(lib.exgb_conv_in1(s, _p(self.x0), B, H, _p(self._view(self.w, "W1")), _p(self._view(self.w, "b1")),
-                                _p(self.pre[0]), _p(self.h[0])), "conv_in1")
+                                _p(self.pre[0]) if keep else None, _p(self.h[0])), "conv_in1")
         for i in range(NMID):
             check(lib.exgb_conv48(s, _p(self.h[i]), B, H, _p(self.w16[i]), _p(self._view(self.w, f"b{i + 2}")), 0,
-                                  None, _p(self.pre[i + 1]), _p(self.h[i + 1])), "conv48")
+                                  None, _p(self.pre[i + 1]) if keep else None, _p(self.h[i + 1])), "conv48")
         if out is None:
             out = torch.empty_like(v)
         check(lib.exgb_conv_out1(s, _p(self.h[NMID]), B, H, _p(self._view(self.w, "W6")),
@@ -184,7 +186,7 @@ class PeriodicConvCorrector:
         torch = _device.torch()
         lib = _lib()
         s = _device.stream()
-        pred = self.forward(v)
+        pred = self.forward(v, keep=True)
         B, H = self._B, self.H
         n = B * H * 64
         nb = 256
@@ -208,6 +210,12 @@ class PeriodicConvCorrector:
                              _p(self._view(self.g, "W1")), _p(self._view(self.g, "b1"))), "wgrad1")
         loss = self.loss_part[:nb].sum() / n
         return loss, pred
+
+    @staticmethod
+    def status():
+        """Synchronise and raise if a bounded device wait of the tensor-core conv kernel gave up
+        since the last check (the results of that launch are then invalid)."""
+        check(_lib().exgb_conv_status(), "conv status")
 
     def adam_step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
         lib = _lib()

@@ -4,21 +4,25 @@ The corrector has no counterpart in the reference; this module is the CPU
 oracle its CUDA forward / backward kernels are checked against.  Network:
 x0 = in_scale * v; h1 = gelu(conv(x0; W1, b1)) (1 -> C); h_i = gelu(conv(h_{i-1};
 W_i, b_i)) (C -> C, i = 2..L-1); out = conv(h_{L-1}; W_L, b_L) (C -> 1);
-pred = v + out_scale * out.  3x3 periodic convolutions, exact GELU,
+pred = v + out_scale * out.  3x3 periodic convolutions, GELU in its tanh
+form (Hendrycks & Gimpel 2016: x / 2 (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3)))),
 weights laid out [tap][co][ci] with tap = (dy + 1) * 3 + (dx + 1) and
 input pixel (y + dy, x + dx) (wrapped).  Loss = mean (pred - target)^2.
 """
 
 import numpy as np
-from scipy.special import erf
+
+_A = np.sqrt(2.0 / np.pi)
+_B = 0.044715
 
 
 def gelu(x):
-    return 0.5 * x * (1.0 + erf(x / np.sqrt(2.0)))
+    return 0.5 * x * (1.0 + np.tanh(_A * (x + _B * x ** 3)))
 
 
 def gelu_d(x):
-    return 0.5 * (1.0 + erf(x / np.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / np.sqrt(2 * np.pi)
+    t = np.tanh(_A * (x + _B * x ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * _A * (1.0 + 3.0 * _B * x * x)
 
 
 def _shift(x, dy, dx):

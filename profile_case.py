@@ -3,6 +3,7 @@
     python profile_case.py --dims 2 --n 256 --batch 32 --steps 10 --reps 3
     python profile_case.py --dims 2 --n 128 --kolmogorov --precision split_bf16
     python profile_case.py --uneven 600 --steps 100 --reps 3
+    python profile_case.py --corrector 256 --reps 10
 
 Builds the stepper (NavierStokesVorticity in 2D, KuramotoSivashinsky-
 Conservative in 1D), creates device-resident Fourier states and launches
@@ -10,7 +11,9 @@ Conservative in 1D), creates device-resident Fourier states and launches
 synchronises.  Prints the CUDA-event time per launch.  With --uneven K it
 instead builds the first K instances of the uneven 1D batch (Burgers / KdV /
 KS-conservative, N in {128 .. 4096}), captures their work-queue rollout in a
-CUDA graph and replays it --reps times.
+CUDA graph and replays it --reps times.  With --corrector B it runs the
+learned corrector's forward pass (64 x 64 grids, batch B, inference) --reps
+times after 5 warm-up passes.
 """
 
 from __future__ import annotations
@@ -31,6 +34,7 @@ def main():
     ap.add_argument("--kolmogorov", action="store_true")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split_bf16"])
     ap.add_argument("--uneven", type=int, default=0, help="instances of the uneven 1D work-queue batch")
+    ap.add_argument("--corrector", type=int, default=0, help="batch of the learned corrector's forward pass")
     ap.add_argument("--pde", default="", choices=["", "burgers", "grayscott"],
                     help="2D/3D Burgers or Gray-Scott on the staged N-D path instead of the vorticity / KS steppers")
     a = ap.parse_args()
@@ -39,6 +43,25 @@ def main():
 
     import exponax_gb300 as ex
     from exponax_gb300 import _device, _lib
+
+    if a.corrector:
+        from exponax_gb300.learned import PeriodicConvCorrector
+
+        net = PeriodicConvCorrector(64, seed=0, max_batch=a.corrector)
+        v = torch.randn(a.corrector, 64, 64, device="cuda")
+        for _ in range(5):
+            net(v)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(a.reps):
+            net(v)
+        e1.record()
+        torch.cuda.synchronize()
+        net.status()
+        print(f"corrector forward (batch {a.corrector}): {e0.elapsed_time(e1) / a.reps:.3f} ms")
+        return
 
     if a.uneven:
         from exponax_gb300.batching import QueueRollout, uneven_config3

@@ -144,3 +144,57 @@ def test_trained_corrector_beats_the_plain_coarse_stepper():
     plain, learned = res["plain"][0], res["learned"][0]
     for t in (1, 10, 30):
         assert learned[t] < 0.85 * plain[t], (t, learned[t], plain[t])
+
+
+def _conv_ref(x, w, dy_dx_taps=True):
+    """Periodic 3x3 conv in float64: out[b, y, x, co] = sum_tap sum_ci w[tap, co, ci] x[b, y + dy, x + dx, ci],
+    tap = (dy + 1) * 3 + (dx + 1)."""
+    out = 0.0
+    for tap in range(9):
+        dy, dx = tap // 3 - 1, tap % 3 - 1
+        xs = np.roll(x, shift=(-dy, -dx), axis=(1, 2))
+        out = out + np.einsum("byxc,oc->byxo", xs, w[tap])
+    return out
+
+
+def _bf16(a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(torch.bfloat16)
+
+
+@pytest.mark.parametrize("B,H", [(1, 64), (16, 64), (3, 6)])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_conv48_tensor_core_layer(B, H, mode):
+    """The 48 -> 48 tcgen05 implicit-GEMM layer alone against a float64 periodic convolution of the same
+    bf16 inputs and weights: forward (bias, tanh-form GELU) and backward-data (times its derivative at the
+    layer below) within
+    the bf16 rounding of the outputs (relative L2 <= 4e-3, measured against the float64 result); B = 16
+    at 64 rows is 512 tiles, more than one per SM, so the two-stage pipeline runs."""
+    from exponax_gb300 import _device
+    from oracle import corrector_np as co
+    from exponax_gb300.learned import PeriodicConvCorrector, _lib
+
+    rng = np.random.default_rng(B * 100 + H + mode)
+    x = _bf16(rng.standard_normal((B, H, 64, 48))).float().numpy().astype(np.float64)
+    w = _bf16(rng.standard_normal((9, 48, 48)) / np.sqrt(9 * 48)).float().numpy().astype(np.float64)
+    bias = (0.1 * rng.standard_normal(48)).astype(np.float32)
+    aux = _bf16(rng.standard_normal((B, H, 64, 48))).float().numpy().astype(np.float64)
+    xd = _bf16(x).cuda()
+    wd = _bf16(w).cuda()
+    bd = torch.from_numpy(bias).cuda()
+    auxd = _bf16(aux).cuda()
+    pre = torch.full((B, H, 64, 48), float("nan"), dtype=torch.bfloat16, device="cuda")
+    post = torch.full_like(pre, float("nan"))
+    lib = _lib()
+    from exponax_gb300.learned import _p
+
+    rc = lib.exgb_conv48(_device.stream(), _p(xd), B, H, _p(wd), _p(bd) if mode == 0 else None, mode,
+                         _p(auxd) if mode == 1 else None, _p(pre), _p(post) if mode == 0 else None)
+    assert rc == 0
+    PeriodicConvCorrector.status()
+    ref = _conv_ref(x, w)
+    if mode == 0:
+        ref = ref + bias.astype(np.float64)
+        assert rel(pre.float().cpu().numpy(), ref) < 4e-3
+        assert rel(post.float().cpu().numpy(), co.gelu(ref)) < 4e-3
+    else:
+        assert rel(pre.float().cpu().numpy(), ref * co.gelu_d(aux)) < 4e-3
