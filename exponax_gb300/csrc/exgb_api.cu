@@ -257,8 +257,20 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
     if (d.num_spatial_dims == 1 && d.nonlin_kind <= EXGB_NL_GENERAL)
       staged = !smooth || !etdrk1d_fits(d.num_points, d.order);
     else if (d.num_spatial_dims == 2 &&
-             (d.nonlin_kind == EXGB_NL_VORTICITY_2D || d.nonlin_kind == EXGB_NL_VORTICITY_2D_KOLMOGOROV))
-      staged = !smooth || d.num_points > 1024;
+             (d.nonlin_kind == EXGB_NL_VORTICITY_2D || d.nonlin_kind == EXGB_NL_VORTICITY_2D_KOLMOGOROV)) {
+      // The fused kernels win up to N = 256 (register FFTs at 64 / 128 / 256, the generic cluster
+      // kernel in between); from N = 320 on the three-pass path wins (measured at 512^2: 1.06e10
+      // against 6.9e9 DOF-steps/s).  EXGB_2D_PATH=fused / staged overrides the choice where the
+      // other path can hold the plan (a comparison knob; both compute the same arithmetic).
+      const int N = d.num_points;
+      const char* path = getenv("EXGB_2D_PATH");
+      const std::string pick = path ? std::string(path) : std::string();
+      const bool reg = (N == 64 || N == 128 || N == 256);
+      bool want_staged = !reg && N >= 320;
+      if (pick == "fused") want_staged = false;
+      if (pick == "staged") want_staged = true;
+      staged = !smooth || N > 1024 || (want_staged && ndgen_pass2d(d));
+    }
   }
   if (d.order >= 1 && d.nonlin_kind != EXGB_NL_ZERO) {
     if (d.nonlin_kind < EXGB_NL_ZERO || d.nonlin_kind > EXGB_NL_BELOUSOV_ZHABOTINSKY)
@@ -379,7 +391,7 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   for (int i = 0; i < D - 1; ++i) per *= (size_t)N;
   p->n_modes = per;
   const size_t nall = per * (size_t)v.lin_ch;
-  const bool transpose = (D == 2 && d.order >= 1 && !staged);
+  const bool transpose = (D == 2 && d.order >= 1 && (!staged || ndgen_pass2d(d)));
   p->tables_transposed = transpose ? 1 : 0;
   double2* d_L = nullptr;
   cudaError_t e;

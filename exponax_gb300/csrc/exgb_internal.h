@@ -136,6 +136,7 @@ int tcdft2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2
                 int project, int nonlinear_only);
 bool ndgen_handles(const exgb_plan_desc& d);
 bool ndgen_can(const exgb_plan_desc& d);
+bool ndgen_pass2d(const exgb_plan_desc& d);
 // 0 when rfftn / irfftn take transforms of length n on this device (any n with a prime factor
 // above 5 up to the Bluestein limit, 2^a 3^b 5^c of any length in 1D), else an EXGB_E* code
 int transform_supported(int n);

@@ -1,0 +1,244 @@
+// exgb_ndops.cuh -- the per-mode and per-point arithmetic of the nonlinear terms that the staged
+// N-D paths evaluate (exgb_ndgen.cu: one kernel per step; exgb_pass2d.cu: three fused passes):
+// the spectra the inverse transforms need (derive), the pointwise products (pointwise) and the
+// post-masked combination of the forward spectra (combine).  Reference: nonlin_fun/_convection.py,
+// _gradient_norm.py, _polynomial.py, _general_nonlinear.py, _vorticity_convection.py,
+// stepper/reaction/*.py (each op below names its lines).
+#pragma once
+
+#include "exgb_internal.h"
+
+namespace exgb {
+namespace ndg {
+
+constexpr int MAXC = 3;
+
+enum Op {
+  OP_CONV_MC_CONS = 0,  // -b/2 sum_j ik_j F[u_i u_j]          (_convection.py:104-138)
+  OP_CONV_MC_NONCONS,   // -b F[sum_j u_j d_j u_i]              (_convection.py:140-171)
+  OP_CONV_SC_CONS,      // -b/2 (sum_d ik_d) F[u^2]             (_convection.py:173-202)
+  OP_CONV_SC_NONCONS,   // -b F[u sum_d d_d u]                  (_convection.py:204-231)
+  OP_GRAD_NORM,         // -b/2 F[|grad u|^2 - mean]            (_gradient_norm.py:68-101)
+  OP_POLY,              // F[sum_k c_k u^k]                     (_polynomial.py:56-76)
+  OP_GENERAL,           // s0 F[u^2] + s1/2 (sum ik) F[u^2] + s2/2 F[|grad u|^2 - mean]
+  OP_CAHN_HILLIARD,     // s Lap F[u^3]                         (_cahn_hilliard.py:31-45)
+  OP_GRAY_SCOTT,        // F[f(1-u0) - u0 u1^2], F[-(f+k) u1 + u0 u1^2]  (_gray_scott.py:30-46)
+  OP_BZ,                // F[u0 + u1 - u0 u1 - u0^2], F[u2 - u1 - u0 u1], F[u0 - u2]  (_belousov_zhabotinsky.py:33-51)
+  OP_VORT,              // -b F[u w_x + v w_y], (u, v) = (d_y, -d_x) Lap^-1 w  (_vorticity_convection.py:78-99),
+                        // + the Kolmogorov injection at (0, k)               (_vorticity_convection.py:166-176)
+};
+
+struct Geo {
+  int D, N, M, C, K;
+  int64_t per;   // modes per field
+  int64_t npts;  // grid points per field
+  float ks;      // 2 pi / L
+};
+
+struct Prog {
+  int op, NI, NF;
+  float s0, s1, s2;  // combine scales
+  float feed, kill;  // Gray-Scott rates (pointwise step)
+  int zmf;
+  int npoly;
+  float poly[8];
+};
+
+// signed wavenumbers of mode r (leading axes fftfreq, last axis rfftfreq)
+__device__ __forceinline__ void mode_of(const Geo& g, int64_t r, int (&k)[3]) {
+  k[0] = k[1] = k[2] = 0;
+  k[g.D - 1] = (int)(r % g.M);
+  int64_t rest = r / g.M;
+  for (int a = g.D - 2; a >= 0; --a) {
+    const int i = (int)(rest % g.N);
+    rest /= g.N;
+    k[a] = (i <= (g.N - 1) / 2) ? i : i - g.N;
+  }
+}
+
+__device__ __forceinline__ bool kept(const Geo& g, const int (&k)[3]) {
+  bool m = true;
+  for (int a = 0; a < g.D; ++a) m = m && (abs(k[a]) <= g.K);
+  return m;
+}
+
+__device__ __forceinline__ float2 times_i(float d, float2 u) { return make_float2(-d * u.y, d * u.x); }
+
+
+// index of the product u_i u_j (i <= j) among the C(C+1)/2 symmetric products
+__device__ __forceinline__ int sym_index(int i, int j, int C) {
+  if (i > j) {
+    const int t = i;
+    i = j;
+    j = t;
+  }
+  return i * C - (i * (i - 1)) / 2 + (j - i);
+}
+
+// The NI spectra of mode k whose inverse transforms the pointwise step needs: channel c of the
+// state at x[c * xs], field f written to w[f * ws]; m = inside the dealiasing mask (pre-mask).
+__device__ __forceinline__ void derive_mode(const Geo& g, const Prog& p, const int (&k)[3], bool m,
+                                            const float2* x, int64_t xs, float2* w, int64_t ws) {
+  float d[3];
+  for (int a = 0; a < 3; ++a) d[a] = g.ks * (float)k[a];
+    const float2 z = make_float2(0.f, 0.f);
+    switch (p.op) {
+      case OP_CONV_MC_NONCONS:
+        for (int c = 0; c < g.C; ++c) {
+          const float2 u = m ? x[c * xs] : z;
+          w[c * ws] = u;
+          for (int j = 0; j < g.D; ++j) w[(g.C + c * g.D + j) * ws] = times_i(d[j], u);
+        }
+        break;
+      case OP_CONV_SC_NONCONS: {
+        const float2 u = m ? x[0] : z;
+        w[0] = u;
+        float s = 0.f;
+        for (int j = 0; j < g.D; ++j) s += d[j];
+        w[ws] = times_i(s, u);
+      } break;
+      case OP_GRAD_NORM:
+        for (int c = 0; c < g.C; ++c) {
+          const float2 u = m ? x[c * xs] : z;
+          for (int j = 0; j < g.D; ++j) w[(c * g.D + j) * ws] = times_i(d[j], u);
+        }
+        break;
+      case OP_GENERAL: {
+        const float2 u = m ? x[0] : z;
+        w[0] = u;
+        for (int j = 0; j < g.D; ++j) w[(1 + j) * ws] = times_i(d[j], u);
+      } break;
+      case OP_VORT: {
+        // stream function psi = w / Lap with 1/Lap = 1 at k = 0; u = i k_y psi, v = -i k_x psi,
+        // w_x = i k_x w, w_y = i k_y w (k_x the leading axis, k_y the rfft axis)
+        const float2 wv = m ? x[0] : z;
+        const float lap = -(d[0] * d[0] + d[1] * d[1]);
+        const float il = lap != 0.f ? 1.f / lap : 1.f;
+        const float2 psi = cscale(wv, il);
+        w[0] = times_i(d[1], psi);
+        w[ws] = times_i(-d[0], psi);
+        w[2 * ws] = times_i(d[0], wv);
+        w[3 * ws] = times_i(d[1], wv);
+      } break;
+      default:  // the masked state itself, one spectrum per channel
+        for (int c = 0; c < g.C; ++c) w[c * ws] = m ? x[c * xs] : z;
+        break;
+    }
+}
+
+// The NF products at one grid point from the NI physical values in[]: field f written to f[i * fs].
+__device__ __forceinline__ void pointwise_point(const Geo& g, const Prog& p, const float* in, float* f, int64_t fs) {
+    switch (p.op) {
+      case OP_CONV_MC_CONS: {
+        int o = 0;
+        for (int i = 0; i < g.C; ++i)
+          for (int j = i; j < g.C; ++j) f[(o++) * fs] = in[i] * in[j];
+      } break;
+      case OP_CONV_MC_NONCONS:
+        for (int i = 0; i < g.C; ++i) {
+          float s = 0.f;
+          for (int j = 0; j < g.D; ++j) s += in[j] * in[g.C + i * g.D + j];
+          f[i * fs] = s;
+        }
+        break;
+      case OP_CONV_SC_CONS:
+        f[0] = in[0] * in[0];
+        break;
+      case OP_CONV_SC_NONCONS:
+        f[0] = in[0] * in[1];
+        break;
+      case OP_GRAD_NORM:
+        for (int c = 0; c < g.C; ++c) {
+          float s = 0.f;
+          for (int j = 0; j < g.D; ++j) s += in[c * g.D + j] * in[c * g.D + j];
+          f[c * fs] = s;
+        }
+        break;
+      case OP_POLY:
+        for (int c = 0; c < g.C; ++c) {
+          // sum_k c_k u^k with the powers accumulated as the reference does
+          const float u = in[c];
+          float pw = 1.f, acc = 0.f;
+          for (int i = 0; i < p.npoly; ++i) {
+            acc += p.poly[i] * pw;
+            pw *= u;
+          }
+          f[c * fs] = acc;
+        }
+        break;
+      case OP_GENERAL: {
+        float s = 0.f;
+        for (int j = 0; j < g.D; ++j) s += in[1 + j] * in[1 + j];
+        f[0] = in[0] * in[0];
+        f[fs] = s;
+      } break;
+      case OP_CAHN_HILLIARD:
+        f[0] = in[0] * in[0] * in[0];
+        break;
+      case OP_GRAY_SCOTT: {
+        const float u0 = in[0], u1 = in[1];
+        const float uvv = u0 * (u1 * u1);
+        f[0] = p.feed * (1.f - u0) - uvv;
+        f[fs] = -(p.feed + p.kill) * u1 + uvv;
+      } break;
+      case OP_VORT:
+        f[0] = fmaf(in[0], in[2], in[1] * in[3]);
+        break;
+      case OP_BZ: {
+        const float u0 = in[0], u1 = in[1], u2 = in[2];
+        const float u01 = u0 * u1;
+        f[0] = u0 + u1 - u01 - u0 * u0;
+        f[fs] = u2 - u1 - u01;
+        f[2 * fs] = u0 - u2;
+      } break;
+    }
+}
+
+// N^ of every channel at mode k from the NF forward spectra h[f * hs] (post-mask m, derivative
+// multipliers, scales); the Kolmogorov injection of the vorticity term included.
+__device__ __forceinline__ void combine_mode(const PlanDev& P, const Geo& g, const Prog& p, const int (&k)[3], bool m,
+                                             const float2* h, int64_t hs, float2 (&nv)[MAXC]) {
+    float d[3];
+    float dsum = 0.f, lap = 0.f;
+    for (int a = 0; a < 3; ++a) {
+      d[a] = g.ks * (float)k[a];
+      if (a < g.D) {
+        dsum += d[a];
+        lap -= d[a] * d[a];
+      }
+    }
+    const bool dc = (k[0] == 0 && k[1] == 0 && k[2] == 0);
+    for (int c = 0; c < MAXC; ++c) nv[c] = make_float2(0.f, 0.f);
+    if (m) {
+      switch (p.op) {
+        case OP_CONV_MC_CONS:
+          for (int i = 0; i < g.C; ++i) {
+            float2 acc = make_float2(0.f, 0.f);
+            for (int j = 0; j < g.D; ++j) acc = cadd(acc, times_i(d[j], h[(sym_index(i, j, g.C)) * hs]));
+            nv[i] = cscale(acc, p.s0);
+          }
+          break;
+        case OP_CONV_SC_CONS:
+          nv[0] = cscale(times_i(dsum, h[0]), p.s0);
+          break;
+        case OP_GRAD_NORM:
+          for (int c = 0; c < g.C; ++c) nv[c] = (p.zmf && dc) ? make_float2(0.f, 0.f) : cscale(h[(c) * hs], p.s0);
+          break;
+        case OP_GENERAL: {
+          const float2 sq = h[0];
+          const float2 gn = (p.zmf && dc) ? make_float2(0.f, 0.f) : h[hs];
+          nv[0] = cadd(cadd(cscale(sq, p.s0), cscale(times_i(dsum, sq), p.s1)), cscale(gn, p.s2));
+        } break;
+        case OP_CAHN_HILLIARD:
+          nv[0] = cscale(h[0], p.s0 * lap);
+          break;
+        default:  // -b F[.] (non-conservative convection, vorticity) or F[.] (polynomial, Gray-Scott): scale s0
+          for (int c = 0; c < g.C; ++c) nv[c] = cscale(h[(c) * hs], p.s0);
+          break;
+      }
+    }
+  if (p.op == OP_VORT && k[0] == 0 && k[1] == P.inj_mode) nv[0].x += P.inj_value;
+}
+
+}  // namespace ndg
+}  // namespace exgb

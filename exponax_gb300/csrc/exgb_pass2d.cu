@@ -1,0 +1,419 @@
+// exgb_pass2d.cu -- 2D ETDRK stages of the staged nonlinearities in three fused passes per stage.
+//
+// The staged N-D path (exgb_ndgen.cu) spends five kernels and about a dozen HBM passes on a stage:
+// derive, inverse transform (two axis passes), pointwise, forward transform (two axis passes),
+// combine.  In 2D the same arithmetic (exgb_ndops.cuh, one definition for both paths) runs here in
+// three passes, each reading and writing global memory once:
+//   pass 1  per tile of ky columns: the NI derived spectra of every mode of the columns (pre-mask),
+//           inverse transforms along kx in shared memory            -> W[f][ky][x]
+//   pass 2  per tile of rows x: for each of the NI fields the c2r transform along y (two real rows
+//           packed in one complex transform, 1/N^2 folded in), the pointwise products, the r2c
+//           transforms of the NF products (packed in pairs)          -> Hq[f][ky][x], ky <= K
+//   pass 3  per tile of ky columns: forward transforms along x, post-mask and multipliers
+//           (combine), the ETDRK stage update of every channel of the mode
+// Only the Kc = K + 1 columns inside the dealiasing mask (all N/2 + 1 without a mask) take part;
+// the columns above it feel the linear part alone (the post-mask zeroes their nonlinear term), so
+// they are advanced by E once per step in a separate elementwise kernel with the same c2r projection.
+// State and stage buffers are column-major per sample ([c][ky][kx], the coefficient tables of such
+// plans share the layout), filled and emptied by transposes at the call boundary.
+//
+// Reference: nonlin_fun/_base.py:73-137 (pre-mask before every inverse transform, post-mask after
+// every forward transform), the nonlinear functions named in exgb_ndops.cuh, etdrk/_etdrk_1..4.py.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "exgb_internal.h"
+#include "exgb_ndops.cuh"
+#include "exgb_stage.cuh"
+
+namespace exgb {
+
+void* workspace(size_t bytes, int slot_offset);
+
+namespace p2d {
+
+using ndg::Geo;
+using ndg::MAXC;
+using ndg::Prog;
+
+struct Args {
+  PlanDev P;
+  Geo g;
+  Prog p;
+  FftPlan fp;          // length N
+  const float2* tw;    // N twiddles
+  int N, M, K, Kc;     // Kc = columns that enter the nonlinear term
+  int TY, TX;          // columns per pass-1/3 CTA, rows per pass-2 CTA
+  int64_t plane;       // M * N modes per channel
+  StageBufs sb;        // [s][c][ky][kx]
+  int64_t sstride;     // C * plane
+  const float2* xin;   // stage input (sb.U, sb.S or sb.S1)
+  float2* W;           // [s][f < NI][ky < Kc][x]
+  float2* Hq;          // [s][f < NF][ky < Kc][x]
+  int stage;           // ETDRK stage, -1: nonlinear term only
+  float2* nout;        // nonlinear term, natural layout [s][c][kx][ky] (stage -1)
+};
+
+__device__ __forceinline__ int sgn_of(int i, int N) { return (i <= (N - 1) / 2) ? i : i - N; }
+
+// ---- pass 1: derived spectra of TY columns, inverse transforms along kx
+__global__ void __launch_bounds__(256) pass1_kernel(const Args a) {
+  extern __shared__ float2 sm1[];
+  const int N = a.N, NI = a.p.NI, TY = a.TY;
+  const int64_t s = blockIdx.y;
+  const int ky0 = blockIdx.x * TY;
+  const int ty = min(TY, a.Kc - ky0);
+  const int count = NI * TY;  // sequence (f, t) at (f * TY + t) * N
+  float2* buf0 = sm1;
+  float2* buf1 = sm1 + (size_t)count * N;
+  const float2* xs = a.xin + s * a.sstride;
+  for (int e = threadIdx.x; e < TY * N; e += blockDim.x) {
+    const int t = e / N, kx = e - t * N;
+    if (t < ty) {
+      const int ky = ky0 + t;
+      const int k[3] = {sgn_of(kx, N), ky, 0};
+      const bool m = abs(k[0]) <= a.K && ky <= a.K;
+      ndg::derive_mode(a.g, a.p, k, m, xs + (int64_t)ky * N + kx, a.plane, buf0 + (size_t)t * N + kx,
+                       (int64_t)TY * N);
+    } else {
+      for (int f = 0; f < NI; ++f) buf0[((size_t)f * TY + t) * N + kx] = make_float2(0.f, 0.f);
+    }
+  }
+  __syncthreads();
+  float2* res = result_buf(a.fp, buf0, buf1);
+  block_fft<true>(a.fp, buf0, buf1, LinMap{res, N}, count, a.tw, threadIdx.x, blockDim.x, BlockSync{});
+  float2* W = a.W + s * (int64_t)NI * a.Kc * N;
+  for (int e = threadIdx.x; e < count * N; e += blockDim.x) {
+    const int q = e / N, x = e - q * N;
+    const int f = q / TY, t = q - f * TY;
+    if (t < ty) W[((int64_t)f * a.Kc + ky0 + t) * N + x] = res[e];
+  }
+}
+
+// ---- pass 2: c2r along y, pointwise products, r2c along y, for TX rows
+__global__ void __launch_bounds__(256) pass2_kernel(const Args a) {
+  extern __shared__ float2 sm2[];
+  const int N = a.N, NI = a.p.NI, NF = a.p.NF, TX = a.TX, Kc = a.Kc;
+  const int M = N / 2 + 1;
+  const bool even = (N & 1) == 0;
+  const int64_t s = blockIdx.y;
+  const int x0 = blockIdx.x * TX;
+  const int tx = min(TX, N - x0);
+  const int NP = (NI > NF ? NI : NF) * TX / 2;  // complex sequences of the larger transform set
+  float2* buf0 = sm2;
+  float2* buf1 = sm2 + (size_t)NP * N;
+  float* phys = reinterpret_cast<float*>(sm2 + 2 * (size_t)NP * N);  // [NI * TX][N]
+  float* prod = phys + (size_t)NI * TX * N;                           // [NF * TX][N]
+  const float2* W = a.W + s * (int64_t)NI * Kc * N;
+  // c2r inputs: sequence j packs real rows q = 2j, 2j + 1 (q = f * TX + xx)
+  const int ni = NI * TX / 2;
+  for (int e = threadIdx.x; e < ni * N; e += blockDim.x) {
+    const int j = e / N, k = e - j * N;
+    const bool ext = k >= M;
+    const int kk = ext ? N - k : k;
+    const bool real_only = (k == 0) || (even && k == N / 2);
+    float2 va = make_float2(0.f, 0.f), vb = va;
+    if (kk < Kc) {
+      const int qa = 2 * j, qb = 2 * j + 1;
+      const int fa = qa / TX, xa = qa - fa * TX, fb = qb / TX, xb = qb - fb * TX;
+      if (xa < tx) va = W[((int64_t)fa * Kc + kk) * N + x0 + xa];
+      if (xb < tx) vb = W[((int64_t)fb * Kc + kk) * N + x0 + xb];
+    }
+    buf0[e] = pack_pair(va, vb, ext, real_only);
+  }
+  __syncthreads();
+  float2* res = result_buf(a.fp, buf0, buf1);
+  block_fft<true>(a.fp, buf0, buf1, LinMap{res, N}, ni, a.tw, threadIdx.x, blockDim.x, BlockSync{});
+  const float inv = 1.f / ((float)N * (float)N);
+  for (int e = threadIdx.x; e < ni * N; e += blockDim.x) {
+    const int j = e / N, y = e - j * N;
+    const float2 z = res[e];
+    phys[(size_t)(2 * j) * N + y] = z.x * inv;
+    phys[(size_t)(2 * j + 1) * N + y] = z.y * inv;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < TX * N; e += blockDim.x) {
+    const int xx = e / N, y = e - xx * N;
+    float in[MAXC + MAXC * 3];
+    for (int f = 0; f < NI; ++f) in[f] = phys[((size_t)f * TX + xx) * N + y];
+    ndg::pointwise_point(a.g, a.p, in, prod + (size_t)xx * N + y, (int64_t)TX * N);
+  }
+  __syncthreads();
+  // r2c: sequence j packs product rows 2j, 2j + 1 (row index q = f * TX + xx)
+  const int nf = NF * TX / 2;
+  for (int e = threadIdx.x; e < nf * N; e += blockDim.x) {
+    const int j = e / N, y = e - j * N;
+    buf0[e] = make_float2(prod[(size_t)(2 * j) * N + y], prod[(size_t)(2 * j + 1) * N + y]);
+  }
+  __syncthreads();
+  res = result_buf(a.fp, buf0, buf1);
+  block_fft<false>(a.fp, buf0, buf1, LinMap{res, N}, nf, a.tw, threadIdx.x, blockDim.x, BlockSync{});
+  float2* Hq = a.Hq + s * (int64_t)NF * Kc * N;
+  for (int e = threadIdx.x; e < nf * Kc; e += blockDim.x) {
+    const int j = e / Kc, k = e - j * Kc;
+    float2 P, Q;
+    unpack_pair(res[(size_t)j * N + k], res[(size_t)j * N + (k == 0 ? 0 : N - k)], P, Q);
+    const int qa = 2 * j, qb = 2 * j + 1;
+    const int fa = qa / TX, xa = qa - fa * TX, fb = qb / TX, xb = qb - fb * TX;
+    if (xa < tx) Hq[((int64_t)fa * Kc + k) * N + x0 + xa] = P;
+    if (xb < tx) Hq[((int64_t)fb * Kc + k) * N + x0 + xb] = Q;
+  }
+}
+
+// ---- pass 3: forward transforms along x, combine, ETDRK stage update
+__global__ void __launch_bounds__(256) pass3_kernel(const Args a) {
+  extern __shared__ float2 sm3[];
+  const int N = a.N, NF = a.p.NF, TY = a.TY, C = a.g.C;
+  const int64_t s = blockIdx.y;
+  const int ky0 = blockIdx.x * TY;
+  const int ty = min(TY, a.Kc - ky0);
+  const int count = NF * TY;
+  float2* buf0 = sm3;
+  float2* buf1 = sm3 + (size_t)count * N;
+  const float2* Hq = a.Hq + s * (int64_t)NF * a.Kc * N;
+  for (int e = threadIdx.x; e < count * N; e += blockDim.x) {
+    const int q = e / N, x = e - q * N;
+    const int f = q / TY, t = q - f * TY;
+    buf0[e] = t < ty ? Hq[((int64_t)f * a.Kc + ky0 + t) * N + x] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  float2* res = result_buf(a.fp, buf0, buf1);
+  block_fft<false>(a.fp, buf0, buf1, LinMap{res, N}, count, a.tw, threadIdx.x, blockDim.x, BlockSync{});
+  for (int e = threadIdx.x; e < ty * N; e += blockDim.x) {
+    const int t = e / N, kx = e - t * N;
+    const int ky = ky0 + t;
+    const int k[3] = {sgn_of(kx, N), ky, 0};
+    const bool m = abs(k[0]) <= a.K && ky <= a.K;
+    float2 nv[MAXC];
+    ndg::combine_mode(a.P, a.g, a.p, k, m, res + (size_t)t * N + kx, (int64_t)TY * N, nv);
+    const int64_t r = (int64_t)ky * N + kx;  // column-major mode index
+    if (a.stage < 0) {
+      float2* o = a.nout + s * a.sstride + (int64_t)kx * a.M + ky;
+      for (int c = 0; c < C; ++c) o[c * a.plane] = nv[c];
+      continue;
+    }
+    for (int c = 0; c < C; ++c) {
+      const int64_t ci = (a.P.lin_ch == 1 ? 0 : (int64_t)c * a.plane) + r;
+      stage_upd_at(a.P, a.sb, s * a.sstride + c * a.plane + r, ci, a.stage, nv[c]);
+    }
+  }
+}
+
+// natural [s][c][kx][ky] <-> column-major [s][c][ky][kx] for the columns ky < ncol (32 x 32 tiles)
+__global__ void transpose_kernel(const float2* __restrict__ in, float2* __restrict__ out, int N, int M, int ncol,
+                                 int64_t fields, int to_cols) {
+  __shared__ float2 tile[32][33];
+  const int64_t f = blockIdx.z;
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;  // bx over kx, by over ky
+  const int64_t plane = (int64_t)N * M;
+  const float2* src = in + f * plane;
+  float2* dst = out + f * plane;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    if (to_cols) {
+      const int kx = bx + j, ky = by + threadIdx.x;
+      if (kx < N && ky < ncol) tile[j][threadIdx.x] = src[(int64_t)kx * M + ky];
+    } else {
+      const int ky = by + j, kx = bx + threadIdx.x;
+      if (kx < N && ky < ncol) tile[threadIdx.x][j] = src[(int64_t)ky * N + kx];
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    if (to_cols) {
+      const int ky = by + j, kx = bx + threadIdx.x;
+      if (kx < N && ky < ncol) dst[(int64_t)ky * N + kx] = tile[threadIdx.x][j];
+    } else {
+      const int kx = bx + j, ky = by + threadIdx.x;
+      if (kx < N && ky < ncol) dst[(int64_t)kx * M + ky] = tile[j][threadIdx.x];
+    }
+  }
+}
+
+// c2r projection of a step's physical round trip on the column-major state: ky = 0 and (N even)
+// ky = N/2 columns, v(kx) <- (v(kx) + conj(v(-kx))) / 2, one thread per {kx, N - kx} pair
+__global__ void project_cols_kernel(float2* __restrict__ U, int N, int M, int Kc, int64_t fields) {
+  const int half = N / 2 + 1;
+  const int64_t total = fields * 2 * half;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = t / (2 * half);
+    const int rr = (int)(t - f * 2 * half);
+    const int col = rr / half, kx = rr - col * half;
+    const int ky = col == 0 ? 0 : N / 2;
+    if (col == 1 && ((N & 1) || ky >= Kc)) continue;  // no Nyquist column, or it is a linear column
+    const int kx2 = (N - kx) % N;
+    float2* c = U + f * (int64_t)N * M + (int64_t)ky * N;
+    const float2 v1 = c[kx], v2 = c[kx2];
+    const float2 pv = make_float2(0.5f * (v1.x + v2.x), 0.5f * (v1.y - v2.y));
+    c[kx] = pv;
+    c[kx2] = cconj(pv);
+  }
+}
+
+// The columns above the mask (ky >= Kc): nsteps of u <- E u (what every ETDRK order gives with a zero
+// nonlinear term), with the projection on ky = N/2; natural layout in and out.  One thread per
+// {kx, N - kx} pair.  E is column-major [lin_ch][ky][kx].
+__global__ void linear_cols_kernel(const float2* __restrict__ E, int lin_ch, int C, int N, int M, int Kc,
+                                   int64_t fields, const float2* __restrict__ in, float2* __restrict__ out,
+                                   int nsteps, int project, int zero) {
+  const int half = N / 2 + 1;
+  const int ncol = M - Kc;
+  const int64_t total = fields * (int64_t)ncol * half;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = t / ((int64_t)ncol * half);
+    const int rr = (int)(t - f * (int64_t)ncol * half);
+    const int ky = Kc + rr / half, kx = rr % half;
+    const int kx2 = (kx == 0) ? 0 : N - kx;
+    if (kx2 < kx) continue;
+    const int64_t base = f * (int64_t)N * M;
+    if (zero) {
+      out[base + (int64_t)kx * M + ky] = make_float2(0.f, 0.f);
+      out[base + (int64_t)kx2 * M + ky] = make_float2(0.f, 0.f);
+      continue;
+    }
+    const int c = (int)(f % C);
+    const float2* Et = E + (lin_ch == 1 ? 0 : (int64_t)c * N * M) + (int64_t)ky * N;
+    const float2 e1 = Et[kx], e2 = Et[kx2];
+    float2 v1 = in[base + (int64_t)kx * M + ky], v2 = in[base + (int64_t)kx2 * M + ky];
+    const bool proj = project && (ky == 0 || ((N & 1) == 0 && ky == N / 2));
+    for (int st = 0; st < nsteps; ++st) {
+      v1 = cmul(e1, v1);
+      v2 = cmul(e2, v2);
+      if (proj) {
+        const float2 pv = make_float2(0.5f * (v1.x + v2.x), 0.5f * (v1.y - v2.y));
+        v1 = pv;
+        v2 = cconj(pv);
+      }
+    }
+    out[base + (int64_t)kx * M + ky] = v1;
+    if (kx2 != kx) out[base + (int64_t)kx2 * M + ky] = v2;
+  }
+}
+
+static unsigned grid_for(int64_t n, int sm) {
+  const int64_t b = (n + 255) / 256;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm * 32));
+}
+
+// shared memory of the three passes for tile sizes TY, TX
+static size_t smem1(int NI, int TY, int N) { return sizeof(float2) * 2 * (size_t)NI * TY * N; }
+static size_t smem2(int NI, int NF, int TX, int N) {
+  const size_t np = (size_t)std::max(NI, NF) * TX / 2;
+  return sizeof(float2) * 2 * np * N + sizeof(float) * (size_t)(NI + NF) * TX * N;
+}
+static size_t smem3(int NF, int TY, int N) { return sizeof(float2) * 2 * (size_t)NF * TY * N; }
+
+static size_t smem_limit() {
+  static int lim = 0;
+  if (!lim) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  return (size_t)lim;
+}
+
+// tiles: about 2048 complex values per transform set, within half the shared memory
+static void tiles(int NI, int NF, int N, int& TY, int& TX) {
+  const size_t cap = smem_limit() / 2;
+  TY = std::max(1, 2048 / (std::max(NI, NF) * N));
+  while (TY > 1 && std::max(smem1(NI, TY, N), smem3(NF, TY, N)) > cap) --TY;
+  TX = std::max(2, 2 * (4096 / (std::max(NI, NF) * N) / 2));
+  while (TX > 2 && smem2(NI, NF, TX, N) > cap) TX -= 2;
+}
+
+}  // namespace p2d
+
+using namespace p2d;
+
+// Can the three-pass path step this 2D staged plan?  N = 2^a 3^b 5^c with the pass-2 tile of two rows
+// within one CTA's shared memory.
+bool pass2d_supported(int D, int N, int NI, int NF) {
+  if (D != 2 || N < 2 || NI < 1 || NF < 1) return false;
+  FftPlan fp;
+  if (!make_fft_plan(N, &fp)) return false;
+  return std::max(p2d::smem1(NI, 1, N), std::max(p2d::smem2(NI, NF, 2, N), p2d::smem3(NF, 1, N))) <=
+         p2d::smem_limit() - 1024;
+}
+
+int pass2d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStream_t st, const float2* in, float2* out,
+               int64_t batch, int nsteps, int project, int nonlinear_only) {
+  const PlanDev& P = plan->dev;
+  const int N = P.N, M = P.M, C = P.C;
+  const int K = std::min(P.kmax, N / 2);
+  const int Kc = std::min(M, K + 1);
+  const int sm = plan->sm_count;
+  const int64_t plane = (int64_t)N * M;
+  if (batch == 0) return EXGB_OK;
+  if (!nonlinear_only && nsteps == 0) {
+    if (in != out) EXGB_CUDA(cudaMemcpyAsync(out, in, sizeof(float2) * batch * C * plane, cudaMemcpyDeviceToDevice, st));
+    return EXGB_OK;
+  }
+  Args a{};
+  a.P = P;
+  a.g = g0;
+  a.p = prog;
+  a.fp = P.fft;
+  a.tw = P.tw;
+  a.N = N;
+  a.M = M;
+  a.K = K;
+  a.Kc = Kc;
+  tiles(prog.NI, prog.NF, N, a.TY, a.TX);
+  a.plane = plane;
+  a.sstride = (int64_t)C * plane;
+  const int nb = stage_nbufs(P.order);
+  const size_t per_sample = sizeof(float2) * ((size_t)(nonlinear_only ? 1 : nb) * C * plane +
+                                              (size_t)(prog.NI + prog.NF) * Kc * N);
+  const int64_t cb = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)((size_t)(1u << 30) / per_sample)));
+  char* ws = (char*)workspace(per_sample * (size_t)cb, 5);
+  if (!ws) return fail(EXGB_ENOMEM, "workspace allocation failed");
+  const size_t s1 = smem1(prog.NI, a.TY, N), s2 = smem2(prog.NI, prog.NF, a.TX, N), s3 = smem3(prog.NF, a.TY, N);
+  EXGB_CUDA(cudaFuncSetAttribute(pass1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
+  EXGB_CUDA(cudaFuncSetAttribute(pass2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+  EXGB_CUDA(cudaFuncSetAttribute(pass3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s3));
+  const int ycols = (Kc + a.TY - 1) / a.TY, xrows = (N + a.TX - 1) / a.TX;
+  for (int64_t b0 = 0; b0 < batch; b0 += cb) {
+    const int64_t n = std::min<int64_t>(cb, batch - b0);
+    if (n * C > 65535) return fail(EXGB_EUNSUPPORTED, "too many fields for one launch");
+    const float2* src = in + b0 * a.sstride;
+    float2* dst = out + b0 * a.sstride;
+    float2* q = (float2*)ws;
+    const int64_t fsz = a.sstride * n;
+    a.sb = stage_bufs(q, nonlinear_only ? 1 : P.order, fsz);
+    q += (int64_t)(nonlinear_only ? 1 : nb) * fsz;
+    a.W = q;
+    q += (int64_t)prog.NI * Kc * N * n;
+    a.Hq = q;
+    // a.sb.U = column-major copy of the masked columns
+    {
+      dim3 grid((N + 31) / 32, (Kc + 31) / 32, (unsigned)(n * C));
+      transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(src, a.sb.U, N, M, Kc, n * C, 1);
+    }
+    const int nst = nonlinear_only ? 1 : P.order;
+    const int Q = nonlinear_only ? 1 : nsteps * P.order;
+    for (int qq = 0; qq < Q; ++qq) {
+      const int stage = qq % nst;
+      a.stage = nonlinear_only ? -1 : stage;
+      a.nout = nonlinear_only ? dst : nullptr;
+      a.xin = (stage == 0) ? a.sb.U : (P.order == 4 && stage == 1) ? a.sb.S1 : a.sb.S;
+      pass1_kernel<<<dim3(ycols, (unsigned)n), 256, s1, st>>>(a);
+      pass2_kernel<<<dim3(xrows, (unsigned)n), 256, s2, st>>>(a);
+      pass3_kernel<<<dim3(ycols, (unsigned)n), 256, s3, st>>>(a);
+      if (!nonlinear_only && stage == nst - 1 && project)
+        project_cols_kernel<<<grid_for(n * C * 2 * (N / 2 + 1), sm), 256, 0, st>>>(a.sb.U, N, M, Kc, n * C);
+      EXGB_CUDA(cudaGetLastError());
+    }
+    if (!nonlinear_only) {
+      dim3 grid((N + 31) / 32, (Kc + 31) / 32, (unsigned)(n * C));
+      transpose_kernel<<<grid, dim3(32, 8), 0, st>>>(a.sb.U, dst, N, M, Kc, n * C, 0);
+    }
+    if (Kc < M)
+      linear_cols_kernel<<<grid_for(n * C * (int64_t)(M - Kc) * (N / 2 + 1), sm), 256, 0, st>>>(
+          P.E, P.lin_ch, C, N, M, Kc, n * C, src, dst, nsteps, project, nonlinear_only);
+    EXGB_CUDA(cudaGetLastError());
+  }
+  return EXGB_OK;
+}
+
+}  // namespace exgb

@@ -87,7 +87,7 @@ __device__ __forceinline__ float2 stage_upd(const PlanDev& P, const StageBufs& b
 }
 
 // Per-CTA state buffers (each `colsz` modes) of an ETDRK method of the given order.
-__device__ __forceinline__ StageBufs stage_bufs(float2* q, int order, int64_t colsz) {
+__host__ __device__ __forceinline__ StageBufs stage_bufs(float2* q, int order, int64_t colsz) {
   StageBufs sb;
   sb.U = q;
   q += colsz;

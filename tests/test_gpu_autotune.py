@@ -61,8 +61,15 @@ def test_every_cluster_size_matches_oracle(n):
     512) with each cluster size 1..8 that fits (rows split unevenly when G does not divide N): one
     ETDRK2 step within 1e-5 of the oracle; sizes that do not fit are refused with
     EXGB_EUNSUPPORTED and leave the plan usable."""
+    import os
+
     from exponax_gb300._lib import EXGB_OK
-    sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
+    os.environ["EXGB_2D_PATH"] = "fused"  # 512^2 runs on the three-pass path unless asked otherwise
+    try:
+        sm = ex.stepper.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
+        sm.plan.handle  # the plan (and its path) is made here, while the variable is set
+    finally:
+        del os.environ["EXGB_2D_PATH"]
     so = o.NavierStokesVorticity(2, 2 * np.pi, n, 0.01, diffusivity=1e-3)
     g = ex.ic.RandomAmplitudePhaseSeries(2, cutoff=5, max_one=True)
     u = np.stack([g(n, key=s) for s in range(3)])

@@ -261,13 +261,21 @@ def test_ns_256_config_short_rollout():
 
 @pytest.mark.parametrize("cluster", [0, 4, 6, 8])
 def test_kolmogorov_512_generic_cluster_kernel(cluster):
-    """Kolmogorov flow 512^2 runs on the generic 2D cluster kernel (its derived fields
-    go through L2): 3 ETDRK2 steps within 1e-5 of the oracle, at the automatic cluster
-    size and at 4, 6 (rows split 86 x 5 + 82) and 8 CTAs per cluster."""
+    """Kolmogorov flow 512^2 on the generic 2D cluster kernel (its derived fields go through L2;
+    EXGB_2D_PATH=fused selects it over the three-pass path): 3 ETDRK2 steps within 1e-5 of the
+    oracle, at the automatic cluster size and at 4, 6 (rows split 86 x 5 + 82) and 8 CTAs per
+    cluster."""
+    import os
+
     from exponax_gb300 import autotune
 
     N = 512
-    sm = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, N, 0.001)
+    os.environ["EXGB_2D_PATH"] = "fused"  # 512^2 runs on the three-pass path unless asked otherwise
+    try:
+        sm = ex.stepper.KolmogorovFlowVorticity(2, 2 * np.pi, N, 0.001)
+        sm.plan.handle  # the plan (and its path) is made here, while the variable is set
+    finally:
+        del os.environ["EXGB_2D_PATH"]
     so = o.KolmogorovFlowVorticity(2, 2 * np.pi, N, 0.001)
     if cluster:
         assert autotune._set(sm.plan, 1, [cluster]) == 0
