@@ -25,6 +25,7 @@
 
 #include "exgb_internal.h"
 #include "exgb_ndops.cuh"
+#include "exgb_regfft.cuh"
 #include "exgb_stage.cuh"
 
 namespace exgb {
@@ -44,13 +45,13 @@ struct Args {
   FftPlan fp;          // length N
   const float2* tw;    // N twiddles
   int N, M, K, Kc;     // Kc = columns that enter the nonlinear term
-  int TY, TX;          // columns per pass-1/3 CTA, rows per pass-2 CTA
+  int TY, TX, TY3;     // columns per pass-1 CTA, rows per pass-2 CTA, columns per pass-3 CTA
   int64_t plane;       // M * N modes per channel
   StageBufs sb;        // [s][c][ky][kx]
   int64_t sstride;     // C * plane
   const float2* xin;   // stage input (sb.U, sb.S or sb.S1)
-  float2* W;           // [s][f < NI][ky < Kc][x]
-  float2* Hq;          // [s][f < NF][ky < Kc][x]
+  float2* W;           // [s][f < NI][x][ky < Kc]
+  float2* Hq;          // [s][f < NF][x][ky < Kc]
   int stage;           // ETDRK stage, -1: nonlinear term only
   float2* nout;        // nonlinear term, natural layout [s][c][kx][ky] (stage -1)
 };
@@ -84,10 +85,11 @@ __global__ void __launch_bounds__(256) pass1_kernel(const Args a) {
   float2* res = result_buf(a.fp, buf0, buf1);
   block_fft<true>(a.fp, buf0, buf1, LinMap{res, N}, count, a.tw, threadIdx.x, blockDim.x, BlockSync{});
   float2* W = a.W + s * (int64_t)NI * a.Kc * N;
+  // consecutive threads: consecutive columns of one row x (TY * 8 contiguous bytes)
   for (int e = threadIdx.x; e < count * N; e += blockDim.x) {
-    const int q = e / N, x = e - q * N;
-    const int f = q / TY, t = q - f * TY;
-    if (t < ty) W[((int64_t)f * a.Kc + ky0 + t) * N + x] = res[e];
+    const int t = e % TY, r = e / TY;
+    const int x = r % N, f = r / N;
+    if (t < ty) W[((int64_t)f * N + x) * a.Kc + ky0 + t] = res[((size_t)f * TY + t) * N + x];
   }
 }
 
@@ -117,8 +119,8 @@ __global__ void __launch_bounds__(256) pass2_kernel(const Args a) {
     if (kk < Kc) {
       const int qa = 2 * j, qb = 2 * j + 1;
       const int fa = qa / TX, xa = qa - fa * TX, fb = qb / TX, xb = qb - fb * TX;
-      if (xa < tx) va = W[((int64_t)fa * Kc + kk) * N + x0 + xa];
-      if (xb < tx) vb = W[((int64_t)fb * Kc + kk) * N + x0 + xb];
+      if (xa < tx) va = W[((int64_t)fa * N + x0 + xa) * Kc + kk];
+      if (xb < tx) vb = W[((int64_t)fb * N + x0 + xb) * Kc + kk];
     }
     buf0[e] = pack_pair(va, vb, ext, real_only);
   }
@@ -156,8 +158,8 @@ __global__ void __launch_bounds__(256) pass2_kernel(const Args a) {
     unpack_pair(res[(size_t)j * N + k], res[(size_t)j * N + (k == 0 ? 0 : N - k)], P, Q);
     const int qa = 2 * j, qb = 2 * j + 1;
     const int fa = qa / TX, xa = qa - fa * TX, fb = qb / TX, xb = qb - fb * TX;
-    if (xa < tx) Hq[((int64_t)fa * Kc + k) * N + x0 + xa] = P;
-    if (xb < tx) Hq[((int64_t)fb * Kc + k) * N + x0 + xb] = Q;
+    if (xa < tx) Hq[((int64_t)fa * N + x0 + xa) * Kc + k] = P;
+    if (xb < tx) Hq[((int64_t)fb * N + x0 + xb) * Kc + k] = Q;
   }
 }
 
@@ -173,9 +175,9 @@ __global__ void __launch_bounds__(256) pass3_kernel(const Args a) {
   float2* buf1 = sm3 + (size_t)count * N;
   const float2* Hq = a.Hq + s * (int64_t)NF * a.Kc * N;
   for (int e = threadIdx.x; e < count * N; e += blockDim.x) {
-    const int q = e / N, x = e - q * N;
-    const int f = q / TY, t = q - f * TY;
-    buf0[e] = t < ty ? Hq[((int64_t)f * a.Kc + ky0 + t) * N + x] : make_float2(0.f, 0.f);
+    const int t = e % TY, r = e / TY;
+    const int x = r % N, f = r / N;
+    buf0[((size_t)f * TY + t) * N + x] = t < ty ? Hq[((int64_t)f * N + x) * a.Kc + ky0 + t] : make_float2(0.f, 0.f);
   }
   __syncthreads();
   float2* res = result_buf(a.fp, buf0, buf1);
@@ -188,6 +190,218 @@ __global__ void __launch_bounds__(256) pass3_kernel(const Args a) {
     float2 nv[MAXC];
     ndg::combine_mode(a.P, a.g, a.p, k, m, res + (size_t)t * N + kx, (int64_t)TY * N, nv);
     const int64_t r = (int64_t)ky * N + kx;  // column-major mode index
+    if (a.stage < 0) {
+      float2* o = a.nout + s * a.sstride + (int64_t)kx * a.M + ky;
+      for (int c = 0; c < C; ++c) o[c * a.plane] = nv[c];
+      continue;
+    }
+    for (int c = 0; c < C; ++c) {
+      const int64_t ci = (a.P.lin_ch == 1 ? 0 : (int64_t)c * a.plane) + r;
+      stage_upd_at(a.P, a.sb, s * a.sstride + c * a.plane + r, ci, a.stage, nv[c]);
+    }
+  }
+}
+
+// ---- the same passes with register (group) FFTs for N = 64, 128, 256, 512: T lanes of a warp hold a
+// length-N sequence (E points each, lane l at positions l + T j), one shared-memory transpose per
+// transform and no block barrier inside a transform (exgb_regfft.cuh)
+template <int N>
+struct RegPass {
+  static constexpr int E = RegCfg<N>::E, T = RegCfg<N>::T;
+  static constexpr int TS = tile_stride<E, T>();
+  // passes 1 and 3 keep each sequence in a slot of SLOT float2 that also serves as its transform's
+  // transpose tile (the sequence is in registers meanwhile); pass 2 builds its sequences from global
+  // memory and has per-group tiles (128 threads at N = 512, where a lane holds 32 points)
+  static constexpr int SLOT = N > TS ? N : TS;
+  static constexpr int THREADS = 256, NG = THREADS / T;
+  static constexpr int THREADS2 = N >= 512 ? 128 : 256, NG2 = THREADS2 / T;
+  // float2 offsets: twiddles, then pass 2's tiles, then the pass's own buffers
+  static constexpr int TWL = 0, TILES = N, FREE13 = N, FREE2 = N + NG2 * TS;
+};
+
+template <int N>
+__device__ __forceinline__ void load_twl(float2* twl, const float2* __restrict__ tw) {
+  constexpr int T = RegCfg<N>::T;
+  for (int t = threadIdx.x; t < N; t += blockDim.x) {
+    const int k1 = t / T, ll = t % T;
+    twl[t] = __ldg(tw + ((ll * k1) % N));  // w_N^(l k1), [k1][l]
+  }
+}
+
+template <int N>
+__device__ __forceinline__ unsigned group_mask() {
+  constexpr int T = RegCfg<N>::T;
+  const int lane = threadIdx.x & 31;
+  return (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
+}
+
+// `count` sequences of N complex values in slots buf + q * SLOT, transformed in place by the groups;
+// a sequence's slot is its transpose tile once the group holds the sequence in registers
+template <int N, bool INV>
+__device__ __forceinline__ void groups_fft(float2* buf, int count, const float2* twl) {
+  using R = RegPass<N>;
+  const int gi = threadIdx.x / R::T, l = threadIdx.x % R::T;
+  const unsigned gmask = group_mask<N>();
+  for (int q = gi; q < count; q += R::NG) {
+    float2* slot = buf + (size_t)q * R::SLOT;
+    float2 v[R::E];
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) v[j] = slot[l + R::T * j];
+    __syncwarp(gmask);  // every lane holds its points before the slot becomes the tile
+    group_fft<R::E, R::T, INV>(v, l, slot, twl, gmask);
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) slot[l + R::T * j] = v[j];
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(RegPass<N>::THREADS) pass1_reg_kernel(const Args a) {
+  using R = RegPass<N>;
+  constexpr int SL = R::SLOT;
+  extern __shared__ __align__(16) float2 smr1[];
+  float2* twl = smr1 + R::TWL;
+  float2* buf = smr1 + R::FREE13;  // [NI * TY][SLOT]
+  const int NI = a.p.NI, TY = a.TY;
+  const int64_t s = blockIdx.y;
+  const int ky0 = blockIdx.x * TY;
+  const int ty = min(TY, a.Kc - ky0);
+  load_twl<N>(twl, a.tw);
+  const float2* xs = a.xin + s * a.sstride;
+  for (int e = threadIdx.x; e < TY * N; e += blockDim.x) {
+    const int t = e / N, kx = e - t * N;
+    if (t < ty) {
+      const int ky = ky0 + t;
+      const int k[3] = {sgn_of(kx, N), ky, 0};
+      const bool m = abs(k[0]) <= a.K && ky <= a.K;
+      ndg::derive_mode(a.g, a.p, k, m, xs + (int64_t)ky * N + kx, a.plane, buf + (size_t)t * SL + kx,
+                       (int64_t)TY * SL);
+    } else {
+      for (int f = 0; f < NI; ++f) buf[((size_t)f * TY + t) * SL + kx] = make_float2(0.f, 0.f);
+    }
+  }
+  __syncthreads();
+  groups_fft<N, true>(buf, NI * TY, twl);
+  __syncthreads();
+  float2* W = a.W + s * (int64_t)NI * a.Kc * N;
+  for (int e = threadIdx.x; e < NI * TY * N; e += blockDim.x) {
+    const int t = e % TY, r = e / TY;
+    const int x = r % N, f = r / N;
+    if (t < ty) W[((int64_t)f * N + x) * a.Kc + ky0 + t] = buf[((size_t)f * TY + t) * SL + x];
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(RegPass<N>::THREADS2) pass2_reg_kernel(const Args a) {
+  using R = RegPass<N>;
+  constexpr int E = R::E, T = R::T, M = N / 2 + 1;
+  extern __shared__ __align__(16) float2 smr2[];
+  float2* twl = smr2 + R::TWL;
+  const int NI = a.p.NI, NF = a.p.NF, TX = a.TX, Kc = a.Kc;
+  float* phys = reinterpret_cast<float*>(smr2 + R::FREE2);  // [NI * TX][N]
+  float* prod = phys + (size_t)NI * TX * N;                 // [NF * TX][N]
+  float2* zb = reinterpret_cast<float2*>(prod + (size_t)NF * TX * N);  // [NF * TX / 2][N]
+  const int64_t s = blockIdx.y;
+  const int x0 = blockIdx.x * TX;
+  const int tx = min(TX, N - x0);
+  load_twl<N>(twl, a.tw);
+  __syncthreads();
+  const int gi = threadIdx.x / T, l = threadIdx.x % T;
+  const unsigned gmask = group_mask<N>();
+  float2* tile = smr2 + R::TILES + (size_t)gi * R::TS;
+  const float2* W = a.W + s * (int64_t)NI * Kc * N;
+  const float inv = 1.f / ((float)N * (float)N);
+  // c2r: sequence j packs rows qa = 2j, qb = 2j + 1 (q = f * TX + xx), gathered straight from W
+  const int ni = NI * TX / 2;
+  for (int j = gi; j < ni; j += R::NG2) {
+    const int qa = 2 * j, qb = qa + 1;
+    const int fa = qa / TX, xa = qa - fa * TX, fb = qb / TX, xb = qb - fb * TX;
+    const float2* wa = W + ((int64_t)fa * N + x0 + xa) * Kc;
+    const float2* wb = W + ((int64_t)fb * N + x0 + xb) * Kc;
+    float2 v[E];
+#pragma unroll
+    for (int jj = 0; jj < E; ++jj) {
+      const int k = l + T * jj;
+      const bool ext = k >= M;
+      const int kk = ext ? N - k : k;
+      const bool real_only = (k == 0) || (k == N / 2);
+      float2 va = make_float2(0.f, 0.f), vb = va;
+      if (kk < Kc) {
+        if (xa < tx) va = wa[kk];
+        if (xb < tx) vb = wb[kk];
+      }
+      v[jj] = pack_pair(va, vb, ext, real_only);
+    }
+    group_fft<E, T, true>(v, l, tile, twl, gmask);
+#pragma unroll
+    for (int jj = 0; jj < E; ++jj) {
+      const int y = l + T * jj;
+      phys[(size_t)qa * N + y] = v[jj].x * inv;
+      phys[(size_t)qb * N + y] = v[jj].y * inv;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < TX * N; e += blockDim.x) {
+    const int xx = e / N, y = e - xx * N;
+    float in[MAXC + MAXC * 3];
+    for (int f = 0; f < NI; ++f) in[f] = phys[((size_t)f * TX + xx) * N + y];
+    ndg::pointwise_point(a.g, a.p, in, prod + (size_t)xx * N + y, (int64_t)TX * N);
+  }
+  __syncthreads();
+  // r2c: sequence j packs product rows 2j, 2j + 1
+  const int nf = NF * TX / 2;
+  for (int j = gi; j < nf; j += R::NG2) {
+    float2 v[E];
+#pragma unroll
+    for (int jj = 0; jj < E; ++jj) {
+      const int y = l + T * jj;
+      v[jj] = make_float2(prod[(size_t)(2 * j) * N + y], prod[(size_t)(2 * j + 1) * N + y]);
+    }
+    group_fft<E, T, false>(v, l, tile, twl, gmask);
+#pragma unroll
+    for (int jj = 0; jj < E; ++jj) zb[(size_t)j * N + l + T * jj] = v[jj];
+  }
+  __syncthreads();
+  float2* Hq = a.Hq + s * (int64_t)NF * Kc * N;
+  for (int e = threadIdx.x; e < nf * Kc; e += blockDim.x) {
+    const int j = e / Kc, k = e - j * Kc;
+    float2 P, Q;
+    unpack_pair(zb[(size_t)j * N + k], zb[(size_t)j * N + (k == 0 ? 0 : N - k)], P, Q);
+    const int qa = 2 * j, qb = qa + 1;
+    const int fa = qa / TX, xa = qa - fa * TX, fb = qb / TX, xb = qb - fb * TX;
+    if (xa < tx) Hq[((int64_t)fa * N + x0 + xa) * Kc + k] = P;
+    if (xb < tx) Hq[((int64_t)fb * N + x0 + xb) * Kc + k] = Q;
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(RegPass<N>::THREADS) pass3_reg_kernel(const Args a) {
+  using R = RegPass<N>;
+  constexpr int SL = R::SLOT;
+  extern __shared__ __align__(16) float2 smr3[];
+  float2* twl = smr3 + R::TWL;
+  float2* buf = smr3 + R::FREE13;  // [NF * TY3][SLOT]
+  const int NF = a.p.NF, TY = a.TY3, C = a.g.C;
+  const int64_t s = blockIdx.y;
+  const int ky0 = blockIdx.x * TY;
+  const int ty = min(TY, a.Kc - ky0);
+  load_twl<N>(twl, a.tw);
+  const float2* Hq = a.Hq + s * (int64_t)NF * a.Kc * N;
+  for (int e = threadIdx.x; e < NF * TY * N; e += blockDim.x) {
+    const int t = e % TY, r = e / TY;
+    const int x = r % N, f = r / N;
+    buf[((size_t)f * TY + t) * SL + x] = t < ty ? Hq[((int64_t)f * N + x) * a.Kc + ky0 + t] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  groups_fft<N, false>(buf, NF * TY, twl);
+  __syncthreads();
+  for (int e = threadIdx.x; e < ty * N; e += blockDim.x) {
+    const int t = e / N, kx = e - t * N;
+    const int ky = ky0 + t;
+    const int k[3] = {sgn_of(kx, N), ky, 0};
+    const bool m = abs(k[0]) <= a.K && ky <= a.K;
+    float2 nv[MAXC];
+    ndg::combine_mode(a.P, a.g, a.p, k, m, buf + (size_t)t * SL + kx, (int64_t)TY * SL, nv);
+    const int64_t r = (int64_t)ky * N + kx;
     if (a.stage < 0) {
       float2* o = a.nout + s * a.sstride + (int64_t)kx * a.M + ky;
       for (int c = 0; c < C; ++c) o[c * a.plane] = nv[c];
@@ -322,6 +536,51 @@ static void tiles(int NI, int NF, int N, int& TY, int& TX) {
   while (TX > 2 && smem2(NI, NF, TX, N) > cap) TX -= 2;
 }
 
+// register-FFT passes: tile sizes and shared memory (bytes) for N in {64, 128, 256, 512}
+template <int N>
+struct RegSizes {
+  using R = RegPass<N>;
+  static size_t s1(int NI, int TY) { return sizeof(float2) * ((size_t)R::FREE13 + (size_t)NI * TY * R::SLOT); }
+  static size_t s2(int NI, int NF, int TX) {
+    return sizeof(float2) * (size_t)R::FREE2 + sizeof(float) * (size_t)(NI + NF) * TX * N +
+           sizeof(float2) * (size_t)NF * TX / 2 * N;
+  }
+  static size_t s3(int NF, int TY3) { return sizeof(float2) * ((size_t)R::FREE13 + (size_t)NF * TY3 * R::SLOT); }
+};
+
+template <int N>
+static bool reg_tiles(int NI, int NF, int& TY, int& TX, int& TY3) {
+  const size_t cap = smem_limit() - 1024;
+  TY = 4;
+  TX = 4;
+  TY3 = std::max(4, std::min(16, RegPass<N>::NG / std::max(1, NF)));  // one sequence per group
+  while (TY > 1 && RegSizes<N>::s1(NI, TY) > cap / 2) --TY;
+  while (TX > 2 && RegSizes<N>::s2(NI, NF, TX) > cap / 2) TX -= 2;
+  while (TY3 > 1 && RegSizes<N>::s3(NF, TY3) > cap / 2) --TY3;
+  return RegSizes<N>::s1(NI, TY) <= cap && RegSizes<N>::s2(NI, NF, TX) <= cap && RegSizes<N>::s3(NF, TY3) <= cap;
+}
+
+template <int N>
+static int set_reg_attrs(const Args& a) {
+  EXGB_CUDA(cudaFuncSetAttribute(pass1_reg_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)RegSizes<N>::s1(a.p.NI, a.TY)));
+  EXGB_CUDA(cudaFuncSetAttribute(pass2_reg_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)RegSizes<N>::s2(a.p.NI, a.p.NF, a.TX)));
+  EXGB_CUDA(cudaFuncSetAttribute(pass3_reg_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)RegSizes<N>::s3(a.p.NF, a.TY3)));
+  return EXGB_OK;
+}
+
+template <int N>
+static void launch_reg(const Args& a, int64_t n, cudaStream_t st) {
+  constexpr int TH = RegPass<N>::THREADS, TH2 = RegPass<N>::THREADS2;
+  const unsigned c1 = (unsigned)((a.Kc + a.TY - 1) / a.TY), c3 = (unsigned)((a.Kc + a.TY3 - 1) / a.TY3);
+  const unsigned r2 = (unsigned)((N + a.TX - 1) / a.TX);
+  pass1_reg_kernel<N><<<dim3(c1, (unsigned)n), TH, RegSizes<N>::s1(a.p.NI, a.TY), st>>>(a);
+  pass2_reg_kernel<N><<<dim3(r2, (unsigned)n), TH2, RegSizes<N>::s2(a.p.NI, a.p.NF, a.TX), st>>>(a);
+  pass3_reg_kernel<N><<<dim3(c3, (unsigned)n), TH, RegSizes<N>::s3(a.p.NF, a.TY3), st>>>(a);
+}
+
 }  // namespace p2d
 
 using namespace p2d;
@@ -359,7 +618,19 @@ int pass2d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStrea
   a.M = M;
   a.K = K;
   a.Kc = Kc;
-  tiles(prog.NI, prog.NF, N, a.TY, a.TX);
+  // register-FFT passes at N = 64, 128, 256, 512, shared-memory Stockham passes otherwise
+  bool reg = false;
+  switch (N) {
+    case 64: reg = reg_tiles<64>(prog.NI, prog.NF, a.TY, a.TX, a.TY3); break;
+    case 128: reg = reg_tiles<128>(prog.NI, prog.NF, a.TY, a.TX, a.TY3); break;
+    case 256: reg = reg_tiles<256>(prog.NI, prog.NF, a.TY, a.TX, a.TY3); break;
+    case 512: reg = reg_tiles<512>(prog.NI, prog.NF, a.TY, a.TX, a.TY3); break;
+    default: break;
+  }
+  if (!reg) {
+    tiles(prog.NI, prog.NF, N, a.TY, a.TX);
+    a.TY3 = a.TY;
+  }
   a.plane = plane;
   a.sstride = (int64_t)C * plane;
   const int nb = stage_nbufs(P.order);
@@ -369,9 +640,20 @@ int pass2d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStrea
   char* ws = (char*)workspace(per_sample * (size_t)cb, 5);
   if (!ws) return fail(EXGB_ENOMEM, "workspace allocation failed");
   const size_t s1 = smem1(prog.NI, a.TY, N), s2 = smem2(prog.NI, prog.NF, a.TX, N), s3 = smem3(prog.NF, a.TY, N);
-  EXGB_CUDA(cudaFuncSetAttribute(pass1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
-  EXGB_CUDA(cudaFuncSetAttribute(pass2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
-  EXGB_CUDA(cudaFuncSetAttribute(pass3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s3));
+  if (reg) {
+    int rc = EXGB_OK;
+    switch (N) {
+      case 64: rc = set_reg_attrs<64>(a); break;
+      case 128: rc = set_reg_attrs<128>(a); break;
+      case 256: rc = set_reg_attrs<256>(a); break;
+      default: rc = set_reg_attrs<512>(a); break;
+    }
+    if (rc) return rc;
+  } else {
+    EXGB_CUDA(cudaFuncSetAttribute(pass1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
+    EXGB_CUDA(cudaFuncSetAttribute(pass2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+    EXGB_CUDA(cudaFuncSetAttribute(pass3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s3));
+  }
   const int ycols = (Kc + a.TY - 1) / a.TY, xrows = (N + a.TX - 1) / a.TX;
   for (int64_t b0 = 0; b0 < batch; b0 += cb) {
     const int64_t n = std::min<int64_t>(cb, batch - b0);
@@ -397,9 +679,18 @@ int pass2d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStrea
       a.stage = nonlinear_only ? -1 : stage;
       a.nout = nonlinear_only ? dst : nullptr;
       a.xin = (stage == 0) ? a.sb.U : (P.order == 4 && stage == 1) ? a.sb.S1 : a.sb.S;
-      pass1_kernel<<<dim3(ycols, (unsigned)n), 256, s1, st>>>(a);
-      pass2_kernel<<<dim3(xrows, (unsigned)n), 256, s2, st>>>(a);
-      pass3_kernel<<<dim3(ycols, (unsigned)n), 256, s3, st>>>(a);
+      if (reg) {
+        switch (N) {
+          case 64: launch_reg<64>(a, n, st); break;
+          case 128: launch_reg<128>(a, n, st); break;
+          case 256: launch_reg<256>(a, n, st); break;
+          default: launch_reg<512>(a, n, st); break;
+        }
+      } else {
+        pass1_kernel<<<dim3(ycols, (unsigned)n), 256, s1, st>>>(a);
+        pass2_kernel<<<dim3(xrows, (unsigned)n), 256, s2, st>>>(a);
+        pass3_kernel<<<dim3(ycols, (unsigned)n), 256, s3, st>>>(a);
+      }
       if (!nonlinear_only && stage == nst - 1 && project)
         project_cols_kernel<<<grid_for(n * C * 2 * (N / 2 + 1), sm), 256, 0, st>>>(a.sb.U, N, M, Kc, n * C);
       EXGB_CUDA(cudaGetLastError());
