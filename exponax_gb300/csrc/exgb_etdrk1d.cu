@@ -234,33 +234,33 @@ struct ProductOut {
 // fuse: pack fused into the first inverse pass and the products into the last (fewer barrier phases;
 // the throughput choice when several work items share an SM).  Otherwise each elementwise step is a
 // phase of its own spread over all threads (the latency choice for one small item per SM).
-template <bool fuse>
+template <bool fuse, class Sync = BlockSync>
 __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m, int stage, float2* X_out,
-                        int tid, int nthr) {
+                        int tid, int nthr, const Sync& sync = Sync{}) {
   const int N = P.N, M = P.M;
   const bool zmf = P.gamma != 0.f && P.zero_mode_fix;
   float2 *res, *other;
   if (fuse && !zmf) {  // compile-time fuse: each kernel carries one of the two paths
     res = io_result_buf(P.fft, b.w0, b.w1);
     other = (res == b.w0) ? b.w1 : b.w0;
-    block_fft_io<true>(P.fft, PackSrc{&P, X, M}, b.w0, b.w1, ProductOut{&P, res}, m, b.tw, tid, nthr, BlockSync{});
+    block_fft_io<true>(P.fft, PackSrc{&P, X, M}, b.w0, b.w1, ProductOut{&P, res}, m, b.tw, tid, nthr, sync);
   } else {
     // separate pack and product phases (the zero-mode fix also needs u_x^2 in a buffer of its own)
     nl_pack(P, X, M, b.w0, m, tid, nthr);
-    __syncthreads();
+    sync();
     res = (P.fft.npass & 1) ? b.w1 : b.w0;
     other = (P.fft.npass & 1) ? b.w0 : b.w1;
-    block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, b.tw, tid, nthr, BlockSync{});
+    block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, b.tw, tid, nthr, sync);
     nl_products(P, res, (float*)other, m, tid, nthr);
-    __syncthreads();
+    sync();
     if (zmf) {
       nl_reduce((const float*)other, b.sums, N, m, tid, nthr);
-      __syncthreads();
+      sync();
     }
   }
   // forward: input in res, passes ping-pong other <-> res
   float2* fres = io_result_buf(P.fft, other, res);
-  block_fft_io<false>(P.fft, LinMap{res, N}, other, res, LinMap{fres, N}, m, b.tw, tid, nthr, BlockSync{});
+  block_fft_io<false>(P.fft, LinMap{res, N}, other, res, LinMap{fres, N}, m, b.tw, tid, nthr, sync);
   for (int t = tid; t < m * M; t += nthr) {
     const int i = t / M, k = t - i * M;
     float2 nv = make_float2(0.f, 0.f);
@@ -278,7 +278,7 @@ __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m,
     if (stage < 0) X_out[t] = nv;
     else stage_update(P, b, i, k, stage, nv, M, 0);
   }
-  __syncthreads();
+  sync();
 }
 
 // First-pass source of the trajectory output: instances 2p and 2p+1 packed as one complex sequence.
@@ -319,13 +319,13 @@ struct EmitOut {
 
 // Physical output of m states (pairs packed in one complex FFT); with `fuse` the pack is the first
 // pass's source and the global stores the last pass's sink, else each is a phase of its own.
-template <bool fuse>
+template <bool fuse, class Sync = BlockSync>
 __device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, int64_t inst_stride, int tid,
-                          int nthr) {
+                          int nthr, const Sync& sync = Sync{}) {
   const int pairs = (m + 1) / 2;
   if constexpr (fuse) {
     block_fft_io<true>(P.fft, EmitSrc{&P, b.U, m}, b.w0, b.w1, EmitOut{out, inst_stride, m}, pairs, b.tw, tid,
-                       nthr, BlockSync{});
+                       nthr, sync);
     return;
   }
   const int N = P.N;
@@ -334,16 +334,139 @@ __device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, in
     const int p = t / N, k = t - p * N;
     b.w0[t] = src(p, k);
   }
-  __syncthreads();
+  sync();
   float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
-  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, b.tw, tid, nthr, BlockSync{});
+  block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, b.tw, tid, nthr, sync);
   for (int t = tid; t < pairs * N; t += nthr) {
     const int p = t / N, x = t - p * N;
     const float2 z = res[t];
     out[(int64_t)(2 * p) * inst_stride + x] = z.x;
     if (2 * p + 1 < m) out[(int64_t)(2 * p + 1) * inst_stride + x] = z.y;
   }
-  __syncthreads();
+  sync();
+}
+
+// One work item (m instances of one plan) through all its steps, by the threads tid < nthr of a group
+// that synchronises with `sync` (the whole block).  `sm`: the
+// group's dynamic shared memory of smem_bytes; `gslot`: its global slot for state buffers that do not
+// fit there (NULL when they always fit).
+template <bool FUSE, class Sync>
+__device__ void run_item(const Item1D& item, const PlanDev& P, float2* sm, int smem_bytes, float* sums,
+                         float2* gslot, int nsteps, int mode, int project, int include_init, int tid, int nthr,
+                         const Sync& sync) {
+  const int N = P.N, M = P.M, m = item.m;
+  // carve shared memory: the ETDRK state buffers and the two work buffers when the item fits in the
+  // launch's reservation; otherwise the state buffers live in this CTA's global slot (L2-resident)
+  // and only the work buffers in shared memory (the work queue reserves what keeps 3 CTAs per SM)
+  Bufs b;
+  const size_t state_elems = (size_t)nbuf_for_order(P.order) * m * M, work_elems = 2 * (size_t)m * N;
+  const bool local = (state_elems + work_elems) * sizeof(float2) <= (size_t)smem_bytes;
+  float2* q = local ? sm : gslot;
+  b.U = q;
+  q += m * M;
+  b.S1 = b.S = b.N0 = b.N1 = b.N2 = nullptr;
+  if (P.order == 2) {
+    b.S = q; q += m * M;
+    b.N0 = q; q += m * M;
+  } else if (P.order == 3) {
+    b.S = q; q += m * M;
+    b.N0 = q; q += m * M;
+    b.N1 = q; q += m * M;
+  } else if (P.order == 4) {
+    b.S1 = q; q += m * M;
+    b.S = q; q += m * M;
+    b.N0 = q; q += m * M;
+    b.N1 = q; q += m * M;
+    b.N2 = q; q += m * M;
+  }
+  if (!local) q = sm;
+  b.w0 = q;
+  q += m * N;
+  b.w1 = q;
+  q += m * N;
+  b.sums = sums;
+  // the twiddles go into the dynamic shared memory left over by this item (the launch reserves the
+  // largest item's footprint, or room for them); the copy is complete at the barrier below
+  if ((size_t)(q - sm + N) * sizeof(float2) <= (size_t)smem_bytes) {
+    for (int i = tid; i < N; i += nthr) q[i] = __ldg(P.tw + i);
+    b.tw = q;
+  } else {
+    b.tw = P.tw;
+  }
+
+  // ---- load initial state
+  if (mode == MODE_TRAJ || mode == MODE_FINAL) {
+    const float* u0 = (const float*)item.in;
+    const int pairs = (m + 1) / 2;
+    for (int t = tid; t < pairs * N; t += nthr) {
+      const int p = t / N, x = t - p * N;
+      const float a = u0[(int64_t)(2 * p) * item.in_stride + x];
+      const float bb = (2 * p + 1 < m) ? u0[(int64_t)(2 * p + 1) * item.in_stride + x] : 0.f;
+      b.w0[t] = make_float2(a, bb);
+      if (mode == MODE_TRAJ && include_init) {
+        float* o = (float*)item.out;
+        o[(int64_t)(2 * p) * item.out_stride + x] = a;
+        if (2 * p + 1 < m) o[(int64_t)(2 * p + 1) * item.out_stride + x] = bb;
+      }
+    }
+    sync();
+    float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
+    block_fft<false>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, b.tw, tid, nthr, sync);
+    for (int t = tid; t < pairs * M; t += nthr) {
+      const int p = t / M, k = t - p * M;
+      float2 A, B;
+      unpack_pair(res[p * N + k], res[p * N + (k == 0 ? 0 : N - k)], A, B);
+      b.U[(2 * p) * M + k] = A;
+      if (2 * p + 1 < m) b.U[(2 * p + 1) * M + k] = B;
+    }
+  } else {
+    const float2* uh = (const float2*)item.in;
+    for (int t = tid; t < m * M; t += nthr) {
+      const int i = t / M, k = t - i * M;
+      b.U[t] = uh[(int64_t)i * item.in_stride + k];
+    }
+  }
+  sync();
+
+  // ---- time steps
+  const int nstages = (P.order == 0 || P.kind == EXGB_NL_ZERO) ? 0 : P.order;
+  for (int step = 0; step < nsteps; ++step) {
+    if (nstages == 0) {
+      for (int t = tid; t < m * M; t += nthr) {
+        const int k = t % M;
+        b.U[t] = cmul(ldg2(P.E + k), b.U[t]);
+      }
+      sync();
+    } else {
+      for (int s = 0; s < nstages; ++s) {
+        const float2* X = (s == 0) ? b.U : (P.order == 4 && s == 1) ? b.S1 : b.S;
+        nl_eval<FUSE>(P, b, X, m, s, nullptr, tid, nthr, sync);
+      }
+    }
+    if (project) {
+      // c2r of the step's physical round trip drops Im at DC and Nyquist
+      for (int i = tid; i < m; i += nthr) {
+        b.U[i * M].y = 0.f;
+        if ((N & 1) == 0) b.U[i * M + N / 2].y = 0.f;
+      }
+      sync();
+    }
+    if (mode == MODE_TRAJ) {
+      float* o = (float*)item.out + (int64_t)(step + include_init) * N;
+      emit_phys<FUSE>(P, b, m, o, item.out_stride, tid, nthr, sync);
+    }
+  }
+
+  // ---- final store
+  if (mode == MODE_FINAL) {
+    emit_phys<FUSE>(P, b, m, (float*)item.out, item.out_stride, tid, nthr, sync);
+  } else if (mode == MODE_FOURIER) {
+    float2* o = (float2*)item.out;
+    for (int t = tid; t < m * M; t += nthr) {
+      const int i = t / M, k = t - i * M;
+      o[(int64_t)i * item.out_stride + k] = b.U[t];
+    }
+  }
 }
 
 template <bool FUSE>
@@ -364,120 +487,8 @@ __global__ void __launch_bounds__(256, 3) etdrk1d_kernel(const Item1D* __restric
     const Item1D item = items[it];
     copy_plan(&Ps, item.plan, tid, nthr);
     __syncthreads();
-    const PlanDev& P = Ps;
-    const int N = P.N, M = P.M, m = item.m;
-    // carve shared memory: the ETDRK state buffers and the two work buffers when the item fits in the
-    // launch's reservation; otherwise the state buffers live in this CTA's global slot (L2-resident)
-    // and only the work buffers in shared memory (the work queue reserves what keeps 3 CTAs per SM)
-    Bufs b;
-    const size_t state_elems = (size_t)nbuf_for_order(P.order) * m * M, work_elems = 2 * (size_t)m * N;
-    const bool local = (state_elems + work_elems) * sizeof(float2) <= (size_t)smem_bytes;
-    float2* q = local ? sm : gstate + (int64_t)blockIdx.x * gstate_stride;
-    b.U = q;
-    q += m * M;
-    b.S1 = b.S = b.N0 = b.N1 = b.N2 = nullptr;
-    if (P.order == 2) {
-      b.S = q; q += m * M;
-      b.N0 = q; q += m * M;
-    } else if (P.order == 3) {
-      b.S = q; q += m * M;
-      b.N0 = q; q += m * M;
-      b.N1 = q; q += m * M;
-    } else if (P.order == 4) {
-      b.S1 = q; q += m * M;
-      b.S = q; q += m * M;
-      b.N0 = q; q += m * M;
-      b.N1 = q; q += m * M;
-      b.N2 = q; q += m * M;
-    }
-    if (!local) q = sm;
-    b.w0 = q;
-    q += m * N;
-    b.w1 = q;
-    q += m * N;
-    b.sums = s_sums;
-    // the twiddles go into the dynamic shared memory left over by this item (the launch reserves the
-    // largest item's footprint, or room for them); the copy is complete at the barrier below
-    if ((size_t)(q - sm + N) * sizeof(float2) <= (size_t)smem_bytes) {
-      for (int i = tid; i < N; i += nthr) q[i] = __ldg(P.tw + i);
-      b.tw = q;
-    } else {
-      b.tw = P.tw;
-    }
-
-    // ---- load initial state
-    if (mode == MODE_TRAJ || mode == MODE_FINAL) {
-      const float* u0 = (const float*)item.in;
-      const int pairs = (m + 1) / 2;
-      for (int t = tid; t < pairs * N; t += nthr) {
-        const int p = t / N, x = t - p * N;
-        const float a = u0[(int64_t)(2 * p) * item.in_stride + x];
-        const float bb = (2 * p + 1 < m) ? u0[(int64_t)(2 * p + 1) * item.in_stride + x] : 0.f;
-        b.w0[t] = make_float2(a, bb);
-        if (mode == MODE_TRAJ && include_init) {
-          float* o = (float*)item.out;
-          o[(int64_t)(2 * p) * item.out_stride + x] = a;
-          if (2 * p + 1 < m) o[(int64_t)(2 * p + 1) * item.out_stride + x] = bb;
-        }
-      }
-      __syncthreads();
-      float2* res = (P.fft.npass & 1) ? b.w1 : b.w0;
-      block_fft<false>(P.fft, b.w0, b.w1, LinMap{res, N}, pairs, b.tw, tid, nthr, BlockSync{});
-      for (int t = tid; t < pairs * M; t += nthr) {
-        const int p = t / M, k = t - p * M;
-        float2 A, B;
-        unpack_pair(res[p * N + k], res[p * N + (k == 0 ? 0 : N - k)], A, B);
-        b.U[(2 * p) * M + k] = A;
-        if (2 * p + 1 < m) b.U[(2 * p + 1) * M + k] = B;
-      }
-    } else {
-      const float2* uh = (const float2*)item.in;
-      for (int t = tid; t < m * M; t += nthr) {
-        const int i = t / M, k = t - i * M;
-        b.U[t] = uh[(int64_t)i * item.in_stride + k];
-      }
-    }
-    __syncthreads();
-
-    // ---- time steps
-    const int nstages = (P.order == 0 || P.kind == EXGB_NL_ZERO) ? 0 : P.order;
-    for (int step = 0; step < nsteps; ++step) {
-      if (nstages == 0) {
-        for (int t = tid; t < m * M; t += nthr) {
-          const int k = t % M;
-          b.U[t] = cmul(ldg2(P.E + k), b.U[t]);
-        }
-        __syncthreads();
-      } else {
-        for (int s = 0; s < nstages; ++s) {
-          const float2* X = (s == 0) ? b.U : (P.order == 4 && s == 1) ? b.S1 : b.S;
-          nl_eval<FUSE>(P, b, X, m, s, nullptr, tid, nthr);
-        }
-      }
-      if (project) {
-        // c2r of the step's physical round trip drops Im at DC and Nyquist
-        for (int i = tid; i < m; i += nthr) {
-          b.U[i * M].y = 0.f;
-          if ((N & 1) == 0) b.U[i * M + N / 2].y = 0.f;
-        }
-        __syncthreads();
-      }
-      if (mode == MODE_TRAJ) {
-        float* o = (float*)item.out + (int64_t)(step + include_init) * N;
-        emit_phys<FUSE>(P, b, m, o, item.out_stride, tid, nthr);
-      }
-    }
-
-    // ---- final store
-    if (mode == MODE_FINAL) {
-      emit_phys<FUSE>(P, b, m, (float*)item.out, item.out_stride, tid, nthr);
-    } else if (mode == MODE_FOURIER) {
-      float2* o = (float2*)item.out;
-      for (int t = tid; t < m * M; t += nthr) {
-        const int i = t / M, k = t - i * M;
-        o[(int64_t)i * item.out_stride + k] = b.U[t];
-      }
-    }
+    run_item<FUSE>(item, Ps, sm, smem_bytes, s_sums, gstate ? gstate + (int64_t)blockIdx.x * gstate_stride : nullptr,
+                   nsteps, mode, project, include_init, tid, nthr, BlockSync{});
     __syncthreads();
   }
 }
