@@ -111,18 +111,24 @@ __device__ __forceinline__ double2 zs(double s) { return make_double2(s, 0.0); }
 // _etdrk_4.py:175-196 (contour means, real part), _etdrk_3/4 :156/:170 (E_half).
 // Output index: same as input (1D, or 2D row-major) or ky-major for 2D
 // when `transpose_2d` is set.
-__global__ void coef_kernel(const double2* __restrict__ L, int64_t total, int N, int M, int transpose_2d, double dt,
+__global__ void coef_kernel(const double2* __restrict__ L, int64_t total, int N, int M, int layout, double dt,
                             int ncp, double radius, int order, float2* __restrict__ E, float2* __restrict__ Eh,
                             float* __restrict__ c, int64_t nmodes_all) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
   int64_t o = i;
-  if (transpose_2d) {
+  if (layout == 1) {
     const int64_t per = (int64_t)N * M;
     const int64_t ch = i / per;
     const int64_t r = i - ch * per;
     const int64_t kx = r / M, ky = r - kx * M;
     o = ch * per + ky * N + kx;
+  } else if (layout == 2) {
+    const int64_t pl = (int64_t)N * N, per = pl * M;
+    const int64_t ch = i / per;
+    const int64_t r = i - ch * per;
+    const int64_t q = r / M, kz = r - q * M;  // q = kx N + ky
+    o = ch * per + kz * pl + q;
   }
   const double2 Ldt = make_double2(L[i].x * dt, L[i].y * dt);
   const double2 e = zexp(Ldt);
@@ -270,6 +276,12 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
       if (pick == "fused") want_staged = false;
       if (pick == "staged") want_staged = true;
       staged = !smooth || N > 1024 || (want_staged && ndgen_pass2d(d));
+    } else if (d.num_spatial_dims == 3 &&
+               (d.nonlin_kind == EXGB_NL_PROJECTED_3D || d.nonlin_kind == EXGB_NL_PROJECTED_3D_KOLMOGOROV)) {
+      // 3D projected convection runs on the three-pass path where it holds the plan (N = 32, 64),
+      // on the five-kernel path of exgb_3d.cu otherwise; EXGB_3D_PATH=generic forces the latter
+      const char* path = getenv("EXGB_3D_PATH");
+      staged = !(path && std::string(path) == "generic") && ndgen_pass3d(d);
     }
   }
   if (d.order >= 1 && d.nonlin_kind != EXGB_NL_ZERO) {
@@ -391,8 +403,14 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   for (int i = 0; i < D - 1; ++i) per *= (size_t)N;
   p->n_modes = per;
   const size_t nall = per * (size_t)v.lin_ch;
-  const bool transpose = (D == 2 && d.order >= 1 && (!staged || ndgen_pass2d(d)));
-  p->tables_transposed = transpose ? 1 : 0;
+  // layout of the coefficient tables: 1 = [lin_ch][ky][kx] (2D fused and three-pass paths),
+  // 2 = [lin_ch][kz][kx][ky] (3D three-pass path), 0 = natural
+  const char* path3 = getenv("EXGB_3D_PATH");
+  const bool generic3 = path3 && std::string(path3) == "generic";
+  const int transpose = (D == 2 && d.order >= 1 && (!staged || ndgen_pass2d(d)))                  ? 1
+                        : (D == 3 && d.order >= 1 && staged && !generic3 && ndgen_pass3d(d)) ? 2
+                                                                                              : 0;
+  p->tables_transposed = transpose;
   double2* d_L = nullptr;
   cudaError_t e;
   if ((e = cudaMalloc(&d_L, sizeof(double2) * nall)) != cudaSuccess ||
@@ -412,7 +430,7 @@ int exgb_plan_create(const exgb_plan_desc* desc, exgb_plan** out) {
   {
     const int th = 128;
     const int64_t blocks = ((int64_t)nall + th - 1) / th;
-    coef_kernel<<<(unsigned)blocks, th>>>(d_L, (int64_t)nall, N, M, transpose ? 1 : 0, d.dt, d.num_circle_points,
+    coef_kernel<<<(unsigned)blocks, th>>>(d_L, (int64_t)nall, N, M, transpose, d.dt, d.num_circle_points,
                                           d.circle_radius, d.order, p->d_E, p->d_Eh, p->d_c, (int64_t)nall);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -459,14 +477,21 @@ int exgb_plan_get_table(const exgb_plan* plan, int which, void* host_out, size_t
                                  : (const void*)(plan->d_c + (size_t)(which - 2) * nall);
   std::vector<char> tmp(need);
   EXGB_CUDA(cudaMemcpy(tmp.data(), src, need, cudaMemcpyDeviceToHost));
-  const bool transposed = plan->tables_transposed != 0;
-  if (!transposed) {
+  if (plan->tables_transposed == 0) {
     std::memcpy(host_out, tmp.data(), need);
     return EXGB_OK;
   }
   const int N = plan->dev.N, M = plan->dev.M;
   const size_t es = cplx ? sizeof(float2) : sizeof(float);
   char* dst = (char*)host_out;
+  if (plan->tables_transposed == 2) {
+    const size_t pl = (size_t)N * N, per = pl * M;
+    for (int ch = 0; ch < plan->dev.lin_ch; ++ch)
+      for (size_t q = 0; q < pl; ++q)
+        for (int kz = 0; kz < M; ++kz)
+          std::memcpy(dst + (ch * per + q * M + kz) * es, tmp.data() + (ch * per + kz * pl + q) * es, es);
+    return EXGB_OK;
+  }
   for (int ch = 0; ch < plan->dev.lin_ch; ++ch)
     for (int kx = 0; kx < N; ++kx)
       for (int ky = 0; ky < M; ++ky) {

@@ -91,7 +91,8 @@ struct exgb_plan {
   long long tc_first_wait_budget = 0;
   // stepped by the staged N-D path (exgb_ndgen.cu) instead of a fused kernel
   int staged = 0;
-  // 2D coefficient tables stored [lin_ch][ky][kx] (the fused 2D kernels' layout)
+  // coefficient table layout: 0 natural, 1 = 2D [lin_ch][ky][kx] (the fused 2D kernels' and the 2D
+  // three-pass layout), 2 = 3D [lin_ch][kz][kx][ky] (the 3D three-pass layout)
   int tables_transposed = 0;
 };
 
@@ -137,6 +138,7 @@ int tcdft2d_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2
 bool ndgen_handles(const exgb_plan_desc& d);
 bool ndgen_can(const exgb_plan_desc& d);
 bool ndgen_pass2d(const exgb_plan_desc& d);
+bool ndgen_pass3d(const exgb_plan_desc& d);
 // 0 when rfftn / irfftn take transforms of length n on this device (any n with a prime factor
 // above 5 up to the Bluestein limit, 2^a 3^b 5^c of any length in 1D), else an EXGB_E* code
 int transform_supported(int n);

@@ -145,6 +145,9 @@ bool ndgen_can(const exgb_plan_desc& d) {
     case EXGB_NL_VORTICITY_2D:
     case EXGB_NL_VORTICITY_2D_KOLMOGOROV:
       return d.num_spatial_dims == 2;
+    case EXGB_NL_PROJECTED_3D:
+    case EXGB_NL_PROJECTED_3D_KOLMOGOROV:
+      return d.num_spatial_dims == 3;
     default:
       return false;
   }
@@ -199,6 +202,11 @@ int ndgen_validate(const exgb_plan_desc& d) {
     case EXGB_NL_VORTICITY_2D_KOLMOGOROV:
       if (D != 2) return fail(EXGB_EUNSUPPORTED, "vorticity convection needs num_spatial_dims == 2");
       if (C != 1) return fail(EXGB_ESHAPE, "vorticity formulation has one channel");
+      return EXGB_OK;
+    case EXGB_NL_PROJECTED_3D:
+    case EXGB_NL_PROJECTED_3D_KOLMOGOROV:
+      if (D != 3) return fail(EXGB_EUNSUPPORTED, "projected convection needs num_spatial_dims == 3");
+      if (C != 3) return fail(EXGB_ESHAPE, "Number of channels in u_hat should match number of spatial dimensions");
       return EXGB_OK;
     default:
       return fail(EXGB_EUNSUPPORTED, "nonlinear function not handled by the staged path");
@@ -261,6 +269,12 @@ static Prog make_prog(const exgb_plan_desc& d) {
       p.NF = 1;
       p.s0 = -b;
       break;
+    case EXGB_NL_PROJECTED_3D:
+    case EXGB_NL_PROJECTED_3D_KOLMOGOROV:
+      p.op = OP_PROJ3D;
+      p.NI = 6;
+      p.NF = 3;
+      break;
     default:  // Gray-Scott
       p.op = OP_GRAY_SCOTT;
       p.NI = p.NF = 2;
@@ -281,6 +295,18 @@ bool ndgen_pass2d(const exgb_plan_desc& d) {
   if (d.num_spatial_dims != 2) return false;
   const Prog p = make_prog(d);
   return pass2d_supported(2, d.num_points, p.NI, p.NF);
+}
+
+bool pass3d_supported(int D, int N, int NI, int NF);
+int pass3d_run(const exgb_plan* plan, const ndg::Geo& g, const ndg::Prog& p, cudaStream_t st, const float2* in,
+               float2* out, int64_t batch, int nsteps, int project, int nonlinear_only);
+
+// Does a 3D staged plan of this description run on the three-pass path (exgb_pass3d.cu)?  Its
+// coefficient tables are then plane-major ([lin_ch][kz][kx][ky]).
+bool ndgen_pass3d(const exgb_plan_desc& d) {
+  if (d.num_spatial_dims != 3 || !ndgen_can(d)) return false;
+  const Prog p = make_prog(d);
+  return pass3d_supported(3, d.num_points, p.NI, p.NF);
 }
 
 // Fourier-space stepping (nsteps steps, c2r projection after each when
@@ -305,6 +331,8 @@ int ndgen_run(const exgb_plan* plan, cudaStream_t st, const float2* in, float2* 
   if (batch == 0) return EXGB_OK;
   if (P.D == 2 && plan->tables_transposed)
     return pass2d_run(plan, g, p, st, in, out, batch, nsteps, project, nonlinear_only);
+  if (P.D == 3 && plan->tables_transposed)
+    return pass3d_run(plan, g, p, st, in, out, batch, nsteps, project, nonlinear_only);
   if (!nonlinear_only && nsteps == 0) {
     if (in != out) EXGB_CUDA(cudaMemcpyAsync(out, in, sizeof(float2) * batch * C * g.per, cudaMemcpyDeviceToDevice, st));
     return EXGB_OK;

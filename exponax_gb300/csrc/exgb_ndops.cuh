@@ -26,6 +26,9 @@ enum Op {
   OP_BZ,                // F[u0 + u1 - u0 u1 - u0^2], F[u2 - u1 - u0 u1], F[u0 - u2]  (_belousov_zhabotinsky.py:33-51)
   OP_VORT,              // -b F[u w_x + v w_y], (u, v) = (d_y, -d_x) Lap^-1 w  (_vorticity_convection.py:78-99),
                         // + the Kolmogorov injection at (0, k)               (_vorticity_convection.py:166-176)
+  OP_PROJ3D,            // P F[u x (curl u)], curl = i k x u^ (mask), P the Leray projection
+                        // (_projected_convection.py:114-136, _leray.py:114-136) + the 3D Kolmogorov
+                        // injection at (0, k, 0), first channel (_projected_convection.py:202-220)
 };
 
 struct Geo {
@@ -120,6 +123,19 @@ __device__ __forceinline__ void derive_mode(const Geo& g, const Prog& p, const i
         w[2 * ws] = times_i(d[0], wv);
         w[3 * ws] = times_i(d[1], wv);
       } break;
+      case OP_PROJ3D: {
+        // w[0..2] = mask (i d x u^) (the curl), w[3..5] = mask u^
+        const float2 u0 = m ? x[0] : z, u1 = m ? x[xs] : z, u2 = m ? x[2 * xs] : z;
+        const float2 a1 = make_float2(d[1] * u2.x - d[2] * u1.x, d[1] * u2.y - d[2] * u1.y);
+        const float2 a2 = make_float2(d[2] * u0.x - d[0] * u2.x, d[2] * u0.y - d[0] * u2.y);
+        const float2 a3 = make_float2(d[0] * u1.x - d[1] * u0.x, d[0] * u1.y - d[1] * u0.y);
+        w[0] = make_float2(-a1.y, a1.x);
+        w[ws] = make_float2(-a2.y, a2.x);
+        w[2 * ws] = make_float2(-a3.y, a3.x);
+        w[3 * ws] = u0;
+        w[4 * ws] = u1;
+        w[5 * ws] = u2;
+      } break;
       default:  // the masked state itself, one spectrum per channel
         for (int c = 0; c < g.C; ++c) w[c * ws] = m ? x[c * xs] : z;
         break;
@@ -184,6 +200,12 @@ __device__ __forceinline__ void pointwise_point(const Geo& g, const Prog& p, con
       case OP_VORT:
         f[0] = fmaf(in[0], in[2], in[1] * in[3]);
         break;
+      case OP_PROJ3D: {  // velocity (in[3..5]) x curl (in[0..2])
+        const float w0 = in[0], w1 = in[1], w2 = in[2], v0 = in[3], v1 = in[4], v2 = in[5];
+        f[0] = v1 * w2 - v2 * w1;
+        f[fs] = v2 * w0 - v0 * w2;
+        f[2 * fs] = v0 * w1 - v1 * w0;
+      } break;
       case OP_BZ: {
         const float u0 = in[0], u1 = in[1], u2 = in[2];
         const float u01 = u0 * u1;
@@ -232,12 +254,29 @@ __device__ __forceinline__ void combine_mode(const PlanDev& P, const Geo& g, con
         case OP_CAHN_HILLIARD:
           nv[0] = cscale(h[0], p.s0 * lap);
           break;
+        case OP_PROJ3D: {
+          // Leray: n + (i d) q, q = -inv_lap (i d . n), inv_lap = 1/lap (0 at k = 0), lap = -|d|^2
+          float2 n0 = h[0], n1 = h[hs], n2 = h[2 * hs];
+          if (lap != 0.f) {
+            const float il = 1.f / lap;
+            const float2 sd = make_float2(d[0] * n0.x + d[1] * n1.x + d[2] * n2.x, d[0] * n0.y + d[1] * n1.y + d[2] * n2.y);
+            const float2 dv = make_float2(-sd.y, sd.x);
+            const float2 q = make_float2(-il * dv.x, -il * dv.y);
+            n0 = cadd(n0, make_float2(-d[0] * q.y, d[0] * q.x));
+            n1 = cadd(n1, make_float2(-d[1] * q.y, d[1] * q.x));
+            n2 = cadd(n2, make_float2(-d[2] * q.y, d[2] * q.x));
+          }
+          nv[0] = n0;
+          nv[1] = n1;
+          nv[2] = n2;
+        } break;
         default:  // -b F[.] (non-conservative convection, vorticity) or F[.] (polynomial, Gray-Scott): scale s0
           for (int c = 0; c < g.C; ++c) nv[c] = cscale(h[(c) * hs], p.s0);
           break;
       }
     }
   if (p.op == OP_VORT && k[0] == 0 && k[1] == P.inj_mode) nv[0].x += P.inj_value;
+  if (p.op == OP_PROJ3D && P.inj_mode >= 0 && k[0] == 0 && k[1] == P.inj_mode && k[2] == 0) nv[0].x += P.inj_value;
 }
 
 }  // namespace ndg

@@ -1,0 +1,488 @@
+// exgb_pass3d.cu -- 3D ETDRK stages (projected convection + Leray, and the nonlinearities of the
+// staged N-D path) in three fused passes per stage, for N = 32 and 64.
+//
+// The 3D counterpart of exgb_pass2d.cu: the rfft axis z takes the role of the 2D column index.
+//   pass 1  per (kz plane, derived field): the field's spectrum on the plane (pre-mask, exgb_ndops.cuh),
+//           2D inverse transform over (kx, ky) in shared memory          -> W[f][kz][x][y]
+//   pass 2  per (x, tile of y): for each of the NI fields the c2r transform along z (two lines packed
+//           in one complex transform, 1/N^3 folded in), the pointwise products (the cross product u x
+//           curl u for projected convection), the r2c transforms of the NF products -> Hq[f][kz][x][y]
+//   pass 3  per kz plane: the NF fields' 2D forward transforms, post-mask, multipliers (Leray
+//           projection and forcing for projected convection) and the ETDRK stage update
+// Only the Kc = K + 1 planes inside the dealiasing mask take part; the planes above it feel the linear
+// part alone and are advanced by E once per step from the input in one elementwise kernel.  State and
+// stage buffers are plane-major ([c][kz][kx][ky], kz < Kc), the coefficient tables of such plans
+// plane-major over all N/2 + 1 planes; transposes at the call boundary.  Transforms are register
+// (group) FFTs (exgb_regfft.cuh).
+//
+// Reference: nonlin_fun/_projected_convection.py:114-226, _leray.py:114-136, nonlin_fun/_base.py:73-137,
+// the nonlinear functions named in exgb_ndops.cuh, etdrk/_etdrk_1..4.py.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "exgb_internal.h"
+#include "exgb_ndops.cuh"
+#include "exgb_regfft.cuh"
+#include "exgb_stage.cuh"
+
+namespace exgb {
+
+void* workspace(size_t bytes, int slot_offset);
+
+namespace p3d {
+
+using ndg::Geo;
+using ndg::MAXC;
+using ndg::Prog;
+
+struct Args {
+  PlanDev P;
+  Geo g;
+  Prog p;
+  const float2* tw;  // N twiddles
+  int N, M, K, Kc;
+  int TY;            // y lines per pass-2 CTA
+  int64_t pl;        // N * N modes of a plane
+  int64_t cstride;   // Kc * pl: one channel of the plane-major state
+  int64_t sstride;   // C * cstride
+  int64_t tstride;   // M * pl: one coefficient set (plane-major tables)
+  StageBufs sb;
+  const float2* xin;
+  float2* W;         // [s][f < NI][kz < Kc][x][y]
+  float2* Hq;        // [s][f < NF][kz < Kc][x][y]
+  int stage;         // -1: nonlinear term only, written to nout (natural layout [s][c][kx][ky][kz])
+  float2* nout;
+};
+
+__device__ __forceinline__ int sgn_of(int i, int N) { return (i <= (N - 1) / 2) ? i : i - N; }
+
+template <int N>
+struct Cfg {
+  static constexpr int E = RegCfg<N>::E, T = RegCfg<N>::T;
+  static constexpr int THREADS = 256, NG = THREADS / T;
+  static constexpr int TS = tile_stride<E, T>();
+  static constexpr int PS = N + 1;  // padded row stride of a plane in shared memory
+  static constexpr int PLANE = N * PS;
+  // float2 offsets: twiddles, transpose tiles, then the pass's planes / buffers
+  static constexpr int TWL = 0, TILES = N, FREE = N + NG * TS;
+};
+
+template <int N>
+__device__ __forceinline__ void load_twl(float2* twl, const float2* __restrict__ tw) {
+  constexpr int T = RegCfg<N>::T;
+  for (int t = threadIdx.x; t < N; t += blockDim.x) {
+    const int k1 = t / T, ll = t % T;
+    twl[t] = __ldg(tw + ((ll * k1) % N));
+  }
+}
+
+template <int N>
+__device__ __forceinline__ unsigned group_mask() {
+  constexpr int T = RegCfg<N>::T;
+  const int lane = threadIdx.x & 31;
+  return (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
+}
+
+// 2D transform of `np` planes (each N x N, row stride PS) in shared memory: rows, then columns
+template <int N, bool INV>
+__device__ __forceinline__ void planes_fft(float2* planes, int np, float2* tiles, const float2* twl) {
+  using R = Cfg<N>;
+  const int gi = threadIdx.x / R::T, l = threadIdx.x % R::T;
+  const unsigned gmask = group_mask<N>();
+  float2* tile = tiles + (size_t)gi * R::TS;
+  for (int q = gi; q < np * N; q += R::NG) {  // row r of plane pi
+    float2* row = planes + (size_t)(q / N) * R::PLANE + (size_t)(q % N) * R::PS;
+    float2 v[R::E];
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) v[j] = row[l + R::T * j];
+    group_fft<R::E, R::T, INV>(v, l, tile, twl, gmask);
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) row[l + R::T * j] = v[j];
+  }
+  __syncthreads();
+  for (int q = gi; q < np * N; q += R::NG) {  // column c of plane pi
+    float2* col = planes + (size_t)(q / N) * R::PLANE + (q % N);
+    float2 v[R::E];
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) v[j] = col[(size_t)(l + R::T * j) * R::PS];
+    group_fft<R::E, R::T, INV>(v, l, tile, twl, gmask);
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) col[(size_t)(l + R::T * j) * R::PS] = v[j];
+  }
+  __syncthreads();
+}
+
+// ---- pass 1: one derived field on one kz plane, 2D inverse over (kx, ky)
+template <int N>
+__global__ void __launch_bounds__(Cfg<N>::THREADS) pass1_3d_kernel(const Args a) {
+  using R = Cfg<N>;
+  extern __shared__ __align__(16) float2 sp1[];
+  float2* twl = sp1 + R::TWL;
+  float2* plane = sp1 + R::FREE;
+  const int kz = blockIdx.x, f = blockIdx.y;
+  const int64_t s = blockIdx.z;
+  load_twl<N>(twl, a.tw);
+  const float2* xs = a.xin + s * a.sstride + (int64_t)kz * a.pl;
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+    const int kx = e / N, ky = e - kx * N;
+    const int k[3] = {sgn_of(kx, N), sgn_of(ky, N), kz};
+    const bool m = abs(k[0]) <= a.K && abs(k[1]) <= a.K && kz <= a.K;
+    float2 w[MAXC + MAXC * 3];
+    ndg::derive_mode(a.g, a.p, k, m, xs + e, a.cstride, w, 1);
+    plane[(size_t)kx * R::PS + ky] = w[f];
+  }
+  __syncthreads();
+  planes_fft<N, true>(plane, 1, sp1 + R::TILES, twl);
+  float2* W = a.W + ((s * a.p.NI + f) * a.Kc + kz) * a.pl;
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) W[e] = plane[(size_t)(e / N) * R::PS + (e % N)];
+}
+
+// ---- pass 2: lines along z at (x, y0 .. y0 + TY): c2r, pointwise, r2c
+template <int N>
+__global__ void __launch_bounds__(Cfg<N>::THREADS) pass2_3d_kernel(const Args a) {
+  using R = Cfg<N>;
+  constexpr int E = R::E, T = R::T, M = N / 2 + 1;
+  extern __shared__ __align__(16) float2 sp2[];
+  float2* twl = sp2 + R::TWL;
+  const int NI = a.p.NI, NF = a.p.NF, TY = a.TY, Kc = a.Kc;
+  float* phys = reinterpret_cast<float*>(sp2 + R::FREE);           // [NI * TY][N]
+  float* prod = phys + (size_t)NI * TY * N;                         // [NF * TY][N]
+  float2* zb = reinterpret_cast<float2*>(prod + (size_t)NF * TY * N);  // [NF * TY / 2][N]
+  const int x = blockIdx.x / (N / TY), y0 = (blockIdx.x % (N / TY)) * TY;
+  const int64_t s = blockIdx.y;
+  load_twl<N>(twl, a.tw);
+  __syncthreads();
+  const int gi = threadIdx.x / T, l = threadIdx.x % T;
+  const unsigned gmask = group_mask<N>();
+  float2* tile = sp2 + R::TILES + (size_t)gi * R::TS;
+  // element (f, kz) of line (x, y) in W / Hq: ((s NI + f) Kc + kz) pl + x N + y
+  const float2* W = a.W + s * (int64_t)NI * Kc * a.pl + (int64_t)x * N + y0;
+  const float inv = 1.f / ((float)N * (float)N * (float)N);
+  const int ni = NI * TY / 2;
+  for (int j = gi; j < ni; j += R::NG) {
+    const int qa = 2 * j, qb = qa + 1;
+    const int fa = qa / TY, ya = qa - fa * TY, fb = qb / TY, yb = qb - fb * TY;
+    float2 v[E];
+#pragma unroll
+    for (int jj = 0; jj < E; ++jj) {
+      const int k = l + T * jj;
+      const bool ext = k >= M;
+      const int kk = ext ? N - k : k;
+      const bool real_only = (k == 0) || (k == N / 2);
+      float2 va = make_float2(0.f, 0.f), vb = va;
+      if (kk < Kc) {
+        va = W[((int64_t)fa * Kc + kk) * a.pl + ya];
+        vb = W[((int64_t)fb * Kc + kk) * a.pl + yb];
+      }
+      v[jj] = pack_pair(va, vb, ext, real_only);
+    }
+    group_fft<E, T, true>(v, l, tile, twl, gmask);
+#pragma unroll
+    for (int jj = 0; jj < E; ++jj) {
+      const int z = l + T * jj;
+      phys[(size_t)qa * N + z] = v[jj].x * inv;
+      phys[(size_t)qb * N + z] = v[jj].y * inv;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < TY * N; e += blockDim.x) {
+    const int yy = e / N, z = e - yy * N;
+    float in[MAXC + MAXC * 3];
+    for (int f = 0; f < NI; ++f) in[f] = phys[((size_t)f * TY + yy) * N + z];
+    ndg::pointwise_point(a.g, a.p, in, prod + (size_t)yy * N + z, (int64_t)TY * N);
+  }
+  __syncthreads();
+  const int nf = NF * TY / 2;
+  for (int j = gi; j < nf; j += R::NG) {
+    float2 v[E];
+#pragma unroll
+    for (int jj = 0; jj < E; ++jj) {
+      const int z = l + T * jj;
+      v[jj] = make_float2(prod[(size_t)(2 * j) * N + z], prod[(size_t)(2 * j + 1) * N + z]);
+    }
+    group_fft<E, T, false>(v, l, tile, twl, gmask);
+#pragma unroll
+    for (int jj = 0; jj < E; ++jj) zb[(size_t)j * N + l + T * jj] = v[jj];
+  }
+  __syncthreads();
+  float2* Hq = a.Hq + s * (int64_t)NF * Kc * a.pl + (int64_t)x * N + y0;
+  for (int e = threadIdx.x; e < nf * Kc; e += blockDim.x) {
+    const int j = e / Kc, k = e - j * Kc;
+    float2 P, Q;
+    unpack_pair(zb[(size_t)j * N + k], zb[(size_t)j * N + (k == 0 ? 0 : N - k)], P, Q);
+    const int qa = 2 * j, qb = qa + 1;
+    const int fa = qa / TY, ya = qa - fa * TY, fb = qb / TY, yb = qb - fb * TY;
+    Hq[((int64_t)fa * Kc + k) * a.pl + ya] = P;
+    Hq[((int64_t)fb * Kc + k) * a.pl + yb] = Q;
+  }
+}
+
+// ---- pass 3: the NF fields of one kz plane, 2D forward, combine, ETDRK update
+template <int N>
+__global__ void __launch_bounds__(Cfg<N>::THREADS) pass3_3d_kernel(const Args a) {
+  using R = Cfg<N>;
+  extern __shared__ __align__(16) float2 sp3[];
+  float2* twl = sp3 + R::TWL;
+  float2* planes = sp3 + R::FREE;  // [NF][N][PS]
+  const int NF = a.p.NF, C = a.g.C;
+  const int kz = blockIdx.x;
+  const int64_t s = blockIdx.y;
+  load_twl<N>(twl, a.tw);
+  for (int e = threadIdx.x; e < NF * N * N; e += blockDim.x) {
+    const int f = e / (N * N), r = e - f * N * N;
+    planes[(size_t)f * R::PLANE + (size_t)(r / N) * R::PS + (r % N)] =
+        a.Hq[((s * NF + f) * a.Kc + kz) * a.pl + r];
+  }
+  __syncthreads();
+  planes_fft<N, false>(planes, NF, sp3 + R::TILES, twl);
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+    const int kx = e / N, ky = e - kx * N;
+    const int k[3] = {sgn_of(kx, N), sgn_of(ky, N), kz};
+    const bool m = abs(k[0]) <= a.K && abs(k[1]) <= a.K && kz <= a.K;
+    float2 nv[MAXC];
+    ndg::combine_mode(a.P, a.g, a.p, k, m, planes + (size_t)kx * R::PS + ky, R::PLANE, nv);
+    if (a.stage < 0) {
+      float2* o = a.nout + s * (int64_t)C * a.tstride + ((int64_t)kx * N + ky) * a.M + kz;
+      for (int c = 0; c < C; ++c) o[c * a.tstride] = nv[c];
+      continue;
+    }
+    const int64_t r = (int64_t)kz * a.pl + e;
+    for (int c = 0; c < C; ++c) {
+      const int64_t ci = (a.P.lin_ch == 1 ? 0 : (int64_t)c * a.tstride) + r;
+      stage_upd_at(a.P, a.sb, s * a.sstride + c * a.cstride + r, ci, a.stage, nv[c]);
+    }
+  }
+}
+
+// natural [f][kx][ky][kz] (rows kx N + ky, M columns) <-> plane-major [f][kz][kx][ky] for kz < ncol;
+// `cols_stride` = elements per field on the plane-major side
+__global__ void transpose3_kernel(const float2* __restrict__ in, float2* __restrict__ out, int64_t rows, int M,
+                                  int ncol, int64_t cols_stride, int to_cols) {
+  __shared__ float2 tile[32][33];
+  const int64_t f = blockIdx.z;
+  const int64_t br = (int64_t)blockIdx.x * 32;
+  const int bc = blockIdx.y * 32;
+  const int64_t nat = rows * M;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    if (to_cols) {
+      const int64_t r = br + j;
+      const int c = bc + threadIdx.x;
+      if (r < rows && c < ncol) tile[j][threadIdx.x] = in[f * nat + r * M + c];
+    } else {
+      const int c = bc + j;
+      const int64_t r = br + threadIdx.x;
+      if (r < rows && c < ncol) tile[threadIdx.x][j] = in[f * cols_stride + (int64_t)c * rows + r];
+    }
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    if (to_cols) {
+      const int c = bc + j;
+      const int64_t r = br + threadIdx.x;
+      if (r < rows && c < ncol) out[f * cols_stride + (int64_t)c * rows + r] = tile[threadIdx.x][j];
+    } else {
+      const int64_t r = br + j;
+      const int c = bc + threadIdx.x;
+      if (r < rows && c < ncol) out[f * nat + r * M + c] = tile[j][threadIdx.x];
+    }
+  }
+}
+
+// c2r projection of a step's round trip on the plane-major state: planes kz = 0 and (N even, inside the
+// mask) kz = N/2, v(kx, ky) <- (v(kx, ky) + conj(v(-kx, -ky))) / 2; one thread per pair
+__global__ void project_planes_kernel(float2* __restrict__ U, int N, int Kc, int64_t cstride, int64_t fields) {
+  const int64_t pl = (int64_t)N * N;
+  const int64_t total = fields * 2 * pl;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = t / (2 * pl);
+    const int64_t rr = t - f * 2 * pl;
+    const int which = (int)(rr / pl);
+    const int64_t q = rr - which * pl;
+    const int kz = which == 0 ? 0 : N / 2;
+    if (which == 1 && ((N & 1) || kz >= Kc)) continue;
+    const int kx = (int)(q / N), ky = (int)(q % N);
+    const int64_t q2 = (int64_t)((N - kx) % N) * N + (N - ky) % N;
+    if (q2 < q) continue;
+    float2* base = U + f * cstride + (int64_t)kz * pl;
+    const float2 v1 = base[q], v2 = base[q2];
+    const float2 pv = make_float2(0.5f * (v1.x + v2.x), 0.5f * (v1.y - v2.y));
+    base[q] = pv;
+    base[q2] = cconj(pv);
+  }
+}
+
+// planes above the mask (kz >= Kc): nsteps of u <- E u, projection on kz = N/2; natural layout in and
+// out, E plane-major [lin_ch][kz][kx][ky]; one thread per {(kx, ky), (-kx, -ky)} pair
+__global__ void linear_planes_kernel(const float2* __restrict__ E, int lin_ch, int C, int N, int M, int Kc,
+                                     int64_t fields, const float2* __restrict__ in, float2* __restrict__ out,
+                                     int nsteps, int project, int zero) {
+  const int64_t pl = (int64_t)N * N;
+  const int np = M - Kc;
+  const int64_t total = fields * np * pl;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t f = t / (np * pl);
+    const int64_t rr = t - f * np * pl;
+    const int kz = Kc + (int)(rr / pl);
+    const int64_t q = rr % pl;
+    const int kx = (int)(q / N), ky = (int)(q % N);
+    const int64_t q2 = (int64_t)((N - kx) % N) * N + (N - ky) % N;
+    if (q2 < q) continue;
+    const int64_t base = f * pl * M;
+    const int64_t i1 = q * M + kz, i2 = q2 * M + kz;
+    if (zero) {
+      out[base + i1] = make_float2(0.f, 0.f);
+      out[base + i2] = make_float2(0.f, 0.f);
+      continue;
+    }
+    const int c = (int)(f % C);
+    const float2* Et = E + (lin_ch == 1 ? 0 : (int64_t)c * M * pl) + (int64_t)kz * pl;
+    const float2 e1 = Et[q], e2 = Et[q2];
+    float2 v1 = in[base + i1], v2 = in[base + i2];
+    const bool proj = project && ((N & 1) == 0 && kz == N / 2);
+    for (int st = 0; st < nsteps; ++st) {
+      v1 = cmul(e1, v1);
+      v2 = cmul(e2, v2);
+      if (proj) {
+        const float2 pv = make_float2(0.5f * (v1.x + v2.x), 0.5f * (v1.y - v2.y));
+        v1 = pv;
+        v2 = cconj(pv);
+      }
+    }
+    out[base + i1] = v1;
+    if (q2 != q) out[base + i2] = v2;
+  }
+}
+
+static unsigned grid_for(int64_t n, int sm) {
+  const int64_t b = (n + 255) / 256;
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm * 32));
+}
+
+template <int N>
+struct Sizes {
+  using R = Cfg<N>;
+  static size_t s1() { return sizeof(float2) * ((size_t)R::FREE + R::PLANE); }
+  static size_t s2(int NI, int NF, int TY) {
+    return sizeof(float2) * (size_t)R::FREE + sizeof(float) * (size_t)(NI + NF) * TY * N +
+           sizeof(float2) * (size_t)NF * TY / 2 * N;
+  }
+  static size_t s3(int NF) { return sizeof(float2) * ((size_t)R::FREE + (size_t)NF * R::PLANE); }
+};
+
+static size_t smem_limit() {
+  static int lim = 0;
+  if (!lim) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&lim, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  return (size_t)lim;
+}
+
+template <int N>
+static int launch(Args& a, int64_t n, cudaStream_t st, bool set_attrs) {
+  constexpr int TH = Cfg<N>::THREADS;
+  const size_t s1 = Sizes<N>::s1(), s2 = Sizes<N>::s2(a.p.NI, a.p.NF, a.TY), s3 = Sizes<N>::s3(a.p.NF);
+  if (set_attrs) {
+    EXGB_CUDA(cudaFuncSetAttribute(pass1_3d_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
+    EXGB_CUDA(cudaFuncSetAttribute(pass2_3d_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
+    EXGB_CUDA(cudaFuncSetAttribute(pass3_3d_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s3));
+    return EXGB_OK;
+  }
+  pass1_3d_kernel<N><<<dim3(a.Kc, a.p.NI, (unsigned)n), TH, s1, st>>>(a);
+  pass2_3d_kernel<N><<<dim3(N * (N / a.TY), (unsigned)n), TH, s2, st>>>(a);
+  pass3_3d_kernel<N><<<dim3(a.Kc, (unsigned)n), TH, s3, st>>>(a);
+  return EXGB_OK;
+}
+
+}  // namespace p3d
+
+using namespace p3d;
+
+// Can the three-pass 3D path step a plan of this size and these field counts?
+bool pass3d_supported(int D, int N, int NI, int NF) {
+  if (D != 3 || (N != 32 && N != 64) || NI < 1 || NF < 1 || NI > MAXC * 4 || NF > 2 * MAXC) return false;
+  const size_t lim = smem_limit() - 1024;
+  if (N == 32)
+    return Sizes<32>::s1() <= lim && Sizes<32>::s2(NI, NF, 8) <= lim && Sizes<32>::s3(NF) <= lim;
+  return Sizes<64>::s1() <= lim && Sizes<64>::s2(NI, NF, 8) <= lim && Sizes<64>::s3(NF) <= lim;
+}
+
+int pass3d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStream_t st, const float2* in, float2* out,
+               int64_t batch, int nsteps, int project, int nonlinear_only) {
+  const PlanDev& P = plan->dev;
+  const int N = P.N, M = P.M, C = P.C;
+  const int K = std::min(P.kmax, N / 2);
+  const int Kc = std::min(M, K + 1);
+  const int sm = plan->sm_count;
+  const int64_t pl = (int64_t)N * N;
+  if (batch == 0) return EXGB_OK;
+  if (!nonlinear_only && nsteps == 0) {
+    if (in != out) EXGB_CUDA(cudaMemcpyAsync(out, in, sizeof(float2) * batch * C * pl * M, cudaMemcpyDeviceToDevice, st));
+    return EXGB_OK;
+  }
+  Args a{};
+  a.P = P;
+  a.g = g0;
+  a.p = prog;
+  a.tw = P.tw;
+  a.N = N;
+  a.M = M;
+  a.K = K;
+  a.Kc = Kc;
+  a.TY = 8;
+  a.pl = pl;
+  a.cstride = (int64_t)Kc * pl;
+  a.sstride = (int64_t)C * a.cstride;
+  a.tstride = (int64_t)M * pl;
+  const int nb = stage_nbufs(P.order);
+  const size_t per_sample = sizeof(float2) * ((size_t)(nonlinear_only ? 1 : nb) * a.sstride +
+                                              (size_t)(prog.NI + prog.NF) * Kc * pl);
+  const int64_t cb = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)((size_t)(1u << 30) / per_sample)));
+  char* ws = (char*)workspace(per_sample * (size_t)cb, 4);
+  if (!ws) return fail(EXGB_ENOMEM, "workspace allocation failed");
+  int rc = (N == 32) ? launch<32>(a, 0, st, true) : launch<64>(a, 0, st, true);
+  if (rc) return rc;
+  for (int64_t b0 = 0; b0 < batch; b0 += cb) {
+    const int64_t n = std::min<int64_t>(cb, batch - b0);
+    if (n * C > 65535) return fail(EXGB_EUNSUPPORTED, "too many fields for one launch");
+    const float2* src = in + b0 * C * pl * M;
+    float2* dst = out + b0 * C * pl * M;
+    float2* q = (float2*)ws;
+    const int64_t fsz = a.sstride * n;
+    a.sb = stage_bufs(q, nonlinear_only ? 1 : P.order, fsz);
+    q += (int64_t)(nonlinear_only ? 1 : nb) * fsz;
+    a.W = q;
+    q += (int64_t)prog.NI * Kc * pl * n;
+    a.Hq = q;
+    {
+      dim3 grid((unsigned)((pl + 31) / 32), (Kc + 31) / 32, (unsigned)(n * C));
+      transpose3_kernel<<<grid, dim3(32, 8), 0, st>>>(src, a.sb.U, pl, M, Kc, a.cstride, 1);
+    }
+    const int nst = nonlinear_only ? 1 : P.order;
+    const int Q = nonlinear_only ? 1 : nsteps * P.order;
+    for (int qq = 0; qq < Q; ++qq) {
+      const int stage = qq % nst;
+      a.stage = nonlinear_only ? -1 : stage;
+      a.nout = nonlinear_only ? dst : nullptr;
+      a.xin = (stage == 0) ? a.sb.U : (P.order == 4 && stage == 1) ? a.sb.S1 : a.sb.S;
+      rc = (N == 32) ? launch<32>(a, n, st, false) : launch<64>(a, n, st, false);
+      if (rc) return rc;
+      if (!nonlinear_only && stage == nst - 1 && project)
+        project_planes_kernel<<<grid_for(n * C * 2 * pl, sm), 256, 0, st>>>(a.sb.U, N, Kc, a.cstride, n * C);
+      EXGB_CUDA(cudaGetLastError());
+    }
+    if (!nonlinear_only) {
+      dim3 grid((unsigned)((pl + 31) / 32), (Kc + 31) / 32, (unsigned)(n * C));
+      transpose3_kernel<<<grid, dim3(32, 8), 0, st>>>(a.sb.U, dst, pl, M, Kc, a.cstride, 0);
+    }
+    if (Kc < M)
+      linear_planes_kernel<<<grid_for(n * C * (int64_t)(M - Kc) * pl, sm), 256, 0, st>>>(
+          P.E, P.lin_ch, C, N, M, Kc, n * C, src, dst, nsteps, project, nonlinear_only);
+    EXGB_CUDA(cudaGetLastError());
+  }
+  return EXGB_OK;
+}
+
+}  // namespace exgb

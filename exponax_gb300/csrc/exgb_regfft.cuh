@@ -204,6 +204,10 @@ __device__ __forceinline__ void group_fft_x2(float2 (&v)[E], float2 (&w)[E], int
 template <int N>
 struct RegCfg;
 template <>
+struct RegCfg<32> {
+  static constexpr int E = 8, T = 4;
+};
+template <>
 struct RegCfg<64> {
   static constexpr int E = 8, T = 8;
 };
