@@ -346,7 +346,7 @@ def _traffic(name):
     tf = os.path.join(ROOT, "profiles", f"{name}_traffic.txt")
     if os.path.exists(tf):
         for ln in open(tf):
-            if ln.startswith("dram_bytes_per_launch="):
+            if ln.startswith("dram_bytes_per_launch=") or ln.startswith("dram_bytes_per_call="):
                 return float(ln.split("=")[1])
     return None
 
@@ -381,6 +381,29 @@ def _oracle_ks_worker(args):
     u = RandomSineWaves1d(1, cutoff=5)(200, key=seed)
     t0 = time.perf_counter()
     o.rollout(st, nsteps, include_init=True)(u)
+    return time.perf_counter() - t0
+
+
+def _ns3d_ic(N, key):
+    """Smooth divergence-free velocity (3, N, N, N), float32: amplitude-phase series per channel, Leray-projected."""
+    from exponax_gb300.ic import RandomAmplitudePhaseSeries
+    from oracle import exponax_np as o
+
+    g = RandomAmplitudePhaseSeries(3, cutoff=5, max_one=True)
+    u = np.concatenate([g(N, key=3 * key + c) for c in range(3)], axis=0).astype(np.float64)
+    d = o.build_derivative_operator(3, 2 * np.pi, N, dtype="float64")
+    P = o.Leray(3, N, derivative_operator=d, dtype="float64")
+    return o.ifft(P(o.fft(u)), num_spatial_dims=3, num_points=N).astype(np.float32)
+
+
+def _oracle_ns3d_worker(args):
+    seed, nsteps = args
+    from oracle import exponax_np as o
+
+    st = o.NavierStokesVelocity(3, 2 * np.pi, 64, 0.01, diffusivity=0.01)
+    u = _ns3d_ic(64, seed)
+    t0 = time.perf_counter()
+    o.repeat(st, nsteps)(u)
     return time.perf_counter() - t0
 
 
@@ -612,6 +635,72 @@ def run_other(args, rank, ws):
                 errs[f"rel_l2_vs_fp64_after_{nn}"] = float(np.max(e))
             line["precision"] = dict(errs, note=("FP32 register transforms" if args.precision == "fp32" else
                                                  "split-BF16 tensor-core DFT") + " vs the float64 oracle, 2 seeds")
+    elif args.workload == "ns3d64":
+        from exponax_gb300 import _device, _lib
+
+        Nk, B, n = 64, 32, 20
+        st = ex.stepper.NavierStokesVelocity(3, 2 * np.pi, Nk, 0.01, diffusivity=0.01)
+        u0h = np.stack([_ns3d_ic(Nk, s) for s in range(B)])
+        uh = ex.fft(torch.from_numpy(u0h).cuda(), num_spatial_dims=3)
+        out = torch.empty_like(uh)
+        lib = _lib.load()
+        h = st.plan.handle
+
+        def run():
+            _lib.check(lib.exgb_repeat_fourier(h, _device.stream(), uh.data_ptr(), out.data_ptr(), B, n))
+
+        ms = _timed(run, args.steps, args.warmup, flush)
+        rep = ex.vmap(ex.repeat(st, n))
+        pin = torch.from_numpy(u0h).pin_memory()
+        pout = torch.empty_like(pin).pin_memory()
+        ems = _timed(lambda: pout.copy_(rep(pin.cuda(non_blocking=True)), non_blocking=True), args.steps,
+                     args.warmup)
+        dof = B * 3 * Nk ** 3 * n
+        # launches per repeat call: 2 transposes + 1 linear-planes kernel + 4 kernels x 2 stages x n steps
+        # (no projection between steps in Fourier space; ncu counts 163 for n = 20)
+        launches = 3 + n * 2 * 4
+        line.update(value=dof / (ms * 1e-3), ms_per_step=ms,
+                    config={"workload": "NavierStokesVelocity 3D 64^3 (projected convection + Leray), domain 2pi, "
+                                        "nu=0.01, dt=0.01, ETDRK2, 2/3 dealiasing, batch 32, 20 steps (repeat), "
+                                        "three-pass 3D path", "l2": "flushed (256 MB write) between timed steps"},
+                    e2e={"value": dof / (ems * 1e-3), "unit": "DOF-steps/s", "ms_per_step": ems,
+                         "h2d_bytes_per_step": int(pin.numel() * 4), "d2h_bytes_per_step": int(pout.numel() * 4)},
+                    gpu_launches=args.steps * launches)
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        bpd = 6 * 8 * (Nk // 2 + 1) / Nk  # 6 complex64 half-spectrum passes per ETDRK2 step
+        achieved = dof * bpd / (ms * 1e-3) / 1e9
+        line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "traffic": _traffic("pass3d_ns3d64_b32"),
+                            "kernel": "pass1/2/3_3d_kernel<64> + combine_planes_kernel (one ETDRK stage)",
+                            "note": f"algorithmic {bpd:.3f} B/DOF-step (state read + write per stage) x "
+                                    f"{B}x3x{Nk}^3x{n} per repeat call, against the call's event time; "
+                                    "traffic = DRAM bytes of the whole call (ncu); peak "
+                                    + ("measured" if "hbm_gbs" in peaks else "fallback")}
+        if not args.no_cpu:
+            nproc = min(cores, 16)
+            ncs = 5
+            ts = _pool_map(_oracle_ns3d_worker, [(s, ncs) for s in range(nproc)])
+            line["cpu_baseline"] = {"value": nproc * 3 * Nk ** 3 * ncs / max(ts), "unit": "DOF-steps/s",
+                                    "cores": nproc, "kind": "port",
+                                    "sample": f"NumPy oracle, {nproc} samples x {ncs} steps, one process each"}
+            from oracle import exponax_np as o
+
+            so64 = o.NavierStokesVelocity(3, 2 * np.pi, Nk, 0.01, diffusivity=0.01, dtype="float64")
+            errs = {}
+            for nn in (1, 20):
+                got = ex.vmap(ex.repeat(st, nn))(torch.from_numpy(u0h[:2]).cuda()).cpu().numpy()
+                e = []
+                for b in range(2):
+                    ref = o.repeat(so64, nn)(u0h[b].astype(np.float64))
+                    e.append(float(np.linalg.norm(got[b] - ref) / np.linalg.norm(ref)))
+                errs[f"rel_l2_vs_fp64_after_{nn}"] = float(np.max(e))
+            errs["sample"] = "2 initial conditions, NumPy float64 oracle"
+            line["fp64_check"] = errs
     print(json.dumps(line), flush=True)
 
 
@@ -624,7 +713,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split_bf16"],
                     help="transform arithmetic of the kolmo128 workload")
-    ap.add_argument("--workload", default="ns256", choices=["ns256", "ks1d", "uneven1d", "kolmo128"],
+    ap.add_argument("--workload", default="ns256", choices=["ns256", "ks1d", "uneven1d", "kolmo128", "ns3d64"],
                     help="ns256 (default, the headline metric) or one of the other benchmark configurations")
     args = ap.parse_args()
     rank, ws = dist_init()

@@ -7,8 +7,9 @@
 //   pass 2  per (x, tile of y): for each of the NI fields the c2r transform along z (two lines packed
 //           in one complex transform, 1/N^3 folded in), the pointwise products (the cross product u x
 //           curl u for projected convection), the r2c transforms of the NF products -> Hq[f][kz][x][y]
-//   pass 3  per kz plane: the NF fields' 2D forward transforms, post-mask, multipliers (Leray
-//           projection and forcing for projected convection) and the ETDRK stage update
+//   pass 3  per (kz plane, product field): 2D forward transform in place in Hq, then one elementwise
+//           kernel over the Kc planes: post-mask, multipliers (Leray projection and forcing for
+//           projected convection) and the ETDRK stage update (Hq still in L2)
 // Only the Kc = K + 1 planes inside the dealiasing mask take part; the planes above it feel the linear
 // part alone and are advanced by E once per step from the input in one elementwise kernel.  State and
 // stage buffers are plane-major ([c][kz][kx][ky], kz < Kc), the coefficient tables of such plans
@@ -53,6 +54,7 @@ struct Args {
   float2* Hq;        // [s][f < NF][kz < Kc][x][y]
   int stage;         // -1: nonlinear term only, written to nout (natural layout [s][c][kx][ky][kz])
   float2* nout;
+  int sm;            // SM count (grid of the elementwise kernels)
 };
 
 __device__ __forceinline__ int sgn_of(int i, int N) { return (i <= (N - 1) / 2) ? i : i - N; }
@@ -218,36 +220,43 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass2_3d_kernel(const Args a)
   }
 }
 
-// ---- pass 3: the NF fields of one kz plane, 2D forward, combine, ETDRK update
+// ---- pass 3a: 2D forward transform of one product field on one kz plane, in place in Hq
 template <int N>
 __global__ void __launch_bounds__(Cfg<N>::THREADS) pass3_3d_kernel(const Args a) {
   using R = Cfg<N>;
   extern __shared__ __align__(16) float2 sp3[];
   float2* twl = sp3 + R::TWL;
-  float2* planes = sp3 + R::FREE;  // [NF][N][PS]
-  const int NF = a.p.NF, C = a.g.C;
-  const int kz = blockIdx.x;
-  const int64_t s = blockIdx.y;
+  float2* plane = sp3 + R::FREE;
+  const int kz = blockIdx.x, f = blockIdx.y;
+  const int64_t s = blockIdx.z;
   load_twl<N>(twl, a.tw);
-  for (int e = threadIdx.x; e < NF * N * N; e += blockDim.x) {
-    const int f = e / (N * N), r = e - f * N * N;
-    planes[(size_t)f * R::PLANE + (size_t)(r / N) * R::PS + (r % N)] =
-        a.Hq[((s * NF + f) * a.Kc + kz) * a.pl + r];
-  }
+  float2* H = a.Hq + ((s * a.p.NF + f) * a.Kc + kz) * a.pl;
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) plane[(size_t)(e / N) * R::PS + (e % N)] = H[e];
   __syncthreads();
-  planes_fft<N, false>(planes, NF, sp3 + R::TILES, twl);
-  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+  planes_fft<N, false>(plane, 1, sp3 + R::TILES, twl);
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) H[e] = plane[(size_t)(e / N) * R::PS + (e % N)];
+}
+
+// ---- pass 3b: post-mask, multipliers and the ETDRK stage update of every mode of the Kc planes
+// (Hq was written by pass 3a just before and is read from L2)
+__global__ void __launch_bounds__(256) combine_planes_kernel(const Args a, int64_t n) {
+  const int N = a.N, C = a.g.C, NF = a.p.NF;
+  const int64_t per = a.Kc * a.pl;
+  const int64_t total = n * per;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = t / per, r = t - s * per;  // r = kz pl + kx N + ky
+    const int kz = (int)(r / a.pl);
+    const int e = (int)(r - (int64_t)kz * a.pl);
     const int kx = e / N, ky = e - kx * N;
     const int k[3] = {sgn_of(kx, N), sgn_of(ky, N), kz};
     const bool m = abs(k[0]) <= a.K && abs(k[1]) <= a.K && kz <= a.K;
     float2 nv[MAXC];
-    ndg::combine_mode(a.P, a.g, a.p, k, m, planes + (size_t)kx * R::PS + ky, R::PLANE, nv);
+    ndg::combine_mode(a.P, a.g, a.p, k, m, a.Hq + s * NF * per + r, per, nv);
     if (a.stage < 0) {
-      float2* o = a.nout + s * (int64_t)C * a.tstride + ((int64_t)kx * N + ky) * a.M + kz;
+      float2* o = a.nout + s * (int64_t)C * a.tstride + (int64_t)e * a.M + kz;
       for (int c = 0; c < C; ++c) o[c * a.tstride] = nv[c];
       continue;
     }
-    const int64_t r = (int64_t)kz * a.pl + e;
     for (int c = 0; c < C; ++c) {
       const int64_t ci = (a.P.lin_ch == 1 ? 0 : (int64_t)c * a.tstride) + r;
       stage_upd_at(a.P, a.sb, s * a.sstride + c * a.cstride + r, ci, a.stage, nv[c]);
@@ -367,7 +376,7 @@ struct Sizes {
     return sizeof(float2) * (size_t)R::FREE + sizeof(float) * (size_t)(NI + NF) * TY * N +
            sizeof(float2) * (size_t)NF * TY / 2 * N;
   }
-  static size_t s3(int NF) { return sizeof(float2) * ((size_t)R::FREE + (size_t)NF * R::PLANE); }
+  static size_t s3() { return s1(); }
 };
 
 static size_t smem_limit() {
@@ -383,7 +392,7 @@ static size_t smem_limit() {
 template <int N>
 static int launch(Args& a, int64_t n, cudaStream_t st, bool set_attrs) {
   constexpr int TH = Cfg<N>::THREADS;
-  const size_t s1 = Sizes<N>::s1(), s2 = Sizes<N>::s2(a.p.NI, a.p.NF, a.TY), s3 = Sizes<N>::s3(a.p.NF);
+  const size_t s1 = Sizes<N>::s1(), s2 = Sizes<N>::s2(a.p.NI, a.p.NF, a.TY), s3 = Sizes<N>::s3();
   if (set_attrs) {
     EXGB_CUDA(cudaFuncSetAttribute(pass1_3d_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
     EXGB_CUDA(cudaFuncSetAttribute(pass2_3d_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
@@ -392,7 +401,8 @@ static int launch(Args& a, int64_t n, cudaStream_t st, bool set_attrs) {
   }
   pass1_3d_kernel<N><<<dim3(a.Kc, a.p.NI, (unsigned)n), TH, s1, st>>>(a);
   pass2_3d_kernel<N><<<dim3(N * (N / a.TY), (unsigned)n), TH, s2, st>>>(a);
-  pass3_3d_kernel<N><<<dim3(a.Kc, (unsigned)n), TH, s3, st>>>(a);
+  pass3_3d_kernel<N><<<dim3(a.Kc, a.p.NF, (unsigned)n), TH, s3, st>>>(a);
+  combine_planes_kernel<<<grid_for(n * a.Kc * a.pl, a.sm), 256, 0, st>>>(a, n);
   return EXGB_OK;
 }
 
@@ -405,8 +415,8 @@ bool pass3d_supported(int D, int N, int NI, int NF) {
   if (D != 3 || (N != 32 && N != 64) || NI < 1 || NF < 1 || NI > MAXC * 4 || NF > 2 * MAXC) return false;
   const size_t lim = smem_limit() - 1024;
   if (N == 32)
-    return Sizes<32>::s1() <= lim && Sizes<32>::s2(NI, NF, 8) <= lim && Sizes<32>::s3(NF) <= lim;
-  return Sizes<64>::s1() <= lim && Sizes<64>::s2(NI, NF, 8) <= lim && Sizes<64>::s3(NF) <= lim;
+    return Sizes<32>::s1() <= lim && Sizes<32>::s2(NI, NF, 8) <= lim;
+  return Sizes<64>::s1() <= lim && Sizes<64>::s2(NI, NF, 8) <= lim;
 }
 
 int pass3d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStream_t st, const float2* in, float2* out,
@@ -431,7 +441,8 @@ int pass3d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStrea
   a.M = M;
   a.K = K;
   a.Kc = Kc;
-  a.TY = 8;
+  a.TY = 8;  // y lines per pass-2 CTA (16 measured no faster at 64^3)
+  a.sm = sm;
   a.pl = pl;
   a.cstride = (int64_t)Kc * pl;
   a.sstride = (int64_t)C * a.cstride;
