@@ -209,14 +209,14 @@ template <int N>
 struct RegPass {
   static constexpr int E = RegCfg<N>::E, T = RegCfg<N>::T;
   static constexpr int TS = tile_stride<E, T>();
-  // passes 1 and 3 keep each sequence in a slot of SLOT float2 that also serves as its transform's
-  // transpose tile (the sequence is in registers meanwhile); pass 2 builds its sequences from global
-  // memory and has per-group tiles (128 threads at N = 512, where a lane holds 32 points)
+  // every pass keeps each sequence in a slot of SLOT float2 that also serves as its transform's
+  // transpose tile (the sequence is in registers meanwhile); pass 2 runs 128 threads at N = 512,
+  // where a lane holds 32 points
   static constexpr int SLOT = N > TS ? N : TS;
   static constexpr int THREADS = 256, NG = THREADS / T;
   static constexpr int THREADS2 = N >= 512 ? 128 : 256, NG2 = THREADS2 / T;
-  // float2 offsets: twiddles, then pass 2's tiles, then the pass's own buffers
-  static constexpr int TWL = 0, TILES = N, FREE13 = N, FREE2 = N + NG2 * TS;
+  // float2 offsets: twiddles, then the pass's slots
+  static constexpr int TWL = 0, FREE13 = N;
 };
 
 template <int N>
@@ -290,16 +290,19 @@ __global__ void __launch_bounds__(RegPass<N>::THREADS) pass1_reg_kernel(const Ar
   }
 }
 
+// Pass 2 keeps everything in sequence slots of SLOT float2: slot j first serves as the transpose tile
+// of the c2r transform of real rows 2j, 2j + 1 (q = f * TX + xx, built from global W in registers),
+// then holds those two rows as floats ([0, N) and [N, 2N)); the pointwise products overwrite the
+// rows of their first NF fields in place (one thread per grid point), and the r2c transform of product
+// rows 2j, 2j + 1 runs in slot j again (rows to registers, slot as tile, spectrum back to the slot).
 template <int N>
 __global__ void __launch_bounds__(RegPass<N>::THREADS2) pass2_reg_kernel(const Args a) {
   using R = RegPass<N>;
-  constexpr int E = R::E, T = R::T, M = N / 2 + 1;
+  constexpr int E = R::E, T = R::T, M = N / 2 + 1, SL = R::SLOT;
   extern __shared__ __align__(16) float2 smr2[];
   float2* twl = smr2 + R::TWL;
+  float2* slots = smr2 + R::FREE13;  // [max(NI, NF) * TX / 2][SLOT]
   const int NI = a.p.NI, NF = a.p.NF, TX = a.TX, Kc = a.Kc;
-  float* phys = reinterpret_cast<float*>(smr2 + R::FREE2);  // [NI * TX][N]
-  float* prod = phys + (size_t)NI * TX * N;                 // [NF * TX][N]
-  float2* zb = reinterpret_cast<float2*>(prod + (size_t)NF * TX * N);  // [NF * TX / 2][N]
   const int64_t s = blockIdx.y;
   const int x0 = blockIdx.x * TX;
   const int tx = min(TX, N - x0);
@@ -307,16 +310,16 @@ __global__ void __launch_bounds__(RegPass<N>::THREADS2) pass2_reg_kernel(const A
   __syncthreads();
   const int gi = threadIdx.x / T, l = threadIdx.x % T;
   const unsigned gmask = group_mask<N>();
-  float2* tile = smr2 + R::TILES + (size_t)gi * R::TS;
   const float2* W = a.W + s * (int64_t)NI * Kc * N;
   const float inv = 1.f / ((float)N * (float)N);
-  // c2r: sequence j packs rows qa = 2j, qb = 2j + 1 (q = f * TX + xx), gathered straight from W
+  // c2r: sequence j packs rows qa = 2j, qb = 2j + 1, gathered straight from W
   const int ni = NI * TX / 2;
   for (int j = gi; j < ni; j += R::NG2) {
     const int qa = 2 * j, qb = qa + 1;
     const int fa = qa / TX, xa = qa - fa * TX, fb = qb / TX, xb = qb - fb * TX;
     const float2* wa = W + ((int64_t)fa * N + x0 + xa) * Kc;
     const float2* wb = W + ((int64_t)fb * N + x0 + xb) * Kc;
+    float2* slot = slots + (size_t)j * SL;
     float2 v[E];
 #pragma unroll
     for (int jj = 0; jj < E; ++jj) {
@@ -331,41 +334,50 @@ __global__ void __launch_bounds__(RegPass<N>::THREADS2) pass2_reg_kernel(const A
       }
       v[jj] = pack_pair(va, vb, ext, real_only);
     }
-    group_fft<E, T, true>(v, l, tile, twl, gmask);
+    group_fft<E, T, true>(v, l, slot, twl, gmask);
+    float* rows = reinterpret_cast<float*>(slot);
 #pragma unroll
     for (int jj = 0; jj < E; ++jj) {
       const int y = l + T * jj;
-      phys[(size_t)qa * N + y] = v[jj].x * inv;
-      phys[(size_t)qb * N + y] = v[jj].y * inv;
+      rows[y] = v[jj].x * inv;
+      rows[N + y] = v[jj].y * inv;
     }
   }
   __syncthreads();
+  // row q at float offset (q / 2) * 2 SL + (q % 2) N; with TX even, field f of point xx sits
+  // f * TX * SL floats after field 0
+  const int64_t fs = (int64_t)TX * SL;
   for (int e = threadIdx.x; e < TX * N; e += blockDim.x) {
     const int xx = e / N, y = e - xx * N;
+    float* base = reinterpret_cast<float*>(slots) + (size_t)(xx >> 1) * 2 * SL + (xx & 1) * N + y;
     float in[MAXC + MAXC * 3];
-    for (int f = 0; f < NI; ++f) in[f] = phys[((size_t)f * TX + xx) * N + y];
-    ndg::pointwise_point(a.g, a.p, in, prod + (size_t)xx * N + y, (int64_t)TX * N);
+    for (int f = 0; f < NI; ++f) in[f] = base[f * fs];
+    ndg::pointwise_point(a.g, a.p, in, base, fs);
   }
   __syncthreads();
-  // r2c: sequence j packs product rows 2j, 2j + 1
+  // r2c: sequence j packs product rows 2j, 2j + 1, in place in slot j
   const int nf = NF * TX / 2;
   for (int j = gi; j < nf; j += R::NG2) {
+    float2* slot = slots + (size_t)j * SL;
+    const float* rows = reinterpret_cast<const float*>(slot);
     float2 v[E];
 #pragma unroll
     for (int jj = 0; jj < E; ++jj) {
       const int y = l + T * jj;
-      v[jj] = make_float2(prod[(size_t)(2 * j) * N + y], prod[(size_t)(2 * j + 1) * N + y]);
+      v[jj] = make_float2(rows[y], rows[N + y]);
     }
-    group_fft<E, T, false>(v, l, tile, twl, gmask);
+    __syncwarp(gmask);  // every lane holds its points before the slot becomes the tile
+    group_fft<E, T, false>(v, l, slot, twl, gmask);
 #pragma unroll
-    for (int jj = 0; jj < E; ++jj) zb[(size_t)j * N + l + T * jj] = v[jj];
+    for (int jj = 0; jj < E; ++jj) slot[l + T * jj] = v[jj];
   }
   __syncthreads();
   float2* Hq = a.Hq + s * (int64_t)NF * Kc * N;
   for (int e = threadIdx.x; e < nf * Kc; e += blockDim.x) {
     const int j = e / Kc, k = e - j * Kc;
+    const float2* zb = slots + (size_t)j * SL;
     float2 P, Q;
-    unpack_pair(zb[(size_t)j * N + k], zb[(size_t)j * N + (k == 0 ? 0 : N - k)], P, Q);
+    unpack_pair(zb[k], zb[k == 0 ? 0 : N - k], P, Q);
     const int qa = 2 * j, qb = qa + 1;
     const int fa = qa / TX, xa = qa - fa * TX, fb = qb / TX, xb = qb - fb * TX;
     if (xa < tx) Hq[((int64_t)fa * N + x0 + xa) * Kc + k] = P;
@@ -542,8 +554,7 @@ struct RegSizes {
   using R = RegPass<N>;
   static size_t s1(int NI, int TY) { return sizeof(float2) * ((size_t)R::FREE13 + (size_t)NI * TY * R::SLOT); }
   static size_t s2(int NI, int NF, int TX) {
-    return sizeof(float2) * (size_t)R::FREE2 + sizeof(float) * (size_t)(NI + NF) * TX * N +
-           sizeof(float2) * (size_t)NF * TX / 2 * N;
+    return sizeof(float2) * ((size_t)R::FREE13 + (size_t)std::max(NI, NF) * TX / 2 * R::SLOT);
   }
   static size_t s3(int NF, int TY3) { return sizeof(float2) * ((size_t)R::FREE13 + (size_t)NF * TY3 * R::SLOT); }
 };
@@ -551,7 +562,7 @@ struct RegSizes {
 template <int N>
 static bool reg_tiles(int NI, int NF, int& TY, int& TX, int& TY3) {
   const size_t cap = smem_limit() - 1024;
-  TY = 4;
+  TY = 4;  // 2 and (pass 2) TX = 8 measured slower at 512^2 and 256^2
   TX = 4;
   TY3 = std::max(4, std::min(16, RegPass<N>::NG / std::max(1, NF)));  // one sequence per group
   while (TY > 1 && RegSizes<N>::s1(NI, TY) > cap / 2) --TY;
