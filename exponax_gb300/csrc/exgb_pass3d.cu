@@ -1,5 +1,5 @@
 // exgb_pass3d.cu -- 3D ETDRK stages (projected convection + Leray, and the nonlinearities of the
-// staged N-D path) in three fused passes per stage, for N = 32 and 64.
+// staged N-D path) in three fused passes per stage, for N = 32, 64 and 128.
 //
 // The 3D counterpart of exgb_pass2d.cu: the rfft axis z takes the role of the 2D column index.
 //   pass 1  per (kz plane, derived field): the field's spectrum on the plane (pre-mask, exgb_ndops.cuh),
@@ -412,11 +412,21 @@ using namespace p3d;
 
 // Can the three-pass 3D path step a plan of this size and these field counts?
 bool pass3d_supported(int D, int N, int NI, int NF) {
-  if (D != 3 || (N != 32 && N != 64) || NI < 1 || NF < 1 || NI > MAXC * 4 || NF > 2 * MAXC) return false;
+  if (D != 3 || (N != 32 && N != 64 && N != 128) || NI < 1 || NF < 1 || NI > MAXC * 4 || NF > 2 * MAXC)
+    return false;
   const size_t lim = smem_limit() - 1024;
-  if (N == 32)
-    return Sizes<32>::s1() <= lim && Sizes<32>::s2(NI, NF, 8) <= lim;
-  return Sizes<64>::s1() <= lim && Sizes<64>::s2(NI, NF, 8) <= lim;
+  if (N == 32) return Sizes<32>::s1() <= lim && Sizes<32>::s2(NI, NF, 8) <= lim;
+  if (N == 64) return Sizes<64>::s1() <= lim && Sizes<64>::s2(NI, NF, 8) <= lim;
+  return Sizes<128>::s1() <= lim && Sizes<128>::s2(NI, NF, 8) <= lim;
+}
+
+template <bool SET>
+static int launch_n(int N, Args& a, int64_t n, cudaStream_t st) {
+  switch (N) {
+    case 32: return launch<32>(a, n, st, SET);
+    case 64: return launch<64>(a, n, st, SET);
+    default: return launch<128>(a, n, st, SET);
+  }
 }
 
 int pass3d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStream_t st, const float2* in, float2* out,
@@ -453,7 +463,7 @@ int pass3d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStrea
   const int64_t cb = std::max<int64_t>(1, std::min<int64_t>(batch, (int64_t)((size_t)(1u << 30) / per_sample)));
   char* ws = (char*)workspace(per_sample * (size_t)cb, 4);
   if (!ws) return fail(EXGB_ENOMEM, "workspace allocation failed");
-  int rc = (N == 32) ? launch<32>(a, 0, st, true) : launch<64>(a, 0, st, true);
+  int rc = launch_n<true>(N, a, 0, st);
   if (rc) return rc;
   for (int64_t b0 = 0; b0 < batch; b0 += cb) {
     const int64_t n = std::min<int64_t>(cb, batch - b0);
@@ -478,7 +488,7 @@ int pass3d_run(const exgb_plan* plan, const Geo& g0, const Prog& prog, cudaStrea
       a.stage = nonlinear_only ? -1 : stage;
       a.nout = nonlinear_only ? dst : nullptr;
       a.xin = (stage == 0) ? a.sb.U : (P.order == 4 && stage == 1) ? a.sb.S1 : a.sb.S;
-      rc = (N == 32) ? launch<32>(a, n, st, false) : launch<64>(a, n, st, false);
+      rc = launch_n<false>(N, a, n, st);
       if (rc) return rc;
       if (!nonlinear_only && stage == nst - 1 && project)
         project_planes_kernel<<<grid_for(n * C * 2 * pl, sm), 256, 0, st>>>(a.sb.U, N, Kc, a.cstride, n * C);

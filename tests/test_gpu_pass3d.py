@@ -1,4 +1,4 @@
-"""The three-pass 3D path (exgb_pass3d.cu: N = 32 and 64) against the oracle and
+"""The three-pass 3D path (exgb_pass3d.cu: N = 32, 64 and 128) against the oracle and
 against the five-kernel 3D path (EXGB_3D_PATH=generic) on the same inputs.
 
 Covers projected convection (NavierStokesVelocity, KolmogorovFlowVelocity with
@@ -68,6 +68,20 @@ def test_ns_velocity_step(N, order):
         assert rel(got[b], so(u[b])) < 1e-5, (N, order, b)
     gen = host(ex.vmap(_generic(mk))(cu(u)))
     assert rel(got, gen) < 2e-6
+
+
+@pytest.mark.parametrize("order", [2, 4])
+def test_ns_velocity_step_128(order):
+    """N = 128: one 172 KB plane per CTA in passes 1 and 3."""
+    N = 128
+    mk = lambda: ex.stepper.NavierStokesVelocity(3, 2 * np.pi, N, 0.01, diffusivity=0.01, order=order)
+    sm = mk()
+    so = o.NavierStokesVelocity(3, 2 * np.pi, N, 0.01, diffusivity=0.01, order=order)
+    u = velocity_ic(N, 2)
+    got = host(sm(cu(u)))
+    assert rel(got, so(u)) < 1e-5
+    rep = host(ex.repeat(sm, 3)(cu(u)))
+    assert rel(rep, host(ex.repeat(_generic(mk), 3)(cu(u)))) < 1e-5
 
 
 @pytest.mark.parametrize("N", [32, 64])
