@@ -64,6 +64,7 @@ struct Cfg {
   static constexpr int E = RegCfg<N>::E, T = RegCfg<N>::T;
   static constexpr int THREADS = 256, NG = THREADS / T;
   static constexpr int TS = tile_stride<E, T>();
+  static constexpr int SLOT = N > TS ? N : TS;  // pass 2: a pair of lines, also its transform's tile
   static constexpr int PS = N + 1;  // padded row stride of a plane in shared memory
   static constexpr int PLANE = N * PS;
   // float2 offsets: twiddles, transpose tiles, then the pass's planes / buffers
@@ -86,25 +87,15 @@ __device__ __forceinline__ unsigned group_mask() {
   return (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
 }
 
-// 2D transform of `np` planes (each N x N, row stride PS) in shared memory: rows, then columns
+// column transforms of a plane in shared memory (rows kx, row stride PS), in place
 template <int N, bool INV>
-__device__ __forceinline__ void planes_fft(float2* planes, int np, float2* tiles, const float2* twl) {
+__device__ __forceinline__ void plane_cols_fft(float2* plane, float2* tiles, const float2* twl) {
   using R = Cfg<N>;
   const int gi = threadIdx.x / R::T, l = threadIdx.x % R::T;
   const unsigned gmask = group_mask<N>();
   float2* tile = tiles + (size_t)gi * R::TS;
-  for (int q = gi; q < np * N; q += R::NG) {  // row r of plane pi
-    float2* row = planes + (size_t)(q / N) * R::PLANE + (size_t)(q % N) * R::PS;
-    float2 v[R::E];
-#pragma unroll
-    for (int j = 0; j < R::E; ++j) v[j] = row[l + R::T * j];
-    group_fft<R::E, R::T, INV>(v, l, tile, twl, gmask);
-#pragma unroll
-    for (int j = 0; j < R::E; ++j) row[l + R::T * j] = v[j];
-  }
-  __syncthreads();
-  for (int q = gi; q < np * N; q += R::NG) {  // column c of plane pi
-    float2* col = planes + (size_t)(q / N) * R::PLANE + (q % N);
+  for (int c = gi; c < N; c += R::NG) {
+    float2* col = plane + c;
     float2 v[R::E];
 #pragma unroll
     for (int j = 0; j < R::E; ++j) v[j] = col[(size_t)(l + R::T * j) * R::PS];
@@ -112,10 +103,28 @@ __device__ __forceinline__ void planes_fft(float2* planes, int np, float2* tiles
 #pragma unroll
     for (int j = 0; j < R::E; ++j) col[(size_t)(l + R::T * j) * R::PS] = v[j];
   }
-  __syncthreads();
 }
 
-// ---- pass 1: one derived field on one kz plane, 2D inverse over (kx, ky)
+// row transforms of a plane in shared memory (rows kx, row stride PS), in place
+template <int N, bool INV>
+__device__ __forceinline__ void plane_rows_fft(float2* plane, float2* tiles, const float2* twl) {
+  using R = Cfg<N>;
+  const int gi = threadIdx.x / R::T, l = threadIdx.x % R::T;
+  const unsigned gmask = group_mask<N>();
+  float2* tile = tiles + (size_t)gi * R::TS;
+  for (int r = gi; r < N; r += R::NG) {
+    float2* row = plane + (size_t)r * R::PS;
+    float2 v[R::E];
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) v[j] = row[l + R::T * j];
+    group_fft<R::E, R::T, INV>(v, l, tile, twl, gmask);
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) row[l + R::T * j] = v[j];
+  }
+}
+
+// ---- pass 1: one derived field on one kz plane (derived by consecutive threads over consecutive
+// modes, into shared memory), 2D inverse over (kx, ky)
 template <int N>
 __global__ void __launch_bounds__(Cfg<N>::THREADS) pass1_3d_kernel(const Args a) {
   using R = Cfg<N>;
@@ -135,36 +144,46 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass1_3d_kernel(const Args a)
     plane[(size_t)kx * R::PS + ky] = w[f];
   }
   __syncthreads();
-  planes_fft<N, true>(plane, 1, sp1 + R::TILES, twl);
+  plane_rows_fft<N, true>(plane, sp1 + R::TILES, twl);
+  __syncthreads();
+  plane_cols_fft<N, true>(plane, sp1 + R::TILES, twl);
+  __syncthreads();
   float2* W = a.W + ((s * a.p.NI + f) * a.Kc + kz) * a.pl;
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) W[e] = plane[(size_t)(e / N) * R::PS + (e % N)];
 }
 
-// ---- pass 2: lines along z at (x, y0 .. y0 + TY): c2r, pointwise, r2c
+// ---- pass 2: lines along z at (x, y0 .. y0 + TY): c2r, pointwise, r2c.  The W values of the tile
+// are staged in shared memory first (runs of TY consecutive y per (field, kz)); each pair of lines
+// has a slot of SLOT float2 that is the transpose tile of its c2r transform, then holds the two
+// physical lines, then (products overwritten in place) the pair's r2c transform and spectrum; the
+// spectra leave as runs of TY consecutive y again.
 template <int N>
 __global__ void __launch_bounds__(Cfg<N>::THREADS) pass2_3d_kernel(const Args a) {
   using R = Cfg<N>;
-  constexpr int E = R::E, T = R::T, M = N / 2 + 1;
+  constexpr int E = R::E, T = R::T, M = N / 2 + 1, SL = R::SLOT;
   extern __shared__ __align__(16) float2 sp2[];
-  float2* twl = sp2 + R::TWL;
   const int NI = a.p.NI, NF = a.p.NF, TY = a.TY, Kc = a.Kc;
-  float* phys = reinterpret_cast<float*>(sp2 + R::FREE);           // [NI * TY][N]
-  float* prod = phys + (size_t)NI * TY * N;                         // [NF * TY][N]
-  float2* zb = reinterpret_cast<float2*>(prod + (size_t)NF * TY * N);  // [NF * TY / 2][N]
+  float2* twl = sp2 + R::TWL;
+  float2* wt = sp2 + N;                            // [NI][Kc][TY]
+  float2* slots = wt + (size_t)NI * Kc * TY;       // [max(NI, NF) * TY / 2][SLOT]
   const int x = blockIdx.x / (N / TY), y0 = (blockIdx.x % (N / TY)) * TY;
   const int64_t s = blockIdx.y;
   load_twl<N>(twl, a.tw);
+  // element (f, kz) of line (x, y) in W / Hq: ((s NI + f) Kc + kz) pl + x N + y
+  const float2* W = a.W + s * (int64_t)NI * Kc * a.pl + (int64_t)x * N + y0;
+  for (int e = threadIdx.x; e < NI * Kc * TY; e += blockDim.x) {
+    const int yy = e % TY, r = e / TY;  // r = f Kc + kz
+    wt[e] = W[(int64_t)r * a.pl + yy];
+  }
   __syncthreads();
   const int gi = threadIdx.x / T, l = threadIdx.x % T;
   const unsigned gmask = group_mask<N>();
-  float2* tile = sp2 + R::TILES + (size_t)gi * R::TS;
-  // element (f, kz) of line (x, y) in W / Hq: ((s NI + f) Kc + kz) pl + x N + y
-  const float2* W = a.W + s * (int64_t)NI * Kc * a.pl + (int64_t)x * N + y0;
   const float inv = 1.f / ((float)N * (float)N * (float)N);
   const int ni = NI * TY / 2;
   for (int j = gi; j < ni; j += R::NG) {
     const int qa = 2 * j, qb = qa + 1;
     const int fa = qa / TY, ya = qa - fa * TY, fb = qb / TY, yb = qb - fb * TY;
+    float2* slot = slots + (size_t)j * SL;
     float2 v[E];
 #pragma unroll
     for (int jj = 0; jj < E; ++jj) {
@@ -174,53 +193,61 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass2_3d_kernel(const Args a)
       const bool real_only = (k == 0) || (k == N / 2);
       float2 va = make_float2(0.f, 0.f), vb = va;
       if (kk < Kc) {
-        va = W[((int64_t)fa * Kc + kk) * a.pl + ya];
-        vb = W[((int64_t)fb * Kc + kk) * a.pl + yb];
+        va = wt[((size_t)fa * Kc + kk) * TY + ya];
+        vb = wt[((size_t)fb * Kc + kk) * TY + yb];
       }
       v[jj] = pack_pair(va, vb, ext, real_only);
     }
-    group_fft<E, T, true>(v, l, tile, twl, gmask);
+    group_fft<E, T, true>(v, l, slot, twl, gmask);
+    float* rows = reinterpret_cast<float*>(slot);
 #pragma unroll
     for (int jj = 0; jj < E; ++jj) {
       const int z = l + T * jj;
-      phys[(size_t)qa * N + z] = v[jj].x * inv;
-      phys[(size_t)qb * N + z] = v[jj].y * inv;
+      rows[z] = v[jj].x * inv;
+      rows[N + z] = v[jj].y * inv;
     }
   }
   __syncthreads();
+  // line q = f TY + yy at float offset (q / 2) 2 SL + (q % 2) N: field f of line yy is f TY SL floats on
+  const int64_t fs = (int64_t)TY * SL;
   for (int e = threadIdx.x; e < TY * N; e += blockDim.x) {
     const int yy = e / N, z = e - yy * N;
+    float* base = reinterpret_cast<float*>(slots) + (size_t)(yy >> 1) * 2 * SL + (yy & 1) * N + z;
     float in[MAXC + MAXC * 3];
-    for (int f = 0; f < NI; ++f) in[f] = phys[((size_t)f * TY + yy) * N + z];
-    ndg::pointwise_point(a.g, a.p, in, prod + (size_t)yy * N + z, (int64_t)TY * N);
+    for (int f = 0; f < NI; ++f) in[f] = base[f * fs];
+    ndg::pointwise_point(a.g, a.p, in, base, fs);
   }
   __syncthreads();
   const int nf = NF * TY / 2;
   for (int j = gi; j < nf; j += R::NG) {
+    float2* slot = slots + (size_t)j * SL;
+    const float* rows = reinterpret_cast<const float*>(slot);
     float2 v[E];
 #pragma unroll
     for (int jj = 0; jj < E; ++jj) {
       const int z = l + T * jj;
-      v[jj] = make_float2(prod[(size_t)(2 * j) * N + z], prod[(size_t)(2 * j + 1) * N + z]);
+      v[jj] = make_float2(rows[z], rows[N + z]);
     }
-    group_fft<E, T, false>(v, l, tile, twl, gmask);
+    __syncwarp(gmask);  // every lane holds its points before the slot becomes the tile
+    group_fft<E, T, false>(v, l, slot, twl, gmask);
 #pragma unroll
-    for (int jj = 0; jj < E; ++jj) zb[(size_t)j * N + l + T * jj] = v[jj];
+    for (int jj = 0; jj < E; ++jj) slot[l + T * jj] = v[jj];
   }
   __syncthreads();
   float2* Hq = a.Hq + s * (int64_t)NF * Kc * a.pl + (int64_t)x * N + y0;
-  for (int e = threadIdx.x; e < nf * Kc; e += blockDim.x) {
-    const int j = e / Kc, k = e - j * Kc;
+  for (int e = threadIdx.x; e < NF * Kc * TY; e += blockDim.x) {
+    const int yy = e % TY, r = e / TY;  // r = f Kc + k
+    const int f = r / Kc, k = r - f * Kc;
+    const int q = f * TY + yy;
+    const float2* zb = slots + (size_t)(q >> 1) * SL;
     float2 P, Q;
-    unpack_pair(zb[(size_t)j * N + k], zb[(size_t)j * N + (k == 0 ? 0 : N - k)], P, Q);
-    const int qa = 2 * j, qb = qa + 1;
-    const int fa = qa / TY, ya = qa - fa * TY, fb = qb / TY, yb = qb - fb * TY;
-    Hq[((int64_t)fa * Kc + k) * a.pl + ya] = P;
-    Hq[((int64_t)fb * Kc + k) * a.pl + yb] = Q;
+    unpack_pair(zb[k], zb[k == 0 ? 0 : N - k], P, Q);
+    Hq[(int64_t)r * a.pl + yy] = (q & 1) ? Q : P;
   }
 }
 
-// ---- pass 3a: 2D forward transform of one product field on one kz plane, in place in Hq
+// ---- pass 3a: 2D forward transform of one product field on one kz plane, in place in Hq; rows go
+// from global memory straight into the registers of their transform group
 template <int N>
 __global__ void __launch_bounds__(Cfg<N>::THREADS) pass3_3d_kernel(const Args a) {
   using R = Cfg<N>;
@@ -230,10 +257,22 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass3_3d_kernel(const Args a)
   const int kz = blockIdx.x, f = blockIdx.y;
   const int64_t s = blockIdx.z;
   load_twl<N>(twl, a.tw);
-  float2* H = a.Hq + ((s * a.p.NF + f) * a.Kc + kz) * a.pl;
-  for (int e = threadIdx.x; e < N * N; e += blockDim.x) plane[(size_t)(e / N) * R::PS + (e % N)] = H[e];
   __syncthreads();
-  planes_fft<N, false>(plane, 1, sp3 + R::TILES, twl);
+  const int gi = threadIdx.x / R::T, l = threadIdx.x % R::T;
+  const unsigned gmask = group_mask<N>();
+  float2* tile = sp3 + R::TILES + (size_t)gi * R::TS;
+  float2* H = a.Hq + ((s * a.p.NF + f) * a.Kc + kz) * a.pl;
+  for (int kx = gi; kx < N; kx += R::NG) {
+    float2 v[R::E];
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) v[j] = H[kx * N + l + R::T * j];
+    group_fft<R::E, R::T, false>(v, l, tile, twl, gmask);
+#pragma unroll
+    for (int j = 0; j < R::E; ++j) plane[(size_t)kx * R::PS + l + R::T * j] = v[j];
+  }
+  __syncthreads();
+  plane_cols_fft<N, false>(plane, sp3 + R::TILES, twl);
+  __syncthreads();
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) H[e] = plane[(size_t)(e / N) * R::PS + (e % N)];
 }
 
@@ -372,9 +411,8 @@ template <int N>
 struct Sizes {
   using R = Cfg<N>;
   static size_t s1() { return sizeof(float2) * ((size_t)R::FREE + R::PLANE); }
-  static size_t s2(int NI, int NF, int TY) {
-    return sizeof(float2) * (size_t)R::FREE + sizeof(float) * (size_t)(NI + NF) * TY * N +
-           sizeof(float2) * (size_t)NF * TY / 2 * N;
+  static size_t s2(int NI, int NF, int TY, int Kc) {
+    return sizeof(float2) * ((size_t)N + (size_t)NI * Kc * TY + (size_t)std::max(NI, NF) * TY / 2 * R::SLOT);
   }
   static size_t s3() { return s1(); }
 };
@@ -392,7 +430,7 @@ static size_t smem_limit() {
 template <int N>
 static int launch(Args& a, int64_t n, cudaStream_t st, bool set_attrs) {
   constexpr int TH = Cfg<N>::THREADS;
-  const size_t s1 = Sizes<N>::s1(), s2 = Sizes<N>::s2(a.p.NI, a.p.NF, a.TY), s3 = Sizes<N>::s3();
+  const size_t s1 = Sizes<N>::s1(), s2 = Sizes<N>::s2(a.p.NI, a.p.NF, a.TY, a.Kc), s3 = Sizes<N>::s3();
   if (set_attrs) {
     EXGB_CUDA(cudaFuncSetAttribute(pass1_3d_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1));
     EXGB_CUDA(cudaFuncSetAttribute(pass2_3d_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s2));
@@ -415,9 +453,9 @@ bool pass3d_supported(int D, int N, int NI, int NF) {
   if (D != 3 || (N != 32 && N != 64 && N != 128) || NI < 1 || NF < 1 || NI > MAXC * 4 || NF > 2 * MAXC)
     return false;
   const size_t lim = smem_limit() - 1024;
-  if (N == 32) return Sizes<32>::s1() <= lim && Sizes<32>::s2(NI, NF, 8) <= lim;
-  if (N == 64) return Sizes<64>::s1() <= lim && Sizes<64>::s2(NI, NF, 8) <= lim;
-  return Sizes<128>::s1() <= lim && Sizes<128>::s2(NI, NF, 8) <= lim;
+  if (N == 32) return Sizes<32>::s1() <= lim && Sizes<32>::s2(NI, NF, 8, 17) <= lim;
+  if (N == 64) return Sizes<64>::s1() <= lim && Sizes<64>::s2(NI, NF, 8, 33) <= lim;
+  return Sizes<128>::s1() <= lim && Sizes<128>::s2(NI, NF, 8, 65) <= lim;
 }
 
 template <bool SET>
