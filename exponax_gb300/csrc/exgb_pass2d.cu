@@ -210,10 +210,11 @@ struct RegPass {
   static constexpr int E = RegCfg<N>::E, T = RegCfg<N>::T;
   static constexpr int TS = tile_stride<E, T>();
   // every pass keeps each sequence in a slot of SLOT float2 that also serves as its transform's
-  // transpose tile (the sequence is in registers meanwhile); pass 2 runs 128 threads at N = 512,
-  // where a lane holds 32 points
+  // transpose tile (the sequence is in registers meanwhile); at N = 512, where a lane holds 32 points
+  // (about 90-128 registers), CTAs of 128 threads (5 per SM against 2 of 256: 2.06e10 -> 2.21e10
+  // DOF-steps/s on Kolmogorov 512^2)
   static constexpr int SLOT = N > TS ? N : TS;
-  static constexpr int THREADS = 256, NG = THREADS / T;
+  static constexpr int THREADS = N >= 512 ? 128 : 256, NG = THREADS / T;
   static constexpr int THREADS2 = N >= 512 ? 128 : 256, NG2 = THREADS2 / T;
   // float2 offsets: twiddles, then the pass's slots
   static constexpr int TWL = 0, FREE13 = N;
@@ -562,7 +563,8 @@ struct RegSizes {
 template <int N>
 static bool reg_tiles(int NI, int NF, int& TY, int& TX, int& TY3) {
   const size_t cap = smem_limit() - 1024;
-  TY = 4;  // 2 and (pass 2) TX = 8 measured slower at 512^2 and 256^2
+  // columns per pass-1 CTA: 4 (2 at N = 512, where 128-thread CTAs take one sequence per group)
+  TY = N >= 512 ? 2 : 4;
   TX = 4;
   TY3 = std::max(4, std::min(16, RegPass<N>::NG / std::max(1, NF)));  // one sequence per group
   while (TY > 1 && RegSizes<N>::s1(NI, TY) > cap / 2) --TY;
