@@ -24,12 +24,14 @@
 namespace exgb {
 
 void* workspace(size_t bytes, int slot_offset);
+int irfftn_impl(cudaStream_t st, int D, int N, int64_t count, const float2* in, float* out);
 
 enum : int {
   MODE_TRAJ = 0,      // physical in, trajectory out
   MODE_FINAL = 1,     // physical in, final physical state out
   MODE_FOURIER = 2,   // Fourier in, final Fourier state out
   MODE_NONLIN = 3,    // Fourier in, N(u^) out
+  MODE_TRAJ_HAT = 4,  // physical in, trajectory of Fourier states out (one batched irfft afterwards)
 };
 
 struct Item1D {
@@ -395,7 +397,7 @@ __device__ void run_item(const Item1D& item, const PlanDev& P, float2* sm, int s
   }
 
   // ---- load initial state
-  if (mode == MODE_TRAJ || mode == MODE_FINAL) {
+  if (mode == MODE_TRAJ || mode == MODE_FINAL || mode == MODE_TRAJ_HAT) {
     const float* u0 = (const float*)item.in;
     const int pairs = (m + 1) / 2;
     for (int t = tid; t < pairs * N; t += nthr) {
@@ -428,6 +430,14 @@ __device__ void run_item(const Item1D& item, const PlanDev& P, float2* sm, int s
   }
   sync();
 
+  if (mode == MODE_TRAJ_HAT && include_init) {  // frame 0 (overwritten by the exact input afterwards)
+    float2* o = (float2*)item.out;
+    for (int t = tid; t < m * M; t += nthr) {
+      const int i = t / M, k = t - i * M;
+      o[(int64_t)i * item.out_stride + k] = b.U[t];
+    }
+  }
+
   // ---- time steps
   const int nstages = (P.order == 0 || P.kind == EXGB_NL_ZERO) ? 0 : P.order;
   for (int step = 0; step < nsteps; ++step) {
@@ -454,6 +464,13 @@ __device__ void run_item(const Item1D& item, const PlanDev& P, float2* sm, int s
     if (mode == MODE_TRAJ) {
       float* o = (float*)item.out + (int64_t)(step + include_init) * N;
       emit_phys<FUSE>(P, b, m, o, item.out_stride, tid, nthr, sync);
+    } else if (mode == MODE_TRAJ_HAT) {
+      // the step's Fourier state; the batched inverse transform after the launch makes it physical
+      float2* o = (float2*)item.out + (int64_t)(step + include_init) * M;
+      for (int t = tid; t < m * M; t += nthr) {
+        const int i = t / M, k = t - i * M;
+        o[(int64_t)i * item.out_stride + k] = b.U[t];
+      }
     }
   }
 
@@ -631,12 +648,21 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
     while (m > 1 && smem_for(P, m, false) > (size_t)smem_limit() - 4096) --m;
   }
   const int T = nsteps + (include_init ? 1 : 0);
+  // A trajectory with at most one item per SM (latency-bound: each SM steps one item) is written as
+  // Fourier states and made physical by one batched inverse transform over all SMs afterwards, which
+  // takes the per-step output transform off the items' critical path.
+  float2* htraj = nullptr;
+  if (mode == MODE_TRAJ && (batch + m - 1) / m <= (int64_t)plan->sm_count && T > 0) {
+    htraj = (float2*)workspace(sizeof(float2) * (size_t)batch * T * P.M, 3);
+    if (!htraj) return fail(EXGB_ENOMEM, "workspace allocation failed");
+    mode = MODE_TRAJ_HAT;
+  }
   std::vector<Item1D> items;
   for (int64_t b0 = 0; b0 < batch; b0 += m) {
     Item1D it{};
     it.plan = plan->d_dev;
     it.m = (int)std::min<int64_t>(m, batch - b0);
-    if (mode == MODE_TRAJ || mode == MODE_FINAL) {
+    if (mode == MODE_TRAJ || mode == MODE_FINAL || mode == MODE_TRAJ_HAT) {
       it.in = u0_phys + b0 * P.N;
       it.in_stride = P.N;
     } else {
@@ -646,6 +672,9 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
     if (mode == MODE_TRAJ) {
       it.out = out_phys + b0 * (int64_t)T * P.N;
       it.out_stride = (int64_t)T * P.N;
+    } else if (mode == MODE_TRAJ_HAT) {
+      it.out = htraj + b0 * (int64_t)T * P.M;
+      it.out_stride = (int64_t)T * P.M;
     } else if (mode == MODE_FINAL) {
       it.out = out_phys + b0 * P.N;
       it.out_stride = P.N;
@@ -670,8 +699,15 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
     }
     if (smem + tw <= kQueueSmemCap) smem += tw;
   }
-  return launch_items(items, smem, st, nsteps, mode, project, include_init, plan->sm_count, nonlinear_only, threads,
-                      gstate_bytes);
+  const int rc = launch_items(items, smem, st, nsteps, mode, project, include_init, plan->sm_count, nonlinear_only,
+                              threads, gstate_bytes);
+  if (rc || mode != MODE_TRAJ_HAT) return rc;
+  const int rc2 = irfftn_impl(st, 1, P.N, batch * T, htraj, out_phys);
+  if (rc2) return rc2;
+  if (include_init)  // the initial frame is the input itself, not its round trip
+    EXGB_CUDA(cudaMemcpy2DAsync(out_phys, sizeof(float) * (size_t)T * P.N, u0_phys, sizeof(float) * P.N,
+                                sizeof(float) * P.N, (size_t)batch, cudaMemcpyDeviceToDevice, st));
+  return EXGB_OK;
 }
 
 }  // namespace exgb
