@@ -393,117 +393,162 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __nv_
   }
 }
 
-// 1 -> 48 forward: pre = conv(x) + b, post = gelu(pre).  One thread per (pixel, 8-channel chunk):
-// the six threads of a pixel share its 9 input values through L1, and a warp stores 512 contiguous
-// bytes per output.  `pre` may be NULL (inference: no backward pass follows).
-__global__ void conv_in1_kernel(const float* __restrict__ x, int B, int H, const float* __restrict__ w,
-                                const float* __restrict__ bias, __nv_bfloat16* __restrict__ pre,
-                                __nv_bfloat16* __restrict__ post) {
-  __shared__ float wsm[9 * kC + kC];
+// 1 -> 48 forward: pre = conv(x) + b, post = gelu(pre).  One thread per pixel of sample blockIdx.y,
+// all 48 channels in chunks of 8, so every weight read is one shared-memory address for the whole warp
+// (a broadcast); a block stages its 256 pixels' 96-byte outputs in shared memory (112-byte rows:
+// conflict-free 16-byte accesses) and stores them as consecutive 16-byte pieces.  `pre` (training
+// only) is written straight from the threads; NULL at inference.
+constexpr int kIn1Pix = 56;  // bf16 per staged output pixel (48 used)
+__global__ void __launch_bounds__(256) conv_in1_kernel(const float* __restrict__ x, int H, const float* __restrict__ w,
+                                                       const float* __restrict__ bias, __nv_bfloat16* __restrict__ pre,
+                                                       __nv_bfloat16* __restrict__ post) {
+  __shared__ __align__(16) float wsm[9 * kC + kC];
+  __shared__ __align__(16) __nv_bfloat16 stage[256 * kIn1Pix];
   for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];  // [tap][co]
   for (int t = threadIdx.x; t < kC; t += blockDim.x) wsm[9 * kC + t] = bias[t];
   __syncthreads();
-  const int64_t n = (int64_t)B * H * kW * (kC / 8);
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = t / (kC / 8);
-    const int cg = (int)(t - p * (kC / 8));
-    const int64_t b = p / (H * kW);
-    const int r = (int)(p - b * H * kW);
-    const int y = r / kW, xx = r % kW;
-    float v[9];
+  const float4* w4 = reinterpret_cast<const float4*>(wsm);
+  const int npix = H * kW;
+  const int p0 = blockIdx.x * 256;
+  const int p = p0 + threadIdx.x;
+  const bool live = p < npix;
+  const float* xb = x + (int64_t)blockIdx.y * npix;
+  const int64_t ob = (int64_t)blockIdx.y * npix;
+  float v[9];
+  {
+    const int pp = live ? p : 0;
+    const int y = pp / kW, xx = pp % kW;
 #pragma unroll
     for (int tap = 0; tap < 9; ++tap) {
       int gy = y + tap / 3 - 1;
       gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
       const int gx = (xx + tap % 3 - 1) & (kW - 1);
-      v[tap] = __ldg(x + (b * H + gy) * kW + gx);
+      v[tap] = __ldg(xb + gy * kW + gx);
+    }
+  }
+#pragma unroll 1
+  for (int q = 0; q < kC / 8; ++q) {
+    float acc[8];
+    {
+      const float4 b0 = w4[(9 * kC + q * 8) / 4], b1 = w4[(9 * kC + q * 8) / 4 + 1];
+      acc[0] = b0.x; acc[1] = b0.y; acc[2] = b0.z; acc[3] = b0.w;
+      acc[4] = b1.x; acc[5] = b1.y; acc[6] = b1.z; acc[7] = b1.w;
+    }
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+      const float4 wa = w4[(tap * kC + q * 8) / 4], wb = w4[(tap * kC + q * 8) / 4 + 1];
+      acc[0] = fmaf(wa.x, v[tap], acc[0]);
+      acc[1] = fmaf(wa.y, v[tap], acc[1]);
+      acc[2] = fmaf(wa.z, v[tap], acc[2]);
+      acc[3] = fmaf(wa.w, v[tap], acc[3]);
+      acc[4] = fmaf(wb.x, v[tap], acc[4]);
+      acc[5] = fmaf(wb.y, v[tap], acc[5]);
+      acc[6] = fmaf(wb.z, v[tap], acc[6]);
+      acc[7] = fmaf(wb.w, v[tap], acc[7]);
     }
     uint32_t hp[4], hq[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int co = cg * 8 + 2 * j;
-      float s0 = wsm[9 * kC + co], s1 = wsm[9 * kC + co + 1];
-#pragma unroll
-      for (int tap = 0; tap < 9; ++tap) {
-        s0 = fmaf(wsm[tap * kC + co], v[tap], s0);
-        s1 = fmaf(wsm[tap * kC + co + 1], v[tap], s1);
-      }
+      const float s0 = acc[2 * j], s1 = acc[2 * j + 1];
       const __nv_bfloat162 a = __floats2bfloat162_rn(s0, s1);
       const __nv_bfloat162 g = __floats2bfloat162_rn(gelu_f(s0), gelu_f(s1));
       hp[j] = *reinterpret_cast<const uint32_t*>(&a);
       hq[j] = *reinterpret_cast<const uint32_t*>(&g);
     }
-    if (pre) *reinterpret_cast<uint4*>(pre + t * 8) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
-    *reinterpret_cast<uint4*>(post + t * 8) = make_uint4(hq[0], hq[1], hq[2], hq[3]);
+    *reinterpret_cast<uint4*>(stage + threadIdx.x * kIn1Pix + q * 8) = make_uint4(hq[0], hq[1], hq[2], hq[3]);
+    if (pre && live) *reinterpret_cast<uint4*>(pre + (ob + p) * kC + q * 8) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
+  }
+  __syncthreads();
+  const int np = min(256, npix - p0);
+  for (int e = threadIdx.x; e < np * (kC / 8); e += blockDim.x) {
+    const int pl = e / (kC / 8), q = e - pl * (kC / 8);
+    *reinterpret_cast<uint4*>(post + (ob + p0 + pl) * kC + q * 8) =
+        *reinterpret_cast<const uint4*>(stage + pl * kIn1Pix + q * 8);
   }
 }
 
-// 48 -> 1 forward: out = base + scale * (conv(h) + b).  Four threads per pixel, 12 channels each
-// (three 8-byte loads per tap, so a warp reads 8 whole 96-byte pixels per tap), partial sums
-// combined by two warp shuffles.
-__global__ void conv_out1_kernel(const __nv_bfloat16* __restrict__ h, int B, int H, const float* __restrict__ w,
-                                 const float* __restrict__ bias, const float* __restrict__ base, float scale,
-                                 float* __restrict__ out) {
-  __shared__ float wsm[9 * kC];
+// 48 -> 1 forward: out = base + scale * (conv(h) + b).  A block computes kOut1Rows output rows of sample
+// blockIdx.y, one thread per output pixel: the kOut1Rows + 2 input rows it needs are first copied to
+// shared memory in 16-byte pieces (pixels padded to 112 bytes, so that the 16-byte reads of 8
+// consecutive pixels hit distinct banks), then each thread reads its 9 x 48 inputs from there and the
+// weights as broadcast float4.  (Reading the inputs through L1, 9 times per value in 8-byte pieces,
+// took 1.3x as long; a thread per column and 4 rows with a chunk's weights in registers, 107
+// registers at 2 warps per block, 1.1x.)
+constexpr int kOut1Rows = 4;    // output rows per block: kOut1Rows x kW = 256 threads
+constexpr int kOut1Pix = 56;    // bf16 per pixel in shared memory (48 used)
+__global__ void __launch_bounds__(kOut1Rows * kW) conv_out1_kernel(const __nv_bfloat16* __restrict__ h, int H,
+                                                                   const float* __restrict__ w,
+                                                                   const float* __restrict__ bias,
+                                                                   const float* __restrict__ base, float scale,
+                                                                   float* __restrict__ out) {
+  __shared__ __align__(16) float wsm[9 * kC];
+  __shared__ __align__(16) __nv_bfloat16 rows[(kOut1Rows + 2) * kW * kOut1Pix];
   for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];  // [tap][ci]
-  __syncthreads();
-  const int64_t n = (int64_t)B * H * kW * 4;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  // whole warps run the same number of iterations (n is a multiple of 4 and the shuffles stay in quads)
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t - (threadIdx.x & 31) < n; t += stride) {
-    const bool live = t < n;
-    const int64_t p = live ? t >> 2 : 0;
-    const int j = (int)(t & 3);
-    const int64_t b = p / (H * kW);
-    const int r = (int)(p - b * H * kW);
-    const int y = r / kW, xx = r % kW;
-    float s = 0.f;
-#pragma unroll 3
-    for (int tap = 0; tap < 9; ++tap) {
-      int gy = y + tap / 3 - 1;
-      gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
-      const int gx = (xx + tap % 3 - 1) & (kW - 1);
-      const uint2* src = reinterpret_cast<const uint2*>(h + ((b * H + gy) * kW + gx) * kC + 12 * j);
-      const float* wt = wsm + tap * kC + 12 * j;
-#pragma unroll
-      for (int q = 0; q < 3; ++q) {
-        const uint2 u = __ldg(src + q);
-        const float2 f0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
-        const float2 f1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
-        s = fmaf(wt[4 * q], f0.x, s);
-        s = fmaf(wt[4 * q + 1], f0.y, s);
-        s = fmaf(wt[4 * q + 2], f1.x, s);
-        s = fmaf(wt[4 * q + 3], f1.y, s);
-      }
-    }
-    s += __shfl_xor_sync(0xffffffffu, s, 1);
-    s += __shfl_xor_sync(0xffffffffu, s, 2);
-    if (live && j == 0) out[p] = (base ? base[p] : 0.f) + scale * (s + bias[0]);
+  const int y0 = blockIdx.x * kOut1Rows;
+  const __nv_bfloat16* hb = h + (int64_t)blockIdx.y * H * kW * kC;
+  for (int e = threadIdx.x; e < (kOut1Rows + 2) * kW * (kC / 8); e += blockDim.x) {
+    const int r = e / (kW * (kC / 8)), rem = e - r * (kW * (kC / 8));
+    const int px = rem / (kC / 8), q = rem - px * (kC / 8);
+    int gy = y0 - 1 + r;
+    gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+    *reinterpret_cast<uint4*>(rows + (r * kW + px) * kOut1Pix + q * 8) =
+        __ldg(reinterpret_cast<const uint4*>(hb + ((int64_t)gy * kW + px) * kC + q * 8));
   }
+  __syncthreads();
+  const int oy = threadIdx.x / kW, ox = threadIdx.x % kW;
+  if (y0 + oy >= H) return;
+  const float4* w4 = reinterpret_cast<const float4*>(wsm);
+  float s = 0.f;
+#pragma unroll 3
+  for (int tap = 0; tap < 9; ++tap) {
+    const int ry = oy + tap / 3;
+    const int gx = (ox + tap % 3 - 1) & (kW - 1);
+    const uint4* src = reinterpret_cast<const uint4*>(rows + (ry * kW + gx) * kOut1Pix);
+#pragma unroll
+    for (int q = 0; q < kC / 8; ++q) {
+      const uint4 u = src[q];
+      const float4 wa = w4[(tap * kC + q * 8) / 4], wb = w4[(tap * kC + q * 8) / 4 + 1];
+      const float2 f0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+      const float2 f1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+      const float2 f2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.z));
+      const float2 f3 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.w));
+      s = fmaf(wa.x, f0.x, s);
+      s = fmaf(wa.y, f0.y, s);
+      s = fmaf(wa.z, f1.x, s);
+      s = fmaf(wa.w, f1.y, s);
+      s = fmaf(wb.x, f2.x, s);
+      s = fmaf(wb.y, f2.y, s);
+      s = fmaf(wb.z, f3.x, s);
+      s = fmaf(wb.w, f3.y, s);
+    }
+  }
+  const int64_t p = ((int64_t)blockIdx.y * H + y0 + oy) * kW + ox;
+  out[p] = (base ? base[p] : 0.f) + scale * (s + bias[0]);
 }
 
 // backward of the 48 -> 1 layer w.r.t. its input, times GELU'(pre):
 // dpre[p][ci] = gelu'(pre[p][ci]) * sum_tap w[tap][ci] * dout[p - shift(tap)].  One thread per
 // (pixel, 8-channel chunk), coalesced 16-byte loads and stores.
-__global__ void conv_out1_bwd_data_kernel(const float* __restrict__ dout, int B, int H, const float* __restrict__ w,
+__global__ void conv_out1_bwd_data_kernel(const float* __restrict__ dout, int H, const float* __restrict__ w,
                                           const __nv_bfloat16* __restrict__ pre, __nv_bfloat16* __restrict__ dpre) {
   __shared__ float wsm[9 * kC];
   for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];
   __syncthreads();
-  const int64_t n = (int64_t)B * H * kW * (kC / 8);
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = t / (kC / 8);
-    const int cg = (int)(t - p * (kC / 8));
-    const int64_t b = p / (H * kW);
-    const int r = (int)(p - b * H * kW);
-    const int y = r / kW, xx = r % kW;
+  const int n = H * kW * (kC / 8);  // per sample (blockIdx.y)
+  const float* db = dout + (int64_t)blockIdx.y * H * kW;
+  const int64_t ob = (int64_t)blockIdx.y * n;
+  for (int tl = blockIdx.x * blockDim.x + threadIdx.x; tl < n; tl += gridDim.x * blockDim.x) {
+    const int p = tl / (kC / 8);
+    const int cg = tl - p * (kC / 8);
+    const int y = p / kW, xx = p % kW;
+    const int64_t t = ob + tl;
     float g[9];
 #pragma unroll
     for (int tap = 0; tap < 9; ++tap) {
       int gy = y - (tap / 3 - 1);
       gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
       const int gx = (xx - (tap % 3 - 1)) & (kW - 1);
-      g[tap] = __ldg(dout + (b * H + gy) * kW + gx);
+      g[tap] = __ldg(db + gy * kW + gx);
     }
     const uint4 pr = *reinterpret_cast<const uint4*>(pre + t * 8);
     const uint32_t prw[4] = {pr.x, pr.y, pr.z, pr.w};
@@ -782,8 +827,9 @@ int exgb_conv_in1(void* stream, const float* x, int B, int H, const float* w, co
   if (!x || !w || !bias || !post || B < 0 || H < 1) return fail(EXGB_EINVAL, "NULL argument or bad shape");
   if ((int64_t)B * H == 0) return EXGB_OK;
   if ((int64_t)B * H > 2147483647LL) return fail(EXGB_EINVAL, "too many rows");
-  conv_in1_kernel<<<blocks_for((int64_t)B * H * kW * (kC / 8)), 256, 0, (cudaStream_t)stream>>>(x, B, H, w, bias, (__nv_bfloat16*)pre,
-                                                                   (__nv_bfloat16*)post);
+  if (B > 65535) return fail(EXGB_EINVAL, "batch above 65535");
+  conv_in1_kernel<<<dim3((H * kW + 255) / 256, B), 256, 0, (cudaStream_t)stream>>>(x, H, w, bias, (__nv_bfloat16*)pre,
+                                                                                   (__nv_bfloat16*)post);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }
@@ -793,17 +839,20 @@ int exgb_conv_out1(void* stream, const void* h, int B, int H, const float* w, co
   if (!h || !w || !bias || !out || B < 0 || H < 1) return fail(EXGB_EINVAL, "NULL argument or bad shape");
   if ((int64_t)B * H == 0) return EXGB_OK;
   if ((int64_t)B * H > 2147483647LL) return fail(EXGB_EINVAL, "too many rows");
-  conv_out1_kernel<<<blocks_for((int64_t)B * H * kW * 4), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)h, B, H, w, bias, base,
-                                                                    scale, out);
+  if (B > 65535) return fail(EXGB_EINVAL, "batch above 65535");
+  conv_out1_kernel<<<dim3((H + kOut1Rows - 1) / kOut1Rows, B), kOut1Rows * kW, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)h, H, w, bias, base, scale, out);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }
 
 int exgb_conv_out1_bwd_data(void* stream, const float* dout, int B, int H, const float* w, const void* pre,
                             void* dpre) {
-  const int64_t n = (int64_t)B * H * kW * (kC / 8);
-  conv_out1_bwd_data_kernel<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(dout, B, H, w, (const __nv_bfloat16*)pre,
-                                                                             (__nv_bfloat16*)dpre);
+  if (!dout || !w || !pre || !dpre || B < 0 || H < 1) return fail(EXGB_EINVAL, "NULL argument or bad shape");
+  if (B == 0) return EXGB_OK;
+  if (B > 65535) return fail(EXGB_EINVAL, "batch above 65535");
+  conv_out1_bwd_data_kernel<<<dim3((H * kW * (kC / 8) + 255) / 256, B), 256, 0, (cudaStream_t)stream>>>(
+      dout, H, w, (const __nv_bfloat16*)pre, (__nv_bfloat16*)dpre);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }
