@@ -191,3 +191,23 @@ def test_projected_convection_term(kolmogorov):
     uh = o.fft(velocity_ic(N, 3))
     got = host(fm(cu(uh)))
     assert rel(got, fo(uh)) < 2e-5
+
+
+def test_128_batch_over_workspace_chunks_and_nonlinear_term():
+    """128^3: 10 samples per 1 GiB workspace chunk (ETDRK2), so a batch of 12 splits in two; the
+    projected-convection term alone at 128^3 against the oracle."""
+    N = 128
+    sm = ex.stepper.NavierStokesVelocity(3, 2 * np.pi, N, 0.01, diffusivity=0.01, order=2)
+    u0 = velocity_ic(N, 5)
+    B, same = 12, (0, 9, 10, 11)
+    batch = np.stack([u0 if b in same else np.roll(u0, 3 * b, axis=-2) * (1 + 0.01 * b) for b in range(B)])
+    got = host(ex.vmap(sm)(cu(batch)))
+    alone = host(sm(cu(u0)))
+    for b in same:
+        assert rel(got[b], alone) < 1e-6, b
+    dm = ex.spectral.build_derivative_operator(3, 2 * np.pi, N)
+    do = o.build_derivative_operator(3, 2 * np.pi, N)
+    fm = ex.nonlin_fun.ProjectedConvection3dKolmogorov(3, N, derivative_operator=dm, dealiasing_fraction=2 / 3)
+    fo = o.ProjectedConvection3dKolmogorov(3, N, derivative_operator=do, dealiasing_fraction=2 / 3)
+    uh = o.fft(u0)
+    assert rel(host(fm(cu(uh))), fo(uh)) < 2e-5
