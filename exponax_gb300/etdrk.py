@@ -64,6 +64,20 @@ class BaseETDRK:
         return p
 
     def _any_plan(self) -> Plan:
+        """A plan to read the coefficient tables from (they depend on the linear operator only): an
+        existing one, else one at the first channel count the nonlinear function accepts among the
+        linear operator's, the number of spatial dimensions, 2 and 3 (projected convection, for one,
+        takes 3 channels with a single-channel operator)."""
+        if self._plans:
+            return next(iter(self._plans.values()))
+        nl = self._nonlinear_fun
+        for C in (self.linear_operator.shape[0], self.num_spatial_dims, 2, 3):
+            if nl is not None:
+                try:
+                    nl._check_channels(C)
+                except ValueError:
+                    continue
+            return self._plan(C)
         return self._plan(self.linear_operator.shape[0])
 
     @property

@@ -56,15 +56,26 @@ def test_fft_ifft_roundtrip_abs_1e5():
 # ------------------------------------------------------------------ coefficients
 
 @pytest.mark.parametrize("order", [1, 2, 3, 4])
-@pytest.mark.parametrize("case", ["ks", "kdv", "ns"])
+@pytest.mark.parametrize("case", ["ks", "kdv", "ns", "ns3d32", "burgers3d32", "ns3d21"])
 def test_phi_coefficients_match_fp64_oracle(order, case):
-    if case == "ks":
+    """The tables read back through exgb_plan_get_table in the natural layout, whichever layout the
+    plan keeps them in (2D fused / three-pass: [ky][kx]; 3D three-pass, N = 32: plane-major)."""
+    if case == "ns3d32":
+        args, mk, mo = (3, 2 * np.pi, 32, 0.01), ex.stepper.NavierStokesVelocity, o.NavierStokesVelocity
+        kw = {"diffusivity": 0.01}
+    elif case == "burgers3d32":
+        args, mk, mo = (3, 2 * np.pi, 32, 0.01), ex.stepper.Burgers, o.Burgers
+        kw = {"diffusivity": 0.05}
+    elif case == "ns3d21":
+        args, mk, mo = (3, 2 * np.pi, 21, 0.01), ex.stepper.NavierStokesVelocity, o.NavierStokesVelocity
+        kw = {"diffusivity": 0.01}
+    elif case == "ks":
         args, mk, mo = (1, 100.0, 200, 0.1), ex.stepper.KuramotoSivashinskyConservative, o.KuramotoSivashinskyConservative
         kw = {}
     elif case == "kdv":
         args, mk, mo = (1, 20.0, 256, 0.01), ex.stepper.KortewegDeVries, o.KortewegDeVries
         kw = {}
-    else:
+    elif case == "ns":
         args, mk, mo = (2, 2 * np.pi, 64, 0.01), ex.stepper.NavierStokesVorticity, o.NavierStokesVorticity
         kw = {"diffusivity": 1e-3}
     mine = mk(*args, order=order, **kw)._integrator
