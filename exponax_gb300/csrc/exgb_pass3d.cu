@@ -63,6 +63,9 @@ template <int N>
 struct Cfg {
   static constexpr int E = RegCfg<N>::E, T = RegCfg<N>::T;
   static constexpr int THREADS = 256, NG = THREADS / T;
+  // pass 2: up to N = 64, 24 transform groups, one per line pair of projected convection's 6 fields
+  // x 8 lines (32 groups left a quarter idle: 32^3 +10 %, 64^3 +2 %); 32 at N = 128 (24: -6 %)
+  static constexpr int NG2 = N <= 64 ? 24 : 32, THREADS2 = NG2 * T;
   static constexpr int TS = tile_stride<E, T>();
   static constexpr int SLOT = N > TS ? N : TS;  // pass 2: a pair of lines, also its transform's tile
   static constexpr int PS = N + 1;  // padded row stride of a plane in shared memory
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass1_3d_kernel(const Args a)
 // physical lines, then (products overwritten in place) the pair's r2c transform and spectrum; the
 // spectra leave as runs of TY consecutive y again.
 template <int N>
-__global__ void __launch_bounds__(Cfg<N>::THREADS) pass2_3d_kernel(const Args a) {
+__global__ void __launch_bounds__(Cfg<N>::THREADS2) pass2_3d_kernel(const Args a) {
   using R = Cfg<N>;
   constexpr int E = R::E, T = R::T, M = N / 2 + 1, SL = R::SLOT;
   extern __shared__ __align__(16) float2 sp2[];
@@ -180,7 +183,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass2_3d_kernel(const Args a)
   const unsigned gmask = group_mask<N>();
   const float inv = 1.f / ((float)N * (float)N * (float)N);
   const int ni = NI * TY / 2;
-  for (int j = gi; j < ni; j += R::NG) {
+  for (int j = gi; j < ni; j += R::NG2) {
     const int qa = 2 * j, qb = qa + 1;
     const int fa = qa / TY, ya = qa - fa * TY, fb = qb / TY, yb = qb - fb * TY;
     float2* slot = slots + (size_t)j * SL;
@@ -219,7 +222,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass2_3d_kernel(const Args a)
   }
   __syncthreads();
   const int nf = NF * TY / 2;
-  for (int j = gi; j < nf; j += R::NG) {
+  for (int j = gi; j < nf; j += R::NG2) {
     float2* slot = slots + (size_t)j * SL;
     const float* rows = reinterpret_cast<const float*>(slot);
     float2 v[E];
@@ -438,7 +441,7 @@ static int launch(Args& a, int64_t n, cudaStream_t st, bool set_attrs) {
     return EXGB_OK;
   }
   pass1_3d_kernel<N><<<dim3(a.Kc, a.p.NI, (unsigned)n), TH, s1, st>>>(a);
-  pass2_3d_kernel<N><<<dim3(N * (N / a.TY), (unsigned)n), TH, s2, st>>>(a);
+  pass2_3d_kernel<N><<<dim3(N * (N / a.TY), (unsigned)n), Cfg<N>::THREADS2, s2, st>>>(a);
   pass3_3d_kernel<N><<<dim3(a.Kc, a.p.NF, (unsigned)n), TH, s3, st>>>(a);
   combine_planes_kernel<<<grid_for(n * a.Kc * a.pl, a.sm), 256, 0, st>>>(a, n);
   return EXGB_OK;
