@@ -160,6 +160,11 @@ REACTION = [
     ("BelousovZhabotinsky", 1, 128, dict(domain_extent=1.0, dt=0.01), 50),
     ("BelousovZhabotinsky", 2, 48, dict(domain_extent=1.0, dt=0.01, diffusivities=(1e-3, 2e-3, 1e-3)), 50),
     ("BelousovZhabotinsky", 3, 16, dict(domain_extent=1.0, dt=0.01), 20),
+    # N = 32: the three-pass 3D path (exgb_pass3d.cu); N = 16 above runs on the five-kernel path
+    ("FisherKPP", 3, 32, dict(domain_extent=1.0, dt=0.001, diffusivity=0.01, reactivity=10.0), 10),
+    ("CahnHilliard", 3, 32, dict(domain_extent=2 * np.pi, dt=0.001, gamma=1e-3), 10),
+    ("GrayScott", 3, 32, dict(domain_extent=1.0, dt=0.5, diffusivity_1=2e-5, diffusivity_2=1e-5), 10),
+    ("BelousovZhabotinsky", 3, 32, dict(domain_extent=1.0, dt=0.01), 10),
 ]
 
 

@@ -211,3 +211,22 @@ def test_128_batch_over_workspace_chunks_and_nonlinear_term():
     fo = o.ProjectedConvection3dKolmogorov(3, N, derivative_operator=do, dealiasing_fraction=2 / 3)
     uh = o.fft(u0)
     assert rel(host(fm(cu(uh))), fo(uh)) < 2e-5
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_burgers_3d_orders_64(order):
+    N = 64
+    sm = ex.stepper.Burgers(3, 2 * np.pi, N, 0.01, diffusivity=0.05, order=order)
+    so = o.Burgers(3, 2 * np.pi, N, 0.01, diffusivity=0.05, order=order)
+    u = _field(N, 3, 11)
+    assert rel(host(sm(cu(u))), so(u)) < 1e-5
+
+
+def test_kuramoto_sivashinsky_3d_32():
+    """Gradient-norm nonlinearity (KuramotoSivashinsky, combustion form) on the three-pass 3D path."""
+    N = 32
+    sm = ex.stepper.KuramotoSivashinsky(3, 20.0, N, 0.05)
+    so = o.KuramotoSivashinsky(3, 20.0, N, 0.05)
+    u = _field(N, 1, 12)
+    assert rel(host(sm(cu(u))), so(u)) < 1e-5
+    assert rel(host(ex.repeat(sm, 10)(cu(u))), o.repeat(so, 10)(u)) < 1e-4
