@@ -101,10 +101,11 @@ def test_kolmogorov_velocity_repeat_and_rollout(N):
 
 
 def test_ns_velocity_no_dealiasing_and_one_half():
-    """No mask (every plane enters the nonlinear term, the Nyquist plane included) and the 1/2 mask."""
+    """No mask (every plane enters the nonlinear term, the Nyquist plane kz = N/2 included, with its
+    c2r projection on the plane-major state), the 1.0 mask and the 1/2 mask."""
     N = 32
     u = velocity_ic(N, 7)
-    for frac in (1.0, 0.5):
+    for frac in (None, 1.0, 0.5):
         sm = ex.stepper.NavierStokesVelocity(3, 2 * np.pi, N, 0.005, diffusivity=0.02, dealiasing_fraction=frac)
         so = o.NavierStokesVelocity(3, 2 * np.pi, N, 0.005, diffusivity=0.02, dealiasing_fraction=frac)
         assert rel(host(ex.repeat(sm, 3)(cu(u))), o.repeat(so, 3)(u)) < 1e-5, frac
