@@ -20,6 +20,7 @@
 //   deterministic reduction.
 // * adam_kernel: FP32 master weights, bf16 working copies (and the flipped
 //   copy used by backward-data).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -72,7 +73,12 @@ __device__ __forceinline__ float gelu_d(float x) {
 //
 // Warp roles, handing tiles over through mbarriers (every wait clock-bounded; a wait that gives up
 // raises a CTA-wide abort flag and the status word read by exgb_conv_status):
-//   warps 0-3   copy a tile's input rows into one of two stages (cp.async), then arrive on full[s]
+//   warp 13     (one thread) loads a tile's 4 input rows with TMA (cp.async.bulk.tensor) into the
+//               dx = 0 copy of one of two stages once empty[s] says the stage is free, completing on
+//               tfull[s] by transaction bytes
+//   warps 0-3   wait tfull[s], build the dx = -1 and dx = +1 copies from the dx = 0 copy (16-byte
+//               shared-memory copies with the periodic wrap along x, which TMA boxes cannot express),
+//               then arrive on full[s]
 //   warp 12     waits full[s] and accumulator a free, issues the 27 MMAs, commits to empty[s] and
 //               accfull[a]
 //   warps 4-11  wait accfull[a], read the accumulator (warp w: TMEM lanes 32 (w % 4).., 24 channels),
@@ -82,7 +88,8 @@ __device__ __forceinline__ float gelu_d(float x) {
 namespace ctc {
 constexpr int kProducerWarps = 4, kEpilogueWarps = 8;
 constexpr int kMmaWarp = kProducerWarps + kEpilogueWarps;      // 12
-constexpr int kThreads = 32 * (kMmaWarp + 1);                  // 416
+constexpr int kTmaWarp = kMmaWarp + 1;                         // 13
+constexpr int kThreads = 32 * (kTmaWarp + 1);                  // 448
 constexpr int kProducerThreads = 32 * kProducerWarps;
 constexpr int kEpilogueThreads = 32 * kEpilogueWarps;
 constexpr int kHaloRows = 4;                                   // 2 output rows + 1 above + 1 below
@@ -96,78 +103,79 @@ constexpr uint32_t kOutBytes = 2 * kW * kC * 2;                // 12288 B: one t
 constexpr uint32_t kOffW = 2 * kStageBytes;
 constexpr uint32_t kOffOut = kOffW + kWBytes;                  // staged `post` (forward) or result (backward)
 constexpr uint32_t kOffOut2 = kOffOut + kOutBytes;             // staged `pre` (forward before a backward pass)
-constexpr uint32_t kOffBar = kOffOut2 + kOutBytes;             // 9 mbarriers
-constexpr uint32_t kSmemBytes = kOffBar + 9 * 8;
+constexpr uint32_t kOffBar = kOffOut2 + kOutBytes;             // 11 mbarriers
+constexpr uint32_t kSmemBytes = kOffBar + 11 * 8;
 constexpr uint32_t kAccCols = 64;                              // accumulator a at TMEM column 64 a
-constexpr int kItems = (int)kSlots * (kC / 8) / kProducerThreads;  // (slot, chunk) copies per producer per tile
+constexpr int kItems = (int)kSlots * (kC / 8) / kProducerThreads;  // (slot, chunk) pairs per producer per tile
 constexpr long long kWaitBudget = 4000000000LL;                // clock cycles (~2 s)
 static_assert(kItems * kProducerThreads == (int)kSlots * (kC / 8), "whole copy items per producer thread");
 static_assert(kSmemBytes + 1024 <= 227 * 1024, "conv tile does not fit in shared memory");
 static_assert(kStageBytes % 16 == 0 && kWBytes % 16 == 0 && kOutBytes % 16 == 0, "16-byte aligned regions");
 }  // namespace ctc
 
+// cuTensorMapEncodeTiled, reached through the runtime's driver entry point (no link against libcuda)
+typedef CUresult (*PFN_encode)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                               const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
 __device__ int g_conv_status;  // EXGB_ETIMEOUT after a bounded wait of the conv kernel gave up
 
-// Copy items of producer thread p, fixed for every tile: item i of the 256 x 6 (slot, chunk) pairs in
-// blocks of 8 slots x 6 chunks, so the 8 threads of a shared-memory store phase write 8 consecutive
-// slots of one chunk (distinct banks) and a warp reads whole 64-byte runs of 4 chunks per pixel.
-struct CopyItems {
-  int src[ctc::kItems];        // element offset inside an input row: column * 48 + chunk * 8
-  int row[ctc::kItems];        // halo row 0..3
-  uint32_t dst[ctc::kItems];   // byte offset in a stage of copy dx = -1 (low 16 bits) and 0 (high 16 bits)
-  uint32_t dst2[ctc::kItems];  // byte offset of copy dx = +1
-};
-
-__device__ __forceinline__ void conv_items(int p, CopyItems& c) {
-#pragma unroll
-  for (int k = 0; k < ctc::kItems; ++k) {
-    const int i = p + ctc::kProducerThreads * k;
-    const int blk = i / 48, rem = i - blk * 48;
-    const int ch = rem >> 3, q = blk * 8 + (rem & 7);
-    const int r = q >> 6, gx = q & (kW - 1);
-    c.src[k] = gx * kC + ch * 8;
-    c.row[k] = r;
-    // copy dx holds x[.][(c + dx) mod 64] at column c, so input column gx lands at c = gx - dx
-    uint32_t o[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-      o[d] = (uint32_t)d * ctc::kCopyBytes + (uint32_t)ch * ctc::kChunkStride +
-             (uint32_t)(r * kW + ((gx - (d - 1)) & (kW - 1))) * 16u;
-    c.dst[k] = o[0] | (o[1] << 16);
-    c.dst2[k] = o[2];
-  }
+// TMA: the tile's 4 input rows (y0 - 1 .. y0 + 2, periodic inside the image) into the dx = 0 copy of
+// a stage, chunk by chunk (box: 8 channels x 64 columns x 4 rows, or 1 row each where the rows wrap),
+// completing on mbarrier `bar` by transaction bytes (kCopyBytes in either case)
+__device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      : "memory");
 }
-
-// Copy the 4 input rows of tile `tile` (rows y0 - 1 .. y0 + 2, periodic inside the image) into the
-// three shifted copies with 16-byte cp.async (L1-allocating, so the three copies of a chunk read
-// global memory once), as one commit group.
-__device__ __forceinline__ void conv_load_tile(const __nv_bfloat16* __restrict__ x, int H, int tile,
-                                               uint32_t stage_saddr, const CopyItems& c) {
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}\n" ::"r"(
+                   tc::smem_u32(mbar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void conv_tma_tile(const CUtensorMap* map4, const CUtensorMap* map1, int H, int tile,
+                                              uint32_t copy0_saddr, uint64_t* bar) {
   const int tiles_per_img = H / 2;
   const int b = tile / tiles_per_img, y0 = (tile - b * tiles_per_img) * 2;
-  const __nv_bfloat16* xb = x + (size_t)b * H * kW * kC;
-  int rows[ctc::kHaloRows];
+  mbar_arrive_expect_tx(bar, ctc::kCopyBytes);
+  const uint32_t mb = tc::smem_u32(bar);
+  if (y0 >= 1 && y0 + 2 <= H - 1) {
 #pragma unroll
-  for (int r = 0; r < ctc::kHaloRows; ++r) {
-    const int gy = y0 + r - 1;
-    rows[r] = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+    for (int ch = 0; ch < kC / 8; ++ch)
+      tma_load3(copy0_saddr + (uint32_t)ch * ctc::kChunkStride, map4, ch * 8, 0, b * H + y0 - 1, mb);
+  } else {
+#pragma unroll
+    for (int r = 0; r < ctc::kHaloRows; ++r) {
+      int gy = y0 + r - 1;
+      gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
+#pragma unroll
+      for (int ch = 0; ch < kC / 8; ++ch)
+        tma_load3(copy0_saddr + (uint32_t)ch * ctc::kChunkStride + (uint32_t)(r * kW) * 16u, map1, ch * 8, 0,
+                  b * H + gy, mb);
+    }
   }
-#pragma unroll
-  for (int k = 0; k < ctc::kItems; ++k) {
-    int gy = rows[0];
-#pragma unroll
-    for (int r = 1; r < ctc::kHaloRows; ++r) gy = c.row[k] == r ? rows[r] : gy;
-    const __nv_bfloat16* src = xb + (size_t)gy * kW * kC + c.src[k];
-    const uint32_t d0 = stage_saddr + (c.dst[k] & 0xFFFFu), d1 = stage_saddr + (c.dst[k] >> 16),
-                   d2 = stage_saddr + c.dst2[k];
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d0), "l"(src) : "memory");
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d1), "l"(src) : "memory");
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d2), "l"(src) : "memory");
-  }
-  asm volatile("cp.async.commit_group;" ::: "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_but_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// The shifted copies of a stage from its dx = 0 copy: copy d (dx = d - 1) holds x[y][(c + dx) mod 64]
+// at column c.  Producer thread p moves (slot, chunk) pairs p, p + 128, ... (consecutive threads:
+// consecutive slots of one chunk, distinct banks).
+__device__ __forceinline__ void conv_shift_tile(unsigned char* stage, int p) {
+  const unsigned char* c0 = stage + ctc::kCopyBytes;
+#pragma unroll 4
+  for (int k = 0; k < ctc::kItems; ++k) {
+    const int i = p + ctc::kProducerThreads * k;
+    const int ch = i / (int)ctc::kSlots, q = i - ch * (int)ctc::kSlots;
+    const int r = q / kW, c = q - r * kW;
+    const uint32_t row = (uint32_t)ch * ctc::kChunkStride + (uint32_t)(r * kW) * 16u;
+    const uint4 left = *reinterpret_cast<const uint4*>(c0 + row + (uint32_t)((c - 1) & (kW - 1)) * 16u);
+    const uint4 right = *reinterpret_cast<const uint4*>(c0 + row + (uint32_t)((c + 1) & (kW - 1)) * 16u);
+    *reinterpret_cast<uint4*>(stage + row + (uint32_t)c * 16u) = left;                            // dx = -1
+    *reinterpret_cast<uint4*>(stage + 2 * ctc::kCopyBytes + row + (uint32_t)c * 16u) = right;    // dx = +1
+  }
+}
+
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
   asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(tc::smem_u32(mbar))
@@ -209,7 +217,8 @@ __device__ __forceinline__ void conv_issue(uint32_t stage_saddr, uint32_t w_sadd
 
 // mode 0: forward  out_post = gelu(conv(x) + bias), and out_pre = conv(x) + bias unless out_pre is NULL
 // mode 1: backward data  out_pre (= dPre of the layer below) = conv_flipped(x = dPre) * gelu'(aux = pre below)
-__global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __nv_bfloat16* __restrict__ x, int B, int H,
+__global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __grid_constant__ CUtensorMap map4,
+                                                                  const __grid_constant__ CUtensorMap map1, int B, int H,
                                                                   const __nv_bfloat16* __restrict__ w,
                                                                   const float* __restrict__ bias, int mode,
                                                                   const __nv_bfloat16* __restrict__ aux,
@@ -224,6 +233,7 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __nv_
   uint64_t* accfull = bars + 4;   // [2] accumulator a holds a finished tile
   uint64_t* accempty = bars + 6;  // [2] the epilogue has read accumulator a
   uint64_t* drain = bars + 8;     // every MMA of this CTA has completed (before the TMEM is released)
+  uint64_t* tfull = bars + 9;     // [2] the TMA bytes of stage s have landed
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ntiles = B * (H / 2);
   const uint32_t sbase = tc::smem_u32(smem);
@@ -252,6 +262,8 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __nv_
       tc::mbar_init(accempty + i, ctc::kEpilogueThreads);
     }
     tc::mbar_init(drain, 1);
+    tc::mbar_init(tfull, 1);
+    tc::mbar_init(tfull + 1, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::fence_proxy_async();
@@ -266,18 +278,34 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __nv_
   };
   auto aborted = [&]() { return *reinterpret_cast<volatile int*>(&s_abort) != 0; };
 
-  if (warp < ctc::kProducerWarps) {
-    // ---------------- producers: tile i of this CTA goes to stage i & 1
-    CopyItems items;
-    conv_items(tid, items);
+  if (warp == ctc::kTmaWarp) {
+    // ---------------- TMA (lane 0): tile i of this CTA goes to stage i & 1 once the stage is free
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map4)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map1)) : "memory");
+      int i = 0;
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+        const int s = i & 1;
+        const uint32_t par = ((uint32_t)(i >> 1) & 1u) ^ 1u;  // the first use of a stage passes at once
+        if (!tc::mbar_wait(empty + s, par, ctc::kWaitBudget)) { give_up(); break; }
+        if (aborted()) break;
+        conv_tma_tile(&map4, &map1, H, tile, sbase + (uint32_t)s * ctc::kStageBytes + ctc::kCopyBytes, tfull + s);
+      }
+      // no TMA copy may still be writing shared memory when the CTA ends (after an abort the producers
+      // may not have waited for the last ones): wait for the last two issued tiles' bytes
+      for (int j = i - 2 < 0 ? 0 : i - 2; j < i; ++j)
+        if (!tc::mbar_wait(tfull + (j & 1), (uint32_t)(j >> 1) & 1u, ctc::kWaitBudget)) give_up();
+    }
+    __syncwarp();
+  } else if (warp < ctc::kProducerWarps) {
+    // ---------------- producers: the shifted copies of tile i in stage i & 1
     int i = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int s = i & 1;
-      const uint32_t par = ((uint32_t)(i >> 1) & 1u) ^ 1u;  // the first use of a stage passes at once
-      if (!tc::mbar_wait(empty + s, par, ctc::kWaitBudget)) { give_up(); break; }
+      const uint32_t par = (uint32_t)(i >> 1) & 1u;
+      if (!tc::mbar_wait(tfull + s, par, ctc::kWaitBudget)) { give_up(); break; }
       if (aborted()) break;
-      conv_load_tile(x, H, tile, sbase + (uint32_t)s * ctc::kStageBytes, items);
-      cp_async_wait_all();
+      conv_shift_tile(smem + (uint32_t)s * ctc::kStageBytes, tid);
       tc::fence_proxy_async();  // the copies -> visible to the tensor core (async proxy)
       mbar_arrive(full + s);
     }
@@ -801,10 +829,36 @@ int exgb_conv48(void* stream, const void* x, int B, int H, const void* w, const 
   }
   const int64_t ntiles = (int64_t)B * (H / 2);
   if (ntiles > 2147483647LL) return fail(EXGB_EINVAL, "exgb_conv48: too many tiles");
+  if (((uintptr_t)x & 15) != 0) return fail(EXGB_EINVAL, "exgb_conv48: input not 16-byte aligned");
+  // tensor maps of the input (bf16, dims innermost first: 48 channels, 64 columns, B H rows), boxes of
+  // 8 channels x 64 columns x 4 rows and x 1 row
+  CUtensorMap map4, map1;
+  {
+    static PFN_encode encode = nullptr;
+    if (!encode) {
+      void* fn = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      EXGB_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+      if (q != cudaDriverEntryPointSuccess || !fn) return fail(EXGB_ECUDA, "cuTensorMapEncodeTiled not available");
+      encode = (PFN_encode)fn;
+    }
+    const cuuint64_t dims[3] = {(cuuint64_t)kC, (cuuint64_t)kW, (cuuint64_t)B * H};
+    const cuuint64_t strides[2] = {(cuuint64_t)kC * 2, (cuuint64_t)kW * kC * 2};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const cuuint32_t box4[3] = {8, (cuuint32_t)kW, (cuuint32_t)ctc::kHaloRows}, box1[3] = {8, (cuuint32_t)kW, 1};
+    CUresult r = encode(&map4, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(x), dims, strides, box4, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r == CUDA_SUCCESS)
+      r = encode(&map1, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(x), dims, strides, box1, estr,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(EXGB_ECUDA, "exgb_conv48: tensor map encoding failed");
+  }
   const unsigned grid = (unsigned)std::min<int64_t>(ntiles, sm_count[dev]);
   conv48_tc_kernel<<<grid, ctc::kThreads, ctc::kSmemBytes, (cudaStream_t)stream>>>(
-      (const __nv_bfloat16*)x, B, H, (const __nv_bfloat16*)w, bias, mode, (const __nv_bfloat16*)aux,
-      (__nv_bfloat16*)out_pre, (__nv_bfloat16*)out_post);
+      map4, map1, B, H, (const __nv_bfloat16*)w, bias, mode, (const __nv_bfloat16*)aux, (__nv_bfloat16*)out_pre,
+      (__nv_bfloat16*)out_post);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
 }
