@@ -59,58 +59,65 @@ __device__ __forceinline__ float gelu_d(float x) {
 }
 
 // 48 -> 48 channels as an implicit GEMM on the tcgen05 tensor cores.  A tile is 2 output rows x 64
-// columns = 128 pixels (M = 128) x 48 output channels (N = 48); K = 9 taps x 48 input channels, 27
-// MMAs of K = 16 issued by one thread with the FP32 accumulator in tensor memory.
+// columns = 128 pixels (M = 128).  A tcgen05.mma of K = 16 costs its issuing thread ~143 cycles for
+// any N up to 256, so the three horizontal taps of a row offset dy are stacked along N: operand B of
+// row offset dy is W[(dy, dx)][co][ci] for dx = -1, 0, +1 one after the other (N = 144 rows n =
+// 48 (dx + 1) + co, K-major), and
+//   D[p][n] = sum_dy sum_ci x[y_p + dy][x_p][ci] W[(dy, dx)][co][ci]
+// holds, for pixel p = (y_p, x_p), input column x_p's contribution to output column x_p - dx: 9 MMAs
+// of N = 144 per tile.  The epilogue adds out[y][x] = D[(y, x - 1)][dx = -1] + D[(y, x)][0] +
+// D[(y, x + 1)][+1] (periodic in x) through a padded FP32 exchange buffer in shared memory.
 //
-// Operand A of tap (dy, dx) is read straight from a shared-memory copy of the 4 input rows the tile
-// needs, with no im2col: the copy for horizontal shift dx holds x[y][(c + dx) mod 64] at pixel slot
-// q = 64 r + c (r the halo row, the periodic wrap applied while copying), stored K-major without
-// swizzle as 8-channel chunks: (q, channel) at chunk * 4096 + q * 16 + (channel % 8) * 2.  Rows of
-// the A operand (pixels) are 16 bytes apart inside and across core matrices (stride byte offset
-// 128), chunks 4096 bytes apart (leading byte offset), so the 128 pixels of output rows (oy, oy+1)
-// under tap (dy, dx) are the 128 consecutive slots from q = 64 (1 + dy) of copy dx: one descriptor.
-// Operand B is W[tap][co][ci] in the K-major layout of exgb_tc.cuh.
+// Operand A of row offset dy is read straight from a stage holding the tile's 4 input rows, unshifted
+// and periodic in y: pixel slot q = 64 r + c holds x[y0 - 1 + r][c], K-major without swizzle as
+// 8-channel chunks ((q, channel) at chunk * 4096 + q * 16 + (channel % 8) * 2), so the 128 pixels of
+// output rows (y0, y0 + 1) under row offset dy are the 128 consecutive slots from q = 64 (1 + dy)
+// (stride byte offset 128, leading byte offset 4096): one descriptor.  The stage is exactly the
+// layout a TMA box of 8 channels x 64 columns x 4 rows lands in.
 //
 // Warp roles, handing tiles over through mbarriers (every wait clock-bounded; a wait that gives up
 // raises a CTA-wide abort flag and the status word read by exgb_conv_status):
-//   warp 13     (one thread) loads a tile's 4 input rows with TMA (cp.async.bulk.tensor) into the
-//               dx = 0 copy of one of two stages once empty[s] says the stage is free, completing on
-//               tfull[s] by transaction bytes
-//   warps 0-3   wait tfull[s], build the dx = -1 and dx = +1 copies from the dx = 0 copy (16-byte
-//               shared-memory copies with the periodic wrap along x, which TMA boxes cannot express),
-//               then arrive on full[s]
-//   warp 12     waits full[s] and accumulator a free, issues the 27 MMAs, commits to empty[s] and
+//   warp 13     (one thread) loads a tile's 4 input rows by TMA (cp.async.bulk.tensor, one box per
+//               8-channel chunk, or per row where the rows wrap in y) into one of kStages stages once
+//               empty[s] says it is free; the bytes complete full[s]
+//   warp 12     waits full[s] and accumulator a free, issues the 9 MMAs, commits to empty[s] and
 //               accfull[a]
-//   warps 4-11  wait accfull[a], read the accumulator (warp w: TMEM lanes 32 (w % 4).., 24 channels),
-//               free it, apply bias and GELU (or GELU' for the backward pass), stage the tile's outputs
-//               in shared memory -- they form the 12 KB the tile occupies contiguously in global
+//   warps 0-11  wait accfull[a], read the accumulator (warp w: TMEM lanes 32 (w % 4).. = pixels, 16
+//               channels of each dx block), free it, publish the dx = -1 / +1 partial sums, add the
+//               neighbours' ones, apply bias and GELU (or GELU' for the backward pass), stage the
+//               tile's outputs in shared memory -- the 12 KB the tile occupies contiguously in global
 //               memory -- and one thread writes them with a bulk copy
 namespace ctc {
-constexpr int kProducerWarps = 4, kEpilogueWarps = 8;
-constexpr int kMmaWarp = kProducerWarps + kEpilogueWarps;      // 12
+constexpr int kEpilogueWarps = 12;
+constexpr int kMmaWarp = kEpilogueWarps;                       // 12
 constexpr int kTmaWarp = kMmaWarp + 1;                         // 13
 constexpr int kThreads = 32 * (kTmaWarp + 1);                  // 448
-constexpr int kProducerThreads = 32 * kProducerWarps;
 constexpr int kEpilogueThreads = 32 * kEpilogueWarps;
+constexpr int kStages = 4;                                     // input stages in flight
 constexpr int kHaloRows = 4;                                   // 2 output rows + 1 above + 1 below
-constexpr uint32_t kSlots = kHaloRows * kW;                    // 256 pixel slots per copy
+constexpr int kN = 3 * kC;                                     // 144: the three dx taps stacked along N
+constexpr int kCe = kC / 3;                                    // 16 channels per epilogue thread
+constexpr uint32_t kSlots = kHaloRows * kW;                    // 256 pixel slots
 constexpr uint32_t kChunkStride = kSlots * 16;                 // 4096 B between 8-channel chunks
-constexpr uint32_t kCopyBytes = (kC / 8) * kChunkStride;       // 24576 B per shifted copy
-constexpr uint32_t kStageBytes = 3 * kCopyBytes;               // dx = -1, 0, +1
-constexpr uint32_t kTapBytes = kC * kC * 2;                    // 4608 B of weights per tap
-constexpr uint32_t kWBytes = 9 * kTapBytes;
+constexpr uint32_t kStageBytes = (kC / 8) * kChunkStride;      // 24576 B per stage
+constexpr uint32_t kDyBytes = kN * kC * 2;                     // 13824 B of weights per row offset dy
+constexpr uint32_t kWBytes = 3 * kDyBytes;
 constexpr uint32_t kOutBytes = 2 * kW * kC * 2;                // 12288 B: one tile of bf16 outputs
-constexpr uint32_t kOffW = 2 * kStageBytes;
+constexpr int kXPix = kC + 4;                                  // floats per pixel in the exchange buffer
+constexpr uint32_t kXBytes = 2u * 128u * kXPix * 4u;           // [dx = -1 | +1][pixel][kXPix] floats
+constexpr uint32_t kOffW = kStages * kStageBytes;
 constexpr uint32_t kOffOut = kOffW + kWBytes;                  // staged `post` (forward) or result (backward)
 constexpr uint32_t kOffOut2 = kOffOut + kOutBytes;             // staged `pre` (forward before a backward pass)
-constexpr uint32_t kOffBar = kOffOut2 + kOutBytes;             // 11 mbarriers
-constexpr uint32_t kSmemBytes = kOffBar + 11 * 8;
-constexpr uint32_t kAccCols = 64;                              // accumulator a at TMEM column 64 a
-constexpr int kItems = (int)kSlots * (kC / 8) / kProducerThreads;  // (slot, chunk) pairs per producer per tile
+constexpr uint32_t kOffX = kOffOut2 + kOutBytes;               // dx = -1 / +1 partial sums of a tile
+constexpr uint32_t kOffBar = kOffX + kXBytes;                  // 2 kStages + 5 mbarriers
+constexpr uint32_t kSmemBytes = kOffBar + (2 * kStages + 5) * 8;
+constexpr uint32_t kAccCols = 256;                             // accumulator a at TMEM column 256 a (144 used)
 constexpr long long kWaitBudget = 4000000000LL;                // clock cycles (~2 s)
-static_assert(kItems * kProducerThreads == (int)kSlots * (kC / 8), "whole copy items per producer thread");
 static_assert(kSmemBytes + 1024 <= 227 * 1024, "conv tile does not fit in shared memory");
-static_assert(kStageBytes % 16 == 0 && kWBytes % 16 == 0 && kOutBytes % 16 == 0, "16-byte aligned regions");
+static_assert(kStageBytes % 1024 == 0 && kWBytes % 16 == 0 && kOutBytes % 16 == 0 && kXBytes % 16 == 0,
+              "aligned regions");
+static_assert(kN % 16 == 0 && kN <= 256, "M = 128 needs N a multiple of 16, at most 256");
+static_assert(kC % 3 == 0 && kCe % 4 == 0, "epilogue channel groups of whole 16-byte pieces");
 }  // namespace ctc
 
 // cuTensorMapEncodeTiled, reached through the runtime's driver entry point (no link against libcuda)
@@ -120,9 +127,9 @@ typedef CUresult (*PFN_encode)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, vo
 
 __device__ int g_conv_status;  // EXGB_ETIMEOUT after a bounded wait of the conv kernel gave up
 
-// TMA: the tile's 4 input rows (y0 - 1 .. y0 + 2, periodic inside the image) into the dx = 0 copy of
-// a stage, chunk by chunk (box: 8 channels x 64 columns x 4 rows, or 1 row each where the rows wrap),
-// completing on mbarrier `bar` by transaction bytes (kCopyBytes in either case)
+// TMA: the tile's 4 input rows (y0 - 1 .. y0 + 2, periodic inside the image) into a stage, chunk by
+// chunk (box: 8 channels x 64 columns x 4 rows, or 1 row each where the rows wrap), completing on
+// mbarrier `bar` by transaction bytes (kStageBytes in either case)
 __device__ __forceinline__ void tma_load3(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t bar) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
@@ -136,15 +143,15 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t b
                : "memory");
 }
 __device__ __forceinline__ void conv_tma_tile(const CUtensorMap* map4, const CUtensorMap* map1, int H, int tile,
-                                              uint32_t copy0_saddr, uint64_t* bar) {
+                                              uint32_t stage_saddr, uint64_t* bar) {
   const int tiles_per_img = H / 2;
   const int b = tile / tiles_per_img, y0 = (tile - b * tiles_per_img) * 2;
-  mbar_arrive_expect_tx(bar, ctc::kCopyBytes);
+  mbar_arrive_expect_tx(bar, ctc::kStageBytes);
   const uint32_t mb = tc::smem_u32(bar);
   if (y0 >= 1 && y0 + 2 <= H - 1) {
 #pragma unroll
     for (int ch = 0; ch < kC / 8; ++ch)
-      tma_load3(copy0_saddr + (uint32_t)ch * ctc::kChunkStride, map4, ch * 8, 0, b * H + y0 - 1, mb);
+      tma_load3(stage_saddr + (uint32_t)ch * ctc::kChunkStride, map4, ch * 8, 0, b * H + y0 - 1, mb);
   } else {
 #pragma unroll
     for (int r = 0; r < ctc::kHaloRows; ++r) {
@@ -152,38 +159,33 @@ __device__ __forceinline__ void conv_tma_tile(const CUtensorMap* map4, const CUt
       gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
 #pragma unroll
       for (int ch = 0; ch < kC / 8; ++ch)
-        tma_load3(copy0_saddr + (uint32_t)ch * ctc::kChunkStride + (uint32_t)(r * kW) * 16u, map1, ch * 8, 0,
+        tma_load3(stage_saddr + (uint32_t)ch * ctc::kChunkStride + (uint32_t)(r * kW) * 16u, map1, ch * 8, 0,
                   b * H + gy, mb);
     }
   }
 }
 
-// The shifted copies of a stage from its dx = 0 copy: copy d (dx = d - 1) holds x[y][(c + dx) mod 64]
-// at column c.  Producer thread p moves (slot, chunk) pairs p, p + 128, ... (consecutive threads:
-// consecutive slots of one chunk, distinct banks).
-__device__ __forceinline__ void conv_shift_tile(unsigned char* stage, int p) {
-  const unsigned char* c0 = stage + ctc::kCopyBytes;
-#pragma unroll 4
-  for (int k = 0; k < ctc::kItems; ++k) {
-    const int i = p + ctc::kProducerThreads * k;
-    const int ch = i / (int)ctc::kSlots, q = i - ch * (int)ctc::kSlots;
-    const int r = q / kW, c = q - r * kW;
-    const uint32_t row = (uint32_t)ch * ctc::kChunkStride + (uint32_t)(r * kW) * 16u;
-    const uint4 left = *reinterpret_cast<const uint4*>(c0 + row + (uint32_t)((c - 1) & (kW - 1)) * 16u);
-    const uint4 right = *reinterpret_cast<const uint4*>(c0 + row + (uint32_t)((c + 1) & (kW - 1)) * 16u);
-    *reinterpret_cast<uint4*>(stage + row + (uint32_t)c * 16u) = left;                            // dx = -1
-    *reinterpret_cast<uint4*>(stage + 2 * ctc::kCopyBytes + row + (uint32_t)c * 16u) = right;    // dx = +1
-  }
-}
-
-
 __device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
   asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(tc::smem_u32(mbar))
                : "memory");
 }
-// named barrier over the epilogue warps only
-__device__ __forceinline__ void epilogue_sync() {
-  asm volatile("bar.sync 1, %0;" ::"n"(ctc::kEpilogueThreads) : "memory");
+// named barrier `id` over the `n` threads of the epilogue warps of one output row
+__device__ __forceinline__ void row_sync(uint32_t id, uint32_t n) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+// the same barrier, returning whether any of its threads passed `c` true: the warps of a row leave their
+// tile loop together (a warp leaving alone would strand the others at the next barrier)
+__device__ __forceinline__ bool row_any(uint32_t id, uint32_t n, bool c) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred pc, pr;\n\t"
+      "setp.ne.u32 pc, %1, 0;\n\t"
+      "bar.red.or.pred pr, %2, %3, pc;\n\t"
+      "selp.u32 %0, 1, 0, pr;\n\t}\n"
+      : "=r"(r)
+      : "r"((uint32_t)c), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
 }
 
 // bulk copy of `bytes` (multiple of 16) from shared to global memory, tracked by the bulk-group counter
@@ -201,16 +203,15 @@ __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.w
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 __device__ __forceinline__ void conv_issue(uint32_t stage_saddr, uint32_t w_saddr, uint32_t d_tmem) {
-  const uint32_t idesc = tc::idesc_bf16(128, kC);
-#pragma unroll 1
-  for (int tap = 0; tap < 9; ++tap) {
-    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-    const uint32_t a0 = stage_saddr + (uint32_t)(dx + 1) * ctc::kCopyBytes + (uint32_t)((1 + dy) * kW) * 16u;
+  const uint32_t idesc = tc::idesc_bf16(128, ctc::kN);
+#pragma unroll
+  for (int dy = 0; dy < 3; ++dy) {
+    const uint32_t a0 = stage_saddr + (uint32_t)(dy * kW) * 16u;  // halo rows dy, dy + 1
 #pragma unroll
     for (int s = 0; s < kC / 16; ++s) {
       const uint64_t ad = tc::smem_desc(a0 + (uint32_t)s * 2u * ctc::kChunkStride, ctc::kChunkStride, 128u);
-      const uint64_t bd = tc::kmaj_desc(w_saddr + (uint32_t)tap * ctc::kTapBytes, kC, s);
-      tc::mma_bf16(d_tmem, ad, bd, idesc, (tap | s) != 0 ? 1u : 0u);
+      const uint64_t bd = tc::kmaj_desc(w_saddr + (uint32_t)dy * ctc::kDyBytes, kC, s);
+      tc::mma_bf16(d_tmem, ad, bd, idesc, (dy | s) != 0 ? 1u : 0u);
     }
   }
 }
@@ -228,12 +229,12 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
   __shared__ uint32_t s_tmem;
   __shared__ int s_abort;
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + ctc::kOffBar);
-  uint64_t* full = bars;          // [2] stage s holds its tile's rows (producer arrivals)
-  uint64_t* empty = bars + 2;     // [2] the MMAs that read stage s have completed
-  uint64_t* accfull = bars + 4;   // [2] accumulator a holds a finished tile
-  uint64_t* accempty = bars + 6;  // [2] the epilogue has read accumulator a
-  uint64_t* drain = bars + 8;     // every MMA of this CTA has completed (before the TMEM is released)
-  uint64_t* tfull = bars + 9;     // [2] the TMA bytes of stage s have landed
+  uint64_t* full = bars;                         // [kStages] the TMA bytes of stage s have landed
+  uint64_t* empty = bars + ctc::kStages;         // [kStages] the MMAs that read stage s have completed
+  uint64_t* accfull = bars + 2 * ctc::kStages;   // [2] accumulator a holds a finished tile
+  uint64_t* accempty = accfull + 2;              // [2] the epilogue has read accumulator a
+  uint64_t* drain = accfull + 4;                 // every MMA of this CTA has completed (before the TMEM is released)
+  float* xbuf = reinterpret_cast<float*>(smem + ctc::kOffX);  // [2][128 pixels][kXPix]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int ntiles = B * (H / 2);
   const uint32_t sbase = tc::smem_u32(smem);
@@ -242,11 +243,13 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
   __nv_bfloat16* out_a = mode == 0 ? out_post : out_pre;
   __nv_bfloat16* out_b = mode == 0 ? out_pre : nullptr;
 
-  // weights -> K-major tiles, one per tap (consecutive threads: consecutive output channels)
-  for (int t = tid; t < 9 * kC * (kC / 8); t += ctc::kThreads) {
-    const int co = t % kC, rest = t / kC;  // rest = tap * 6 + chunk
-    const int ch = rest % (kC / 8), tap = rest / (kC / 8);
-    *reinterpret_cast<uint4*>(smem + ctc::kOffW + tap * ctc::kTapBytes + tc::kmaj_chunk(co, ch, kC)) =
+  // weights -> one K-major tile of N = 144 rows per row offset dy: row n = 48 (dx + 1) + co holds
+  // W[tap = 3 (dy + 1) + (dx + 1)][co][ci] (consecutive threads: consecutive rows)
+  for (int t = tid; t < 3 * ctc::kN * (kC / 8); t += ctc::kThreads) {
+    const int n = t % ctc::kN, rest = t / ctc::kN;  // rest = dy * 6 + chunk
+    const int ch = rest % (kC / 8), dy = rest / (kC / 8);
+    const int tap = 3 * dy + n / kC, co = n % kC;
+    *reinterpret_cast<uint4*>(smem + ctc::kOffW + dy * ctc::kDyBytes + tc::kmaj_chunk(n, ch, kC)) =
         *reinterpret_cast<const uint4*>(w + ((size_t)tap * kC + co) * kC + ch * 8);
   }
   if (warp == ctc::kMmaWarp) {
@@ -255,15 +258,15 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
   }
   if (tid == 0) {
     s_abort = 0;
-    for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(full + i, ctc::kProducerThreads);
+    for (int i = 0; i < ctc::kStages; ++i) {
+      tc::mbar_init(full + i, 1);
       tc::mbar_init(empty + i, 1);
+    }
+    for (int i = 0; i < 2; ++i) {
       tc::mbar_init(accfull + i, 1);
       tc::mbar_init(accempty + i, ctc::kEpilogueThreads);
     }
     tc::mbar_init(drain, 1);
-    tc::mbar_init(tfull, 1);
-    tc::mbar_init(tfull + 1, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::fence_proxy_async();
@@ -279,45 +282,33 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
   auto aborted = [&]() { return *reinterpret_cast<volatile int*>(&s_abort) != 0; };
 
   if (warp == ctc::kTmaWarp) {
-    // ---------------- TMA (lane 0): tile i of this CTA goes to stage i & 1 once the stage is free
+    // ---------------- TMA (lane 0): tile i of this CTA goes to stage i % kStages once the stage is free
     if (lane == 0) {
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map4)) : "memory");
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map1)) : "memory");
       int i = 0;
       for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
-        const int s = i & 1;
-        const uint32_t par = ((uint32_t)(i >> 1) & 1u) ^ 1u;  // the first use of a stage passes at once
+        const int s = i % ctc::kStages;
+        const uint32_t par = ((uint32_t)(i / ctc::kStages) & 1u) ^ 1u;  // the first use of a stage passes at once
         if (!tc::mbar_wait(empty + s, par, ctc::kWaitBudget)) { give_up(); break; }
         if (aborted()) break;
-        conv_tma_tile(&map4, &map1, H, tile, sbase + (uint32_t)s * ctc::kStageBytes + ctc::kCopyBytes, tfull + s);
+        conv_tma_tile(&map4, &map1, H, tile, sbase + (uint32_t)s * ctc::kStageBytes, full + s);
       }
-      // no TMA copy may still be writing shared memory when the CTA ends (after an abort the producers
-      // may not have waited for the last ones): wait for the last two issued tiles' bytes
-      for (int j = i - 2 < 0 ? 0 : i - 2; j < i; ++j)
-        if (!tc::mbar_wait(tfull + (j & 1), (uint32_t)(j >> 1) & 1u, ctc::kWaitBudget)) give_up();
+      // no TMA copy may still be writing shared memory when the CTA ends (after an abort the MMA
+      // thread may not have waited for the last ones): wait for the last issued tiles' bytes
+      for (int j = i - ctc::kStages < 0 ? 0 : i - ctc::kStages; j < i; ++j)
+        if (!tc::mbar_wait(full + (j % ctc::kStages), (uint32_t)(j / ctc::kStages) & 1u, ctc::kWaitBudget)) give_up();
     }
     __syncwarp();
-  } else if (warp < ctc::kProducerWarps) {
-    // ---------------- producers: the shifted copies of tile i in stage i & 1
-    int i = 0;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
-      const int s = i & 1;
-      const uint32_t par = (uint32_t)(i >> 1) & 1u;
-      if (!tc::mbar_wait(tfull + s, par, ctc::kWaitBudget)) { give_up(); break; }
-      if (aborted()) break;
-      conv_shift_tile(smem + (uint32_t)s * ctc::kStageBytes, tid);
-      tc::fence_proxy_async();  // the copies -> visible to the tensor core (async proxy)
-      mbar_arrive(full + s);
-    }
   } else if (warp == ctc::kMmaWarp) {
     // ---------------- MMA issuer (lane 0)
     if (lane == 0) {
       int i = 0;
       for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
-        const int s = i & 1, a = i & 1;
-        const uint32_t par = (uint32_t)(i >> 1) & 1u;
-        if (!tc::mbar_wait(full + s, par, ctc::kWaitBudget)) { give_up(); break; }
-        if (!tc::mbar_wait(accempty + a, par ^ 1u, ctc::kWaitBudget)) { give_up(); break; }
+        const int s = i % ctc::kStages, a = i & 1;
+        const uint32_t spar = (uint32_t)(i / ctc::kStages) & 1u, apar = (uint32_t)(i >> 1) & 1u;
+        if (!tc::mbar_wait(full + s, spar, ctc::kWaitBudget)) { give_up(); break; }
+        if (!tc::mbar_wait(accempty + a, apar ^ 1u, ctc::kWaitBudget)) { give_up(); break; }
         if (aborted()) break;
         tc::fence_after_sync();
         conv_issue(sbase + (uint32_t)s * ctc::kStageBytes, wsaddr, tmem + (uint32_t)a * ctc::kAccCols);
@@ -330,43 +321,74 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
     }
     __syncwarp();
   } else {
-    // ---------------- epilogue: warp w reads TMEM lanes 32 (w % 4) + lane = pixel m, 24 channels
-    constexpr int kCg = kC / 2;
-    const int ew = warp - ctc::kProducerWarps;
+    // ---------------- epilogue: warp w reads TMEM lanes 32 (w % 4) + lane = pixel m, channels
+    // 16 (w / 4) .. + 15 of each dx block.  The 6 warps of an output row (quadrants 2 r, 2 r + 1) sync
+    // among themselves only: the horizontal neighbours are in the same row, and the row's outputs are
+    // 6 KB contiguous in global memory, stored by the row's own leader.
+    constexpr int kCe = ctc::kCe;
+    constexpr uint32_t kRowThreads = ctc::kEpilogueThreads / 2;
     const int m = 32 * (warp & 3) + lane;
-    const int c0 = kCg * (ew >> 2);
-    const bool leader = ew == 0 && lane == 0;
-    float bv[kCg];
+    const int c0 = kCe * (warp >> 2);
+    const int orow = (warp & 3) >> 1;
+    const uint32_t rbar = 1u + (uint32_t)orow;
+    const bool leader = (warp >> 2) == 0 && (warp & 1) == 0 && lane == 0;  // warps 0 and 2
+    const int row = m / kW, xx = m % kW;
+    const int ml = row * kW + ((xx - 1) & (kW - 1)), mr = row * kW + ((xx + 1) & (kW - 1));
+    float bv[kCe];
 #pragma unroll
-    for (int j = 0; j < kCg; ++j) bv[j] = mode == 0 ? bias[c0 + j] : 0.f;
+    for (int j = 0; j < kCe; ++j) bv[j] = mode == 0 ? bias[c0 + j] : 0.f;
     const uint32_t stg = (uint32_t)(m * kC + c0) * 2u;  // byte offset of this thread's outputs in a staged tile
+    float* xm = xbuf + m * ctc::kXPix + c0;                     // this pixel's dx = -1 partials
+    float* xp = xbuf + (128 + m) * ctc::kXPix + c0;             // this pixel's dx = +1 partials
+    const float* xl = xbuf + ml * ctc::kXPix + c0;              // left neighbour's dx = -1 partials
+    const float* xr = xbuf + (128 + mr) * ctc::kXPix + c0;      // right neighbour's dx = +1 partials
     int i = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int a = i & 1;
       const uint32_t par = (uint32_t)(i >> 1) & 1u;
       const bool ok = tc::mbar_wait(accfull + a, par, ctc::kWaitBudget);
       if (!ok) give_up();
-      if (!ok || aborted()) break;
       tc::fence_after_sync();
       const uint32_t ta = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)a * ctc::kAccCols + (uint32_t)c0;
-      float v[kCg];
-      {
-        float a8[8], b8[8], c8[8];
-        tc::tmem_ld8x2(ta, ta + 8u, a8, b8);
-        tc::tmem_ld8(ta + 16u, c8);
+      // d[b][j]: accumulator column 48 b + c0 + j, block b = dx + 1 (not read if the wait gave up)
+      float d[3][kCe];
+      if (ok) {
+        tc::tmem_ld16(ta, d[0]);
+        tc::tmem_ld16(ta + (uint32_t)kC, d[1]);
+        tc::tmem_ld16(ta + 2u * kC, d[2]);
+      } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          v[j] = a8[j];
-          v[8 + j] = b8[j];
-          v[16 + j] = c8[j];
-        }
+        for (int b = 0; b < 3; ++b)
+#pragma unroll
+          for (int j = 0; j < kCe; ++j) d[b][j] = 0.f;
       }
       tc::fence_before_sync();
       mbar_arrive(accempty + a);  // accumulator a may be overwritten by the MMAs of tile i + 2
-      uint32_t ra[kCg / 2], rb[kCg / 2];
+      // publish the dx = -1 / +1 partial sums (the previous tile's readers passed the barrier before
+      // the staging of that tile)
+#pragma unroll
+      for (int q = 0; q < kCe / 4; ++q) {
+        *reinterpret_cast<float4*>(xm + 4 * q) = make_float4(d[0][4 * q], d[0][4 * q + 1], d[0][4 * q + 2], d[0][4 * q + 3]);
+        *reinterpret_cast<float4*>(xp + 4 * q) = make_float4(d[2][4 * q], d[2][4 * q + 1], d[2][4 * q + 2], d[2][4 * q + 3]);
+      }
+      if (leader) bulk_wait_read();  // the row's previous staged outputs have left shared memory
+      // one barrier of the row: partial sums published, staging free, and its warps agree whether to stop
+      if (row_any(rbar, kRowThreads, !ok || aborted())) break;
+      // out[x] = D[x - 1][dx = -1] + D[x][dx = 0] + D[x + 1][dx = +1] (periodic in x within the row)
+      float v[kCe];
+#pragma unroll
+      for (int q = 0; q < kCe / 4; ++q) {
+        const float4 l4 = *reinterpret_cast<const float4*>(xl + 4 * q);
+        const float4 r4 = *reinterpret_cast<const float4*>(xr + 4 * q);
+        v[4 * q] = d[1][4 * q] + l4.x + r4.x;
+        v[4 * q + 1] = d[1][4 * q + 1] + l4.y + r4.y;
+        v[4 * q + 2] = d[1][4 * q + 2] + l4.z + r4.z;
+        v[4 * q + 3] = d[1][4 * q + 3] + l4.w + r4.w;
+      }
+      uint32_t ra[kCe / 2], rb[kCe / 2];
       if (mode == 0) {
 #pragma unroll
-        for (int j = 0; j < kCg / 2; ++j) {
+        for (int j = 0; j < kCe / 2; ++j) {
           const float v0 = v[2 * j] + bv[2 * j], v1 = v[2 * j + 1] + bv[2 * j + 1];
           const __nv_bfloat162 p = __floats2bfloat162_rn(v0, v1);
           const __nv_bfloat162 g = __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
@@ -377,7 +399,7 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
         // pixel m of this tile: 128 * tile + m in the batch (tiles are consecutive row pairs)
         const size_t o = ((size_t)tile * 128 + m) * kC + c0;
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
+        for (int q = 0; q < kCe / 8; ++q) {
           const uint4 pr = *reinterpret_cast<const uint4*>(aux + o + 8 * q);
           const uint32_t prw[4] = {pr.x, pr.y, pr.z, pr.w};
 #pragma unroll
@@ -390,22 +412,21 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
           }
         }
       }
-      if (leader) bulk_wait_read();  // the previous tile's staged outputs have left shared memory
-      epilogue_sync();
 #pragma unroll
-      for (int q = 0; q < 3; ++q) {
+      for (int q = 0; q < kCe / 8; ++q) {
         *reinterpret_cast<uint4*>(smem + ctc::kOffOut + stg + 16 * q) =
             make_uint4(ra[4 * q], ra[4 * q + 1], ra[4 * q + 2], ra[4 * q + 3]);
         if (out_b)
           *reinterpret_cast<uint4*>(smem + ctc::kOffOut2 + stg + 16 * q) =
               make_uint4(rb[4 * q], rb[4 * q + 1], rb[4 * q + 2], rb[4 * q + 3]);
       }
-      tc::fence_proxy_async();  // staged outputs -> visible to the bulk copy
-      epilogue_sync();
+      tc::fence_proxy_async();    // staged outputs -> visible to the bulk copy
+      row_sync(rbar, kRowThreads);  // also: the row's threads have read this tile's neighbour partials
       if (leader) {
-        const size_t off = (size_t)tile * (ctc::kOutBytes / 2);  // in bf16 elements
-        bulk_store(out_a + off, sbase + ctc::kOffOut, ctc::kOutBytes);
-        if (out_b) bulk_store(out_b + off, sbase + ctc::kOffOut2, ctc::kOutBytes);
+        const uint32_t rb_ = (uint32_t)orow * (ctc::kOutBytes / 2);                         // bytes
+        const size_t off = (size_t)tile * (ctc::kOutBytes / 2) + (size_t)orow * (kW * kC);  // bf16 elements
+        bulk_store(out_a + off, sbase + ctc::kOffOut + rb_, ctc::kOutBytes / 2);
+        if (out_b) bulk_store(out_b + off, sbase + ctc::kOffOut2 + rb_, ctc::kOutBytes / 2);
         bulk_commit();
       }
     }
