@@ -84,9 +84,8 @@ __device__ __forceinline__ float gelu_d(float x) {
 //               accfull[a]
 //   warps 0-11  wait accfull[a], read the accumulator (warp w: TMEM lanes 32 (w % 4).. = pixels, 16
 //               channels of each dx block), free it, publish the dx = -1 / +1 partial sums, add the
-//               neighbours' ones, apply bias and GELU (or GELU' for the backward pass), stage the
-//               tile's outputs in shared memory -- the 12 KB the tile occupies contiguously in global
-//               memory -- and one thread writes them with a bulk copy
+//               neighbours' ones, apply bias and GELU (or GELU' for the backward pass) and store
+//               their pixel's channels (32-byte sectors)
 namespace ctc {
 constexpr int kEpilogueWarps = 12;
 constexpr int kMmaWarp = kEpilogueWarps;                       // 12
@@ -102,19 +101,16 @@ constexpr uint32_t kChunkStride = kSlots * 16;                 // 4096 B between
 constexpr uint32_t kStageBytes = (kC / 8) * kChunkStride;      // 24576 B per stage
 constexpr uint32_t kDyBytes = kN * kC * 2;                     // 13824 B of weights per row offset dy
 constexpr uint32_t kWBytes = 3 * kDyBytes;
-constexpr uint32_t kOutBytes = 2 * kW * kC * 2;                // 12288 B: one tile of bf16 outputs
 constexpr int kXPix = kC + 4;                                  // floats per pixel in the exchange buffer
 constexpr uint32_t kXBytes = 2u * 128u * kXPix * 4u;           // [dx = -1 | +1][pixel][kXPix] floats
 constexpr uint32_t kOffW = kStages * kStageBytes;
-constexpr uint32_t kOffOut = kOffW + kWBytes;                  // staged `post` (forward) or result (backward)
-constexpr uint32_t kOffOut2 = kOffOut + kOutBytes;             // staged `pre` (forward before a backward pass)
-constexpr uint32_t kOffX = kOffOut2 + kOutBytes;               // dx = -1 / +1 partial sums of a tile
+constexpr uint32_t kOffX = kOffW + kWBytes;                    // dx = -1 / +1 partial sums of a tile
 constexpr uint32_t kOffBar = kOffX + kXBytes;                  // 2 kStages + 5 mbarriers
 constexpr uint32_t kSmemBytes = kOffBar + (2 * kStages + 5) * 8;
 constexpr uint32_t kAccCols = 256;                             // accumulator a at TMEM column 256 a (144 used)
 constexpr long long kWaitBudget = 4000000000LL;                // clock cycles (~2 s)
 static_assert(kSmemBytes + 1024 <= 227 * 1024, "conv tile does not fit in shared memory");
-static_assert(kStageBytes % 1024 == 0 && kWBytes % 16 == 0 && kOutBytes % 16 == 0 && kXBytes % 16 == 0,
+static_assert(kStageBytes % 1024 == 0 && kWBytes % 16 == 0 && kXBytes % 16 == 0,
               "aligned regions");
 static_assert(kN % 16 == 0 && kN <= 256, "M = 128 needs N a multiple of 16, at most 256");
 static_assert(kC % 3 == 0 && kCe % 4 == 0, "epilogue channel groups of whole 16-byte pieces");
@@ -173,8 +169,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
 __device__ __forceinline__ void row_sync(uint32_t id, uint32_t n) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
-// the same barrier, returning whether any of its threads passed `c` true: the warps of a row leave their
-// tile loop together (a warp leaving alone would strand the others at the next barrier)
+// the same barrier, returning whether any of its threads passed `c` true: the warps of a row leave
+// their tile loop together (a warp leaving alone would strand the others at the next barrier)
 __device__ __forceinline__ bool row_any(uint32_t id, uint32_t n, bool c) {
   uint32_t r;
   asm volatile(
@@ -323,25 +319,22 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
   } else {
     // ---------------- epilogue: warp w reads TMEM lanes 32 (w % 4) + lane = pixel m, channels
     // 16 (w / 4) .. + 15 of each dx block.  The 6 warps of an output row (quadrants 2 r, 2 r + 1) sync
-    // among themselves only: the horizontal neighbours are in the same row, and the row's outputs are
-    // 6 KB contiguous in global memory, stored by the row's own leader.
+    // among themselves only: the horizontal neighbours are in the same row.  Each thread stores its
+    // pixel's 16 channels (one whole 32-byte sector) straight to global memory.
     constexpr int kCe = ctc::kCe;
     constexpr uint32_t kRowThreads = ctc::kEpilogueThreads / 2;
     const int m = 32 * (warp & 3) + lane;
     const int c0 = kCe * (warp >> 2);
     const int orow = (warp & 3) >> 1;
     const uint32_t rbar = 1u + (uint32_t)orow;
-    const bool leader = (warp >> 2) == 0 && (warp & 1) == 0 && lane == 0;  // warps 0 and 2
     const int row = m / kW, xx = m % kW;
     const int ml = row * kW + ((xx - 1) & (kW - 1)), mr = row * kW + ((xx + 1) & (kW - 1));
     float bv[kCe];
 #pragma unroll
     for (int j = 0; j < kCe; ++j) bv[j] = mode == 0 ? bias[c0 + j] : 0.f;
-    const uint32_t stg = (uint32_t)(m * kC + c0) * 2u;  // byte offset of this thread's outputs in a staged tile
-    float* xm = xbuf + m * ctc::kXPix + c0;                     // this pixel's dx = -1 partials
-    float* xp = xbuf + (128 + m) * ctc::kXPix + c0;             // this pixel's dx = +1 partials
-    const float* xl = xbuf + ml * ctc::kXPix + c0;              // left neighbour's dx = -1 partials
-    const float* xr = xbuf + (128 + mr) * ctc::kXPix + c0;      // right neighbour's dx = +1 partials
+    const int xm = m * ctc::kXPix + c0;              // this pixel's dx = -1 partials (+ kXHalf / 2: dx = +1)
+    const int xl = ml * ctc::kXPix + c0;             // left neighbour's dx = -1 partials
+    const int xr = (128 + mr) * ctc::kXPix + c0;     // right neighbour's dx = +1 partials
     int i = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int a = i & 1;
@@ -364,22 +357,24 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
       }
       tc::fence_before_sync();
       mbar_arrive(accempty + a);  // accumulator a may be overwritten by the MMAs of tile i + 2
-      // publish the dx = -1 / +1 partial sums (the previous tile's readers passed the barrier before
-      // the staging of that tile)
+      // publish the dx = -1 / +1 partial sums (the row's readers of the previous tile passed its final
+      // barrier; a second buffer for alternate tiles would cost an input stage, measured slower)
+      float* xh = xbuf;
 #pragma unroll
       for (int q = 0; q < kCe / 4; ++q) {
-        *reinterpret_cast<float4*>(xm + 4 * q) = make_float4(d[0][4 * q], d[0][4 * q + 1], d[0][4 * q + 2], d[0][4 * q + 3]);
-        *reinterpret_cast<float4*>(xp + 4 * q) = make_float4(d[2][4 * q], d[2][4 * q + 1], d[2][4 * q + 2], d[2][4 * q + 3]);
+        *reinterpret_cast<float4*>(xh + xm + 4 * q) =
+            make_float4(d[0][4 * q], d[0][4 * q + 1], d[0][4 * q + 2], d[0][4 * q + 3]);
+        *reinterpret_cast<float4*>(xh + 128 * ctc::kXPix + xm + 4 * q) =
+            make_float4(d[2][4 * q], d[2][4 * q + 1], d[2][4 * q + 2], d[2][4 * q + 3]);
       }
-      if (leader) bulk_wait_read();  // the row's previous staged outputs have left shared memory
-      // one barrier of the row: partial sums published, staging free, and its warps agree whether to stop
+      // one barrier of the row: partial sums published, and its warps agree whether to stop
       if (row_any(rbar, kRowThreads, !ok || aborted())) break;
       // out[x] = D[x - 1][dx = -1] + D[x][dx = 0] + D[x + 1][dx = +1] (periodic in x within the row)
       float v[kCe];
 #pragma unroll
       for (int q = 0; q < kCe / 4; ++q) {
-        const float4 l4 = *reinterpret_cast<const float4*>(xl + 4 * q);
-        const float4 r4 = *reinterpret_cast<const float4*>(xr + 4 * q);
+        const float4 l4 = *reinterpret_cast<const float4*>(xh + xl + 4 * q);
+        const float4 r4 = *reinterpret_cast<const float4*>(xh + xr + 4 * q);
         v[4 * q] = d[1][4 * q] + l4.x + r4.x;
         v[4 * q + 1] = d[1][4 * q + 1] + l4.y + r4.y;
         v[4 * q + 2] = d[1][4 * q + 2] + l4.z + r4.z;
@@ -412,25 +407,16 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
           }
         }
       }
-#pragma unroll
-      for (int q = 0; q < kCe / 8; ++q) {
-        *reinterpret_cast<uint4*>(smem + ctc::kOffOut + stg + 16 * q) =
-            make_uint4(ra[4 * q], ra[4 * q + 1], ra[4 * q + 2], ra[4 * q + 3]);
-        if (out_b)
-          *reinterpret_cast<uint4*>(smem + ctc::kOffOut2 + stg + 16 * q) =
-              make_uint4(rb[4 * q], rb[4 * q + 1], rb[4 * q + 2], rb[4 * q + 3]);
+      // this thread's 16 channels of pixel m: one whole 32-byte sector of the output
+      const size_t o = ((size_t)tile * 128 + m) * kC + c0;
+      *reinterpret_cast<uint4*>(out_a + o) = make_uint4(ra[0], ra[1], ra[2], ra[3]);
+      *reinterpret_cast<uint4*>(out_a + o + 8) = make_uint4(ra[4], ra[5], ra[6], ra[7]);
+      if (out_b) {
+        *reinterpret_cast<uint4*>(out_b + o) = make_uint4(rb[0], rb[1], rb[2], rb[3]);
+        *reinterpret_cast<uint4*>(out_b + o + 8) = make_uint4(rb[4], rb[5], rb[6], rb[7]);
       }
-      tc::fence_proxy_async();    // staged outputs -> visible to the bulk copy
-      row_sync(rbar, kRowThreads);  // also: the row's threads have read this tile's neighbour partials
-      if (leader) {
-        const uint32_t rb_ = (uint32_t)orow * (ctc::kOutBytes / 2);                         // bytes
-        const size_t off = (size_t)tile * (ctc::kOutBytes / 2) + (size_t)orow * (kW * kC);  // bf16 elements
-        bulk_store(out_a + off, sbase + ctc::kOffOut + rb_, ctc::kOutBytes / 2);
-        if (out_b) bulk_store(out_b + off, sbase + ctc::kOffOut2 + rb_, ctc::kOutBytes / 2);
-        bulk_commit();
-      }
+      row_sync(rbar, kRowThreads);  // the row's threads have read this tile's neighbour partials
     }
-    if (leader) bulk_wait_all();
   }
 
   // every MMA this CTA issued has completed (drain barrier above) before the tensor memory is released
