@@ -428,11 +428,30 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
   }
 }
 
+// Packed FP32 helpers (add/mul/fma .f32x2: two lanes of a channel pair per instruction, each rounded like
+// the scalar operation it replaces).
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 gelu_f2(float2 x) {
+  const float2 u = __fmul2_rn(x, __ffma2_rn(__fmul2_rn(x, x), bc2(kGeluB), bc2(kGeluA)));
+  const float2 t = make_float2(tanh_hw(u.x), tanh_hw(u.y));
+  const float2 h = __fmul2_rn(x, bc2(0.5f));
+  return __ffma2_rn(h, t, h);
+}
+__device__ __forceinline__ float2 bf2_to_f2(uint32_t u) {
+  return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u));
+}
+__device__ __forceinline__ uint32_t f2_to_bf2(float2 v) {  // round to nearest, v.x in the low half
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(v.y), "f"(v.x));
+  return r;
+}
+
 // 1 -> 48 forward: pre = conv(x) + b, post = gelu(pre).  One thread per pixel of sample blockIdx.y,
 // all 48 channels in chunks of 8, so every weight read is one shared-memory address for the whole warp
-// (a broadcast); a block stages its 256 pixels' 96-byte outputs in shared memory (112-byte rows:
-// conflict-free 16-byte accesses) and stores them as consecutive 16-byte pieces.  `pre` (training
-// only) is written straight from the threads; NULL at inference.
+// (a broadcast); the multiply-adds and the GELU's arithmetic run on the packed FP32 pipe over output
+// channel pairs (each input held as a broadcast pair).  A block stages its 256 pixels' 96-byte outputs
+// in shared memory (112-byte rows: conflict-free 16-byte accesses) and stores them as consecutive
+// 16-byte pieces.  `pre` (training only) is written straight from the threads; NULL at inference.
 constexpr int kIn1Pix = 56;  // bf16 per staged output pixel (48 used)
 __global__ void __launch_bounds__(256) conv_in1_kernel(const float* __restrict__ x, int H, const float* __restrict__ w,
                                                        const float* __restrict__ bias, __nv_bfloat16* __restrict__ pre,
@@ -449,7 +468,7 @@ __global__ void __launch_bounds__(256) conv_in1_kernel(const float* __restrict__
   const bool live = p < npix;
   const float* xb = x + (int64_t)blockIdx.y * npix;
   const int64_t ob = (int64_t)blockIdx.y * npix;
-  float v[9];
+  float2 vb[9];
   {
     const int pp = live ? p : 0;
     const int y = pp / kW, xx = pp % kW;
@@ -458,37 +477,32 @@ __global__ void __launch_bounds__(256) conv_in1_kernel(const float* __restrict__
       int gy = y + tap / 3 - 1;
       gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
       const int gx = (xx + tap % 3 - 1) & (kW - 1);
-      v[tap] = __ldg(xb + gy * kW + gx);
+      vb[tap] = bc2(__ldg(xb + gy * kW + gx));
     }
   }
-#pragma unroll 1
+#pragma unroll 2
   for (int q = 0; q < kC / 8; ++q) {
-    float acc[8];
+    float2 acc[4];
     {
       const float4 b0 = w4[(9 * kC + q * 8) / 4], b1 = w4[(9 * kC + q * 8) / 4 + 1];
-      acc[0] = b0.x; acc[1] = b0.y; acc[2] = b0.z; acc[3] = b0.w;
-      acc[4] = b1.x; acc[5] = b1.y; acc[6] = b1.z; acc[7] = b1.w;
+      acc[0] = make_float2(b0.x, b0.y);
+      acc[1] = make_float2(b0.z, b0.w);
+      acc[2] = make_float2(b1.x, b1.y);
+      acc[3] = make_float2(b1.z, b1.w);
     }
 #pragma unroll
     for (int tap = 0; tap < 9; ++tap) {
       const float4 wa = w4[(tap * kC + q * 8) / 4], wb = w4[(tap * kC + q * 8) / 4 + 1];
-      acc[0] = fmaf(wa.x, v[tap], acc[0]);
-      acc[1] = fmaf(wa.y, v[tap], acc[1]);
-      acc[2] = fmaf(wa.z, v[tap], acc[2]);
-      acc[3] = fmaf(wa.w, v[tap], acc[3]);
-      acc[4] = fmaf(wb.x, v[tap], acc[4]);
-      acc[5] = fmaf(wb.y, v[tap], acc[5]);
-      acc[6] = fmaf(wb.z, v[tap], acc[6]);
-      acc[7] = fmaf(wb.w, v[tap], acc[7]);
+      acc[0] = __ffma2_rn(make_float2(wa.x, wa.y), vb[tap], acc[0]);
+      acc[1] = __ffma2_rn(make_float2(wa.z, wa.w), vb[tap], acc[1]);
+      acc[2] = __ffma2_rn(make_float2(wb.x, wb.y), vb[tap], acc[2]);
+      acc[3] = __ffma2_rn(make_float2(wb.z, wb.w), vb[tap], acc[3]);
     }
     uint32_t hp[4], hq[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const float s0 = acc[2 * j], s1 = acc[2 * j + 1];
-      const __nv_bfloat162 a = __floats2bfloat162_rn(s0, s1);
-      const __nv_bfloat162 g = __floats2bfloat162_rn(gelu_f(s0), gelu_f(s1));
-      hp[j] = *reinterpret_cast<const uint32_t*>(&a);
-      hq[j] = *reinterpret_cast<const uint32_t*>(&g);
+      hp[j] = f2_to_bf2(acc[j]);
+      hq[j] = f2_to_bf2(gelu_f2(acc[j]));
     }
     *reinterpret_cast<uint4*>(stage + threadIdx.x * kIn1Pix + q * 8) = make_uint4(hq[0], hq[1], hq[2], hq[3]);
     if (pre && live) *reinterpret_cast<uint4*>(pre + (ob + p) * kC + q * 8) = make_uint4(hp[0], hp[1], hp[2], hp[3]);
@@ -502,63 +516,81 @@ __global__ void __launch_bounds__(256) conv_in1_kernel(const float* __restrict__
   }
 }
 
-// 48 -> 1 forward: out = base + scale * (conv(h) + b).  A block computes kOut1Rows output rows of sample
-// blockIdx.y, one thread per output pixel: the kOut1Rows + 2 input rows it needs are first copied to
-// shared memory in 16-byte pieces (pixels padded to 112 bytes, so that the 16-byte reads of 8
-// consecutive pixels hit distinct banks), then each thread reads its 9 x 48 inputs from there and the
-// weights as broadcast float4.  (Reading the inputs through L1, 9 times per value in 8-byte pieces,
-// took 1.3x as long; a thread per column and 4 rows with a chunk's weights in registers, 107
-// registers at 2 warps per block, 1.1x.)
-constexpr int kOut1Rows = 4;    // output rows per block: kOut1Rows x kW = 256 threads
-constexpr int kOut1Pix = 56;    // bf16 per pixel in shared memory (48 used)
-__global__ void __launch_bounds__(kOut1Rows * kW) conv_out1_kernel(const __nv_bfloat16* __restrict__ h, int H,
-                                                                   const float* __restrict__ w,
-                                                                   const float* __restrict__ bias,
-                                                                   const float* __restrict__ base, float scale,
-                                                                   float* __restrict__ out) {
-  __shared__ __align__(16) float wsm[9 * kC];
-  __shared__ __align__(16) __nv_bfloat16 rows[(kOut1Rows + 2) * kW * kOut1Pix];
-  for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];  // [tap][ci]
+// 48 -> 1 forward: out = base + scale * (conv(h) + b), as tap sums.  A block owns kOut1Rows output rows
+// of sample blockIdx.y.  Each thread first takes kOut1Px pixels of the kOut1Rows + 2 input rows (the
+// halo included), reads each pixel's 48 channels once and forms its nine tap sums
+// P[tap][p] = sum_ci w[tap][ci] h[p][ci] on the packed FP32 pipe (channel pairs; every weight read from
+// shared memory serves all of the thread's pixels) into shared memory; then each output pixel adds the
+// sums of its neighbours, out[y][x] = b + sum_tap P[tap][y + dy][x + dx].  (A thread per output pixel
+// reading its 9 x 48 inputs from rows staged in shared memory took 68 us at batch 256 of 64^2 grids,
+// bound by those reads.)
+constexpr int kOut1Rows = 8;                          // output rows per block
+constexpr int kOut1In = kOut1Rows + 2;                // input rows per block
+constexpr int kOut1Px = 2;                            // input pixels per thread in the tap-sum phase
+constexpr int kOut1Threads = kOut1In * kW / kOut1Px;  // 320
+__global__ void __launch_bounds__(kOut1Threads) conv_out1_kernel(const __nv_bfloat16* __restrict__ h, int H,
+                                                                 const float* __restrict__ w,
+                                                                 const float* __restrict__ bias,
+                                                                 const float* __restrict__ base, float scale,
+                                                                 float* __restrict__ out) {
+  __shared__ __align__(16) float wsm[9 * kC];  // [tap][ci]
+  __shared__ float part[9][kOut1In * kW];      // [tap][input pixel of the block]
+  for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];
   const int y0 = blockIdx.x * kOut1Rows;
   const __nv_bfloat16* hb = h + (int64_t)blockIdx.y * H * kW * kC;
-  for (int e = threadIdx.x; e < (kOut1Rows + 2) * kW * (kC / 8); e += blockDim.x) {
-    const int r = e / (kW * (kC / 8)), rem = e - r * (kW * (kC / 8));
-    const int px = rem / (kC / 8), q = rem - px * (kC / 8);
-    int gy = y0 - 1 + r;
-    gy = gy < 0 ? gy + H : (gy >= H ? gy - H : gy);
-    *reinterpret_cast<uint4*>(rows + (r * kW + px) * kOut1Pix + q * 8) =
-        __ldg(reinterpret_cast<const uint4*>(hb + ((int64_t)gy * kW + px) * kC + q * 8));
+  const uint4* src[kOut1Px];
+#pragma unroll
+  for (int i = 0; i < kOut1Px; ++i) {
+    const int pl = threadIdx.x + i * kOut1Threads;  // 0 .. kOut1In * kW - 1
+    int gy = (y0 - 1 + pl / kW) % H;
+    if (gy < 0) gy += H;
+    src[i] = reinterpret_cast<const uint4*>(hb + ((int64_t)gy * kW + pl % kW) * kC);
   }
   __syncthreads();
-  const int oy = threadIdx.x / kW, ox = threadIdx.x % kW;
-  if (y0 + oy >= H) return;
   const float4* w4 = reinterpret_cast<const float4*>(wsm);
-  float s = 0.f;
-#pragma unroll 3
-  for (int tap = 0; tap < 9; ++tap) {
-    const int ry = oy + tap / 3;
-    const int gx = (ox + tap % 3 - 1) & (kW - 1);
-    const uint4* src = reinterpret_cast<const uint4*>(rows + (ry * kW + gx) * kOut1Pix);
+  float2 acc[kOut1Px][9];
 #pragma unroll
-    for (int q = 0; q < kC / 8; ++q) {
-      const uint4 u = src[q];
+  for (int i = 0; i < kOut1Px; ++i)
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) acc[i][tap] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < kC / 8; ++q) {
+    float2 a[kOut1Px][4];
+#pragma unroll
+    for (int i = 0; i < kOut1Px; ++i) {
+      const uint4 u = __ldg(src[i] + q);
+      a[i][0] = bf2_to_f2(u.x);
+      a[i][1] = bf2_to_f2(u.y);
+      a[i][2] = bf2_to_f2(u.z);
+      a[i][3] = bf2_to_f2(u.w);
+    }
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
       const float4 wa = w4[(tap * kC + q * 8) / 4], wb = w4[(tap * kC + q * 8) / 4 + 1];
-      const float2 f0 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
-      const float2 f1 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
-      const float2 f2 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.z));
-      const float2 f3 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.w));
-      s = fmaf(wa.x, f0.x, s);
-      s = fmaf(wa.y, f0.y, s);
-      s = fmaf(wa.z, f1.x, s);
-      s = fmaf(wa.w, f1.y, s);
-      s = fmaf(wb.x, f2.x, s);
-      s = fmaf(wb.y, f2.y, s);
-      s = fmaf(wb.z, f3.x, s);
-      s = fmaf(wb.w, f3.y, s);
+#pragma unroll
+      for (int i = 0; i < kOut1Px; ++i) {
+        acc[i][tap] = __ffma2_rn(a[i][0], make_float2(wa.x, wa.y), acc[i][tap]);
+        acc[i][tap] = __ffma2_rn(a[i][1], make_float2(wa.z, wa.w), acc[i][tap]);
+        acc[i][tap] = __ffma2_rn(a[i][2], make_float2(wb.x, wb.y), acc[i][tap]);
+        acc[i][tap] = __ffma2_rn(a[i][3], make_float2(wb.z, wb.w), acc[i][tap]);
+      }
     }
   }
-  const int64_t p = ((int64_t)blockIdx.y * H + y0 + oy) * kW + ox;
-  out[p] = (base ? base[p] : 0.f) + scale * (s + bias[0]);
+#pragma unroll
+  for (int i = 0; i < kOut1Px; ++i)
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) part[tap][threadIdx.x + i * kOut1Threads] = acc[i][tap].x + acc[i][tap].y;
+  __syncthreads();
+  const float b0 = __ldg(bias);
+  for (int o = threadIdx.x; o < kOut1Rows * kW; o += kOut1Threads) {
+    const int oy = o / kW, ox = o % kW;
+    if (y0 + oy >= H) break;
+    float s = b0;
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) s += part[tap][(oy + tap / 3) * kW + ((ox + tap % 3 - 1) & (kW - 1))];
+    const int64_t pi = ((int64_t)blockIdx.y * H + y0 + oy) * kW + ox;
+    out[pi] = (base ? base[pi] : 0.f) + scale * s;
+  }
 }
 
 // backward of the 48 -> 1 layer w.r.t. its input, times GELU'(pre):
@@ -901,7 +933,7 @@ int exgb_conv_out1(void* stream, const void* h, int B, int H, const float* w, co
   if ((int64_t)B * H == 0) return EXGB_OK;
   if ((int64_t)B * H > 2147483647LL) return fail(EXGB_EINVAL, "too many rows");
   if (B > 65535) return fail(EXGB_EINVAL, "batch above 65535");
-  conv_out1_kernel<<<dim3((H + kOut1Rows - 1) / kOut1Rows, B), kOut1Rows * kW, 0, (cudaStream_t)stream>>>(
+  conv_out1_kernel<<<dim3((H + kOut1Rows - 1) / kOut1Rows, B), kOut1Threads, 0, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)h, H, w, bias, base, scale, out);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;

@@ -198,3 +198,45 @@ def test_conv48_tensor_core_layer(B, H, mode):
         assert rel(post.float().cpu().numpy(), co.gelu(ref)) < 4e-3
     else:
         assert rel(pre.float().cpu().numpy(), ref * co.gelu_d(aux)) < 4e-3
+
+
+@pytest.mark.parametrize("B,H", [(1, 64), (16, 64), (3, 13), (2, 2), (2, 1)])
+def test_thin_layers(B, H):
+    """The 1 -> 48 and 48 -> 1 layers alone against float64 periodic convolutions of the same inputs:
+    1 -> 48 (FP32 input, bias, tanh-form GELU, bf16 outputs) within the bf16 rounding (relative L2 <=
+    4e-3), 48 -> 1 (bf16 input, FP32 tap sums, out = base + scale (conv + b)) within 1e-5.  H = 13 leaves
+    a partial block of output rows, H = 1 and 2 make the periodic halo rows repeat."""
+    from exponax_gb300 import _device
+    from oracle import corrector_np as co
+    from exponax_gb300.learned import PeriodicConvCorrector, _lib, _p
+
+    rng = np.random.default_rng(7 * B + H)
+    lib = _lib()
+    # 1 -> 48
+    x = rng.standard_normal((B, H, 64)).astype(np.float32)
+    w1 = (rng.standard_normal((9, 48)) / 3.0).astype(np.float32)
+    b1 = (0.1 * rng.standard_normal(48)).astype(np.float32)
+    pre = torch.full((B, H, 64, 48), float("nan"), dtype=torch.bfloat16, device="cuda")
+    post = torch.full_like(pre, float("nan"))
+    xd, w1d, b1d = (torch.from_numpy(a).cuda() for a in (x, w1, b1))
+    assert lib.exgb_conv_in1(_device.stream(), _p(xd), B, H, _p(w1d), _p(b1d), _p(pre), _p(post)) == 0
+    PeriodicConvCorrector.status()
+    ref = _conv_ref(x.astype(np.float64)[..., None], w1.astype(np.float64)[:, :, None]) + b1
+    assert rel(pre.float().cpu().numpy(), ref) < 4e-3
+    assert rel(post.float().cpu().numpy(), co.gelu(ref)) < 4e-3
+    # 48 -> 1
+    h = _bf16(rng.standard_normal((B, H, 64, 48))).float().numpy().astype(np.float64)
+    w6 = (rng.standard_normal((9, 48)) / np.sqrt(9 * 48)).astype(np.float32)
+    b6 = np.array([0.3], np.float32)
+    base = rng.standard_normal((B, H, 64)).astype(np.float32)
+    out = torch.full((B, H, 64), float("nan"), dtype=torch.float32, device="cuda")
+    hd = _bf16(h).cuda()
+    w6d, b6d, based = (torch.from_numpy(a).cuda() for a in (w6, b6, base))
+    for with_base in (True, False):
+        assert lib.exgb_conv_out1(_device.stream(), _p(hd), B, H, _p(w6d), _p(b6d), _p(based) if with_base else None,
+                                  0.7, _p(out)) == 0
+        PeriodicConvCorrector.status()
+        ref = 0.7 * (_conv_ref(h, w6.astype(np.float64)[:, None, :])[..., 0] + b6[0])
+        if with_base:
+            ref = ref + base
+        assert rel(out.cpu().numpy(), ref) < 1e-5
