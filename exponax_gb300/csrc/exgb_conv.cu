@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 #include "exgb_internal.h"
 #include "exgb_tc.cuh"
@@ -56,6 +57,24 @@ __device__ __forceinline__ float gelu_d(float x) {
   const float t = tanh_hw(x * fmaf(kGeluB, x2, kGeluA));
   const float du = fmaf(3.f * kGeluB, x2, kGeluA);
   return fmaf(0.5f * x * du, fmaf(-t, t, 1.f), fmaf(0.5f, t, 0.5f));
+}
+
+// Packed FP32 helpers (add/mul/fma .f32x2: two lanes of a channel pair per instruction, each rounded like
+// the scalar operation it replaces).
+__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float2 gelu_f2(float2 x) {
+  const float2 u = __fmul2_rn(x, __ffma2_rn(__fmul2_rn(x, x), bc2(kGeluB), bc2(kGeluA)));
+  const float2 t = make_float2(tanh_hw(u.x), tanh_hw(u.y));
+  const float2 h = __fmul2_rn(x, bc2(0.5f));
+  return __ffma2_rn(h, t, h);
+}
+__device__ __forceinline__ float2 bf2_to_f2(uint32_t u) {
+  return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u));
+}
+__device__ __forceinline__ uint32_t f2_to_bf2(float2 v) {  // round to nearest, v.x in the low half
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(v.y), "f"(v.x));
+  return r;
 }
 
 // 48 -> 48 channels as an implicit GEMM on the tcgen05 tensor cores.  A tile is 2 output rows x 64
@@ -370,25 +389,27 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
       // one barrier of the row: partial sums published, and its warps agree whether to stop
       if (row_any(rbar, kRowThreads, !ok || aborted())) break;
       // out[x] = D[x - 1][dx = -1] + D[x][dx = 0] + D[x + 1][dx = +1] (periodic in x within the row)
-      float v[kCe];
+      float v[kCe];  // channel pairs on the packed FP32 pipe
 #pragma unroll
       for (int q = 0; q < kCe / 4; ++q) {
         const float4 l4 = *reinterpret_cast<const float4*>(xh + xl + 4 * q);
         const float4 r4 = *reinterpret_cast<const float4*>(xh + xr + 4 * q);
-        v[4 * q] = d[1][4 * q] + l4.x + r4.x;
-        v[4 * q + 1] = d[1][4 * q + 1] + l4.y + r4.y;
-        v[4 * q + 2] = d[1][4 * q + 2] + l4.z + r4.z;
-        v[4 * q + 3] = d[1][4 * q + 3] + l4.w + r4.w;
+        const float2 s0 = __fadd2_rn(__fadd2_rn(make_float2(d[1][4 * q], d[1][4 * q + 1]), make_float2(l4.x, l4.y)),
+                                     make_float2(r4.x, r4.y));
+        const float2 s1 = __fadd2_rn(
+            __fadd2_rn(make_float2(d[1][4 * q + 2], d[1][4 * q + 3]), make_float2(l4.z, l4.w)), make_float2(r4.z, r4.w));
+        v[4 * q] = s0.x;
+        v[4 * q + 1] = s0.y;
+        v[4 * q + 2] = s1.x;
+        v[4 * q + 3] = s1.y;
       }
       uint32_t ra[kCe / 2], rb[kCe / 2];
       if (mode == 0) {
 #pragma unroll
         for (int j = 0; j < kCe / 2; ++j) {
-          const float v0 = v[2 * j] + bv[2 * j], v1 = v[2 * j + 1] + bv[2 * j + 1];
-          const __nv_bfloat162 p = __floats2bfloat162_rn(v0, v1);
-          const __nv_bfloat162 g = __floats2bfloat162_rn(gelu_f(v0), gelu_f(v1));
-          rb[j] = *reinterpret_cast<const uint32_t*>(&p);
-          ra[j] = *reinterpret_cast<const uint32_t*>(&g);
+          const float2 v01 = __fadd2_rn(make_float2(v[2 * j], v[2 * j + 1]), make_float2(bv[2 * j], bv[2 * j + 1]));
+          rb[j] = f2_to_bf2(v01);
+          ra[j] = f2_to_bf2(gelu_f2(v01));
         }
       } else {
         // pixel m of this tile: 128 * tile + m in the batch (tiles are consecutive row pairs)
@@ -428,40 +449,27 @@ __global__ void __launch_bounds__(ctc::kThreads, 1) conv48_tc_kernel(const __gri
   }
 }
 
-// Packed FP32 helpers (add/mul/fma .f32x2: two lanes of a channel pair per instruction, each rounded like
-// the scalar operation it replaces).
-__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
-__device__ __forceinline__ float2 gelu_f2(float2 x) {
-  const float2 u = __fmul2_rn(x, __ffma2_rn(__fmul2_rn(x, x), bc2(kGeluB), bc2(kGeluA)));
-  const float2 t = make_float2(tanh_hw(u.x), tanh_hw(u.y));
-  const float2 h = __fmul2_rn(x, bc2(0.5f));
-  return __ffma2_rn(h, t, h);
-}
-__device__ __forceinline__ float2 bf2_to_f2(uint32_t u) {
-  return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u));
-}
-__device__ __forceinline__ uint32_t f2_to_bf2(float2 v) {  // round to nearest, v.x in the low half
-  uint32_t r;
-  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(v.y), "f"(v.x));
-  return r;
-}
 
-// 1 -> 48 forward: pre = conv(x) + b, post = gelu(pre).  One thread per pixel of sample blockIdx.y,
-// all 48 channels in chunks of 8, so every weight read is one shared-memory address for the whole warp
-// (a broadcast); the multiply-adds and the GELU's arithmetic run on the packed FP32 pipe over output
-// channel pairs (each input held as a broadcast pair).  A block stages its 256 pixels' 96-byte outputs
-// in shared memory (112-byte rows: conflict-free 16-byte accesses) and stores them as consecutive
-// 16-byte pieces.  `pre` (training only) is written straight from the threads; NULL at inference.
+// Weights of the thin layers live in the constant bank.  Every thread of a warp reads the same weight
+// at once, and an FMA takes a constant-bank operand with no load instruction and no traffic through
+// L1 (read from shared memory as broadcast 16-byte loads, the 432 weights per pixel kept the L1 data
+// return 88 % busy in the 1 -> 48 layer).  Each launch first copies its layer's weights in on its own
+// stream (exgb_conv_in1 / exgb_conv_out1 order the users of a bank across streams).
+__constant__ __align__(16) float c_in1[9 * kC + kC];  // [tap][co], then the bias [co]
+__constant__ __align__(16) float c_out1[9 * kC + 4];  // [tap][ci], then the bias
+__device__ __forceinline__ float2 cpair(const float* c, int i) { return *reinterpret_cast<const float2*>(c + i); }
+
+// 1 -> 48 forward: pre = conv(x) + b, post = gelu(pre).  One thread per pixel of sample blockIdx.y; the
+// multiply-adds and the GELU's arithmetic run on the packed FP32 pipe over output channel pairs (each
+// input held as a broadcast pair, the weights constant-bank operands).  A block stages its 256 pixels'
+// 96-byte outputs in shared memory (112-byte rows: conflict-free 16-byte accesses) and stores them as
+// consecutive 16-byte pieces.  `pre` (training only) is written straight from the threads; NULL at
+// inference.
 constexpr int kIn1Pix = 56;  // bf16 per staged output pixel (48 used)
-__global__ void __launch_bounds__(256) conv_in1_kernel(const float* __restrict__ x, int H, const float* __restrict__ w,
-                                                       const float* __restrict__ bias, __nv_bfloat16* __restrict__ pre,
+__global__ void __launch_bounds__(256) conv_in1_kernel(const float* __restrict__ x, int H,
+                                                       __nv_bfloat16* __restrict__ pre,
                                                        __nv_bfloat16* __restrict__ post) {
-  __shared__ __align__(16) float wsm[9 * kC + kC];
   __shared__ __align__(16) __nv_bfloat16 stage[256 * kIn1Pix];
-  for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];  // [tap][co]
-  for (int t = threadIdx.x; t < kC; t += blockDim.x) wsm[9 * kC + t] = bias[t];
-  __syncthreads();
-  const float4* w4 = reinterpret_cast<const float4*>(wsm);
   const int npix = H * kW;
   const int p0 = blockIdx.x * 256;
   const int p = p0 + threadIdx.x;
@@ -480,24 +488,15 @@ __global__ void __launch_bounds__(256) conv_in1_kernel(const float* __restrict__
       vb[tap] = bc2(__ldg(xb + gy * kW + gx));
     }
   }
-#pragma unroll 2
+#pragma unroll
   for (int q = 0; q < kC / 8; ++q) {
     float2 acc[4];
-    {
-      const float4 b0 = w4[(9 * kC + q * 8) / 4], b1 = w4[(9 * kC + q * 8) / 4 + 1];
-      acc[0] = make_float2(b0.x, b0.y);
-      acc[1] = make_float2(b0.z, b0.w);
-      acc[2] = make_float2(b1.x, b1.y);
-      acc[3] = make_float2(b1.z, b1.w);
-    }
 #pragma unroll
-    for (int tap = 0; tap < 9; ++tap) {
-      const float4 wa = w4[(tap * kC + q * 8) / 4], wb = w4[(tap * kC + q * 8) / 4 + 1];
-      acc[0] = __ffma2_rn(make_float2(wa.x, wa.y), vb[tap], acc[0]);
-      acc[1] = __ffma2_rn(make_float2(wa.z, wa.w), vb[tap], acc[1]);
-      acc[2] = __ffma2_rn(make_float2(wb.x, wb.y), vb[tap], acc[2]);
-      acc[3] = __ffma2_rn(make_float2(wb.z, wb.w), vb[tap], acc[3]);
-    }
+    for (int j = 0; j < 4; ++j) acc[j] = cpair(c_in1, 9 * kC + q * 8 + 2 * j);
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[j] = __ffma2_rn(cpair(c_in1, tap * kC + q * 8 + 2 * j), vb[tap], acc[j]);
     uint32_t hp[4], hq[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -519,23 +518,18 @@ __global__ void __launch_bounds__(256) conv_in1_kernel(const float* __restrict__
 // 48 -> 1 forward: out = base + scale * (conv(h) + b), as tap sums.  A block owns kOut1Rows output rows
 // of sample blockIdx.y.  Each thread first takes kOut1Px pixels of the kOut1Rows + 2 input rows (the
 // halo included), reads each pixel's 48 channels once and forms its nine tap sums
-// P[tap][p] = sum_ci w[tap][ci] h[p][ci] on the packed FP32 pipe (channel pairs; every weight read from
-// shared memory serves all of the thread's pixels) into shared memory; then each output pixel adds the
-// sums of its neighbours, out[y][x] = b + sum_tap P[tap][y + dy][x + dx].  (A thread per output pixel
-// reading its 9 x 48 inputs from rows staged in shared memory took 68 us at batch 256 of 64^2 grids,
-// bound by those reads.)
+// P[tap][p] = sum_ci w[tap][ci] h[p][ci] on the packed FP32 pipe (channel pairs, the weights
+// constant-bank operands) into shared memory; then each output pixel adds the sums of its neighbours,
+// out[y][x] = b + sum_tap P[tap][y + dy][x + dx].  (A thread per output pixel reading its 9 x 48 inputs
+// from rows staged in shared memory took 68 us at batch 256 of 64^2 grids, bound by those reads.)
 constexpr int kOut1Rows = 8;                          // output rows per block
 constexpr int kOut1In = kOut1Rows + 2;                // input rows per block
 constexpr int kOut1Px = 2;                            // input pixels per thread in the tap-sum phase
 constexpr int kOut1Threads = kOut1In * kW / kOut1Px;  // 320
-__global__ void __launch_bounds__(kOut1Threads) conv_out1_kernel(const __nv_bfloat16* __restrict__ h, int H,
-                                                                 const float* __restrict__ w,
-                                                                 const float* __restrict__ bias,
+__global__ void __launch_bounds__(kOut1Threads, 3) conv_out1_kernel(const __nv_bfloat16* __restrict__ h, int H,
                                                                  const float* __restrict__ base, float scale,
                                                                  float* __restrict__ out) {
-  __shared__ __align__(16) float wsm[9 * kC];  // [tap][ci]
-  __shared__ float part[9][kOut1In * kW];      // [tap][input pixel of the block]
-  for (int t = threadIdx.x; t < 9 * kC; t += blockDim.x) wsm[t] = w[t];
+  __shared__ float part[9][kOut1In * kW];  // [tap][input pixel of the block]
   const int y0 = blockIdx.x * kOut1Rows;
   const __nv_bfloat16* hb = h + (int64_t)blockIdx.y * H * kW * kC;
   const uint4* src[kOut1Px];
@@ -546,8 +540,6 @@ __global__ void __launch_bounds__(kOut1Threads) conv_out1_kernel(const __nv_bflo
     if (gy < 0) gy += H;
     src[i] = reinterpret_cast<const uint4*>(hb + ((int64_t)gy * kW + pl % kW) * kC);
   }
-  __syncthreads();
-  const float4* w4 = reinterpret_cast<const float4*>(wsm);
   float2 acc[kOut1Px][9];
 #pragma unroll
   for (int i = 0; i < kOut1Px; ++i)
@@ -565,23 +557,20 @@ __global__ void __launch_bounds__(kOut1Threads) conv_out1_kernel(const __nv_bflo
       a[i][3] = bf2_to_f2(u.w);
     }
 #pragma unroll
-    for (int tap = 0; tap < 9; ++tap) {
-      const float4 wa = w4[(tap * kC + q * 8) / 4], wb = w4[(tap * kC + q * 8) / 4 + 1];
+    for (int tap = 0; tap < 9; ++tap)
 #pragma unroll
-      for (int i = 0; i < kOut1Px; ++i) {
-        acc[i][tap] = __ffma2_rn(a[i][0], make_float2(wa.x, wa.y), acc[i][tap]);
-        acc[i][tap] = __ffma2_rn(a[i][1], make_float2(wa.z, wa.w), acc[i][tap]);
-        acc[i][tap] = __ffma2_rn(a[i][2], make_float2(wb.x, wb.y), acc[i][tap]);
-        acc[i][tap] = __ffma2_rn(a[i][3], make_float2(wb.z, wb.w), acc[i][tap]);
+      for (int j = 0; j < 4; ++j) {
+        const float2 wp = cpair(c_out1, tap * kC + q * 8 + 2 * j);
+#pragma unroll
+        for (int i = 0; i < kOut1Px; ++i) acc[i][tap] = __ffma2_rn(a[i][j], wp, acc[i][tap]);
       }
-    }
   }
 #pragma unroll
   for (int i = 0; i < kOut1Px; ++i)
 #pragma unroll
     for (int tap = 0; tap < 9; ++tap) part[tap][threadIdx.x + i * kOut1Threads] = acc[i][tap].x + acc[i][tap].y;
   __syncthreads();
-  const float b0 = __ldg(bias);
+  const float b0 = c_out1[9 * kC];
   for (int o = threadIdx.x; o < kOut1Rows * kW; o += kOut1Threads) {
     const int oy = o / kW, ox = o % kW;
     if (y0 + oy >= H) break;
@@ -845,6 +834,39 @@ static unsigned blocks_for(int64_t n) {
   return (unsigned)(b < 1 ? 1 : (b > 65535 * 4 ? 65535 * 4 : b));
 }
 
+// The users of one constant bank of thin-layer weights, in launch order: a launch waits (on its stream)
+// for the previous user's kernel before its copy overwrites the bank.  Inside a stream capture the
+// graph's own order applies.
+struct ConstBank {
+  std::mutex mu;
+  cudaEvent_t done = nullptr;
+};
+static ConstBank g_bank_in1, g_bank_out1;
+
+// Copy nw weights and nb bias values (one copy where the bias follows the weights, as in the
+// corrector's parameter vector) into the constant bank `sym` on `st`, then run `launch` on `st`.
+template <class F>
+static int with_const_weights(ConstBank& bk, const void* sym, const float* w, int nw, const float* b, int nb,
+                              cudaStream_t st, F&& launch) {
+  std::lock_guard<std::mutex> lock(bk.mu);
+  if (!bk.done) EXGB_CUDA(cudaEventCreateWithFlags(&bk.done, cudaEventDisableTiming));
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  EXGB_CUDA(cudaStreamIsCapturing(st, &cs));
+  const bool captured = cs != cudaStreamCaptureStatusNone;
+  if (!captured) EXGB_CUDA(cudaStreamWaitEvent(st, bk.done, 0));
+  if (b == w + nw) {
+    EXGB_CUDA(cudaMemcpyToSymbolAsync(sym, w, sizeof(float) * (size_t)(nw + nb), 0, cudaMemcpyDeviceToDevice, st));
+  } else {
+    EXGB_CUDA(cudaMemcpyToSymbolAsync(sym, w, sizeof(float) * (size_t)nw, 0, cudaMemcpyDeviceToDevice, st));
+    EXGB_CUDA(cudaMemcpyToSymbolAsync(sym, b, sizeof(float) * (size_t)nb, sizeof(float) * (size_t)nw,
+                                      cudaMemcpyDeviceToDevice, st));
+  }
+  launch();
+  EXGB_CUDA(cudaGetLastError());
+  if (!captured) EXGB_CUDA(cudaEventRecord(bk.done, st));
+  return EXGB_OK;
+}
+
 }  // namespace exgb
 
 using namespace exgb;
@@ -921,10 +943,10 @@ int exgb_conv_in1(void* stream, const float* x, int B, int H, const float* w, co
   if ((int64_t)B * H == 0) return EXGB_OK;
   if ((int64_t)B * H > 2147483647LL) return fail(EXGB_EINVAL, "too many rows");
   if (B > 65535) return fail(EXGB_EINVAL, "batch above 65535");
-  conv_in1_kernel<<<dim3((H * kW + 255) / 256, B), 256, 0, (cudaStream_t)stream>>>(x, H, w, bias, (__nv_bfloat16*)pre,
-                                                                                   (__nv_bfloat16*)post);
-  EXGB_CUDA(cudaGetLastError());
-  return EXGB_OK;
+  return with_const_weights(g_bank_in1, (const void*)c_in1, w, 9 * kC, bias, kC, (cudaStream_t)stream, [&]() {
+    conv_in1_kernel<<<dim3((H * kW + 255) / 256, B), 256, 0, (cudaStream_t)stream>>>(x, H, (__nv_bfloat16*)pre,
+                                                                                     (__nv_bfloat16*)post);
+  });
 }
 
 int exgb_conv_out1(void* stream, const void* h, int B, int H, const float* w, const float* bias, const float* base,
@@ -933,10 +955,10 @@ int exgb_conv_out1(void* stream, const void* h, int B, int H, const float* w, co
   if ((int64_t)B * H == 0) return EXGB_OK;
   if ((int64_t)B * H > 2147483647LL) return fail(EXGB_EINVAL, "too many rows");
   if (B > 65535) return fail(EXGB_EINVAL, "batch above 65535");
-  conv_out1_kernel<<<dim3((H + kOut1Rows - 1) / kOut1Rows, B), kOut1Threads, 0, (cudaStream_t)stream>>>(
-      (const __nv_bfloat16*)h, H, w, bias, base, scale, out);
-  EXGB_CUDA(cudaGetLastError());
-  return EXGB_OK;
+  return with_const_weights(g_bank_out1, (const void*)c_out1, w, 9 * kC, bias, 1, (cudaStream_t)stream, [&]() {
+    conv_out1_kernel<<<dim3((H + kOut1Rows - 1) / kOut1Rows, B), kOut1Threads, 0, (cudaStream_t)stream>>>(
+        (const __nv_bfloat16*)h, H, base, scale, out);
+  });
 }
 
 int exgb_conv_out1_bwd_data(void* stream, const float* dout, int B, int H, const float* w, const void* pre,
