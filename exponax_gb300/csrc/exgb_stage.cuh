@@ -86,6 +86,139 @@ __device__ __forceinline__ float2 stage_upd(const PlanDev& P, const StageBufs& b
   return stage_upd_at(P, b, o, o, stage, nv);
 }
 
+// R modes at once, each as stage_upd (o[j] indexes the state buffers and the coefficient tables;
+// modes with ok[j] false are read at a valid index and not written).  All global loads of the R
+// updates are issued before the first store, so their latencies overlap: in a loop of single updates
+// the compiler must keep each mode's loads behind the previous mode's stores, which may alias them.
+template <int R>
+__device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs& b, const int64_t (&o)[R],
+                                               const bool (&ok)[R], int stage, float2 (&nv)[R]) {
+  if (P.order == 1 || (P.order == 2 && stage == 0) || (P.order == 3 && stage == 0) ||
+      (P.order == 4 && stage <= 1)) {
+    // s = E' U + c0 nv with E' = E (orders 1, 2) or E_{h/2} (orders 3, 4)
+    const float2* Ep = (P.order <= 2) ? P.E : P.Eh;
+    float2 e[R], u[R];
+    float k0[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      e[j] = __ldg(Ep + o[j]);
+      u[j] = b.U[o[j]];
+      k0[j] = __ldg(P.c[0] + o[j]);
+    }
+    float2* Nd = (P.order == 1) ? nullptr : (P.order == 4 && stage == 1) ? b.N1 : b.N0;
+    float2* Sd = (P.order == 1) ? b.U : (P.order == 4 && stage == 0) ? b.S1 : b.S;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const float2 s = cadd(cmul(e[j], u[j]), cscale(nv[j], k0[j]));
+      if (ok[j]) {
+        if (Nd) Nd[o[j]] = nv[j];
+        Sd[o[j]] = s;
+      }
+      nv[j] = s;
+    }
+  } else if (P.order == 2) {
+    float2 sv[R], n0[R];
+    float k1[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      sv[j] = b.S[o[j]];
+      n0[j] = b.N0[o[j]];
+      k1[j] = __ldg(P.c[1] + o[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const float2 r = cadd(sv[j], cscale(csub(nv[j], n0[j]), k1[j]));
+      if (ok[j]) b.U[o[j]] = r;
+      nv[j] = r;
+    }
+  } else if (P.order == 3 && stage == 1) {
+    float2 e[R], u[R], n0[R];
+    float k1[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      e[j] = __ldg(P.E + o[j]);
+      u[j] = b.U[o[j]];
+      n0[j] = b.N0[o[j]];
+      k1[j] = __ldg(P.c[1] + o[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const float2 t = csub(cscale(nv[j], 2.f), n0[j]);
+      const float2 s = cadd(cmul(e[j], u[j]), cscale(t, k1[j]));
+      if (ok[j]) {
+        b.N1[o[j]] = nv[j];
+        b.S[o[j]] = s;
+      }
+      nv[j] = s;
+    }
+  } else if (P.order == 3) {
+    float2 e[R], u[R], n0[R], n1[R];
+    float k2[R], k3[R], k4[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      e[j] = __ldg(P.E + o[j]);
+      u[j] = b.U[o[j]];
+      n0[j] = b.N0[o[j]];
+      n1[j] = b.N1[o[j]];
+      k2[j] = __ldg(P.c[2] + o[j]);
+      k3[j] = __ldg(P.c[3] + o[j]);
+      k4[j] = __ldg(P.c[4] + o[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      float2 r = cmul(e[j], u[j]);
+      r = cadd(r, cscale(n0[j], k2[j]));
+      r = cadd(r, cscale(n1[j], k3[j]));
+      r = cadd(r, cscale(nv[j], k4[j]));
+      if (ok[j]) b.U[o[j]] = r;
+      nv[j] = r;
+    }
+  } else if (stage == 2) {
+    float2 e[R], s1[R], n0[R];
+    float k0[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      e[j] = __ldg(P.Eh + o[j]);
+      s1[j] = b.S1[o[j]];
+      n0[j] = b.N0[o[j]];
+      k0[j] = __ldg(P.c[0] + o[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const float2 t = csub(cscale(nv[j], 2.f), n0[j]);
+      const float2 s = cadd(cmul(e[j], s1[j]), cscale(t, k0[j]));
+      if (ok[j]) {
+        b.N2[o[j]] = nv[j];
+        b.S[o[j]] = s;
+      }
+      nv[j] = s;
+    }
+  } else {
+    float2 e[R], u[R], n0[R], n1[R], n2[R];
+    float k3[R], k4[R], k5[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      e[j] = __ldg(P.E + o[j]);
+      u[j] = b.U[o[j]];
+      n0[j] = b.N0[o[j]];
+      n1[j] = b.N1[o[j]];
+      n2[j] = b.N2[o[j]];
+      k3[j] = __ldg(P.c[3] + o[j]);
+      k4[j] = __ldg(P.c[4] + o[j]);
+      k5[j] = __ldg(P.c[5] + o[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      float2 r = cmul(e[j], u[j]);
+      r = cadd(r, cscale(n0[j], k3[j]));
+      r = cadd(r, cscale(cadd(n1[j], n2[j]), 2.f * k4[j]));
+      r = cadd(r, cscale(nv[j], k5[j]));
+      if (ok[j]) b.U[o[j]] = r;
+      nv[j] = r;
+    }
+  }
+}
+
 // Per-CTA state buffers (each `colsz` modes) of an ETDRK method of the given order.
 __host__ __device__ __forceinline__ StageBufs stage_bufs(float2* q, int order, int64_t colsz) {
   StageBufs sb;

@@ -345,10 +345,27 @@ __global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
           uout[(int64_t)kx * M + col0 + c] = colbuf[cb(kx, c)];
         }
       } else {
-        for (int t = tid; t < ncols * N; t += THREADS) {
-          const int c = t / N, kx = t % N;
-          const int64_t o = (int64_t)(col0 + c) * N + kx;
-          colbuf[cb(kx, c)] = stage_upd(P, sb, o, st, colbuf[cb(kx, c)]);
+        // kRU modes per thread at a time, their L2 loads in flight together
+        constexpr int kRU = 4;
+        for (int t0 = tid; t0 < ncols * N; t0 += kRU * THREADS) {
+          int64_t o[kRU];
+          bool ok[kRU];
+          float2 nv[kRU];
+          int ci[kRU];
+#pragma unroll
+          for (int j = 0; j < kRU; ++j) {
+            const int t = t0 + j * THREADS;
+            ok[j] = t < ncols * N;
+            const int tt = ok[j] ? t : t0;
+            const int c = tt / N, kx = tt % N;
+            o[j] = (int64_t)(col0 + c) * N + kx;
+            ci[j] = cb(kx, c);
+            nv[j] = colbuf[ci[j]];
+          }
+          stage_upd_many<kRU>(P, sb, o, ok, st, nv);
+#pragma unroll
+          for (int j = 0; j < kRU; ++j)
+            if (ok[j]) colbuf[ci[j]] = nv[j];
         }
       }
       if (!a.nonlinear_only) {
