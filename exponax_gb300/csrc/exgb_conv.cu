@@ -11,11 +11,13 @@
 //
 // * conv48_tc_kernel: 48 -> 48 channels as an implicit GEMM on the tcgen05
 //   tensor cores (kind::f16, bf16 x bf16 -> FP32 in tensor memory): a tile
-//   is 2 rows x 64 columns x 48 output channels, its operands read by
-//   shared-memory descriptors from shifted copies of the input rows; the
-//   epilogue adds the bias and applies GELU (forward) or multiplies by
-//   GELU'(pre) of the layer below (backward-data, with flipped weights).
-// * conv_in1 / conv_out1: the 1 -> 48 and 48 -> 1 layers (SIMT).
+//   is 2 rows x 64 columns, the three horizontal taps of a row offset
+//   stacked along N (N = 144), inputs by TMA; the epilogue adds the
+//   neighbours' partial sums, the bias and applies GELU (forward) or
+//   multiplies by GELU'(pre) of the layer below (backward-data, with
+//   flipped weights).
+// * conv_in1 / conv_out1: the 1 -> 48 and 48 -> 1 layers (SIMT, weights
+//   in the constant bank).
 // * weight gradients: per-CTA partial sums over pixel chunks, then a
 //   deterministic reduction.
 // * adam_kernel: FP32 master weights, bf16 working copies (and the flipped
@@ -975,8 +977,12 @@ int exgb_conv_out1_bwd_data(void* stream, const float* dout, int B, int H, const
 // part must hold nchunk * 9*48*48 floats (48->48) or nchunk * 9*48 (thin); part_b nchunk * 48.
 int exgb_wgrad(void* stream, int kind, const void* a, const void* bsrc, int B, int H, float* part, float* part_b,
                float* dw, float* db) {
+  if (!a || !bsrc || !part || !part_b || !dw || !db || B < 0 || H < 1 || kind < 0 || kind > 2)
+    return fail(EXGB_EINVAL, "exgb_wgrad: NULL argument, bad shape or kind");
+  if (B == 0) return EXGB_OK;
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t n = (int64_t)B * H * kW;
+  if ((n + kChunk - 1) / kChunk > 2147483647LL) return fail(EXGB_EINVAL, "exgb_wgrad: too many pixels");
   const int nchunk = (int)((n + kChunk - 1) / kChunk);
   if (kind == 0) {  // 48 -> 48: a = dpre (bf16), bsrc = layer input (bf16)
     wgrad48_kernel<<<dim3(nchunk, 9), 256, 0, st>>>((const __nv_bfloat16*)a, (const __nv_bfloat16*)bsrc, B, H, part,
@@ -998,6 +1004,9 @@ int exgb_wgrad(void* stream, int kind, const void* a, const void* bsrc, int B, i
 
 int exgb_adam(void* stream, float* w, float* m, float* v, const float* g, int64_t n, float lr, float b1, float b2,
               float eps, int64_t t, void* w16, void* wflip, int is48) {
+  if (!w || !m || !v || !g || !w16 || n < 0 || t < 1 || (is48 && (!wflip || n != 9 * kC * kC)))
+    return fail(EXGB_EINVAL, "exgb_adam: NULL argument, n < 0, t < 1, or a 48 -> 48 layer of other than 9*48*48 weights");
+  if (n == 0) return EXGB_OK;
   const float bc1 = 1.f - powf(b1, (float)t), bc2 = 1.f - powf(b2, (float)t);
   adam_kernel<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(w, m, v, g, n, lr, b1, b2, eps, bc1, bc2,
                                                                (__nv_bfloat16*)w16, (__nv_bfloat16*)wflip, is48);
@@ -1006,6 +1015,9 @@ int exgb_adam(void* stream, float* w, float* m, float* v, const float* g, int64_
 }
 
 int exgb_cast_weights(void* stream, const float* w, int64_t n, void* w16, void* wflip, int is48) {
+  if (!w || !w16 || n < 0 || (is48 && (!wflip || n != 9 * kC * kC)))
+    return fail(EXGB_EINVAL, "exgb_cast_weights: NULL argument, n < 0, or a 48 -> 48 layer of other than 9*48*48 weights");
+  if (n == 0) return EXGB_OK;
   cast_weights_kernel<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(w, n, (__nv_bfloat16*)w16,
                                                                        (__nv_bfloat16*)wflip, is48);
   EXGB_CUDA(cudaGetLastError());
@@ -1014,6 +1026,8 @@ int exgb_cast_weights(void* stream, const float* w, int64_t n, void* w16, void* 
 
 int exgb_mse(void* stream, const float* pred, const float* target, int64_t n, float scale, float* grad,
              float* loss_part, int nblocks) {
+  if (!pred || !target || !grad || !loss_part || n < 0 || nblocks < 1 || nblocks > 65535)
+    return fail(EXGB_EINVAL, "exgb_mse: NULL argument, n < 0 or nblocks outside 1..65535");
   mse_kernel<<<nblocks, 256, 0, (cudaStream_t)stream>>>(pred, target, n, scale, grad, loss_part);
   EXGB_CUDA(cudaGetLastError());
   return EXGB_OK;
@@ -1021,6 +1035,9 @@ int exgb_mse(void* stream, const float* pred, const float* target, int64_t n, fl
 
 int exgb_guard(void* stream, const void* corr_hat, const void* plain_hat, int B, int H, int kg, float thresh,
                const float* plain, float* state, int* tripped) {
+  if (!corr_hat || !plain_hat || !plain || !state || !tripped || B < 0 || H < 1 || kg < 0)
+    return fail(EXGB_EINVAL, "exgb_guard: NULL argument or bad shape");
+  if (B == 0) return EXGB_OK;
   guard_kernel<<<B, 256, 0, (cudaStream_t)stream>>>((const float2*)corr_hat, (const float2*)plain_hat, B, H, kg,
                                                     thresh, plain, state, tripped);
   EXGB_CUDA(cudaGetLastError());

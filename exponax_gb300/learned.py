@@ -33,23 +33,26 @@ NMID = 4
 TAPS = 9
 
 
+_V, _I, _I64, _F = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
+# argument types of the corrector entry points (include/exgb_corrector.h)
+CORRECTOR_SIGNATURES = {
+    "exgb_conv48": [_V, _V, _I, _I, _V, _V, _I, _V, _V, _V],
+    "exgb_conv_in1": [_V, _V, _I, _I, _V, _V, _V, _V],
+    "exgb_conv_out1": [_V, _V, _I, _I, _V, _V, _V, _F, _V],
+    "exgb_conv_out1_bwd_data": [_V, _V, _I, _I, _V, _V, _V],
+    "exgb_wgrad": [_V, _I, _V, _V, _I, _I, _V, _V, _V, _V],
+    "exgb_adam": [_V, _V, _V, _V, _V, _I64, _F, _F, _F, _F, _I64, _V, _V, _I],
+    "exgb_cast_weights": [_V, _V, _I64, _V, _V, _I],
+    "exgb_mse": [_V, _V, _V, _I64, _F, _V, _V, _I],
+    "exgb_guard": [_V, _V, _V, _I, _I, _I, _F, _V, _V, _V],
+    "exgb_conv_status": [],
+}
+
+
 def _lib():
     lib = load()
     if not hasattr(lib, "_conv_sigs"):
-        V, I, I64, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_float
-        sigs = {
-            "exgb_conv48": [V, V, I, I, V, V, I, V, V, V],
-            "exgb_conv_in1": [V, V, I, I, V, V, V, V],
-            "exgb_conv_out1": [V, V, I, I, V, V, V, F, V],
-            "exgb_conv_out1_bwd_data": [V, V, I, I, V, V, V],
-            "exgb_wgrad": [V, I, V, V, I, I, V, V, V, V],
-            "exgb_adam": [V, V, V, V, V, I64, F, F, F, F, I64, V, V, I],
-            "exgb_cast_weights": [V, V, I64, V, V, I],
-            "exgb_mse": [V, V, V, I64, F, V, V, I],
-            "exgb_guard": [V, V, V, I, I, I, F, V, V, V],
-            "exgb_conv_status": [],
-        }
-        for name, args in sigs.items():
+        for name, args in CORRECTOR_SIGNATURES.items():
             fn = getattr(lib, name)
             fn.argtypes = args
             fn.restype = ctypes.c_int

@@ -42,7 +42,7 @@ extern "C" {
 #define EXGB_EUNSUPPORTED (-8)    /* valid for the reference, not built here */
 #define EXGB_ENOTIMPL (-9)        /* ETDRK order outside 0..4 */
 
-/* nonlinear function kinds (exponax/nonlin_fun/*) */
+/* nonlinear function kinds (exponax/nonlin_fun/) */
 #define EXGB_NL_ZERO 0               /* ZeroNonlinearFun            _zero.py:7-38 */
 #define EXGB_NL_CONVECTION 1         /* ConvectionNonlinearFun      _convection.py:7-245 */
 #define EXGB_NL_GRADIENT_NORM 2      /* GradientNormNonlinearFun    _gradient_norm.py:8-101 */
@@ -177,7 +177,7 @@ int exgb_irfftn(void* stream, int num_spatial_dims, int num_points, int64_t coun
  *   = ETDRKn.step_fourier, vmapped over the batch.
  * exgb_step replaces BaseStepper.__call__/step (_base_stepper.py:201-271).
  * exgb_nonlinear replaces BaseNonlinearFun.__call__ of the plan's
- *   nonlinear function (nonlin_fun/*), vmapped. */
+ *   nonlinear function (nonlin_fun/), vmapped. */
 int exgb_step_fourier(const exgb_plan* plan, void* stream, const void* u_hat_in, void* u_hat_out,
                       int64_t batch);
 int exgb_step(const exgb_plan* plan, void* stream, const float* u_in, float* u_out, int64_t batch);

@@ -19,8 +19,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "exgb.h")
 
 
-def _declared_functions():
-    src = open(HEADER).read()
+CORRECTOR_HEADER = os.path.join(ROOT, "include", "exgb_corrector.h")
+
+
+def _declared_functions(header=HEADER):
+    src = open(header).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(exgb_[a-z0-9_]+)\s*\(", src)))
 
@@ -32,6 +35,39 @@ def test_library_exports_every_declared_symbol():
     for n in names:
         assert hasattr(lib, n), n
     assert {s[0] for s in _lib.SIGNATURES} == set(names)
+
+
+def test_library_exports_every_corrector_symbol():
+    from exponax_gb300.learned import CORRECTOR_SIGNATURES
+
+    lib = _lib.load()
+    names = _declared_functions(CORRECTOR_HEADER)
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(CORRECTOR_SIGNATURES) == set(names)
+    assert not set(names) & set(_declared_functions())
+
+
+def test_corrector_headers_compile_together_as_c():
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        open(c, "w").write(f'#include "{HEADER}"\n#include "{CORRECTOR_HEADER}"\nint main(void){{return 0;}}\n')
+        subprocess.run(["gcc", "-Wall", "-Werror", c, "-o", os.path.join(d, "t")], check=True)
+
+
+def test_corrector_null_arguments_are_rejected_without_touching_the_gpu():
+    from exponax_gb300.learned import _lib as corr_lib
+
+    lib = corr_lib()
+    assert lib.exgb_conv_in1(None, None, 1, 64, None, None, None, None) == _lib.EXGB_EINVAL
+    assert lib.exgb_conv_out1(None, None, 1, 64, None, None, None, 1.0, None) == _lib.EXGB_EINVAL
+    assert lib.exgb_conv48(None, None, 1, 63, None, None, 0, None, None, None) == _lib.EXGB_EINVAL
+    assert lib.exgb_wgrad(None, 3, None, None, 1, 64, None, None, None, None) == _lib.EXGB_EINVAL
+    assert lib.exgb_adam(None, None, None, None, None, 10, 1e-3, 0.9, 0.999, 1e-8, 1, None, None, 0) == _lib.EXGB_EINVAL
+    assert lib.exgb_cast_weights(None, None, 10, None, None, 1) == _lib.EXGB_EINVAL
+    assert lib.exgb_mse(None, None, None, 10, 1.0, None, None, 0) == _lib.EXGB_EINVAL
+    assert lib.exgb_guard(None, None, None, 1, 64, 8, 0.1, None, None, None) == _lib.EXGB_EINVAL
+    assert b"NULL" in lib.exgb_last_error() or b"bad" in lib.exgb_last_error()
 
 
 def test_version_and_error_string_without_gpu():
