@@ -1004,8 +1004,8 @@ int exgb_wgrad(void* stream, int kind, const void* a, const void* bsrc, int B, i
 
 int exgb_adam(void* stream, float* w, float* m, float* v, const float* g, int64_t n, float lr, float b1, float b2,
               float eps, int64_t t, void* w16, void* wflip, int is48) {
-  if (!w || !m || !v || !g || !w16 || n < 0 || t < 1 || (is48 && (!wflip || n != 9 * kC * kC)))
-    return fail(EXGB_EINVAL, "exgb_adam: NULL argument, n < 0, t < 1, or a 48 -> 48 layer of other than 9*48*48 weights");
+  if (!w || !m || !v || !g || n < 0 || t < 1 || (is48 && wflip && n != 9 * kC * kC))
+    return fail(EXGB_EINVAL, "exgb_adam: NULL argument, n < 0, t < 1, or a flipped copy of other than 9*48*48 weights");
   if (n == 0) return EXGB_OK;
   const float bc1 = 1.f - powf(b1, (float)t), bc2 = 1.f - powf(b2, (float)t);
   adam_kernel<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(w, m, v, g, n, lr, b1, b2, eps, bc1, bc2,
@@ -1015,8 +1015,8 @@ int exgb_adam(void* stream, float* w, float* m, float* v, const float* g, int64_
 }
 
 int exgb_cast_weights(void* stream, const float* w, int64_t n, void* w16, void* wflip, int is48) {
-  if (!w || !w16 || n < 0 || (is48 && (!wflip || n != 9 * kC * kC)))
-    return fail(EXGB_EINVAL, "exgb_cast_weights: NULL argument, n < 0, or a 48 -> 48 layer of other than 9*48*48 weights");
+  if (!w || n < 0 || (is48 && wflip && n != 9 * kC * kC))
+    return fail(EXGB_EINVAL, "exgb_cast_weights: NULL argument, n < 0, or a flipped copy of other than 9*48*48 weights");
   if (n == 0) return EXGB_OK;
   cast_weights_kernel<<<blocks_for(n), 256, 0, (cudaStream_t)stream>>>(w, n, (__nv_bfloat16*)w16,
                                                                        (__nv_bfloat16*)wflip, is48);

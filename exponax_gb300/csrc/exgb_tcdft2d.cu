@@ -37,6 +37,9 @@
 // -- 10 MMA chains, all operands in shared memory, accumulators in 4 slots of
 // 128 TMEM columns.  Modes outside the kept set evolve linearly (E^n, the c2r
 // projection on the half-axis columns 0 and N/2) exactly as in the FP32 kernels.
+// The complex helpers' scalar forms: in this kernel (SIMT work between MMA chains) they measured 2 %
+// faster than the packed f32x2 ones the FFT kernels use (26.15 against 26.69 ms at kolmo128).
+#define EXGB_SCALAR_COMPLEX 1
 #include <cuda_runtime.h>
 
 #include <algorithm>

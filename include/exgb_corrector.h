@@ -71,12 +71,14 @@ int exgb_wgrad(void* stream, int kind, const void* a, const void* bsrc, int B, i
                float* dw, float* db);
 
 /* One Adam step (bias-corrected, step count t >= 1) on n FP32 master weights
- * w with moments m, v and gradient g; writes the bf16 working copy w16 and,
- * for a 48 -> 48 layer (is48, n = 9*48*48), the flipped copy wflip. */
+ * w with moments m, v and gradient g; writes the bf16 working copy w16
+ * unless it is NULL and, for a 48 -> 48 layer (is48, n = 9*48*48), the
+ * flipped copy wflip unless it is NULL. */
 int exgb_adam(void* stream, float* w, float* m, float* v, const float* g, int64_t n, float lr, float b1, float b2,
               float eps, int64_t t, void* w16, void* wflip, int is48);
 
-/* The bf16 working copy (and flipped copy, is48) of n FP32 weights. */
+/* The bf16 working copy (and flipped copy, is48) of n FP32 weights; either
+ * output may be NULL. */
 int exgb_cast_weights(void* stream, const float* w, int64_t n, void* w16, void* wflip, int is48);
 
 /* Mean squared error: loss_part[b] = per-block sums of (pred - target)^2 over

@@ -240,3 +240,53 @@ def test_thin_layers(B, H):
         if with_base:
             ref = ref + base
         assert rel(out.cpu().numpy(), ref) < 1e-5
+
+
+@pytest.mark.parametrize("B,H", [(2, 64), (3, 13)])
+def test_backward_kernels_per_layer(B, H):
+    """The backward kernels alone against float64 on the same bf16 / FP32 inputs, at the bar of their
+    FP32 accumulation: the weight and bias gradients of all three layer kinds (per-chunk FP32 partial
+    sums over 512 pixels, then an FP32 reduction) within 2e-6 relative L2, and the 48 -> 1 layer's
+    backward-data (FP32 sums, bf16 output) within the bf16 rounding (4e-3)."""
+    from exponax_gb300 import _device
+    from oracle import corrector_np as co
+    from exponax_gb300.learned import PeriodicConvCorrector, _lib, _p
+
+    rng = np.random.default_rng(11 * B + H)
+    lib = _lib()
+    s = _device.stream()
+    n = B * H * 64
+    nchunk = (n + 511) // 512
+    part = torch.empty(nchunk * 9 * 48 * 48, dtype=torch.float32, device="cuda")
+    part_b = torch.empty(nchunk * 48, dtype=torch.float32, device="cuda")
+    dpre = _bf16(rng.standard_normal((B, H, 64, 48))).float().numpy().astype(np.float64)
+    x48 = _bf16(rng.standard_normal((B, H, 64, 48))).float().numpy().astype(np.float64)
+    x1 = rng.standard_normal((B, H, 64)).astype(np.float32)
+    dout = rng.standard_normal((B, H, 64)).astype(np.float32)
+    dw = torch.full((9 * 48 * 48,), float("nan"), device="cuda")
+    db = torch.full((48,), float("nan"), device="cuda")
+    dpre_d, x48_d = _bf16(dpre).cuda(), _bf16(x48).cuda()
+    x1_d, dout_d = torch.from_numpy(x1).cuda(), torch.from_numpy(dout).cuda()
+    # 48 -> 48
+    assert lib.exgb_wgrad(s, 0, _p(dpre_d), _p(x48_d), B, H, _p(part), _p(part_b), _p(dw), _p(db)) == 0
+    assert rel(dw.cpu().numpy(), co.conv_wgrad(dpre, x48)) < 2e-6
+    assert rel(db.cpu().numpy(), dpre.sum(axis=(0, 1, 2))) < 2e-6
+    # 1 -> 48: the input field is the single channel
+    assert lib.exgb_wgrad(s, 1, _p(dpre_d), _p(x1_d), B, H, _p(part), _p(part_b), _p(dw), _p(db)) == 0
+    ref = co.conv_wgrad(dpre, x1.astype(np.float64)[..., None])[:, :, 0]  # (9, 48) = W[tap][co]
+    assert rel(dw[:9 * 48].cpu().numpy(), ref) < 2e-6
+    assert rel(db.cpu().numpy(), dpre.sum(axis=(0, 1, 2))) < 2e-6
+    # 48 -> 1: the output gradient is the single channel
+    assert lib.exgb_wgrad(s, 2, _p(dout_d), _p(x48_d), B, H, _p(part), _p(part_b), _p(dw), _p(db)) == 0
+    ref = co.conv_wgrad(dout.astype(np.float64)[..., None], x48)[:, 0, :]  # (9, 48) = W[tap][ci]
+    assert rel(dw[:9 * 48].cpu().numpy(), ref) < 2e-6
+    assert abs(float(db[0]) - float(dout.astype(np.float64).sum())) <= 2e-6 * float(np.abs(dout).sum())
+    # 48 -> 1 backward-data, times gelu' of the pre-activations
+    w6 = (rng.standard_normal((9, 48)) / np.sqrt(9 * 48)).astype(np.float32)
+    pre = _bf16(rng.standard_normal((B, H, 64, 48))).float().numpy().astype(np.float64)
+    out = torch.full((B, H, 64, 48), float("nan"), dtype=torch.bfloat16, device="cuda")
+    assert lib.exgb_conv_out1_bwd_data(s, _p(dout_d), B, H, _p(torch.from_numpy(w6).cuda()), _p(_bf16(pre).cuda()),
+                                       _p(out)) == 0
+    ref = co.conv_T(dout.astype(np.float64)[..., None], w6.astype(np.float64)[:, None, :]) * co.gelu_d(pre)
+    assert rel(out.float().cpu().numpy(), ref) < 4e-3
+    PeriodicConvCorrector.status()

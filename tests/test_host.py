@@ -64,7 +64,7 @@ def test_corrector_null_arguments_are_rejected_without_touching_the_gpu():
     assert lib.exgb_conv48(None, None, 1, 63, None, None, 0, None, None, None) == _lib.EXGB_EINVAL
     assert lib.exgb_wgrad(None, 3, None, None, 1, 64, None, None, None, None) == _lib.EXGB_EINVAL
     assert lib.exgb_adam(None, None, None, None, None, 10, 1e-3, 0.9, 0.999, 1e-8, 1, None, None, 0) == _lib.EXGB_EINVAL
-    assert lib.exgb_cast_weights(None, None, 10, None, None, 1) == _lib.EXGB_EINVAL
+    assert lib.exgb_cast_weights(None, None, 10, None, None, 1) == _lib.EXGB_EINVAL  # w NULL
     assert lib.exgb_mse(None, None, None, 10, 1.0, None, None, 0) == _lib.EXGB_EINVAL
     assert lib.exgb_guard(None, None, None, 1, 64, 8, 0.1, None, None, None) == _lib.EXGB_EINVAL
     assert b"NULL" in lib.exgb_last_error() or b"bad" in lib.exgb_last_error()
