@@ -836,14 +836,20 @@ static unsigned blocks_for(int64_t n) {
   return (unsigned)(b < 1 ? 1 : (b > 65535 * 4 ? 65535 * 4 : b));
 }
 
-// The users of one constant bank of thin-layer weights, in launch order: a launch waits (on its stream)
-// for the previous user's kernel before its copy overwrites the bank.  Inside a stream capture the
-// graph's own order applies.
+// The users of one constant bank of thin-layer weights on one device, in launch order: a launch waits
+// (on its stream) for the previous user's kernel before its copy overwrites the bank.  Inside a stream
+// capture the graph's own order applies.
 struct ConstBank {
   std::mutex mu;
   cudaEvent_t done = nullptr;
 };
-static ConstBank g_bank_in1, g_bank_out1;
+constexpr int kMaxDevices = 64;
+static ConstBank g_bank_in1[kMaxDevices], g_bank_out1[kMaxDevices];
+static int bank_device(int* dev) {
+  EXGB_CUDA(cudaGetDevice(dev));
+  if (*dev < 0 || *dev >= kMaxDevices) return fail(EXGB_EUNSUPPORTED, "device index out of range");
+  return EXGB_OK;
+}
 
 // Copy nw weights and nb bias values (one copy where the bias follows the weights, as in the
 // corrector's parameter vector) into the constant bank `sym` on `st`, then run `launch` on `st`.
@@ -945,7 +951,9 @@ int exgb_conv_in1(void* stream, const float* x, int B, int H, const float* w, co
   if ((int64_t)B * H == 0) return EXGB_OK;
   if ((int64_t)B * H > 2147483647LL) return fail(EXGB_EINVAL, "too many rows");
   if (B > 65535) return fail(EXGB_EINVAL, "batch above 65535");
-  return with_const_weights(g_bank_in1, (const void*)c_in1, w, 9 * kC, bias, kC, (cudaStream_t)stream, [&]() {
+  int dev = 0;
+  if (const int rc = bank_device(&dev)) return rc;
+  return with_const_weights(g_bank_in1[dev], (const void*)c_in1, w, 9 * kC, bias, kC, (cudaStream_t)stream, [&]() {
     conv_in1_kernel<<<dim3((H * kW + 255) / 256, B), 256, 0, (cudaStream_t)stream>>>(x, H, (__nv_bfloat16*)pre,
                                                                                      (__nv_bfloat16*)post);
   });
@@ -957,7 +965,9 @@ int exgb_conv_out1(void* stream, const void* h, int B, int H, const float* w, co
   if ((int64_t)B * H == 0) return EXGB_OK;
   if ((int64_t)B * H > 2147483647LL) return fail(EXGB_EINVAL, "too many rows");
   if (B > 65535) return fail(EXGB_EINVAL, "batch above 65535");
-  return with_const_weights(g_bank_out1, (const void*)c_out1, w, 9 * kC, bias, 1, (cudaStream_t)stream, [&]() {
+  int dev = 0;
+  if (const int rc = bank_device(&dev)) return rc;
+  return with_const_weights(g_bank_out1[dev], (const void*)c_out1, w, 9 * kC, bias, 1, (cudaStream_t)stream, [&]() {
     conv_out1_kernel<<<dim3((H + kOut1Rows - 1) / kOut1Rows, B), kOut1Threads, 0, (cudaStream_t)stream>>>(
         (const __nv_bfloat16*)h, H, base, scale, out);
   });
