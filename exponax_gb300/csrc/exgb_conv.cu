@@ -861,7 +861,16 @@ static int with_const_weights(ConstBank& bk, const void* sym, const float* w, in
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   EXGB_CUDA(cudaStreamIsCapturing(st, &cs));
   const bool captured = cs != cudaStreamCaptureStatusNone;
-  if (!captured) EXGB_CUDA(cudaStreamWaitEvent(st, bk.done, 0));
+  if (!captured) {
+    cudaError_t e = cudaStreamWaitEvent(st, bk.done, 0);
+    if (e == cudaErrorInvalidResourceHandle) {
+      // the event went with a context torn down since (cudaDeviceReset): start a new one
+      cudaGetLastError();
+      EXGB_CUDA(cudaEventCreateWithFlags(&bk.done, cudaEventDisableTiming));
+      e = cudaStreamWaitEvent(st, bk.done, 0);
+    }
+    EXGB_CUDA(e);
+  }
   if (b == w + nw) {
     EXGB_CUDA(cudaMemcpyToSymbolAsync(sym, w, sizeof(float) * (size_t)(nw + nb), 0, cudaMemcpyDeviceToDevice, st));
   } else {
@@ -891,11 +900,9 @@ int exgb_conv48(void* stream, const void* x, int B, int H, const void* w, const 
   int dev = 0;
   EXGB_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(EXGB_EUNSUPPORTED, "device index out of range");
-  if (!sm_count[dev]) {
-    EXGB_CUDA(cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev));
-    EXGB_CUDA(cudaFuncSetAttribute(conv48_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)ctc::kSmemBytes));
-  }
+  if (!sm_count[dev]) EXGB_CUDA(cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev));
+  // set on every call: a context re-created after cudaDeviceReset starts without it
+  EXGB_CUDA(cudaFuncSetAttribute(conv48_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctc::kSmemBytes));
   const int64_t ntiles = (int64_t)B * (H / 2);
   if (ntiles > 2147483647LL) return fail(EXGB_EINVAL, "exgb_conv48: too many tiles");
   if (((uintptr_t)x & 15) != 0) return fail(EXGB_EINVAL, "exgb_conv48: input not 16-byte aligned");
