@@ -80,66 +80,77 @@ __device__ __forceinline__ int sym_index(int i, int j, int C) {
 
 // The NI spectra of mode k whose inverse transforms the pointwise step needs: channel c of the
 // state at x[c * xs], field f written to w[f * ws]; m = inside the dealiasing mask (pre-mask).
-__device__ __forceinline__ void derive_mode(const Geo& g, const Prog& p, const int (&k)[3], bool m,
-                                            const float2* x, int64_t xs, float2* w, int64_t ws) {
+// The derived spectra at one mode: channel c read as x(c), derived spectrum i written as w(i, value).
+// Callers pass pointer accessors (derive_mode below) or registers loaded ahead, and a sink that
+// stores every spectrum or keeps only the one they need (a runtime-indexed local array would live
+// in local memory).
+template <class X, class O>
+__device__ __forceinline__ void derive_mode_xo(const Geo& g, const Prog& p, const int (&k)[3], bool m, const X& x,
+                                               const O& w) {
   float d[3];
   for (int a = 0; a < 3; ++a) d[a] = g.ks * (float)k[a];
-    const float2 z = make_float2(0.f, 0.f);
-    switch (p.op) {
-      case OP_CONV_MC_NONCONS:
-        for (int c = 0; c < g.C; ++c) {
-          const float2 u = m ? x[c * xs] : z;
-          w[c * ws] = u;
-          for (int j = 0; j < g.D; ++j) w[(g.C + c * g.D + j) * ws] = times_i(d[j], u);
-        }
-        break;
-      case OP_CONV_SC_NONCONS: {
-        const float2 u = m ? x[0] : z;
-        w[0] = u;
-        float s = 0.f;
-        for (int j = 0; j < g.D; ++j) s += d[j];
-        w[ws] = times_i(s, u);
-      } break;
-      case OP_GRAD_NORM:
-        for (int c = 0; c < g.C; ++c) {
-          const float2 u = m ? x[c * xs] : z;
-          for (int j = 0; j < g.D; ++j) w[(c * g.D + j) * ws] = times_i(d[j], u);
-        }
-        break;
-      case OP_GENERAL: {
-        const float2 u = m ? x[0] : z;
-        w[0] = u;
-        for (int j = 0; j < g.D; ++j) w[(1 + j) * ws] = times_i(d[j], u);
-      } break;
-      case OP_VORT: {
-        // stream function psi = w / Lap with 1/Lap = 1 at k = 0; u = i k_y psi, v = -i k_x psi,
-        // w_x = i k_x w, w_y = i k_y w (k_x the leading axis, k_y the rfft axis)
-        const float2 wv = m ? x[0] : z;
-        const float lap = -(d[0] * d[0] + d[1] * d[1]);
-        const float il = lap != 0.f ? 1.f / lap : 1.f;
-        const float2 psi = cscale(wv, il);
-        w[0] = times_i(d[1], psi);
-        w[ws] = times_i(-d[0], psi);
-        w[2 * ws] = times_i(d[0], wv);
-        w[3 * ws] = times_i(d[1], wv);
-      } break;
-      case OP_PROJ3D: {
-        // w[0..2] = mask (i d x u^) (the curl), w[3..5] = mask u^
-        const float2 u0 = m ? x[0] : z, u1 = m ? x[xs] : z, u2 = m ? x[2 * xs] : z;
-        const float2 a1 = make_float2(d[1] * u2.x - d[2] * u1.x, d[1] * u2.y - d[2] * u1.y);
-        const float2 a2 = make_float2(d[2] * u0.x - d[0] * u2.x, d[2] * u0.y - d[0] * u2.y);
-        const float2 a3 = make_float2(d[0] * u1.x - d[1] * u0.x, d[0] * u1.y - d[1] * u0.y);
-        w[0] = make_float2(-a1.y, a1.x);
-        w[ws] = make_float2(-a2.y, a2.x);
-        w[2 * ws] = make_float2(-a3.y, a3.x);
-        w[3 * ws] = u0;
-        w[4 * ws] = u1;
-        w[5 * ws] = u2;
-      } break;
-      default:  // the masked state itself, one spectrum per channel
-        for (int c = 0; c < g.C; ++c) w[c * ws] = m ? x[c * xs] : z;
-        break;
-    }
+  const float2 z = make_float2(0.f, 0.f);
+  switch (p.op) {
+    case OP_CONV_MC_NONCONS:
+      for (int c = 0; c < g.C; ++c) {
+        const float2 u = m ? x(c) : z;
+        w(c, u);
+        for (int j = 0; j < g.D; ++j) w(g.C + c * g.D + j, times_i(d[j], u));
+      }
+      break;
+    case OP_CONV_SC_NONCONS: {
+      const float2 u = m ? x(0) : z;
+      w(0, u);
+      float s = 0.f;
+      for (int j = 0; j < g.D; ++j) s += d[j];
+      w(1, times_i(s, u));
+    } break;
+    case OP_GRAD_NORM:
+      for (int c = 0; c < g.C; ++c) {
+        const float2 u = m ? x(c) : z;
+        for (int j = 0; j < g.D; ++j) w(c * g.D + j, times_i(d[j], u));
+      }
+      break;
+    case OP_GENERAL: {
+      const float2 u = m ? x(0) : z;
+      w(0, u);
+      for (int j = 0; j < g.D; ++j) w(1 + j, times_i(d[j], u));
+    } break;
+    case OP_VORT: {
+      // stream function psi = w / Lap with 1/Lap = 1 at k = 0; u = i k_y psi, v = -i k_x psi,
+      // w_x = i k_x w, w_y = i k_y w (k_x the leading axis, k_y the rfft axis)
+      const float2 wv = m ? x(0) : z;
+      const float lap = -(d[0] * d[0] + d[1] * d[1]);
+      const float il = lap != 0.f ? 1.f / lap : 1.f;
+      const float2 psi = cscale(wv, il);
+      w(0, times_i(d[1], psi));
+      w(1, times_i(-d[0], psi));
+      w(2, times_i(d[0], wv));
+      w(3, times_i(d[1], wv));
+    } break;
+    case OP_PROJ3D: {
+      // w[0..2] = mask (i d x u^) (the curl), w[3..5] = mask u^
+      const float2 u0 = m ? x(0) : z, u1 = m ? x(1) : z, u2 = m ? x(2) : z;
+      const float2 a1 = make_float2(d[1] * u2.x - d[2] * u1.x, d[1] * u2.y - d[2] * u1.y);
+      const float2 a2 = make_float2(d[2] * u0.x - d[0] * u2.x, d[2] * u0.y - d[0] * u2.y);
+      const float2 a3 = make_float2(d[0] * u1.x - d[1] * u0.x, d[0] * u1.y - d[1] * u0.y);
+      w(0, make_float2(-a1.y, a1.x));
+      w(1, make_float2(-a2.y, a2.x));
+      w(2, make_float2(-a3.y, a3.x));
+      w(3, u0);
+      w(4, u1);
+      w(5, u2);
+    } break;
+    default:  // the masked state itself, one spectrum per channel
+      for (int c = 0; c < g.C; ++c) w(c, m ? x(c) : z);
+      break;
+  }
+}
+
+__device__ __forceinline__ void derive_mode(const Geo& g, const Prog& p, const int (&k)[3], bool m,
+                                            const float2* x, int64_t xs, float2* w, int64_t ws) {
+  derive_mode_xo(
+      g, p, k, m, [x, xs](int c) { return x[c * xs]; }, [w, ws](int i, float2 v) { w[i * ws] = v; });
 }
 
 // The NF products at one grid point from the NI physical values in[]: field f written to f[i * fs].
@@ -234,7 +245,9 @@ __device__ __forceinline__ void combine_mode(const PlanDev& P, const Geo& g, con
     if (m) {
       switch (p.op) {
         case OP_CONV_MC_CONS:
-          for (int i = 0; i < g.C; ++i) {
+#pragma unroll
+          for (int i = 0; i < MAXC; ++i) {  // compile-time channel indices keep nv in registers
+            if (i >= g.C) break;
             float2 acc = make_float2(0.f, 0.f);
             for (int j = 0; j < g.D; ++j) acc = cadd(acc, times_i(d[j], h[(sym_index(i, j, g.C)) * hs]));
             nv[i] = cscale(acc, p.s0);
@@ -244,7 +257,11 @@ __device__ __forceinline__ void combine_mode(const PlanDev& P, const Geo& g, con
           nv[0] = cscale(times_i(dsum, h[0]), p.s0);
           break;
         case OP_GRAD_NORM:
-          for (int c = 0; c < g.C; ++c) nv[c] = (p.zmf && dc) ? make_float2(0.f, 0.f) : cscale(h[(c) * hs], p.s0);
+#pragma unroll
+          for (int c = 0; c < MAXC; ++c) {
+            if (c >= g.C) break;
+            nv[c] = (p.zmf && dc) ? make_float2(0.f, 0.f) : cscale(h[(c) * hs], p.s0);
+          }
           break;
         case OP_GENERAL: {
           const float2 sq = h[0];
@@ -271,7 +288,11 @@ __device__ __forceinline__ void combine_mode(const PlanDev& P, const Geo& g, con
           nv[2] = n2;
         } break;
         default:  // -b F[.] (non-conservative convection, vorticity) or F[.] (polynomial, Gray-Scott): scale s0
-          for (int c = 0; c < g.C; ++c) nv[c] = cscale(h[(c) * hs], p.s0);
+#pragma unroll
+          for (int c = 0; c < MAXC; ++c) {
+            if (c >= g.C) break;
+            nv[c] = cscale(h[(c) * hs], p.s0);
+          }
           break;
       }
     }

@@ -138,13 +138,40 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass1_3d_kernel(const Args a)
   const int64_t s = blockIdx.z;
   load_twl<N>(twl, a.tw);
   const float2* xs = a.xin + s * a.sstride + (int64_t)kz * a.pl;
-  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
-    const int kx = e / N, ky = e - kx * N;
-    const int k[3] = {sgn_of(kx, N), sgn_of(ky, N), kz};
-    const bool m = abs(k[0]) <= a.K && abs(k[1]) <= a.K && kz <= a.K;
-    float2 w[MAXC + MAXC * 3];
-    ndg::derive_mode(a.g, a.p, k, m, xs + e, a.cstride, w, 1);
-    plane[(size_t)kx * R::PS + ky] = w[f];
+  // kU modes per thread at a time: their channel loads are issued together, and only field f of the
+  // derived spectra is kept (in a register, not a runtime-indexed local array)
+  constexpr int kU = 4;
+  static_assert(MAXC == 3, "the channel accessor below picks among 3 registers");
+  const int C = a.g.C;
+  for (int e0 = threadIdx.x; e0 < N * N; e0 += kU * (int)blockDim.x) {
+    float2 xv[kU][MAXC];
+    int kk[kU][3];
+    bool mk[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = e0 + u * (int)blockDim.x;
+      const int ee = e < N * N ? e : e0;
+      const int kx = ee / N, ky = ee - kx * N;
+      kk[u][0] = sgn_of(kx, N);
+      kk[u][1] = sgn_of(ky, N);
+      kk[u][2] = kz;
+      mk[u] = abs(kk[u][0]) <= a.K && abs(kk[u][1]) <= a.K && kz <= a.K;
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c)
+        xv[u][c] = (mk[u] && c < C) ? xs[ee + (int64_t)c * a.cstride] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = e0 + u * (int)blockDim.x;
+      if (e >= N * N) break;
+      float2 r = make_float2(0.f, 0.f);
+      ndg::derive_mode_xo(
+          a.g, a.p, kk[u], mk[u], [&](int c) { return c == 0 ? xv[u][0] : (c == 1 ? xv[u][1] : xv[u][2]); },
+          [&](int i, float2 v) {
+            if (i == f) r = v;
+          });
+      plane[(size_t)(e / N) * R::PS + (e % N)] = r;
+    }
   }
   __syncthreads();
   plane_rows_fft<N, true>(plane, sp1 + R::TILES, twl);
@@ -216,6 +243,14 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS2) pass2_3d_kernel(const Args a
   for (int e = threadIdx.x; e < TY * N; e += blockDim.x) {
     const int yy = e / N, z = e - yy * N;
     float* base = reinterpret_cast<float*>(slots) + (size_t)(yy >> 1) * 2 * SL + (yy & 1) * N + z;
+    if (a.p.op == ndg::OP_PROJ3D) {  // u x (curl u) with fixed indices (the generic form indexes a local array)
+      const float w0 = base[0], w1 = base[fs], w2 = base[2 * fs];
+      const float v0 = base[3 * fs], v1 = base[4 * fs], v2 = base[5 * fs];
+      base[0] = v1 * w2 - v2 * w1;
+      base[fs] = v2 * w0 - v0 * w2;
+      base[2 * fs] = v0 * w1 - v1 * w0;
+      continue;
+    }
     float in[MAXC + MAXC * 3];
     for (int f = 0; f < NI; ++f) in[f] = base[f * fs];
     ndg::pointwise_point(a.g, a.p, in, base, fs);
@@ -296,10 +331,14 @@ __global__ void __launch_bounds__(256) combine_planes_kernel(const Args a, int64
     ndg::combine_mode(a.P, a.g, a.p, k, m, a.Hq + s * NF * per + r, per, nv);
     if (a.stage < 0) {
       float2* o = a.nout + s * (int64_t)C * a.tstride + (int64_t)e * a.M + kz;
-      for (int c = 0; c < C; ++c) o[c * a.tstride] = nv[c];
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c)
+        if (c < C) o[c * a.tstride] = nv[c];
       continue;
     }
-    for (int c = 0; c < C; ++c) {
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c) {  // compile-time channel indices keep nv in registers
+      if (c >= C) break;
       const int64_t ci = (a.P.lin_ch == 1 ? 0 : (int64_t)c * a.tstride) + r;
       stage_upd_at(a.P, a.sb, s * a.sstride + c * a.cstride + r, ci, a.stage, nv[c]);
     }
