@@ -57,9 +57,9 @@ __global__ void pointwise_kernel(Geo g, Prog p, int64_t cb, const float* __restr
     const int64_t b = t / g.npts, q = t - b * g.npts;
     const float* src = Ph + b * p.NI * g.npts + q;
     float* f = Q + b * p.NF * g.npts + q;
-    float in[MAXC + MAXC * 3];
-    for (int i = 0; i < p.NI; ++i) in[i] = src[i * g.npts];
-    pointwise_point(g, p, in, f, g.npts);
+    float in[kMaxNI];
+    load_point(src, g.npts, p.NI, in);
+    pointwise_point_reg(g, p, in, f, g.npts);
   }
 }
 
@@ -77,10 +77,14 @@ __global__ void combine_kernel(PlanDev P, Geo g, Prog p, int64_t cb, const float
     combine_mode(P, g, p, k, m, H + b * p.NF * g.per + r, g.per, nv);
     const int64_t base = b * g.C * g.per + r;
     if (stage < 0) {
-      for (int c = 0; c < g.C; ++c) nout[base + c * g.per] = nv[c];
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c)
+        if (c < g.C) nout[base + c * g.per] = nv[c];
       continue;
     }
-    for (int c = 0; c < g.C; ++c) {
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c) {  // compile-time channel indices keep nv in registers
+      if (c >= g.C) break;
       const int64_t ci = (P.lin_ch == 1 ? 0 : (int64_t)c * g.per) + r;
       stage_upd_at(P, sb, base + c * g.per, ci, stage, nv[c]);
     }

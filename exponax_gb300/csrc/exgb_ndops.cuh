@@ -153,79 +153,130 @@ __device__ __forceinline__ void derive_mode(const Geo& g, const Prog& p, const i
       g, p, k, m, [x, xs](int c) { return x[c * xs]; }, [w, ws](int i, float2 v) { w[i * ws] = v; });
 }
 
-// The NF products at one grid point from the NI physical values in[]: field f written to f[i * fs].
-__device__ __forceinline__ void pointwise_point(const Geo& g, const Prog& p, const float* in, float* f, int64_t fs) {
-    switch (p.op) {
-      case OP_CONV_MC_CONS: {
-        int o = 0;
-        for (int i = 0; i < g.C; ++i)
-          for (int j = i; j < g.C; ++j) f[(o++) * fs] = in[i] * in[j];
-      } break;
-      case OP_CONV_MC_NONCONS:
-        for (int i = 0; i < g.C; ++i) {
-          float s = 0.f;
-          for (int j = 0; j < g.D; ++j) s += in[j] * in[g.C + i * g.D + j];
-          f[i * fs] = s;
-        }
-        break;
-      case OP_CONV_SC_CONS:
-        f[0] = in[0] * in[0];
-        break;
-      case OP_CONV_SC_NONCONS:
-        f[0] = in[0] * in[1];
-        break;
-      case OP_GRAD_NORM:
-        for (int c = 0; c < g.C; ++c) {
-          float s = 0.f;
-          for (int j = 0; j < g.D; ++j) s += in[c * g.D + j] * in[c * g.D + j];
-          f[c * fs] = s;
-        }
-        break;
-      case OP_POLY:
-        for (int c = 0; c < g.C; ++c) {
-          // sum_k c_k u^k with the powers accumulated as the reference does
-          const float u = in[c];
-          float pw = 1.f, acc = 0.f;
-          for (int i = 0; i < p.npoly; ++i) {
-            acc += p.poly[i] * pw;
-            pw *= u;
-          }
-          f[c * fs] = acc;
-        }
-        break;
-      case OP_GENERAL: {
-        float s = 0.f;
-        for (int j = 0; j < g.D; ++j) s += in[1 + j] * in[1 + j];
-        f[0] = in[0] * in[0];
-        f[fs] = s;
-      } break;
-      case OP_CAHN_HILLIARD:
-        f[0] = in[0] * in[0] * in[0];
-        break;
-      case OP_GRAY_SCOTT: {
-        const float u0 = in[0], u1 = in[1];
-        const float uvv = u0 * (u1 * u1);
-        f[0] = p.feed * (1.f - u0) - uvv;
-        f[fs] = -(p.feed + p.kill) * u1 + uvv;
-      } break;
-      case OP_VORT:
-        f[0] = fmaf(in[0], in[2], in[1] * in[3]);
-        break;
-      case OP_PROJ3D: {  // velocity (in[3..5]) x curl (in[0..2])
-        const float w0 = in[0], w1 = in[1], w2 = in[2], v0 = in[3], v1 = in[4], v2 = in[5];
-        f[0] = v1 * w2 - v2 * w1;
-        f[fs] = v2 * w0 - v0 * w2;
-        f[2 * fs] = v0 * w1 - v1 * w0;
-      } break;
-      case OP_BZ: {
-        const float u0 = in[0], u1 = in[1], u2 = in[2];
-        const float u01 = u0 * u1;
-        f[0] = u0 + u1 - u01 - u0 * u0;
-        f[fs] = u2 - u1 - u01;
-        f[2 * fs] = u0 - u2;
-      } break;
-    }
+constexpr int kMaxNI = MAXC + MAXC * 3;  // derived fields of a program, at most
+
+template <int C, int D>
+__device__ __forceinline__ void pw_mc_noncons(const float (&in)[kMaxNI], float* f, int64_t fs) {
+#pragma unroll
+  for (int i = 0; i < C; ++i) {
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < D; ++j) s += in[j] * in[C + i * D + j];
+    f[i * fs] = s;
+  }
 }
+template <int C>
+__device__ __forceinline__ void pw_mc_cons(const float (&in)[kMaxNI], float* f, int64_t fs) {
+  int o = 0;
+#pragma unroll
+  for (int i = 0; i < C; ++i)
+#pragma unroll
+    for (int j = i; j < C; ++j) f[(o++) * fs] = in[i] * in[j];
+}
+template <int C, int D>
+__device__ __forceinline__ void pw_grad_norm(const float (&in)[kMaxNI], float* f, int64_t fs) {
+#pragma unroll
+  for (int c = 0; c < C; ++c) {
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < D; ++j) s += in[c * D + j] * in[c * D + j];
+    f[c * fs] = s;
+  }
+}
+#define EXGB_CD_DISPATCH(FN)                    \
+  switch (g.C * 4 + g.D) {                      \
+    case 5: FN<1, 1>(in, f, fs); break;         \
+    case 6: FN<1, 2>(in, f, fs); break;         \
+    case 7: FN<1, 3>(in, f, fs); break;         \
+    case 9: FN<2, 1>(in, f, fs); break;         \
+    case 10: FN<2, 2>(in, f, fs); break;        \
+    case 11: FN<2, 3>(in, f, fs); break;        \
+    case 13: FN<3, 1>(in, f, fs); break;        \
+    case 14: FN<3, 2>(in, f, fs); break;        \
+    default: FN<3, 3>(in, f, fs); break;        \
+  }
+
+// The NF products at one grid point from the NI physical values in[] (registers the caller loaded:
+// every index below is a compile-time constant, the channel and dimension counts being dispatched to
+// templates, so in[] never goes to local memory): field i written to f[i * fs].
+__device__ __forceinline__ void pointwise_point_reg(const Geo& g, const Prog& p, const float (&in)[kMaxNI], float* f,
+                                                    int64_t fs) {
+  switch (p.op) {
+    case OP_CONV_MC_CONS:
+      if (g.C == 1) pw_mc_cons<1>(in, f, fs);
+      else if (g.C == 2) pw_mc_cons<2>(in, f, fs);
+      else pw_mc_cons<3>(in, f, fs);
+      break;
+    case OP_CONV_MC_NONCONS:
+      EXGB_CD_DISPATCH(pw_mc_noncons)
+      break;
+    case OP_CONV_SC_CONS:
+      f[0] = in[0] * in[0];
+      break;
+    case OP_CONV_SC_NONCONS:
+      f[0] = in[0] * in[1];
+      break;
+    case OP_GRAD_NORM:
+      EXGB_CD_DISPATCH(pw_grad_norm)
+      break;
+    case OP_POLY:
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c) {
+        if (c >= g.C) break;
+        // sum_k c_k u^k with the powers accumulated as the reference does
+        const float u = in[c];
+        float pw = 1.f, acc = 0.f;
+        for (int i = 0; i < p.npoly; ++i) {
+          acc += p.poly[i] * pw;
+          pw *= u;
+        }
+        f[c * fs] = acc;
+      }
+      break;
+    case OP_GENERAL: {
+      float s = 0.f;
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        if (j < g.D) s += in[1 + j] * in[1 + j];
+      f[0] = in[0] * in[0];
+      f[fs] = s;
+    } break;
+    case OP_CAHN_HILLIARD:
+      f[0] = in[0] * in[0] * in[0];
+      break;
+    case OP_GRAY_SCOTT: {
+      const float u0 = in[0], u1 = in[1];
+      const float uvv = u0 * (u1 * u1);
+      f[0] = p.feed * (1.f - u0) - uvv;
+      f[fs] = -(p.feed + p.kill) * u1 + uvv;
+    } break;
+    case OP_VORT:
+      f[0] = fmaf(in[0], in[2], in[1] * in[3]);
+      break;
+    case OP_PROJ3D: {  // velocity (in[3..5]) x curl (in[0..2])
+      const float w0 = in[0], w1 = in[1], w2 = in[2], v0 = in[3], v1 = in[4], v2 = in[5];
+      f[0] = v1 * w2 - v2 * w1;
+      f[fs] = v2 * w0 - v0 * w2;
+      f[2 * fs] = v0 * w1 - v1 * w0;
+    } break;
+    case OP_BZ: {
+      const float u0 = in[0], u1 = in[1], u2 = in[2];
+      const float u01 = u0 * u1;
+      f[0] = u0 + u1 - u01 - u0 * u0;
+      f[fs] = u2 - u1 - u01;
+      f[2 * fs] = u0 - u2;
+    } break;
+  }
+}
+#undef EXGB_CD_DISPATCH
+
+// The NI physical values at v[i * vs] into registers (then pointwise_point_reg may write its products
+// over them in place).
+__device__ __forceinline__ void load_point(const float* v, int64_t vs, int NI, float (&in)[kMaxNI]) {
+#pragma unroll
+  for (int i = 0; i < kMaxNI; ++i) in[i] = i < NI ? v[i * vs] : 0.f;
+}
+
 
 // N^ of every channel at mode k from the NF forward spectra h[f * hs] (post-mask m, derivative
 // multipliers, scales); the Kolmogorov injection of the vorticity term included.

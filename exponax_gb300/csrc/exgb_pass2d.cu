@@ -137,9 +137,9 @@ __global__ void __launch_bounds__(256) pass2_kernel(const Args a) {
   __syncthreads();
   for (int e = threadIdx.x; e < TX * N; e += blockDim.x) {
     const int xx = e / N, y = e - xx * N;
-    float in[MAXC + MAXC * 3];
-    for (int f = 0; f < NI; ++f) in[f] = phys[((size_t)f * TX + xx) * N + y];
-    ndg::pointwise_point(a.g, a.p, in, prod + (size_t)xx * N + y, (int64_t)TX * N);
+    float in[ndg::kMaxNI];
+    ndg::load_point(phys + (size_t)xx * N + y, (int64_t)TX * N, NI, in);
+    ndg::pointwise_point_reg(a.g, a.p, in, prod + (size_t)xx * N + y, (int64_t)TX * N);
   }
   __syncthreads();
   // r2c: sequence j packs product rows 2j, 2j + 1 (row index q = f * TX + xx)
@@ -192,10 +192,14 @@ __global__ void __launch_bounds__(256) pass3_kernel(const Args a) {
     const int64_t r = (int64_t)ky * N + kx;  // column-major mode index
     if (a.stage < 0) {
       float2* o = a.nout + s * a.sstride + (int64_t)kx * a.M + ky;
-      for (int c = 0; c < C; ++c) o[c * a.plane] = nv[c];
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c)
+        if (c < C) o[c * a.plane] = nv[c];
       continue;
     }
-    for (int c = 0; c < C; ++c) {
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c) {  // compile-time channel indices keep nv in registers
+      if (c >= C) break;
       const int64_t ci = (a.P.lin_ch == 1 ? 0 : (int64_t)c * a.plane) + r;
       stage_upd_at(a.P, a.sb, s * a.sstride + c * a.plane + r, ci, a.stage, nv[c]);
     }
@@ -352,9 +356,9 @@ __global__ void __launch_bounds__(RegPass<N>::THREADS2, (N >= 512 ? 5 : 1)) pass
   for (int e = threadIdx.x; e < TX * N; e += blockDim.x) {
     const int xx = e / N, y = e - xx * N;
     float* base = reinterpret_cast<float*>(slots) + (size_t)(xx >> 1) * 2 * SL + (xx & 1) * N + y;
-    float in[MAXC + MAXC * 3];
-    for (int f = 0; f < NI; ++f) in[f] = base[f * fs];
-    ndg::pointwise_point(a.g, a.p, in, base, fs);
+    float in[ndg::kMaxNI];
+    ndg::load_point(base, fs, NI, in);
+    ndg::pointwise_point_reg(a.g, a.p, in, base, fs);
   }
   __syncthreads();
   // r2c: sequence j packs product rows 2j, 2j + 1, in place in slot j
@@ -418,10 +422,14 @@ __global__ void __launch_bounds__(RegPass<N>::THREADS) pass3_reg_kernel(const Ar
     const int64_t r = (int64_t)ky * N + kx;
     if (a.stage < 0) {
       float2* o = a.nout + s * a.sstride + (int64_t)kx * a.M + ky;
-      for (int c = 0; c < C; ++c) o[c * a.plane] = nv[c];
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c)
+        if (c < C) o[c * a.plane] = nv[c];
       continue;
     }
-    for (int c = 0; c < C; ++c) {
+#pragma unroll
+    for (int c = 0; c < MAXC; ++c) {  // compile-time channel indices keep nv in registers
+      if (c >= C) break;
       const int64_t ci = (a.P.lin_ch == 1 ? 0 : (int64_t)c * a.plane) + r;
       stage_upd_at(a.P, a.sb, s * a.sstride + c * a.plane + r, ci, a.stage, nv[c]);
     }

