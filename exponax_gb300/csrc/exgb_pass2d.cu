@@ -272,16 +272,42 @@ __global__ void __launch_bounds__(RegPass<N>::THREADS) pass1_reg_kernel(const Ar
   const int ty = min(TY, a.Kc - ky0);
   load_twl<N>(twl, a.tw);
   const float2* xs = a.xin + s * a.sstride;
-  for (int e = threadIdx.x; e < TY * N; e += blockDim.x) {
-    const int t = e / N, kx = e - t * N;
-    if (t < ty) {
+  // kU modes per thread at a time, their channel loads issued together
+  constexpr int kU = 4;
+  static_assert(MAXC == 3, "the channel accessor below picks among 3 registers");
+  const int C = a.g.C;
+  const int64_t fstride = (int64_t)TY * SL;
+  for (int e0 = threadIdx.x; e0 < TY * N; e0 += kU * (int)blockDim.x) {
+    float2 xv[kU][MAXC];
+    int kk[kU][3];
+    bool mk[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = e0 + u * (int)blockDim.x;
+      const int ee = e < TY * N ? e : e0;
+      const int t = ee / N, kx = ee - t * N;
       const int ky = ky0 + t;
-      const int k[3] = {sgn_of(kx, N), ky, 0};
-      const bool m = abs(k[0]) <= a.K && ky <= a.K;
-      ndg::derive_mode(a.g, a.p, k, m, xs + (int64_t)ky * N + kx, a.plane, buf + (size_t)t * SL + kx,
-                       (int64_t)TY * SL);
-    } else {
-      for (int f = 0; f < NI; ++f) buf[((size_t)f * TY + t) * SL + kx] = make_float2(0.f, 0.f);
+      kk[u][0] = sgn_of(kx, N);
+      kk[u][1] = ky;
+      kk[u][2] = 0;
+      mk[u] = t < ty && abs(kk[u][0]) <= a.K && ky <= a.K;
+#pragma unroll
+      for (int c = 0; c < MAXC; ++c)
+        xv[u][c] = (mk[u] && c < C) ? xs[(int64_t)ky * N + kx + (int64_t)c * a.plane] : make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = e0 + u * (int)blockDim.x;
+      if (e >= TY * N) break;
+      const int t = e / N, kx = e - t * N;
+      float2* o = buf + (size_t)t * SL + kx;
+      if (t < ty) {
+        ndg::derive_mode_xo(
+            a.g, a.p, kk[u], mk[u], [&](int c) { return c == 0 ? xv[u][0] : (c == 1 ? xv[u][1] : xv[u][2]); },
+            [&](int i, float2 v) { o[i * fstride] = v; });
+      } else {
+        for (int f = 0; f < NI; ++f) o[f * fstride] = make_float2(0.f, 0.f);
+      }
     }
   }
   __syncthreads();
