@@ -201,6 +201,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS2) pass2_3d_kernel(const Args a
   load_twl<N>(twl, a.tw);
   // element (f, kz) of line (x, y) in W / Hq: ((s NI + f) Kc + kz) pl + x N + y
   const float2* W = a.W + s * (int64_t)NI * Kc * a.pl + (int64_t)x * N + y0;
+#pragma unroll 4
   for (int e = threadIdx.x; e < NI * Kc * TY; e += blockDim.x) {
     const int yy = e % TY, r = e / TY;  // r = f Kc + kz
     wt[e] = W[(int64_t)r * a.pl + yy];
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass3_3d_kernel(const Args a)
 
 // ---- pass 3b: post-mask, multipliers and the ETDRK stage update of every mode of the Kc planes
 // (Hq was written by pass 3a just before and is read from L2)
-__global__ void __launch_bounds__(256) combine_planes_kernel(const Args a, int64_t n) {
+__global__ void __launch_bounds__(256, 5) combine_planes_kernel(const Args a, int64_t n) {
   const int N = a.N, C = a.g.C, NF = a.p.NF;
   const int64_t per = a.Kc * a.pl;
   const int64_t total = n * per;
