@@ -82,12 +82,15 @@ __global__ void combine_kernel(PlanDev P, Geo g, Prog p, int64_t cb, const float
         if (c < g.C) nout[base + c * g.per] = nv[c];
       continue;
     }
+    // every channel's stage loads in flight together (compile-time channel indices keep nv in registers)
+    int64_t so[MAXC], co[MAXC];
 #pragma unroll
-    for (int c = 0; c < MAXC; ++c) {  // compile-time channel indices keep nv in registers
-      if (c >= g.C) break;
-      const int64_t ci = (P.lin_ch == 1 ? 0 : (int64_t)c * g.per) + r;
-      stage_upd_at(P, sb, base + c * g.per, ci, stage, nv[c]);
+    for (int c = 0; c < MAXC; ++c) {
+      const int cc = c < g.C ? c : 0;
+      so[c] = base + cc * g.per;
+      co[c] = (P.lin_ch == 1 ? 0 : (int64_t)cc * g.per) + r;
     }
+    stage_upd_channels<MAXC>(P, sb, g.C, so, co, stage, nv);
   }
 }
 

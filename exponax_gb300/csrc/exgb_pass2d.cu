@@ -197,12 +197,15 @@ __global__ void __launch_bounds__(256) pass3_kernel(const Args a) {
         if (c < C) o[c * a.plane] = nv[c];
       continue;
     }
+    // every channel's stage loads in flight together (compile-time channel indices keep nv in registers)
+    int64_t so[MAXC], co[MAXC];
 #pragma unroll
-    for (int c = 0; c < MAXC; ++c) {  // compile-time channel indices keep nv in registers
-      if (c >= C) break;
-      const int64_t ci = (a.P.lin_ch == 1 ? 0 : (int64_t)c * a.plane) + r;
-      stage_upd_at(a.P, a.sb, s * a.sstride + c * a.plane + r, ci, a.stage, nv[c]);
+    for (int c = 0; c < MAXC; ++c) {
+      const int cc = c < C ? c : 0;
+      so[c] = s * a.sstride + cc * a.plane + r;
+      co[c] = (a.P.lin_ch == 1 ? 0 : (int64_t)cc * a.plane) + r;
     }
+    stage_upd_channels<MAXC>(a.P, a.sb, C, so, co, a.stage, nv);
   }
 }
 
@@ -453,12 +456,15 @@ __global__ void __launch_bounds__(RegPass<N>::THREADS) pass3_reg_kernel(const Ar
         if (c < C) o[c * a.plane] = nv[c];
       continue;
     }
+    // every channel's stage loads in flight together (compile-time channel indices keep nv in registers)
+    int64_t so[MAXC], co[MAXC];
 #pragma unroll
-    for (int c = 0; c < MAXC; ++c) {  // compile-time channel indices keep nv in registers
-      if (c >= C) break;
-      const int64_t ci = (a.P.lin_ch == 1 ? 0 : (int64_t)c * a.plane) + r;
-      stage_upd_at(a.P, a.sb, s * a.sstride + c * a.plane + r, ci, a.stage, nv[c]);
+    for (int c = 0; c < MAXC; ++c) {
+      const int cc = c < C ? c : 0;
+      so[c] = s * a.sstride + cc * a.plane + r;
+      co[c] = (a.P.lin_ch == 1 ? 0 : (int64_t)cc * a.plane) + r;
     }
+    stage_upd_channels<MAXC>(a.P, a.sb, C, so, co, a.stage, nv);
   }
 }
 

@@ -86,13 +86,14 @@ __device__ __forceinline__ float2 stage_upd(const PlanDev& P, const StageBufs& b
   return stage_upd_at(P, b, o, o, stage, nv);
 }
 
-// R modes at once, each as stage_upd (o[j] indexes the state buffers and the coefficient tables;
-// modes with ok[j] false are read at a valid index and not written).  All global loads of the R
+// R modes at once, each as stage_upd_at (o[j] indexes the state buffers, co[j] the coefficient
+// tables; modes with ok[j] false are read at a valid index and not written).  All global loads of the R
 // updates are issued before the first store, so their latencies overlap: in a loop of single updates
 // the compiler must keep each mode's loads behind the previous mode's stores, which may alias them.
 template <int R>
-__device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs& b, const int64_t (&o)[R],
-                                               const bool (&ok)[R], int stage, float2 (&nv)[R]) {
+__device__ __forceinline__ void stage_upd_many_at(const PlanDev& P, const StageBufs& b, const int64_t (&o)[R],
+                                                  const int64_t (&co)[R], const bool (&ok)[R], int stage,
+                                                  float2 (&nv)[R]) {
   if (P.order == 1 || (P.order == 2 && stage == 0) || (P.order == 3 && stage == 0) ||
       (P.order == 4 && stage <= 1)) {
     // s = E' U + c0 nv with E' = E (orders 1, 2) or E_{h/2} (orders 3, 4)
@@ -101,9 +102,9 @@ __device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs
     float k0[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      e[j] = __ldg(Ep + o[j]);
+      e[j] = __ldg(Ep + co[j]);
       u[j] = b.U[o[j]];
-      k0[j] = __ldg(P.c[0] + o[j]);
+      k0[j] = __ldg(P.c[0] + co[j]);
     }
     float2* Nd = (P.order == 1) ? nullptr : (P.order == 4 && stage == 1) ? b.N1 : b.N0;
     float2* Sd = (P.order == 1) ? b.U : (P.order == 4 && stage == 0) ? b.S1 : b.S;
@@ -123,7 +124,7 @@ __device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs
     for (int j = 0; j < R; ++j) {
       sv[j] = b.S[o[j]];
       n0[j] = b.N0[o[j]];
-      k1[j] = __ldg(P.c[1] + o[j]);
+      k1[j] = __ldg(P.c[1] + co[j]);
     }
 #pragma unroll
     for (int j = 0; j < R; ++j) {
@@ -136,10 +137,10 @@ __device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs
     float k1[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      e[j] = __ldg(P.E + o[j]);
+      e[j] = __ldg(P.E + co[j]);
       u[j] = b.U[o[j]];
       n0[j] = b.N0[o[j]];
-      k1[j] = __ldg(P.c[1] + o[j]);
+      k1[j] = __ldg(P.c[1] + co[j]);
     }
 #pragma unroll
     for (int j = 0; j < R; ++j) {
@@ -156,13 +157,13 @@ __device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs
     float k2[R], k3[R], k4[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      e[j] = __ldg(P.E + o[j]);
+      e[j] = __ldg(P.E + co[j]);
       u[j] = b.U[o[j]];
       n0[j] = b.N0[o[j]];
       n1[j] = b.N1[o[j]];
-      k2[j] = __ldg(P.c[2] + o[j]);
-      k3[j] = __ldg(P.c[3] + o[j]);
-      k4[j] = __ldg(P.c[4] + o[j]);
+      k2[j] = __ldg(P.c[2] + co[j]);
+      k3[j] = __ldg(P.c[3] + co[j]);
+      k4[j] = __ldg(P.c[4] + co[j]);
     }
 #pragma unroll
     for (int j = 0; j < R; ++j) {
@@ -178,10 +179,10 @@ __device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs
     float k0[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      e[j] = __ldg(P.Eh + o[j]);
+      e[j] = __ldg(P.Eh + co[j]);
       s1[j] = b.S1[o[j]];
       n0[j] = b.N0[o[j]];
-      k0[j] = __ldg(P.c[0] + o[j]);
+      k0[j] = __ldg(P.c[0] + co[j]);
     }
 #pragma unroll
     for (int j = 0; j < R; ++j) {
@@ -198,14 +199,14 @@ __device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs
     float k3[R], k4[R], k5[R];
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-      e[j] = __ldg(P.E + o[j]);
+      e[j] = __ldg(P.E + co[j]);
       u[j] = b.U[o[j]];
       n0[j] = b.N0[o[j]];
       n1[j] = b.N1[o[j]];
       n2[j] = b.N2[o[j]];
-      k3[j] = __ldg(P.c[3] + o[j]);
-      k4[j] = __ldg(P.c[4] + o[j]);
-      k5[j] = __ldg(P.c[5] + o[j]);
+      k3[j] = __ldg(P.c[3] + co[j]);
+      k4[j] = __ldg(P.c[4] + co[j]);
+      k5[j] = __ldg(P.c[5] + co[j]);
     }
 #pragma unroll
     for (int j = 0; j < R; ++j) {
@@ -216,6 +217,28 @@ __device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs
       if (ok[j]) b.U[o[j]] = r;
       nv[j] = r;
     }
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void stage_upd_many(const PlanDev& P, const StageBufs& b, const int64_t (&o)[R],
+                                               const bool (&ok)[R], int stage, float2 (&nv)[R]) {
+  stage_upd_many_at<R>(P, b, o, o, ok, stage, nv);
+}
+
+// The stage update of one mode's C <= MC channels (state index so[c], coefficient index co[c]; entries
+// c >= C must hold valid indices): one update for a single channel, otherwise every channel's loads
+// issued together.
+template <int MC>
+__device__ __forceinline__ void stage_upd_channels(const PlanDev& P, const StageBufs& b, int C, const int64_t (&so)[MC],
+                                                   const int64_t (&co)[MC], int stage, float2 (&nv)[MC]) {
+  if (C == 1) {
+    nv[0] = stage_upd_at(P, b, so[0], co[0], stage, nv[0]);
+  } else {
+    bool ok[MC];
+#pragma unroll
+    for (int c = 0; c < MC; ++c) ok[c] = c < C;
+    stage_upd_many_at<MC>(P, b, so, co, ok, stage, nv);
   }
 }
 
