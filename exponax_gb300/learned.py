@@ -13,7 +13,7 @@ not finite.
 
 No counterpart in the reference (its closest precedent is the 1D CNN
 emulator notebook); the plain method (exponax_gb300.stepper) generates the
-training data and judges the error.
+training data and measures the error.
 """
 
 from __future__ import annotations
