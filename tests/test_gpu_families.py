@@ -93,6 +93,19 @@ def test_nonlinear_fun_matches_oracle(kind, D, N):
     assert rel(got, want) < 2e-5, (kind, D, N)
 
 
+@pytest.mark.parametrize("kind", ND_KINDS)
+@pytest.mark.parametrize("D,N", [(2, 64), (3, 32)])
+def test_nonlinear_fun_three_pass_register_sizes(kind, D, N):
+    """Every staged nonlinearity at the sizes the register-FFT three-pass kernels take (2D 64^2, 3D 32^3):
+    their derive (channel values loaded ahead), products (register inputs per channel / dimension count)
+    and combine against the oracle, two samples at once."""
+    fm, fo, C = _nl_pair(kind, D, N)
+    uh = np.stack([spectrum(D, N, C, key=N + D + b) for b in range(2)])
+    got = host(ex.vmap(fm)(cu(uh)))
+    for b in range(2):
+        assert rel(got[b], fo(uh[b])) < 2e-5, (kind, D, N, b)
+
+
 @pytest.mark.parametrize("kind", ["cahn_hilliard", "gray_scott"])
 @pytest.mark.parametrize("N", [64, 100])
 def test_reaction_nonlinear_fun_1d(kind, N):
