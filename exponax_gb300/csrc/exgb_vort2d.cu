@@ -74,7 +74,7 @@ __device__ __forceinline__ int sgn_k(int i) {
 }
 
 template <int N, int THREADS>
-__global__ void __launch_bounds__(THREADS, 1) vort2d_kernel(const ArgsV2 a) {
+__global__ void __launch_bounds__(THREADS, (N == 64 ? 2 : 1)) vort2d_kernel(const ArgsV2 a) {
   using Lay = V2Layout<N, THREADS>;
   constexpr int E = Lay::E, T = Lay::T, NG = Lay::NG, TS = Lay::TS;
   constexpr int M = N / 2 + 1;
