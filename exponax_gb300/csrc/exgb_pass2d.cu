@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(RegPass<N>::THREADS) pass1_reg_kernel(const Ar
 // rows 2j, 2j + 1 runs in slot j again (rows to registers, slot as tile, spectrum back to the slot).
 // (at N = 512 capped to 102 registers for 5 CTAs per SM: 96 without spills, 128 uncapped)
 template <int N>
-__global__ void __launch_bounds__(RegPass<N>::THREADS2, (N >= 512 ? 5 : 1)) pass2_reg_kernel(const Args a) {
+__global__ void __launch_bounds__(RegPass<N>::THREADS2, (N >= 512 ? 5 : 3)) pass2_reg_kernel(const Args a) {
   using R = RegPass<N>;
   constexpr int E = R::E, T = R::T, M = N / 2 + 1, SL = R::SLOT;
   extern __shared__ __align__(16) float2 smr2[];
