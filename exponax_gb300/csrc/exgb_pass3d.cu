@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass1_3d_kernel(const Args a)
 // physical lines, then (products overwritten in place) the pair's r2c transform and spectrum; the
 // spectra leave as runs of TY consecutive y again.
 template <int N>
-__global__ void __launch_bounds__(Cfg<N>::THREADS2) pass2_3d_kernel(const Args a) {
+__global__ void __launch_bounds__(Cfg<N>::THREADS2, (N == 32 ? 16 : N == 64 ? 8 : 4)) pass2_3d_kernel(const Args a) {
   using R = Cfg<N>;
   constexpr int E = R::E, T = R::T, M = N / 2 + 1, SL = R::SLOT;
   extern __shared__ __align__(16) float2 sp2[];
