@@ -231,14 +231,137 @@ struct ProductOut {
   __device__ __forceinline__ Ref operator()(int i, int x) const { return Ref{P, res + i * P->N + x}; }
 };
 
+// ---- one-warp register transforms for the latency variant (one item per SM): N = A * B with
+// A = A1 * A2 <= 32 and B <= 32.  Lane l < A loads x[l + A j] (j < B), takes a length-B DFT in
+// registers and the twiddle w_N^(l k1); a transpose through the output buffer (__syncwarp only);
+// lane k1 < B then takes a length-A DFT over l in registers and writes X[k1 + B k2].  A whole
+// transform is one barrier phase instead of one per radix pass.
+
+// length R1 * R2 DFT in registers, in place: input x[n] in v[n], n = R2 n1 + n2; output X[k1 + R1 k2]
+// in v[R2 k1 + k2].  The inner twiddles w_R^(n2 k1) = tw[tstep n2 k1] come from the N-point table
+// (tstep = N / R).
+template <int R1, int R2, bool INV>
+__device__ __forceinline__ void lane_dft(float2 (&v)[R1 * R2], const float2* __restrict__ tw, int tstep) {
+  if constexpr (R2 == 1) {
+    dftR<R1, INV>(v);
+  } else {
+#pragma unroll
+    for (int n2 = 0; n2 < R2; ++n2) {
+      float2 t[R1];
+#pragma unroll
+      for (int n1 = 0; n1 < R1; ++n1) t[n1] = v[R2 * n1 + n2];
+      dftR<R1, INV>(t);
+#pragma unroll
+      for (int k1 = 0; k1 < R1; ++k1) {
+        float2 z = t[k1];
+        if (n2 > 0 && k1 > 0) {
+          float2 w = tw[tstep * n2 * k1];
+          if (INV) w.y = -w.y;
+          z = cmul(z, w);
+        }
+        v[R2 * k1 + n2] = z;
+      }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < R1; ++k1) {
+      float2 t[R2];
+#pragma unroll
+      for (int n2 = 0; n2 < R2; ++n2) t[n2] = v[R2 * k1 + n2];
+      dftR<R2, INV>(t);
+#pragma unroll
+      for (int k2 = 0; k2 < R2; ++k2) v[R2 * k1 + k2] = t[k2];
+    }
+  }
+}
+
+// One length-N transform by one warp, in -> out (in == out allowed); `out` also holds the transpose
+// tile (N = A * B entries, row k1 rotated by k1 against bank conflicts).  No 1/N scaling.
+template <int A1, int A2, int B, bool INV>
+__device__ __forceinline__ void warp_fft(const float2* in, float2* out, const float2* __restrict__ tw, int lane) {
+  constexpr int A = A1 * A2, N = A * B;
+  static_assert(A <= 32 && B <= 32 && B <= A, "one warp, B <= A");
+  float2 v[B];
+  if (lane < A) {
+#pragma unroll
+    for (int j = 0; j < B; ++j) v[j] = in[lane + A * j];
+    dftR<B, INV>(v);
+#pragma unroll
+    for (int k1 = 1; k1 < B; ++k1) {
+      float2 w = tw[lane * k1];
+      if (INV) w.y = -w.y;
+      v[k1] = cmul(v[k1], w);
+    }
+  }
+  __syncwarp();
+  if (lane < A) {
+#pragma unroll
+    for (int k1 = 0; k1 < B; ++k1) {
+      const int c = lane + k1;
+      out[k1 * A + (c < A ? c : c - A)] = v[k1];
+    }
+  }
+  __syncwarp();
+  float2 u[A];
+  if (lane < B) {
+#pragma unroll
+    for (int l = 0; l < A; ++l) {
+      const int c = l + lane;
+      u[l] = out[lane * A + (c < A ? c : c - A)];
+    }
+  }
+  __syncwarp();
+  if (lane < B) {
+    lane_dft<A1, A2, INV>(u, tw, N / A);
+#pragma unroll
+    for (int q1 = 0; q1 < A1; ++q1)
+#pragma unroll
+      for (int q2 = 0; q2 < A2; ++q2) out[lane + B * (q1 + A1 * q2)] = u[A2 * q1 + q2];
+  }
+}
+
+// Sizes with a one-warp transform (WN = N = A1 * A2 * B); WN = 0: block Stockham passes.  Each size is
+// a kernel instantiation of its own: one function holding several transforms' registers spills.
+template <int WN>
+struct WarpShape;
+template <>
+struct WarpShape<64> {
+  static constexpr int A1 = 8, A2 = 1, B = 8;
+};
+template <>
+struct WarpShape<128> {
+  static constexpr int A1 = 4, A2 = 4, B = 8;
+};
+template <>
+struct WarpShape<200> {
+  static constexpr int A1 = 5, A2 = 5, B = 8;
+};
+template <>
+struct WarpShape<256> {
+  static constexpr int A1 = 4, A2 = 8, B = 8;
+};
+
+// m length-WN transforms in -> out (stride WN), one warp per sequence
+template <int WN, bool INV>
+__device__ __forceinline__ void warp_fft_many(const float2* in, float2* out, int m, const float2* __restrict__ tw,
+                                              int tid, int nthr) {
+  using S = WarpShape<WN>;
+  const int lane = tid & 31;
+  for (int i = tid >> 5; i < m; i += nthr >> 5) {
+    warp_fft<S::A1, S::A2, S::B, INV>(in + (size_t)i * WN, out + (size_t)i * WN, tw, lane);
+    __syncwarp();
+  }
+}
+
 // One nonlinear evaluation of the m states X followed by the stage update
 // (stage >= 0) or a plain store of N^ into X_out (stage < 0).
 // fuse: pack fused into the first inverse pass and the products into the last (fewer barrier phases;
 // the throughput choice when several work items share an SM).  Otherwise each elementwise step is a
 // phase of its own spread over all threads (the latency choice for one small item per SM).
-template <bool fuse, class Sync = BlockSync>
+// WN != 0 (latency variant only, N == WN): each transform is one warp_fft phase.
+template <bool fuse, int WN = 0, class Sync = BlockSync>
 __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m, int stage, float2* X_out,
                         int tid, int nthr, const Sync& sync = Sync{}) {
+  static_assert(WN == 0 || !fuse, "warp transforms belong to the latency variant");
   const int N = P.N, M = P.M;
   const bool zmf = P.gamma != 0.f && P.zero_mode_fix;
   float2 *res, *other;
@@ -252,7 +375,12 @@ __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m,
     sync();
     res = (P.fft.npass & 1) ? b.w1 : b.w0;
     other = (P.fft.npass & 1) ? b.w0 : b.w1;
-    block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, b.tw, tid, nthr, sync);
+    if constexpr (WN != 0) {
+      warp_fft_many<WN, true>(b.w0, res, m, b.tw, tid, nthr);
+      sync();
+    } else {
+      block_fft<true>(P.fft, b.w0, b.w1, LinMap{res, N}, m, b.tw, tid, nthr, sync);
+    }
     nl_products(P, res, (float*)other, m, tid, nthr);
     sync();
     if (zmf) {
@@ -261,8 +389,15 @@ __device__ void nl_eval(const PlanDev& P, const Bufs& b, const float2* X, int m,
     }
   }
   // forward: input in res, passes ping-pong other <-> res
-  float2* fres = io_result_buf(P.fft, other, res);
-  block_fft_io<false>(P.fft, LinMap{res, N}, other, res, LinMap{fres, N}, m, b.tw, tid, nthr, sync);
+  float2* fres;
+  if constexpr (WN != 0) {
+    fres = res;
+    warp_fft_many<WN, false>(res, fres, m, b.tw, tid, nthr);
+    sync();
+  } else {
+    fres = io_result_buf(P.fft, other, res);
+    block_fft_io<false>(P.fft, LinMap{res, N}, other, res, LinMap{fres, N}, m, b.tw, tid, nthr, sync);
+  }
   for (int t = tid; t < m * M; t += nthr) {
     const int i = t / M, k = t - i * M;
     float2 nv = make_float2(0.f, 0.f);
@@ -352,7 +487,7 @@ __device__ void emit_phys(const PlanDev& P, const Bufs& b, int m, float* out, in
 // that synchronises with `sync` (the whole block).  `sm`: the
 // group's dynamic shared memory of smem_bytes; `gslot`: its global slot for state buffers that do not
 // fit there (NULL when they always fit).
-template <bool FUSE, class Sync>
+template <bool FUSE, int WN, class Sync>
 __device__ void run_item(const Item1D& item, const PlanDev& P, float2* sm, int smem_bytes, float* sums,
                          float2* gslot, int nsteps, int mode, int project, int include_init, int tid, int nthr,
                          const Sync& sync) {
@@ -450,7 +585,7 @@ __device__ void run_item(const Item1D& item, const PlanDev& P, float2* sm, int s
     } else {
       for (int s = 0; s < nstages; ++s) {
         const float2* X = (s == 0) ? b.U : (P.order == 4 && s == 1) ? b.S1 : b.S;
-        nl_eval<FUSE>(P, b, X, m, s, nullptr, tid, nthr, sync);
+        nl_eval<FUSE, WN>(P, b, X, m, s, nullptr, tid, nthr, sync);
       }
     }
     if (project) {
@@ -486,8 +621,10 @@ __device__ void run_item(const Item1D& item, const PlanDev& P, float2* sm, int s
   }
 }
 
-template <bool FUSE>
-__global__ void __launch_bounds__(256, 3) etdrk1d_kernel(const Item1D* __restrict__ items, int n_items,
+// FUSE: the throughput variant (more items than SMs, 3 CTAs per SM); otherwise one CTA per SM, whose
+// transforms are warp transforms when WN = N, block passes when WN = 0
+template <bool FUSE, int WN>
+__global__ void __launch_bounds__(256, FUSE ? 3 : 1) etdrk1d_kernel(const Item1D* __restrict__ items, int n_items,
                                                       int* __restrict__ head, int nsteps, int mode, int project,
                                                       int include_init, int smem_bytes, float2* gstate,
                                                       int64_t gstate_stride) {
@@ -504,7 +641,7 @@ __global__ void __launch_bounds__(256, 3) etdrk1d_kernel(const Item1D* __restric
     const Item1D item = items[it];
     copy_plan(&Ps, item.plan, tid, nthr);
     __syncthreads();
-    run_item<FUSE>(item, Ps, sm, smem_bytes, s_sums, gstate ? gstate + (int64_t)blockIdx.x * gstate_stride : nullptr,
+    run_item<FUSE, WN>(item, Ps, sm, smem_bytes, s_sums, gstate ? gstate + (int64_t)blockIdx.x * gstate_stride : nullptr,
                    nsteps, mode, project, include_init, tid, nthr, BlockSync{});
     __syncthreads();
   }
@@ -584,9 +721,27 @@ static int choose_m(const PlanDev& P, int64_t batch, int sm_count, bool nonlin_o
   return m;
 }
 
+using Kern1D = void (*)(const Item1D*, int, int*, int, int, int, int, int, float2*, int64_t);
+
+// The kernel of a launch: the fused variant when there are more work items than SMs (throughput-
+// bound, the fused elementwise steps pay); otherwise each SM runs one item at latency with separate
+// all-thread elementwise phases, and with one-warp transforms when every item's N (n_uniform; 0 if
+// the items differ) has one (one CTA of 256 threads, 3.79 -> 2.12 ms for 16 instances of N = 200 x
+// 500 ETDRK2 steps).
+static Kern1D kernel_1d(bool fuse, int n_uniform) {
+  if (fuse) return etdrk1d_kernel<true, 0>;
+  switch (n_uniform) {
+    case 64: return etdrk1d_kernel<false, 64>;
+    case 128: return etdrk1d_kernel<false, 128>;
+    case 200: return etdrk1d_kernel<false, 200>;
+    case 256: return etdrk1d_kernel<false, 256>;
+    default: return etdrk1d_kernel<false, 0>;
+  }
+}
+
 static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStream_t st, int nsteps, int mode,
-                        int project, int include_init, int sm_count, bool nonlin_only, int threads = 256,
-                        size_t gstate_bytes = 0) {
+                        int project, int include_init, int sm_count, bool nonlin_only, int n_uniform,
+                        int threads = 256, size_t gstate_bytes = 0) {
   if (items.empty()) return EXGB_OK;
   {
     // the item list below is copied from host memory that is gone when a captured graph replays
@@ -612,10 +767,7 @@ static int launch_items(const std::vector<Item1D>& items, size_t smem, cudaStrea
     EXGB_CUDA(cudaFuncSetAttribute(nonlin1d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     nonlin1d_kernel<<<(unsigned)items.size(), 256, smem, st>>>((const Item1D*)ws, (int)items.size());
   } else {
-    // more work items than SMs: throughput-bound, the fused elementwise steps pay; otherwise each SM
-    // runs one item at latency and the separate all-thread phases are shorter
-    const bool fuse = (int64_t)items.size() > (int64_t)sm_count;
-    auto kern = fuse ? etdrk1d_kernel<true> : etdrk1d_kernel<false>;
+    const Kern1D kern = kernel_1d((int64_t)items.size() > (int64_t)sm_count, n_uniform);
     EXGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;
     EXGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
@@ -700,7 +852,7 @@ int etdrk1d_run(const exgb_plan* plan, cudaStream_t st, const float* u0_phys, co
     if (smem + tw <= kQueueSmemCap) smem += tw;
   }
   const int rc = launch_items(items, smem, st, nsteps, mode, project, include_init, plan->sm_count, nonlinear_only,
-                              threads, gstate_bytes);
+                              P.N, threads, gstate_bytes);
   if (rc || mode != MODE_TRAJ_HAT) return rc;
   const int rc2 = irfftn_impl(st, 1, P.N, batch * T, htraj, out_phys);
   if (rc2) return rc2;
@@ -719,7 +871,8 @@ namespace exgb {
 // Groups consecutive instances of the same plan with evenly strided buffers
 // into items of up to m instances and sorts the items longest first.
 static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps, int include_init,
-                       std::vector<Item1D>& sorted, size_t& smem, int& sm_count, size_t& gstate_bytes) {
+                       std::vector<Item1D>& sorted, size_t& smem, int& sm_count, size_t& gstate_bytes,
+                       int& n_uniform) {
   if (n_items < 0 || (n_items > 0 && !items)) return fail(EXGB_EINVAL, "bad work item list");
   if (nsteps < 0) return fail(EXGB_EINVAL, "nsteps must be >= 0");
   const int T = nsteps + (include_init ? 1 : 0);
@@ -729,6 +882,7 @@ static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps,
   gstate_bytes = 0;
   size_t full_max = 0;
   sm_count = 0;
+  n_uniform = -1;
   for (int64_t i = 0; i < n_items;) {
     const exgb_plan* p = items[i].plan;
     if (!p || !items[i].u0 || !items[i].traj) return fail(EXGB_EINVAL, "work item with NULL plan or buffer");
@@ -737,6 +891,7 @@ static int build_queue(const exgb_work_item* items, int64_t n_items, int nsteps,
                   "the work queue runs 1D single-channel plans of N = 2^a 3^b 5^c that fit in one CTA");
     sm_count = p->sm_count;
     const int N = p->dev.N;
+    n_uniform = (n_uniform == -1 || n_uniform == N) ? N : 0;
     const int mmax = std::min(64, std::max(1, 2048 / N));  // 2048 / N measured best (1024: -8 %, 4096: -22 %)
     int m = 1;
     while (m < mmax && i + m < n_items && items[i + m].plan == p &&
@@ -790,6 +945,7 @@ struct exgb_queue {
   int sm_count = 1;
   int nsteps = 0;
   int include_init = 0;
+  int n_uniform = 0;  // every item's N, or 0 if they differ (kernel_1d)
 };
 
 extern "C" int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, int32_t nsteps,
@@ -797,11 +953,11 @@ extern "C" int exgb_queue_rollout(const exgb_work_item* items, int64_t n_items, 
   if (n_items == 0) return EXGB_OK;
   std::vector<Item1D> sorted;
   size_t smem = 0, gstate_bytes = 0;
-  int sm_count = 0;
-  const int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count, gstate_bytes);
+  int sm_count = 0, n_uniform = 0;
+  const int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count, gstate_bytes, n_uniform);
   if (rc) return rc;
-  return launch_items(sorted, smem, (cudaStream_t)stream, nsteps, MODE_TRAJ, 1, include_init, sm_count, false, 256,
-                      gstate_bytes);
+  return launch_items(sorted, smem, (cudaStream_t)stream, nsteps, MODE_TRAJ, 1, include_init, sm_count, false,
+                      n_uniform, 256, gstate_bytes);
 }
 
 extern "C" int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, int32_t nsteps, int32_t include_init,
@@ -811,8 +967,8 @@ extern "C" int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, 
   if (n_items < 1) return fail(EXGB_EINVAL, "empty work item list");
   std::vector<Item1D> sorted;
   size_t smem = 0, gstate_bytes = 0;
-  int sm_count = 0;
-  int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count, gstate_bytes);
+  int sm_count = 0, n_uniform = 0;
+  int rc = build_queue(items, n_items, nsteps, include_init, sorted, smem, sm_count, gstate_bytes, n_uniform);
   if (rc) return rc;
   exgb_queue* q = new exgb_queue();
   q->n_items = (int)sorted.size();
@@ -821,8 +977,8 @@ extern "C" int exgb_queue_prepare(const exgb_work_item* items, int64_t n_items, 
   q->nsteps = nsteps;
   q->include_init = include_init ? 1 : 0;
   q->sm_count = sm_count;
-  // the fused kernel variant when the queue holds more items than there are SMs (see launch_items)
-  auto kern = q->n_items > q->sm_count ? etdrk1d_kernel<true> : etdrk1d_kernel<false>;
+  q->n_uniform = n_uniform;
+  const Kern1D kern = kernel_1d(q->n_items > q->sm_count, q->n_uniform);
   cudaError_t e;
   if ((e = cudaMalloc(&q->d_items, sizeof(Item1D) * sorted.size())) != cudaSuccess ||
       (e = cudaMalloc(&q->d_head, sizeof(int))) != cudaSuccess ||
@@ -847,7 +1003,7 @@ extern "C" int exgb_queue_launch(exgb_queue* q, void* stream) {
   if (!q) return fail(EXGB_EINVAL, "NULL queue");
   cudaStream_t st = (cudaStream_t)stream;
   EXGB_CUDA(cudaMemsetAsync(q->d_head, 0, sizeof(int), st));
-  auto kern = q->n_items > q->sm_count ? etdrk1d_kernel<true> : etdrk1d_kernel<false>;
+  const Kern1D kern = kernel_1d(q->n_items > q->sm_count, q->n_uniform);
   kern<<<q->grid, 256, q->smem, st>>>(q->d_items, q->n_items, q->d_head, q->nsteps, MODE_TRAJ, 1, q->include_init,
                                       (int)q->smem, q->d_gstate, (int64_t)(q->gstate_bytes / sizeof(float2)));
   EXGB_CUDA(cudaGetLastError());
