@@ -89,7 +89,7 @@ def test_uniform_queue_items_with_several_instances():
     sm = ex.stepper.Burgers(1, 1.0, 128, 1e-3, diffusivity=0.01)
     so = o.Burgers(1, 1.0, 128, 1e-3, diffusivity=0.01)
     B, n, N = 40, 20, 128
-    u0 = np.stack([_ic(N, k) for k in range(B)])[:, None, :]  # (B, 1, N), contiguous per instance
+    u0 = np.stack([_ic(N, k) for k in range(B)])  # (B, 1, N), contiguous per instance
     u0d = cu(u0)
     tr = torch.empty((B, n + 1, 1, N), dtype=torch.float32, device="cuda")
     items = [_lib.WorkItem(sm.plan.handle.value, u0d[b].data_ptr(), tr[b].data_ptr()) for b in range(B)]
