@@ -90,39 +90,53 @@ __device__ __forceinline__ unsigned group_mask() {
   return (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (lane & ~(T - 1)));
 }
 
-// column transforms of a plane in shared memory (rows kx, row stride PS), in place
-template <int N, bool INV>
-__device__ __forceinline__ void plane_cols_fft(float2* plane, float2* tiles, const float2* twl) {
+// Transforms of the lines of a plane in shared memory (rows kx, row stride PS), in place: ROWS along
+// the second index (line r at plane[r PS + x]), otherwise along the first (line c at plane[x PS + c]).
+// K >= 0 takes only the lines with |signed index| <= K (the others are zero, or their outputs are not
+// needed); K < 0 takes all N.  When the plane has at least two lines per transform group, a group
+// takes two lines at once (group_fft_x2), so that the lines of a plane need half the rounds.
+template <int N, bool INV, bool ROWS>
+__device__ __forceinline__ void plane_fft(float2* plane, float2* tiles, const float2* twl, int K) {
   using R = Cfg<N>;
+  constexpr bool kPair = N >= 2 * R::NG;
   const int gi = threadIdx.x / R::T, l = threadIdx.x % R::T;
   const unsigned gmask = group_mask<N>();
   float2* tile = tiles + (size_t)gi * R::TS;
-  for (int c = gi; c < N; c += R::NG) {
-    float2* col = plane + c;
-    float2 v[R::E];
+  const int nl = (K >= 0 && 2 * K + 1 < N) ? 2 * K + 1 : N;
+  auto line = [&](int q) { return q <= (nl - 1) / 2 || nl == N ? q : q + (N - nl); };
+  auto at = [&](int ln, int j) -> float2& {
+    return ROWS ? plane[(size_t)ln * R::PS + l + R::T * j] : plane[(size_t)(l + R::T * j) * R::PS + ln];
+  };
+  if constexpr (kPair) {
+    for (int q = 2 * gi; q < nl; q += 2 * R::NG) {
+      const int a = line(q);
+      float2 v[R::E];
 #pragma unroll
-    for (int j = 0; j < R::E; ++j) v[j] = col[(size_t)(l + R::T * j) * R::PS];
-    group_fft<R::E, R::T, INV>(v, l, tile, twl, gmask);
+      for (int j = 0; j < R::E; ++j) v[j] = at(a, j);
+      if (q + 1 < nl) {
+        const int b = line(q + 1);
+        float2 w[R::E];
 #pragma unroll
-    for (int j = 0; j < R::E; ++j) col[(size_t)(l + R::T * j) * R::PS] = v[j];
-  }
-}
-
-// row transforms of a plane in shared memory (rows kx, row stride PS), in place
-template <int N, bool INV>
-__device__ __forceinline__ void plane_rows_fft(float2* plane, float2* tiles, const float2* twl) {
-  using R = Cfg<N>;
-  const int gi = threadIdx.x / R::T, l = threadIdx.x % R::T;
-  const unsigned gmask = group_mask<N>();
-  float2* tile = tiles + (size_t)gi * R::TS;
-  for (int r = gi; r < N; r += R::NG) {
-    float2* row = plane + (size_t)r * R::PS;
-    float2 v[R::E];
+        for (int j = 0; j < R::E; ++j) w[j] = at(b, j);
+        group_fft_x2<R::E, R::T, INV>(v, w, l, tile, twl, gmask);
 #pragma unroll
-    for (int j = 0; j < R::E; ++j) v[j] = row[l + R::T * j];
-    group_fft<R::E, R::T, INV>(v, l, tile, twl, gmask);
+        for (int j = 0; j < R::E; ++j) at(b, j) = w[j];
+      } else {
+        group_fft<R::E, R::T, INV>(v, l, tile, twl, gmask);
+      }
 #pragma unroll
-    for (int j = 0; j < R::E; ++j) row[l + R::T * j] = v[j];
+      for (int j = 0; j < R::E; ++j) at(a, j) = v[j];
+    }
+  } else {
+    for (int q = gi; q < nl; q += R::NG) {
+      const int a = line(q);
+      float2 v[R::E];
+#pragma unroll
+      for (int j = 0; j < R::E; ++j) v[j] = at(a, j);
+      group_fft<R::E, R::T, INV>(v, l, tile, twl, gmask);
+#pragma unroll
+      for (int j = 0; j < R::E; ++j) at(a, j) = v[j];
+    }
   }
 }
 
@@ -174,9 +188,9 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass1_3d_kernel(const Args a)
     }
   }
   __syncthreads();
-  plane_rows_fft<N, true>(plane, sp1 + R::TILES, twl);
+  plane_fft<N, true, true>(plane, sp1 + R::TILES, twl, a.K);  // rows |kx| > K are zero
   __syncthreads();
-  plane_cols_fft<N, true>(plane, sp1 + R::TILES, twl);
+  plane_fft<N, true, false>(plane, sp1 + R::TILES, twl, -1);
   __syncthreads();
   float2* W = a.W + ((s * a.p.NI + f) * a.Kc + kz) * a.pl;
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) W[e] = plane[(size_t)(e / N) * R::PS + (e % N)];
@@ -310,7 +324,7 @@ __global__ void __launch_bounds__(Cfg<N>::THREADS) pass3_3d_kernel(const Args a)
     for (int j = 0; j < R::E; ++j) plane[(size_t)kx * R::PS + l + R::T * j] = v[j];
   }
   __syncthreads();
-  plane_cols_fft<N, false>(plane, sp3 + R::TILES, twl);
+  plane_fft<N, false, false>(plane, sp3 + R::TILES, twl, a.K);  // the combine reads |ky| <= K only
   __syncthreads();
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) H[e] = plane[(size_t)(e / N) * R::PS + (e % N)];
 }
