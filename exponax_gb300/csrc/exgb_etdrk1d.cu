@@ -232,8 +232,8 @@ struct ProductOut {
 };
 
 // ---- one-warp register transforms for the latency variant (one item per SM): N = A * B with
-// A = A1 * A2 <= 32 and B <= 32.  Lane l < A loads x[l + A j] (j < B), takes a length-B DFT in
-// registers and the twiddle w_N^(l k1); a transpose through the output buffer (__syncwarp only);
+// A = A1 * A2 <= 32 and B = B1 * B2 <= A.  Lane l < A loads x[l + A j] (j < B), takes a length-B DFT
+// in registers and the twiddle w_N^(l k1); a transpose through the output buffer (__syncwarp only);
 // lane k1 < B then takes a length-A DFT over l in registers and writes X[k1 + B k2].  A whole
 // transform is one barrier phase instead of one per radix pass.
 
@@ -276,29 +276,37 @@ __device__ __forceinline__ void lane_dft(float2 (&v)[R1 * R2], const float2* __r
 
 // One length-N transform by one warp, in -> out (in == out allowed); `out` also holds the transpose
 // tile (N = A * B entries, row k1 rotated by k1 against bank conflicts).  No 1/N scaling.
-template <int A1, int A2, int B, bool INV>
+template <int A1, int A2, int B1, int B2, bool INV>
 __device__ __forceinline__ void warp_fft(const float2* in, float2* out, const float2* __restrict__ tw, int lane) {
-  constexpr int A = A1 * A2, N = A * B;
+  constexpr int A = A1 * A2, B = B1 * B2, N = A * B;
   static_assert(A <= 32 && B <= 32 && B <= A, "one warp, B <= A");
-  float2 v[B];
+  float2 v[B];  // after the first DFT: X[q1 + B1 q2] in v[B2 q1 + q2]
   if (lane < A) {
 #pragma unroll
     for (int j = 0; j < B; ++j) v[j] = in[lane + A * j];
-    dftR<B, INV>(v);
+    lane_dft<B1, B2, INV>(v, tw, N / B);
 #pragma unroll
-    for (int k1 = 1; k1 < B; ++k1) {
-      float2 w = tw[lane * k1];
-      if (INV) w.y = -w.y;
-      v[k1] = cmul(v[k1], w);
-    }
+    for (int q1 = 0; q1 < B1; ++q1)
+#pragma unroll
+      for (int q2 = 0; q2 < B2; ++q2) {
+        const int k1 = q1 + B1 * q2;
+        if (k1 > 0) {
+          float2 w = tw[lane * k1];
+          if (INV) w.y = -w.y;
+          v[B2 * q1 + q2] = cmul(v[B2 * q1 + q2], w);
+        }
+      }
   }
   __syncwarp();
   if (lane < A) {
 #pragma unroll
-    for (int k1 = 0; k1 < B; ++k1) {
-      const int c = lane + k1;
-      out[k1 * A + (c < A ? c : c - A)] = v[k1];
-    }
+    for (int q1 = 0; q1 < B1; ++q1)
+#pragma unroll
+      for (int q2 = 0; q2 < B2; ++q2) {
+        const int k1 = q1 + B1 * q2;
+        const int c = lane + k1;
+        out[k1 * A + (c < A ? c : c - A)] = v[B2 * q1 + q2];
+      }
   }
   __syncwarp();
   float2 u[A];
@@ -319,25 +327,25 @@ __device__ __forceinline__ void warp_fft(const float2* in, float2* out, const fl
   }
 }
 
-// Sizes with a one-warp transform (WN = N = A1 * A2 * B); WN = 0: block Stockham passes.  Each size is
+// Sizes with a one-warp transform (WN = N = A1 * A2 * B1 * B2); WN = 0: block Stockham passes.  Each size is
 // a kernel instantiation of its own: one function holding several transforms' registers spills.
 template <int WN>
 struct WarpShape;
 template <>
 struct WarpShape<64> {
-  static constexpr int A1 = 8, A2 = 1, B = 8;
+  static constexpr int A1 = 8, A2 = 1, B1 = 8, B2 = 1;
 };
 template <>
 struct WarpShape<128> {
-  static constexpr int A1 = 4, A2 = 4, B = 8;
+  static constexpr int A1 = 4, A2 = 4, B1 = 8, B2 = 1;
 };
 template <>
-struct WarpShape<200> {
-  static constexpr int A1 = 5, A2 = 5, B = 8;
+struct WarpShape<200> {  // 20 lanes x 10 points, then 10 lanes x 20 points
+  static constexpr int A1 = 4, A2 = 5, B1 = 2, B2 = 5;
 };
 template <>
 struct WarpShape<256> {
-  static constexpr int A1 = 4, A2 = 8, B = 8;
+  static constexpr int A1 = 4, A2 = 8, B1 = 8, B2 = 1;
 };
 
 // m length-WN transforms in -> out (stride WN), one warp per sequence
@@ -347,7 +355,7 @@ __device__ __forceinline__ void warp_fft_many(const float2* in, float2* out, int
   using S = WarpShape<WN>;
   const int lane = tid & 31;
   for (int i = tid >> 5; i < m; i += nthr >> 5) {
-    warp_fft<S::A1, S::A2, S::B, INV>(in + (size_t)i * WN, out + (size_t)i * WN, tw, lane);
+    warp_fft<S::A1, S::A2, S::B1, S::B2, INV>(in + (size_t)i * WN, out + (size_t)i * WN, tw, lane);
     __syncwarp();
   }
 }
