@@ -344,8 +344,8 @@ struct WarpShape<200> {  // 20 lanes x 10 points, then 10 lanes x 20 points
   static constexpr int A1 = 4, A2 = 5, B1 = 2, B2 = 5;
 };
 template <>
-struct WarpShape<256> {
-  static constexpr int A1 = 4, A2 = 8, B1 = 8, B2 = 1;
+struct WarpShape<256> {  // 16 lanes x 16 points, twice
+  static constexpr int A1 = 4, A2 = 4, B1 = 4, B2 = 4;
 };
 
 // m length-WN transforms in -> out (stride WN), one warp per sequence
